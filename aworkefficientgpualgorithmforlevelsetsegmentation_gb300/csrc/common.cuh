@@ -1,0 +1,186 @@
+// Shared host/device helpers of the level-set engine: error type, CUDA call
+// checking, device error word, bounded waits and the 16^3-tile indexing of
+// the reference's int8 fields.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+
+#include "lss.h"
+
+namespace lss {
+
+// Host-side error carrying an lss_status; converted to a return code at the
+// C ABI boundary (lss_api.cpp).
+struct Error : std::runtime_error {
+    lss_status status;
+    Error(lss_status s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+#define LSS_CUDA(call)                                                                  \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess)                                                          \
+            throw ::lss::Error(e_ == cudaErrorMemoryAllocation ? LSS_ERR_OUT_OF_MEMORY  \
+                                                               : LSS_ERR_CUDA,          \
+                               std::string(#call) + ": " + cudaGetErrorString(e_));     \
+    } while (0)
+
+#define LSS_REQUIRE(cond, status, msg)                   \
+    do {                                                 \
+        if (!(cond)) throw ::lss::Error((status), (msg)); \
+    } while (0)
+
+// Device-side error word bits (read back after each step).
+enum : uint32_t {
+    ERR_BARRIER_TIMEOUT = 1u << 0,  // a grid barrier wait gave up
+    ERR_LOOKBACK_TIMEOUT = 1u << 1, // a decoupled-lookback wait gave up
+    ERR_TMA_TIMEOUT = 1u << 2,      // an mbarrier wait for a TMA load gave up
+    ERR_BOUNDS = 1u << 3,           // an index failed its bounds check
+    ERR_CAPACITY = 1u << 4,         // a list would have overflowed its buffer
+};
+
+// Every spin-wait gives up after this many nanoseconds of %globaltimer.
+constexpr uint64_t kWaitLimitNs = 2000000000ull;
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ uint64_t ld_acquire_u64(const uint64_t* p) {
+    uint64_t v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_u64(uint64_t* p, uint64_t v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void set_error(uint32_t* err, uint32_t bit) { atomicOr(err, bit); }
+
+// --------------------------------------------------------------------------
+// Decoupled-lookback tile prefix (single pass).  status[] holds one word per
+// tile: bits 63..62 = flag (0 invalid, 1 aggregate, 2 inclusive prefix),
+// bits 61..0 = value.  Values may pack two 31-bit counters (hi, lo); packed
+// sums add field-wise as long as no field overflows.  status[0..ntiles) must
+// be zero before the pass.  Called by all threads of the block; returns the
+// exclusive prefix of `tile`.  Tiles must be acquired in increasing order by
+// running blocks (a dynamic tile counter), so every wait is on a tile whose
+// block is resident; each wait still gives up after kWaitLimitNs.
+constexpr uint64_t kFlagA = 1ull << 62, kFlagP = 2ull << 62, kValMask = (1ull << 62) - 1;
+
+__device__ __forceinline__ uint64_t tile_exclusive_prefix(uint64_t* status, uint32_t tile,
+                                                          uint64_t aggregate, uint32_t* err) {
+    __shared__ uint64_t s_prefix;
+    if (threadIdx.x == 0) {
+        uint64_t excl = 0;
+        if (tile == 0) {
+            st_release_u64(&status[0], kFlagP | (aggregate & kValMask));
+        } else {
+            st_release_u64(&status[tile], kFlagA | (aggregate & kValMask));
+            int64_t j = (int64_t)tile - 1;
+            uint64_t t0 = 0;
+            while (j >= 0) {
+                uint64_t s = ld_acquire_u64(&status[j]);
+                if ((s >> 62) == 0) {
+                    if (t0 == 0) t0 = globaltimer_ns();
+                    else if (globaltimer_ns() - t0 > kWaitLimitNs) {
+                        set_error(err, ERR_LOOKBACK_TIMEOUT);
+                        break;
+                    }
+                    continue;
+                }
+                excl += s & kValMask;
+                if ((s >> 62) == 2) break;
+                --j;
+                t0 = 0;
+            }
+            st_release_u64(&status[tile], kFlagP | ((excl + aggregate) & kValMask));
+        }
+        s_prefix = excl;
+    }
+    __syncthreads();
+    uint64_t r = s_prefix;
+    __syncthreads();
+    return r;
+}
+
+// Block-wide exclusive sum of one uint32 per thread (blockDim.x a multiple of
+// 32, at most 1024).  Returns the thread's exclusive prefix; *total gets the
+// block sum.
+__device__ __forceinline__ uint32_t block_exclusive_sum(uint32_t v, uint32_t* total) {
+    __shared__ uint32_t s_warp[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < nw ? s_warp[lane] : 0;
+        uint32_t ws = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, ws, o);
+            if (lane >= o) ws += y;
+        }
+        if (lane < nw) s_warp[lane] = ws - w;
+        if (lane == nw - 1) s_warp[31] = ws;
+    }
+    __syncthreads();
+    uint32_t r = s_warp[warp] + x - v;
+    *total = s_warp[31];
+    __syncthreads();
+    return r;
+}
+
+// Same for 64-bit values (packed counters).
+__device__ __forceinline__ uint64_t block_exclusive_sum64(uint64_t v, uint64_t* total) {
+    __shared__ uint64_t s_warp64[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint64_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint64_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp64[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint64_t w = lane < nw ? s_warp64[lane] : 0;
+        uint64_t ws = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint64_t y = __shfl_up_sync(0xffffffffu, ws, o);
+            if (lane >= o) ws += y;
+        }
+        if (lane < nw) s_warp64[lane] = ws - w;
+        if (lane == nw - 1) s_warp64[31] = ws;
+    }
+    __syncthreads();
+    uint64_t r = s_warp64[warp] + x - v;
+    *total = s_warp64[31];
+    __syncthreads();
+    return r;
+}
+
+// Host-side fault injection for tests: LSS_FAULT=alloc|launch|timeout makes
+// the named host step fail with LSS_ERR_INJECTED (no GPU fault is made).
+bool fault_injected(const char* what);
+
+}  // namespace lss

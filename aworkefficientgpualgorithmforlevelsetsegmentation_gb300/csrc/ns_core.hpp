@@ -1,0 +1,98 @@
+// NsCore: device state of one or many LSS_MODE_NS volumes sharing one global
+// brick space, one set of brick bitmaps/lists and one persistent launch.
+#pragma once
+
+#include <cuda.h>
+
+#include <vector>
+
+#include "engine.hpp"
+
+namespace lss {
+
+struct NsVol;
+struct NsVolState;
+struct NsCtl;
+struct NsArgs;
+
+struct BrickConfig {
+    int bx, by, bz, threads;
+};
+
+const std::vector<BrickConfig>& brick_configs();
+
+class NsCore {
+   public:
+    NsCore(EngineBase* owner, uint64_t budget);
+    ~NsCore();
+
+    int add_volume(const float* data, int nx, int ny, int nz, const lss_params& p);
+    void set_params(int v, const lss_params& p) { vols_.at(v).p = p; upload_descriptors(); }
+    void set_bias(int v, const float* bias);
+    void configure(const BrickConfig& c);
+    void init_active();
+    void sphere_union(int v, float cx, float cy, float cz, float r);
+    void set_phi(int v, const float* phi);
+    void fill_phi(int v, float value);
+    int run(int max_iters, const lss_conv* conv, float* ms);
+    void read_phi(int v, float* out);
+    uint64_t read_active(int v, uint64_t* out, uint64_t cap);
+    void estimate(int v, float* t, float* w);
+    void state(int v, NsVolState* out);
+    uint32_t vol_parity(int v);
+    void check_errors();
+    void d2h(void* dst, const void* src, size_t bytes);
+
+    int nvol() const { return (int)vols_.size(); }
+    bool configured() const { return configured_; }
+    bool initialized() const { return initialized_; }
+    const BrickConfig& config() const { return cfg_; }
+    uint64_t held() const { return arena_.held() + brick_arena_.held(); }
+    uint32_t parity() const { return parity_; }
+    uint64_t bricks() const { return NB_; }
+    int grid() const { return grid_; }
+
+    struct VolHost {
+        int nx = 0, ny = 0, nz = 0, px = 0, py = 0, pz = 0, nbx = 0, nby = 0, nbz = 0;
+        uint32_t brick_base = 0;
+        float* phi[2] = {nullptr, nullptr};
+        float* img = nullptr;
+        float* bias = nullptr;
+        float* bias_buf = nullptr;
+        lss_params p{};
+        std::vector<uint8_t> frozen;
+        unsigned long long iterations = 0;
+    };
+    std::vector<VolHost>& vols() { return vols_; }
+
+   private:
+    size_t dyn_smem() const;
+    void upload_descriptors();
+    NsArgs args(uint32_t parity0, int max_iters, const lss_conv* conv) const;
+
+    EngineBase* owner_;
+    DeviceArena arena_;        // volumes (phi, intensities, bias)
+    DeviceArena brick_arena_;  // brick-shape dependent state
+    std::vector<VolHost> vols_;
+    BrickConfig cfg_{8, 8, 8, 256};
+    int words_ = 8;
+    uint64_t NB_ = 0;
+    uint32_t NW_ = 0;
+    int grid_ = 0;
+    uint32_t parity_ = 0;
+    bool configured_ = false, initialized_ = false;
+    NsVol* d_vols_ = nullptr;
+    NsVolState* d_vstate_ = nullptr;
+    CUtensorMap* d_tmaps_ = nullptr;
+    unsigned long long* d_masks_[2] = {nullptr, nullptr};
+    uint32_t* d_bits_[2] = {nullptr, nullptr};
+    unsigned long long* d_cnt_[2] = {nullptr, nullptr};
+    uint16_t* d_brick_vol_ = nullptr;
+    uint32_t* d_A_ = nullptr;
+    uint32_t* d_F_ = nullptr;
+    uint64_t* d_status_ = nullptr;
+    NsCtl* d_ctl_ = nullptr;
+    uint32_t* d_misc_ = nullptr;
+};
+
+}  // namespace lss

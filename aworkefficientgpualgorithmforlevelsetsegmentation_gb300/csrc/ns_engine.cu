@@ -1,0 +1,564 @@
+// LSS_MODE_NS host side: volume/brick bookkeeping, tensor maps, the launch
+// of the persistent kernel (plain engine = one volume, batched form = many),
+// initialisation, readback and the brick-shape autotuner.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "engine.hpp"
+#include "ns_core.hpp"
+#include "ns_kernels.cuh"
+
+namespace lss {
+
+// ---------------------------------------------------------------------------
+// Tensor-map encoding through the driver entry point.
+void encode_tmap_f32_3d(CUtensorMap* out, const float* base, uint64_t nx, uint64_t ny,
+                        uint64_t nz, uint64_t pitch_x, uint64_t pitch_xy, uint32_t bx,
+                        uint32_t by, uint32_t bz) {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    });
+    LSS_REQUIRE(fn, LSS_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    cuuint64_t dims[3] = {nx, ny, nz};
+    cuuint64_t strides[2] = {pitch_x * 4, pitch_xy * 4};
+    cuuint32_t box[3] = {bx, by, bz};
+    cuuint32_t es[3] = {1, 1, 1};
+    CUresult r = fn(out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)base, dims, strides, box, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    LSS_REQUIRE(r == CUDA_SUCCESS, LSS_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+}
+
+namespace {
+
+__global__ void k_ns_scatter(float* dst, const float* src, int nx, int ny, int nz, int px, int py) {
+    const uint64_t n = (uint64_t)nx * ny * nz;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t x = i % nx, y = (i / nx) % ny, z = i / ((uint64_t)nx * ny);
+        dst[(z * py + y) * px + x] = src[i];
+    }
+}
+
+__global__ void k_ns_gather(float* dst, const float* src, int nx, int ny, int nz, int px, int py) {
+    const uint64_t n = (uint64_t)nx * ny * nz;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t x = i % nx, y = (i / nx) % ny, z = i / ((uint64_t)nx * ny);
+        dst[i] = src[(z * py + y) * px + x];
+    }
+}
+
+__global__ void k_ns_fill(float* p, uint64_t n, float v) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
+// phi = min(phi, clamp(|x - c| - r)) over the logical volume.
+__global__ void k_ns_sphere_union(float* phi, int nx, int ny, int nz, int px, int py, float cx,
+                                  float cy, float cz, float r, float lo, float hi) {
+    const uint64_t n = (uint64_t)nx * ny * nz;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((uint64_t)nx * ny));
+        const double dx = x - (double)cx, dy = y - (double)cy, dz = z - (double)cz;
+        double d = sqrt(dx * dx + dy * dy + dz * dz) - (double)r;
+        d = d < lo ? lo : (d > hi ? hi : d);
+        float* q = &phi[((uint64_t)z * py + y) * px + x];
+        *q = fminf(*q, (float)d);
+    }
+}
+
+// Voxel coordinates of the active list, compacted in brick-major order with a
+// single-pass decoupled lookback over the per-brick counts (tiles of NT bricks).
+template <int BX, int BY, int BZ, int NT>
+__global__ void __launch_bounds__(NT) k_ns_emit(NsArgs a, uint32_t p, uint64_t* out,
+                                               uint32_t* tile_counter) {
+    using S = Brick<BX, BY, BZ>;
+    __shared__ uint32_t s_tile;
+    const uint32_t nA = a.ctl->nA;
+    const uint32_t ntiles = (nA + NT - 1) / NT;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1u);
+        __syncthreads();
+        const uint32_t tile = s_tile;
+        __syncthreads();
+        if (tile >= ntiles) break;
+        const uint32_t i = tile * NT + threadIdx.x;
+        uint32_t b = 0, cnt = 0;
+        unsigned long long w[S::WORDS];
+        if (i < nA) {
+            b = a.A_list[i];
+            for (int q = 0; q < S::WORDS; ++q) {
+                w[q] = a.masks[p][(size_t)b * S::WORDS + q];
+                cnt += __popcll(w[q]);
+            }
+        }
+        uint64_t total;
+        const uint64_t excl = block_exclusive_sum64(cnt, &total);
+        const uint64_t prefix = tile_exclusive_prefix(a.status, tile, total, &a.ctl->err);
+        if (i < nA) {
+            const NsVol& V = a.vols[a.brick_vol[b]];
+            const uint32_t lb = b - V.brick_base;
+            const int kx = lb % V.nbx, ky = (lb / V.nbx) % V.nby, kz = lb / (V.nbx * V.nby);
+            uint64_t o = prefix + excl;
+            for (int q = 0; q < S::WORDS; ++q) {
+                unsigned long long m = w[q];
+                while (m) {
+                    const int bit = __ffsll(m) - 1;
+                    m &= m - 1;
+                    const int j = q * 64 + bit;
+                    const uint64_t x = kx * S::X + j % S::X, y = ky * S::Y + (j / S::X) % S::Y,
+                                   z = kz * S::Z + j / (S::X * S::Y);
+                    out[o++] = (z * V.ny + y) * V.nx + x;
+                }
+            }
+        }
+    }
+}
+
+// Sum, sum of squares and count of the intensities where phi <= 0.
+__global__ void k_ns_collect(const float* img, const float* phi, int nx, int ny, int nz, int px,
+                             int py, double mean, double* acc) {
+    const uint64_t n = (uint64_t)nx * ny * nz;
+    double s = 0, q = 0, c = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t x = i % nx, y = (i / nx) % ny, z = i / ((uint64_t)nx * ny);
+        const uint64_t k = (z * py + y) * px + x;
+        if (phi[k] <= 0.0f) {
+            const double v = img[k];
+            s += v;
+            q += (v - mean) * (v - mean);
+            c += 1;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_down_sync(0xffffffffu, s, o);
+        q += __shfl_down_sync(0xffffffffu, q, o);
+        c += __shfl_down_sync(0xffffffffu, c, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&acc[0], s);
+        atomicAdd(&acc[1], q);
+        atomicAdd(&acc[2], c);
+    }
+}
+
+struct KernelSet {
+    void* persistent;
+    void* init_active;
+    void* build_list;
+    void* emit;
+    int words;
+};
+
+template <int BX, int BY, int BZ, int NT>
+KernelSet kernels_for() {
+    using S = Brick<BX, BY, BZ>;
+    return KernelSet{(void*)&k_ns_persistent<BX, BY, BZ, NT>, (void*)&k_ns_init_active<BX, BY, BZ, NT>,
+                     (void*)&k_ns_build_list<S::WORDS, NT>, (void*)&k_ns_emit<BX, BY, BZ, NT>,
+                     S::WORDS};
+}
+
+}  // namespace
+
+// The instantiated (brick shape, threads per brick) configurations.
+const std::vector<BrickConfig>& brick_configs() {
+    static const std::vector<BrickConfig> v = {
+        {8, 8, 8, 256}, {8, 8, 8, 128}, {8, 8, 8, 512}, {8, 8, 4, 128}, {8, 8, 4, 256}, {4, 4, 4, 64}};
+    return v;
+}
+
+static KernelSet kernels(const BrickConfig& c) {
+    if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 256) return kernels_for<8, 8, 8, 256>();
+    if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 128) return kernels_for<8, 8, 8, 128>();
+    if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 512) return kernels_for<8, 8, 8, 512>();
+    if (c.bx == 8 && c.by == 8 && c.bz == 4 && c.threads == 128) return kernels_for<8, 8, 4, 128>();
+    if (c.bx == 8 && c.by == 8 && c.bz == 4 && c.threads == 256) return kernels_for<8, 8, 4, 256>();
+    if (c.bx == 4 && c.by == 4 && c.bz == 4 && c.threads == 64) return kernels_for<4, 4, 4, 64>();
+    throw Error(LSS_ERR_UNSUPPORTED, "unsupported brick configuration");
+}
+
+// ---------------------------------------------------------------------------
+// NsCore
+
+NsCore::NsCore(EngineBase* owner, uint64_t budget) : owner_(owner), arena_(budget), brick_arena_(0) {}
+NsCore::~NsCore() = default;
+
+int NsCore::add_volume(const float* data, int nx, int ny, int nz, const lss_params& p) {
+    LSS_REQUIRE(data && nx > 0 && ny > 0 && nz > 0, LSS_ERR_INVALID_ARGUMENT, "bad volume");
+    LSS_REQUIRE(vols_.size() < 4096, LSS_ERR_CAPACITY, "at most 4096 volumes per batch");
+    VolHost v;
+    v.nx = nx; v.ny = ny; v.nz = nz;
+    v.px = (nx + 7) / 8 * 8; v.py = (ny + 7) / 8 * 8; v.pz = (nz + 7) / 8 * 8;
+    v.p = p;
+    const uint64_t P = (uint64_t)v.px * v.py * v.pz;
+    v.img = (float*)arena_.alloc(P * 4);
+    v.phi[0] = (float*)arena_.alloc(P * 4);
+    v.phi[1] = (float*)arena_.alloc(P * 4);
+    cudaStream_t st = owner_->stream;
+    LSS_CUDA(cudaMemsetAsync(v.img, 0, P * 4, st));
+    float* tmp = (float*)arena_.alloc((uint64_t)nx * ny * nz * 4);
+    LSS_CUDA(cudaMemcpyAsync(tmp, data, (uint64_t)nx * ny * nz * 4, cudaMemcpyHostToDevice, st));
+    k_ns_scatter<<<owner_->num_sms * 4, 256, 0, st>>>(v.img, tmp, nx, ny, nz, v.px, v.py);
+    k_ns_fill<<<owner_->num_sms * 4, 256, 0, st>>>(v.phi[0], P, p.phi_max);
+    k_ns_fill<<<owner_->num_sms * 4, 256, 0, st>>>(v.phi[1], P, p.phi_max);
+    LSS_CUDA(cudaGetLastError());
+    owner_->sync();
+    arena_.free_last(tmp);
+    v.frozen.assign((size_t)nx * ny * nz, 0);
+    vols_.push_back(v);
+    configured_ = false;
+    return (int)vols_.size() - 1;
+}
+
+void NsCore::set_bias(int v, const float* bias) {
+    VolHost& V = vols_.at(v);
+    const uint64_t P = (uint64_t)V.px * V.py * V.pz;
+    if (!bias) {
+        V.bias = nullptr;
+    } else {
+        if (!V.bias_buf) V.bias_buf = (float*)arena_.alloc(P * 4);
+        LSS_CUDA(cudaMemsetAsync(V.bias_buf, 0, P * 4, owner_->stream));
+        float* tmp = (float*)arena_.alloc((uint64_t)V.nx * V.ny * V.nz * 4);
+        LSS_CUDA(cudaMemcpyAsync(tmp, bias, (uint64_t)V.nx * V.ny * V.nz * 4, cudaMemcpyHostToDevice,
+                                 owner_->stream));
+        k_ns_scatter<<<owner_->num_sms * 4, 256, 0, owner_->stream>>>(V.bias_buf, tmp, V.nx, V.ny, V.nz,
+                                                                     V.px, V.py);
+        owner_->sync();
+        arena_.free_last(tmp);
+        V.bias = V.bias_buf;
+    }
+    upload_descriptors();
+}
+
+void NsCore::configure(const BrickConfig& c) {
+    LSS_REQUIRE(!vols_.empty(), LSS_ERR_STATE, "no volume");
+    owner_->sync();
+    cfg_ = c;
+    KernelSet ks = kernels(c);
+    words_ = ks.words;
+    brick_arena_.release();
+    NB_ = 0;
+    for (VolHost& v : vols_) {
+        v.nbx = v.px / c.bx; v.nby = v.py / c.by; v.nbz = v.pz / c.bz;
+        v.brick_base = (uint32_t)NB_;
+        NB_ += (uint64_t)v.nbx * v.nby * v.nbz;
+    }
+    LSS_REQUIRE(NB_ < (1ull << 31), LSS_ERR_CAPACITY, "too many bricks");
+    NW_ = (uint32_t)((NB_ + 31) / 32);
+    brick_arena_.set_budget(arena_.budget_left());
+    auto A = [&](size_t n) { return brick_arena_.alloc(n); };
+    d_vols_ = (NsVol*)A(sizeof(NsVol) * vols_.size());
+    d_vstate_ = (NsVolState*)A(sizeof(NsVolState) * vols_.size());
+    d_tmaps_ = (CUtensorMap*)A(sizeof(CUtensorMap) * 5 * vols_.size());
+    for (int q = 0; q < 2; ++q) {
+        d_masks_[q] = (unsigned long long*)A(NB_ * words_ * 8);
+        d_bits_[q] = (uint32_t*)A((size_t)NW_ * 4);
+        d_cnt_[q] = (unsigned long long*)A(8 * vols_.size());
+    }
+    d_brick_vol_ = (uint16_t*)A(NB_ * 2);
+    d_A_ = (uint32_t*)A(NB_ * 4 + 4);
+    d_F_ = (uint32_t*)A(NB_ * 4 + 4);
+    d_status_ = (uint64_t*)A((std::max<uint64_t>(NW_, NB_) / 32 + 16) * 8);
+    d_ctl_ = (NsCtl*)A(sizeof(NsCtl));
+    d_misc_ = (uint32_t*)A(64);
+    std::vector<uint16_t> bv(NB_);
+    for (size_t i = 0; i < vols_.size(); ++i) {
+        const VolHost& v = vols_[i];
+        std::fill(bv.begin() + v.brick_base, bv.begin() + v.brick_base + (size_t)v.nbx * v.nby * v.nbz,
+                  (uint16_t)i);
+    }
+    cudaStream_t st = owner_->stream;
+    LSS_CUDA(cudaMemcpyAsync(d_brick_vol_, bv.data(), NB_ * 2, cudaMemcpyHostToDevice, st));
+    std::vector<CUtensorMap> maps(5 * vols_.size());
+    for (size_t i = 0; i < vols_.size(); ++i) {
+        const VolHost& v = vols_[i];
+        const uint64_t pxy = (uint64_t)v.px * v.py;
+        for (int q = 0; q < 2; ++q) {
+            encode_tmap_f32_3d(&maps[5 * i + q], v.phi[q], v.nx, v.ny, v.nz, v.px, pxy, c.bx + 8,
+                               c.by + 2, c.bz + 2);
+            encode_tmap_f32_3d(&maps[5 * i + 2 + q], v.phi[q], v.nx, v.ny, v.nz, v.px, pxy, c.bx, c.by,
+                               c.bz);
+        }
+        encode_tmap_f32_3d(&maps[5 * i + 4], v.img, v.nx, v.ny, v.nz, v.px, pxy, c.bx, c.by, c.bz);
+    }
+    LSS_CUDA(cudaMemcpyAsync(d_tmaps_, maps.data(), maps.size() * sizeof(CUtensorMap),
+                             cudaMemcpyHostToDevice, st));
+    LSS_CUDA(cudaMemsetAsync(d_vstate_, 0, sizeof(NsVolState) * vols_.size(), st));
+    LSS_CUDA(cudaMemsetAsync(d_ctl_, 0, sizeof(NsCtl), st));
+    upload_descriptors();
+    // Co-residency of the persistent grid.
+    const size_t dyn = dyn_smem();
+    int per_sm = 0;
+    LSS_CUDA(cudaFuncSetAttribute(ks.persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    LSS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ks.persistent, c.threads, dyn));
+    LSS_REQUIRE(per_sm > 0, LSS_ERR_CUDA, "persistent kernel does not fit on an SM");
+    grid_ = owner_->num_sms * per_sm;
+    configured_ = true;
+    owner_->sync();
+}
+
+size_t NsCore::dyn_smem() const {
+    const size_t V = vols_.size();
+    return 4 * 4 * ((3 * V + 3) / 4) + 8 * V;
+}
+
+void NsCore::upload_descriptors() {
+    std::vector<NsVol> d(vols_.size());
+    for (size_t i = 0; i < vols_.size(); ++i) {
+        const VolHost& v = vols_[i];
+        NsVol& o = d[i];
+        std::memset(&o, 0, sizeof(o));
+        o.nx = v.nx; o.ny = v.ny; o.nz = v.nz;
+        o.px = v.px; o.py = v.py; o.pz = v.pz;
+        o.nbx = v.nbx; o.nby = v.nby; o.nbz = v.nbz;
+        o.brick_base = v.brick_base;
+        o.phi[0] = v.phi[0]; o.phi[1] = v.phi[1];
+        o.img = v.img;
+        o.bias = v.bias;
+        o.T = v.p.target; o.eps = v.p.window; o.alpha = v.p.curvature; o.dt = v.p.time_step;
+        o.lo = v.p.phi_min; o.hi = v.p.phi_max;
+        o.thr_t = v.p.temporal_threshold; o.thr_s = v.p.spatial_threshold;
+        o.alpha_data = v.p.alpha_role == LSS_ALPHA_CURVATURE ? 0 : 1;
+        o.nbh = v.p.neighbourhood == 6 ? 6 : 26;
+        o.tmap_base = (uint32_t)(5 * i);
+    }
+    if (d_vols_)
+        LSS_CUDA(cudaMemcpyAsync(d_vols_, d.data(), d.size() * sizeof(NsVol), cudaMemcpyHostToDevice,
+                                 owner_->stream));
+}
+
+NsArgs NsCore::args(uint32_t parity0, int max_iters, const lss_conv* conv) const {
+    NsArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.vols = d_vols_;
+    a.vstate = d_vstate_;
+    a.nvol = (int32_t)vols_.size();
+    a.tmaps = d_tmaps_;
+    for (int q = 0; q < 2; ++q) {
+        a.masks[q] = d_masks_[q];
+        a.bits[q] = d_bits_[q];
+        a.cnt[q] = d_cnt_[q];
+    }
+    a.brick_vol = d_brick_vol_;
+    a.A_list = d_A_;
+    a.F_list = d_F_;
+    a.status = d_status_;
+    a.ctl = d_ctl_;
+    a.NB = (uint32_t)NB_;
+    a.NW = NW_;
+    a.parity0 = parity0;
+    a.max_iters = max_iters;
+    a.conv_mode = conv ? 1 : 0;
+    if (conv) {
+        a.rel = conv->rel_threshold;
+        a.patience = conv->patience;
+        a.abs_thr = conv->abs_threshold;
+    }
+    return a;
+}
+
+// Rebuilds masks, bits and lists of every volume from the current phi (the
+// paper's initial active set, main.tex:217-231).  Both phi buffers are made
+// equal first.
+void NsCore::init_active() {
+    LSS_REQUIRE(configured_, LSS_ERR_STATE, "not configured");
+    cudaStream_t st = owner_->stream;
+    for (VolHost& v : vols_) {
+        const uint64_t P = (uint64_t)v.px * v.py * v.pz;
+        float* cur = v.phi[parity_];
+        float* oth = v.phi[parity_ ^ 1];
+        LSS_CUDA(cudaMemcpyAsync(oth, cur, P * 4, cudaMemcpyDeviceToDevice, st));
+    }
+    for (int q = 0; q < 2; ++q) {
+        LSS_CUDA(cudaMemsetAsync(d_masks_[q], 0, NB_ * words_ * 8, st));
+        LSS_CUDA(cudaMemsetAsync(d_bits_[q], 0, (size_t)NW_ * 4, st));
+        LSS_CUDA(cudaMemsetAsync(d_cnt_[q], 0, 8 * vols_.size(), st));
+    }
+    LSS_CUDA(cudaMemsetAsync(d_ctl_, 0, sizeof(NsCtl), st));
+    LSS_CUDA(cudaMemsetAsync(d_status_, 0, (NW_ / 64 + 8) * 8, st));
+    KernelSet ks = kernels(cfg_);
+    NsArgs a = args(parity_, 0, nullptr);
+    uint32_t p = parity_;
+    void* params[] = {&a, &p};
+    const int grid = (int)std::min<uint64_t>(NB_, (uint64_t)owner_->num_sms * 16);
+    LSS_CUDA(cudaLaunchKernel(ks.init_active, dim3(grid), dim3(cfg_.threads), params, 0, st));
+    LSS_CUDA(cudaLaunchKernel(ks.build_list, dim3(std::max(1, owner_->num_sms)), dim3(cfg_.threads), params,
+                              0, st));
+    std::vector<unsigned long long> n0(vols_.size());
+    LSS_CUDA(cudaMemcpyAsync(n0.data(), d_cnt_[parity_], 8 * vols_.size(), cudaMemcpyDeviceToHost, st));
+    owner_->sync();
+    std::vector<NsVolState> vs(vols_.size());
+    for (size_t i = 0; i < vols_.size(); ++i) {
+        std::memset(&vs[i], 0, sizeof(NsVolState));
+        vs[i].n0 = n0[i];
+        vs[i].n_cur = n0[i];
+        vs[i].parity = (int32_t)parity_;
+        vols_[i].iterations = 0;
+    }
+    LSS_CUDA(cudaMemcpyAsync(d_vstate_, vs.data(), vs.size() * sizeof(NsVolState), cudaMemcpyHostToDevice,
+                             st));
+    owner_->sync();
+    check_errors();
+    initialized_ = true;
+}
+
+void NsCore::sphere_union(int v, float cx, float cy, float cz, float r) {
+    VolHost& V = vols_.at(v);
+    k_ns_sphere_union<<<owner_->num_sms * 4, 256, 0, owner_->stream>>>(
+        V.phi[parity_], V.nx, V.ny, V.nz, V.px, V.py, cx, cy, cz, r, V.p.phi_min, V.p.phi_max);
+    LSS_CUDA(cudaGetLastError());
+}
+
+void NsCore::set_phi(int v, const float* phi) {
+    VolHost& V = vols_.at(v);
+    float* tmp = (float*)arena_.alloc((uint64_t)V.nx * V.ny * V.nz * 4);
+    LSS_CUDA(cudaMemcpyAsync(tmp, phi, (uint64_t)V.nx * V.ny * V.nz * 4, cudaMemcpyHostToDevice,
+                             owner_->stream));
+    k_ns_scatter<<<owner_->num_sms * 4, 256, 0, owner_->stream>>>(V.phi[parity_], tmp, V.nx, V.ny, V.nz,
+                                                                 V.px, V.py);
+    owner_->sync();
+    arena_.free_last(tmp);
+}
+
+void NsCore::fill_phi(int v, float value) {
+    VolHost& V = vols_.at(v);
+    k_ns_fill<<<owner_->num_sms * 4, 256, 0, owner_->stream>>>(V.phi[parity_], (uint64_t)V.px * V.py * V.pz,
+                                                              value);
+    LSS_CUDA(cudaGetLastError());
+}
+
+int NsCore::run(int max_iters, const lss_conv* conv, float* ms) {
+    LSS_REQUIRE(initialized_, LSS_ERR_STATE, "no seed / phi set");
+    if (max_iters <= 0) return 0;
+    cudaStream_t st = owner_->stream;
+    KernelSet ks = kernels(cfg_);
+    NsArgs a = args(parity_, max_iters, conv);
+    void* params[] = {&a};
+    cudaEvent_t e0, e1;
+    LSS_CUDA(cudaEventCreate(&e0));
+    LSS_CUDA(cudaEventCreate(&e1));
+    LSS_CUDA(cudaEventRecord(e0, st));
+    if (fault_injected("launch")) throw Error(LSS_ERR_INJECTED, "injected launch failure");
+    LSS_CUDA(cudaLaunchCooperativeKernel(ks.persistent, dim3(grid_), dim3(cfg_.threads), params, dyn_smem(),
+                                         st));
+    LSS_CUDA(cudaEventRecord(e1, st));
+    LSS_CUDA(cudaEventSynchronize(e1));
+    float t = 0;
+    cudaEventElapsedTime(&t, e0, e1);
+    if (ms) *ms = t;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    NsCtl c;
+    d2h(&c, d_ctl_, sizeof(c));
+    if (fault_injected("timeout")) c.err |= ERR_BARRIER_TIMEOUT;
+    LSS_REQUIRE(c.err == 0, LSS_ERR_TIMEOUT,
+                "device-side wait gave up (error word " + std::to_string(c.err) + ")");
+    std::vector<NsVolState> vs(vols_.size());
+    d2h(vs.data(), d_vstate_, vs.size() * sizeof(NsVolState));
+    parity_ = (parity_ + c.iters_run) & 1u;
+    for (size_t i = 0; i < vols_.size(); ++i) vols_[i].iterations = vs[i].iterations;
+    return (int)c.iters_run;
+}
+
+void NsCore::d2h(void* dst, const void* src, size_t bytes) {
+    LSS_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, owner_->stream));
+    owner_->sync();
+}
+
+void NsCore::state(int v, NsVolState* out) {
+    std::vector<NsVolState> vs(vols_.size());
+    d2h(vs.data(), d_vstate_, vs.size() * sizeof(NsVolState));
+    *out = vs.at(v);
+}
+
+uint32_t NsCore::vol_parity(int v) {
+    NsVolState s;
+    state(v, &s);
+    return (uint32_t)s.parity;
+}
+
+void NsCore::read_phi(int v, float* out) {
+    VolHost& V = vols_.at(v);
+    const uint32_t p = vols_.size() == 1 ? parity_ : vol_parity(v);
+    float* tmp = (float*)arena_.alloc((uint64_t)V.nx * V.ny * V.nz * 4);
+    k_ns_gather<<<owner_->num_sms * 4, 256, 0, owner_->stream>>>(tmp, V.phi[p], V.nx, V.ny, V.nz, V.px,
+                                                                V.py);
+    LSS_CUDA(cudaMemcpyAsync(out, tmp, (uint64_t)V.nx * V.ny * V.nz * 4, cudaMemcpyDeviceToHost,
+                             owner_->stream));
+    owner_->sync();
+    arena_.free_last(tmp);
+}
+
+uint64_t NsCore::read_active(int v, uint64_t* out, uint64_t cap) {
+    LSS_REQUIRE(vols_.size() == 1 && v == 0, LSS_ERR_UNSUPPORTED, "active list of a single volume only");
+    NsCtl c;
+    d2h(&c, d_ctl_, sizeof(c));
+    NsVolState s;
+    state(0, &s);
+    const uint64_t n = s.n_cur;
+    if (!out) return n;
+    uint64_t* dout = (uint64_t*)arena_.alloc(std::max<uint64_t>(n, 1) * 8);
+    LSS_CUDA(cudaMemsetAsync(d_status_, 0, ((uint64_t)c.nA / cfg_.threads + 2) * 8, owner_->stream));
+    LSS_CUDA(cudaMemsetAsync(d_misc_, 0, 4, owner_->stream));
+    KernelSet ks = kernels(cfg_);
+    NsArgs a = args(parity_, 0, nullptr);
+    uint32_t p = parity_;
+    uint64_t* o = dout;
+    uint32_t* tc = d_misc_;
+    void* params[] = {&a, &p, &o, &tc};
+    LSS_CUDA(cudaLaunchKernel(ks.emit, dim3(owner_->num_sms * 2), dim3(cfg_.threads), params, 0,
+                              owner_->stream));
+    const uint64_t m = std::min(n, cap);
+    if (m) LSS_CUDA(cudaMemcpyAsync(out, dout, m * 8, cudaMemcpyDeviceToHost, owner_->stream));
+    owner_->sync();
+    arena_.free_last(dout);
+    check_errors();
+    return n;
+}
+
+void NsCore::estimate(int v, float* t, float* w) {
+    VolHost& V = vols_.at(v);
+    double* acc = (double*)arena_.alloc(32);
+    double h[3];
+    double mean = 0;
+    for (int pass = 0; pass < 2; ++pass) {
+        LSS_CUDA(cudaMemsetAsync(acc, 0, 24, owner_->stream));
+        k_ns_collect<<<owner_->num_sms * 4, 256, 0, owner_->stream>>>(V.img, V.phi[parity_], V.nx, V.ny,
+                                                                     V.nz, V.px, V.py, mean, acc);
+        LSS_CUDA(cudaMemcpyAsync(h, acc, 24, cudaMemcpyDeviceToHost, owner_->stream));
+        owner_->sync();
+        LSS_REQUIRE(h[2] >= 2, LSS_ERR_STATE, "fewer than two segmented voxels");
+        if (pass == 0) mean = h[0] / h[2];
+    }
+    arena_.free_last(acc);
+    *t = (float)mean;
+    *w = (float)std::sqrt(h[1] / (h[2] - 1));
+}
+
+void NsCore::check_errors() {
+    LSS_CUDA(cudaGetLastError());
+    NsCtl c;
+    d2h(&c, d_ctl_, sizeof(c));
+    LSS_REQUIRE(c.err == 0, LSS_ERR_TIMEOUT, "device-side wait gave up (error word " + std::to_string(c.err) + ")");
+}
+
+}  // namespace lss

@@ -1,0 +1,318 @@
+"""Benchmark of the sparse level-set engine (one JSON line on rank 0).
+
+Workload (default): the 256^3 three-shell phantom (seeded synthetic stand-in
+for the reference's BrainWeb MRI) with four radius-3 seeds, T=0.8, eps=0.1,
+alpha=0.85, dt=0.5, run until the active count stays under 0.1% of the
+initial count for 5 iterations (at most 2000).  One step = reseed from the
+device-resident volume (fill phi, union the seed spheres, rebuild the active
+set) + the full run to convergence, in LSS_MODE_NS.
+
+metric: active-voxel updates per second (sum over iterations of the active
+count, from the device counter) over the device time of the steps.
+e2e: the same metric through the public API with host buffers each step
+(volume upload, seeding, run, mask readback).
+roofline: 20 algorithmic bytes per active-voxel update (phi in, I, phi out,
+coordinate in/out) over the persistent kernel's CUDA-event time, against the
+measured HBM copy bandwidth.
+--impl reference: the CPU restatement of the path (the FP64 oracle, all host
+threads) on a bounded sample of the same workload.
+Multi-GPU: replicas only (each rank runs the whole workload on its GPU).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BYTES_PER_UPDATE = 20
+FALLBACK_HBM_GBS = 6800.0
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.samples: list[list[str]] = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = [r for r in self.samples if len(r) == 6 and r[0].isdigit()]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[2 + i] == "Active"})
+        return {"sm_mhz": statistics.median(float(r[0]) for r in rows),
+                "sm_max_mhz": max(float(r[1]) for r in rows), "reasons": reasons,
+                "samples": len(rows)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, value: float) -> float:
+    if ws == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(ws, value: float) -> float:
+    if ws == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def cpu_reference(cfg, iters: int, threads: int):
+    """The FP64 CPU restatement on the first `iters` iterations of the run."""
+    from oracle.oracle import NsOracle
+    p = cfg["params"]
+    o = NsOracle(cfg["image"], threads=threads)
+    o.set_params(p.target, p.window, p.curvature, p.time_step, alpha_data=p.alpha_role)
+    o.set_phi(cfg["phi0"])
+    t0 = time.perf_counter()
+    o.step(iters)
+    dt = time.perf_counter() - t0
+    return o.updates, dt
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    from aworkefficientgpualgorithmforlevelsetsegmentation_gb300 import phantoms as P
+    cfg = P.config2(args.scale)
+    threads = os.cpu_count() or 1
+    times, ups = [], []
+    for s in range(args.warmup + args.steps):
+        u, dt = cpu_reference(cfg, args.ref_iters, threads)
+        if s >= args.warmup:
+            times.append(dt)
+            ups.append(u)
+    value = sum(ups) / sum(times)
+    line = {
+        "impl": "reference", "metric": "active_voxel_updates_per_s", "value": value,
+        "unit": "voxel_updates/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": cfg["name"] + "_three_shell_phantom",
+                   "sample": f"first {args.ref_iters} iterations from the seeds"},
+        "cpu_baseline": {"value": value, "unit": "voxel_updates/s", "cores": threads, "kind": "port",
+                         "sample": f"first {args.ref_iters} iterations of {cfg['name']} per step"},
+        "e2e": {"value": value, "unit": "voxel_updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, ws, rank, local):
+    import torch
+    import aworkefficientgpualgorithmforlevelsetsegmentation_gb300 as lss
+    from aworkefficientgpualgorithmforlevelsetsegmentation_gb300 import phantoms as P
+
+    torch.cuda.set_device(local)
+    cfg = P.config2(args.scale)
+    p = cfg["params"]
+    conv = cfg["conv"]
+    brick = tuple(args.brick) if args.brick else (0, 0, 0)
+    seg = lss.Segmenter(lss.MODE_NS, device=local, brick=brick, threads_per_brick=args.threads)
+    stream = torch.cuda.Stream(device=local)
+    import ctypes
+    seg._chk(seg._lib.lss_set_stream(seg._h, ctypes.c_void_p(stream.cuda_stream)))
+    seg.load_volume(cfg["image"])
+    seg.set_parameters(p.target, p.window, p.curvature, p.time_step, alpha_role=p.alpha_role)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def one_step():
+        seg.clear_current_segmentation()
+        seg.set_seed_spheres(cfg["spheres"])
+        return seg.step_until_converged(conv["rel"], conv["patience"], conv["max_iterations"])
+
+    for _ in range(args.warmup):
+        one_step()
+    torch.cuda.synchronize()
+    barrier(ws)
+    ev_ms, kern_ms, updates, iters = 0.0, 0.0, 0, []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1)  # L2 flush between timed steps (outside the events)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            it = one_step()
+            e1.record(stream)
+            e1.synchronize()
+            ev_ms += e0.elapsed_time(e1)
+            st = seg.stats()
+            kern_ms += st["last_step_ms"]
+            updates += st["voxel_updates"]
+            iters.append(it)
+    torch.cuda.synchronize()
+    barrier(ws)
+    t_max = max_over_ranks(ws, ev_ms)
+    total_updates = sum_over_ranks(ws, float(updates))
+    value = total_updates / (t_max / 1e3)
+    st = seg.stats()
+    mask = seg.get_saveable_segmentation()
+
+    # e2e through the public API with host buffers.
+    e2e_ms = 0.0
+    e2e_updates = 0
+    img = np.ascontiguousarray(cfg["image"])
+    for s in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        seg.load_volume(img)
+        seg.set_parameters(p.target, p.window, p.curvature, p.time_step, alpha_role=p.alpha_role)
+        seg.set_seed_spheres(cfg["spheres"])
+        seg.step_until_converged(conv["rel"], conv["patience"], conv["max_iterations"])
+        m = seg.get_saveable_segmentation()
+        t1 = time.perf_counter()
+        if s >= args.warmup:
+            e2e_ms += 1e3 * (t1 - t0)
+            e2e_updates += seg.stats()["voxel_updates"]
+    assert np.array_equal(m, mask)
+    e2e_value = sum_over_ranks(ws, float(e2e_updates)) / (max_over_ranks(ws, e2e_ms) / 1e3)
+
+    # Dense all-voxel GPU update with the same math and the same iteration count.
+    dense = lss.Segmenter(lss.MODE_NS, device=local, brick=(8, 8, 8), threads_per_brick=256)
+    dense.load_volume(cfg["image"])
+    dense.set_parameters(p.target, p.window, p.curvature, p.time_step, alpha_role=p.alpha_role,
+                         temporal_threshold=-1.0, spatial_threshold=-1.0)
+    dense.set_seed_spheres(cfg["spheres"])
+    dense.step(3)
+    dense.step(args.dense_iters)
+    dense_ms_per_it = dense.stats()["last_step_ms"] / args.dense_iters
+    sparse_ms = ev_ms / args.steps
+    dense_ms = dense_ms_per_it * statistics.mean(iters)
+    del dense
+
+    peak, peak_kind = measured_peak()
+    achieved = BYTES_PER_UPDATE * updates / (kern_ms / 1e3) / 1e9
+    launches_per_step = 8
+    if rank == 0:
+        cpu_u, cpu_t = (None, None)
+        if not args.no_cpu:
+            cpu_u, cpu_t = cpu_reference(cfg, args.ref_iters, os.cpu_count() or 1)
+        line = {
+            "metric": "active_voxel_updates_per_s", "value": value, "unit": "voxel_updates/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": cfg["name"] + "_three_shell_phantom", "mode": "LSS_MODE_NS",
+                       "stopping": "n < 0.1% n0 for 5 iterations, max 2000",
+                       "iterations_to_converge": iters[-1],
+                       "converge_ms": sparse_ms,
+                       "brick": [st["brick_x"], st["brick_y"], st["brick_z"]],
+                       "threads_per_brick": st["threads_per_brick"],
+                       "l2": "flushed between steps (256 MiB write); volume 192 MiB > L2",
+                       "parallelism": "replicas" if ws > 1 else "single"},
+            "dense_gpu": {"ms_to_same_iterations": dense_ms, "ms_per_iteration": dense_ms_per_it,
+                          "sparse_speedup": dense_ms / sparse_ms},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                         "bytes_per_update": BYTES_PER_UPDATE},
+            "cpu_baseline": None if cpu_u is None else {
+                "value": cpu_u / cpu_t, "unit": "voxel_updates/s", "cores": os.cpu_count(),
+                "kind": "port", "sample": f"first {args.ref_iters} iterations of {cfg['name']}"},
+            "e2e": {"value": e2e_value, "unit": "voxel_updates/s",
+                    "h2d_bytes_per_step": int(img.nbytes),
+                    "d2h_bytes_per_step": int(mask.nbytes)},
+            "gpu_launches": launches_per_step * args.steps,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--brick", type=int, nargs=3, default=None)
+    ap.add_argument("--threads", type=int, default=0)
+    ap.add_argument("--ref-iters", type=int, default=40)
+    ap.add_argument("--dense-iters", type=int, default=20)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_ours(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

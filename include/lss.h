@@ -22,10 +22,14 @@
  *                 in 16^3 tiles, integer intensities, 6-connected output
  *                 into seven offset buffers, tag-volume duplicate filter,
  *                 few/many-active path choice);
- *   LSS_MODE_NS   fp32 phi and intensity, upwind |grad phi|, mean curvature
- *                 div(grad phi/|grad phi|), speed D = eps - |I - T|, phi
- *                 clamped to [phi_min, phi_max], bricked active set with
- *                 26-neighbour expansion.
+ *   LSS_MODE_NS   fp32 phi and intensity:
+ *                   phi += dt * (wc * div(grad phi/|grad phi|) |grad phi|
+ *                                - wd * D * |grad phi|_upwind),
+ *                   D = clamp((eps - |I - T|) / eps, -1, 1) + bias,
+ *                 phi clamped to [phi_min, phi_max], inside = phi <= 0,
+ *                 (wc, wd) = (1 - alpha, alpha) or (alpha, 1 - alpha) by
+ *                 lss_params.alpha_role; bricked active set with 26-neighbour
+ *                 expansion.
  */
 #ifndef LSS_H
 #define LSS_H
@@ -62,6 +66,12 @@ typedef enum lss_dtype {
 
 typedef enum lss_mode { LSS_MODE_REF = 0, LSS_MODE_NS = 1 } lss_mode;
 
+/* Which term alpha weights in LSS_MODE_NS.  LSS_ALPHA_CURVATURE is the
+ * reference's and the paper's speed F = alpha*C + (1-alpha)*D
+ * (UpdateLevelSetVolume.cu:303; main.tex:178); LSS_ALPHA_DATA is
+ * F = alpha*D + (1-alpha)*C (Lefohn et al. 2004), the default. */
+typedef enum lss_alpha_role { LSS_ALPHA_CURVATURE = 0, LSS_ALPHA_DATA = 1 } lss_alpha_role;
+
 typedef struct lss_engine lss_engine;
 
 /* Engine construction options. */
@@ -93,6 +103,7 @@ typedef struct lss_params {
     float   convergence_threshold;/* REF: finished when n <= this and iterations > 500
                                      (Segmenter.cpp:1053-1056)                          */
     int32_t neighbourhood;        /* expansion neighbourhood: 6 (REF) or 26 (NS)         */
+    int32_t alpha_role;           /* NS: lss_alpha_role (default LSS_ALPHA_DATA)         */
 } lss_params;
 
 /* Stopping rule of lss_step_until_converged. */

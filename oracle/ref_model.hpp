@@ -61,6 +61,8 @@ inline uint32_t lin(uint32_t x, uint32_t y, uint32_t z, Dims d) {
 // ComputeIndex3DToTiled1D (Coordinates.cu:65-96): 16^3 tiles in x-fastest tile
 // order, voxels x-fastest inside a tile.
 inline uint32_t tiled(uint32_t x, uint32_t y, uint32_t z, Dims d) {
+    if (x >= d.x || y >= d.y || z >= d.z)
+        throw std::out_of_range("coordinate outside the volume (the reference would index out of bounds)");
     uint32_t tile = (z >> 4) * ((d.y >> 4) * (d.x >> 4)) + (y >> 4) * (d.x >> 4) + (x >> 4);
     return tile * 4096u + ((z & 15u) * 16u + (y & 15u)) * 16u + (x & 15u);
 }

@@ -1,0 +1,70 @@
+"""CPU-only checks of the C-ABI library: it builds, loads without a GPU and
+exports every entry point that include/lss.h and include/lss_phantom.h
+declare; the Python binding covers the same set; without a device the
+engine refuses cleanly."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import aworkefficientgpualgorithmforlevelsetsegmentation_gb300 as lss
+from aworkefficientgpualgorithmforlevelsetsegmentation_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared(header):
+    text = open(os.path.join(ROOT, "include", header)).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return set(re.findall(r"^\s*(?:const\s+)?[\w\s\*]+?\b(lss_\w+)\s*\(", text, flags=re.M))
+
+
+def test_headers_declare_entry_points():
+    names = declared("lss.h") | declared("lss_phantom.h")
+    assert "lss_create" in names and "lss_step" in names and "lss_batch_run" in names
+    assert len(names) >= 40
+
+
+def test_library_exports_every_declared_symbol():
+    L = lss.load()
+    for name in sorted(declared("lss.h") | declared("lss_phantom.h")):
+        assert hasattr(L, name), name
+
+
+def test_binding_matches_headers():
+    assert set(_lib.SIGNATURES) == declared("lss.h") | declared("lss_phantom.h")
+
+
+def test_defaults_and_errors_without_device():
+    L = lss.load()
+    c = _lib.lss_config()
+    assert L.lss_config_default(C.byref(c)) == 0 and c.mode == 1 and c.ref_quirk_i3 == 1
+    p = _lib.lss_params()
+    assert L.lss_params_default(0, C.byref(p)) == 0
+    assert abs(p.temporal_threshold - 0.008) < 1e-9 and p.neighbourhood == 6
+    assert L.lss_params_default(1, C.byref(p)) == 0 and p.phi_max == 4 and p.neighbourhood == 26
+    assert L.lss_params_default(7, C.byref(p)) == 1
+    assert L.lss_create(None, None) == 1
+    assert L.lss_step(None, 1, None) == 1
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if not has_gpu:
+        h = C.c_void_p()
+        assert L.lss_create(C.byref(h), None) == 7  # LSS_ERR_NO_DEVICE
+
+
+def test_phantoms_are_deterministic():
+    from aworkefficientgpualgorithmforlevelsetsegmentation_gb300 import phantoms as P
+    a = P.config2(0.25)["image"]
+    b = P.config2(0.25)["image"]
+    assert np.array_equal(a, b)
+    assert a.dtype == np.float32 and a.shape == (64, 64, 64)
+    # intensities of the inner shell around 0.8, background 0
+    assert 0.7 < float(a[32, 32, 32]) < 0.9
+    e = P.ellipsoid((8, 8, 8), (3.5, 3.5, 3.5), (2, 2, 2), 1.0, 0.0, 0.0, 0)
+    assert e[4, 4, 4] == 1.0 and e[0, 0, 0] == 0.0

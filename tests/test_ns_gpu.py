@@ -1,0 +1,222 @@
+"""LSS_MODE_NS on the GPU against the FP64 oracle (oracle/ns_model.hpp).
+
+Tolerances (spec parity criteria):
+  * one iteration from an identical state: max |phi_gpu - phi_fp64| <= 1e-4;
+  * active lists: bit-exact (order included) given identical phi, i.e. the
+    oracle's expansion rule applied to the GPU's own before/after values;
+  * after running to the stopping rule: mask disagreement <= 0.01% of voxels
+    and Dice >= 0.999 against the FP64 run.
+"""
+import numpy as np
+import pytest
+
+import aworkefficientgpualgorithmforlevelsetsegmentation_gb300 as lss
+from aworkefficientgpualgorithmforlevelsetsegmentation_gb300 import phantoms as P
+from oracle.oracle import NsOracle
+from tests.gpu_util import dice
+
+pytestmark = pytest.mark.gpu
+
+PHI_TOL = 1e-4
+
+
+def make_gpu(cfg, brick=(8, 8, 8), threads=256, **pk):
+    s = lss.Segmenter(lss.MODE_NS, brick=brick, threads_per_brick=threads)
+    s.load_volume(cfg["image"])
+    p = cfg["params"]
+    s.set_parameters(p.target, p.window, p.curvature, p.time_step, alpha_role=p.alpha_role, **pk)
+    s.set_phi(cfg["phi0"])
+    return s
+
+
+def make_oracle(cfg, brick=(8, 8, 8), nbh=26):
+    p = cfg["params"]
+    o = NsOracle(cfg["image"], brick=brick, threads=8)
+    o.set_params(p.target, p.window, p.curvature, p.time_step, p.phi_min, p.phi_max,
+                 p.temporal_threshold, p.spatial_threshold, nbh, p.alpha_role)
+    return o
+
+
+@pytest.mark.parametrize("which,scale", [("config1", 0.5), ("config2", 0.25)])
+def test_ns_each_iteration_vs_fp64(which, scale):
+    cfg = getattr(P, which)(scale)
+    s = make_gpu(cfg)
+    o = make_oracle(cfg)
+    o.set_phi(cfg["phi0"])
+    assert np.array_equal(s.active_linear(), o.active()), "initial active set"
+    worst = 0.0
+    for it in range(40):
+        before = s.read_phi()
+        act = s.active_linear()
+        o.set_state(before, act)
+        assert np.array_equal(o.active(), act)
+        o.step(1)
+        s.step(1)
+        after = s.read_phi()
+        err = float(np.max(np.abs(after.astype(np.float64) - o.read_phi64())))
+        worst = max(worst, err)
+        assert err <= PHI_TOL, (it, err)
+        flat_b, flat_a = before.ravel(), after.ravel()
+        idx = act.astype(np.int64)
+        expect = o.expand_given(act, flat_b[idx], flat_a[idx])
+        assert np.array_equal(s.active_linear(), expect), it
+        if s.n == 0:
+            break
+    assert worst < PHI_TOL
+
+
+@pytest.mark.parametrize("which,scale", [("config1", 0.5), ("config2", 0.25)])
+def test_ns_converged_mask_vs_fp64(which, scale):
+    cfg = getattr(P, which)(scale)
+    s = make_gpu(cfg)
+    it_g = s.step_until_converged(1e-3, 5, 2000)
+    o = make_oracle(cfg)
+    o.set_phi(cfg["phi0"])
+    it_o = o.run(1e-3, 5, 2000)
+    mg = s.get_saveable_segmentation().astype(bool)
+    mo = o.read_phi() <= 0
+    disagree = float(np.mean(mg != mo))
+    assert disagree <= 1e-4, disagree
+    assert dice(mg, mo) >= 0.999
+    assert abs(it_g - it_o) <= max(3, 0.02 * it_o), (it_g, it_o)
+    st = s.stats()
+    assert st["voxel_updates"] > 0 and st["iterations"] == it_g
+
+
+def test_ns_brick_configs_are_voxel_exact():
+    cfg = P.config2(0.25)
+    ref_phi = ref_act = None
+    for (bx, by, bz, t) in [(8, 8, 8, 256), (8, 8, 8, 128), (8, 8, 8, 512), (8, 8, 4, 128),
+                            (8, 8, 4, 256), (4, 4, 4, 64)]:
+        s = make_gpu(cfg, brick=(bx, by, bz), threads=t)
+        s.step(30)
+        phi = s.read_phi()
+        act = np.sort(s.active_linear())
+        if ref_phi is None:
+            ref_phi, ref_act = phi, act
+        else:
+            assert np.array_equal(phi, ref_phi), (bx, by, bz, t)
+            assert np.array_equal(act, ref_act), (bx, by, bz, t)
+        st = s.stats()
+        assert (st["brick_x"], st["brick_y"], st["brick_z"], st["threads_per_brick"]) == (bx, by, bz, t)
+
+
+def test_ns_six_neighbourhood_vs_fp64():
+    cfg = P.config1(0.25)
+    s = make_gpu(cfg, neighbourhood=6)
+    o = make_oracle(cfg, nbh=6)
+    o.set_phi(cfg["phi0"])
+    for _ in range(20):
+        o.step(1)
+        s.step(1)
+        assert np.array_equal(s.active_linear(), o.active())
+    assert float(np.max(np.abs(s.read_phi() - o.read_phi()))) < 1e-3
+
+
+def test_ns_ragged_dims_and_alpha_role():
+    img = P.ellipsoid((21, 30, 37), (18, 15, 10), (12, 9, 6), 0.7, 0.2, 0.05, 9)
+    phi0 = P.sdf_spheres(img.shape, [(18, 15, 10, 3)])
+    for role in (lss.ALPHA_DATA, lss.ALPHA_CURVATURE):
+        p = P.ns_params(0.7, 0.12, 0.3 if role == lss.ALPHA_CURVATURE else 0.7)
+        p.alpha_role = role
+        cfg = {"image": img, "phi0": phi0, "params": p}
+        s = make_gpu(cfg)
+        o = make_oracle(cfg)
+        o.set_phi(phi0)
+        for _ in range(25):
+            before = s.read_phi()
+            o.set_state(before, s.active_linear())
+            o.step(1)
+            s.step(1)
+            assert float(np.max(np.abs(s.read_phi() - o.read_phi64()))) <= PHI_TOL
+
+
+def test_ns_param_change_reinitialises_active_set():
+    cfg = P.config1(0.25)
+    s = make_gpu(cfg)
+    s.step(10)
+    phi = s.read_phi()
+    s.set_parameters(target=0.65)
+    s.step(1)
+    o = make_oracle(cfg)
+    o._L.ons_set_params(o._h, 0.65, 0.12, 0.9, 0.5, -4.0, 4.0, 0.01, 0.0, 26)
+    o.set_phi(phi)  # re-init from the current phi, as the engine does
+    o.step(1)
+    assert np.array_equal(s.active_linear(), o.active())
+
+
+def test_ns_seeds_and_readbacks():
+    cfg = P.config1(0.25)
+    s = lss.Segmenter(lss.MODE_NS, brick=(8, 8, 8), threads_per_brick=256)
+    s.load_volume(cfg["image"])
+    p = cfg["params"]
+    s.set_parameters(p.target, p.window, p.curvature, p.time_step)
+    s.set_seed_spheres(cfg["spheres"])
+    assert np.allclose(s.read_phi(), cfg["phi0"], atol=1e-6)
+    n0 = s.get_active_element_count()
+    assert n0 == len(s.active_xyz()) > 0
+    av = s.read_active_volume()
+    assert int((av == 127).sum()) == n0
+    s.step(20)
+    m = s.get_saveable_segmentation()
+    assert np.array_equal(m.astype(bool), s.read_phi() <= 0)
+    s.freeze_current_segmentation()
+    s.clear_current_segmentation()
+    assert s.get_active_element_count() == 0
+    assert np.array_equal(s.get_saveable_segmentation(), m)  # the frozen part stays
+    s.clear_all_segmentations()
+    assert s.get_saveable_segmentation().sum() == 0
+
+
+def test_ns_estimate_params():
+    cfg = P.config1(0.25)
+    s = make_gpu(cfg)
+    s.step(60)
+    t, w = s.calculate_segmentation_parameters()
+    img, m = cfg["image"], s.read_phi() <= 0
+    assert abs(t - img[m].mean()) < 1e-4
+    assert abs(w - img[m].std(ddof=1)) < 1e-4
+
+
+def test_ns_host_fault_injection(monkeypatch):
+    cfg = P.config1(0.25)
+    s = make_gpu(cfg)
+    monkeypatch.setenv("LSS_FAULT", "timeout")
+    with pytest.raises(lss.LssError) as e:
+        s.step(2)
+    assert e.value.status == 5
+    monkeypatch.setenv("LSS_FAULT", "alloc")
+    t = lss.Segmenter(lss.MODE_NS)
+    with pytest.raises(lss.LssError) as e:
+        t.load_volume(cfg["image"])
+    assert e.value.status == 8
+    monkeypatch.delenv("LSS_FAULT")
+    s.step(2)  # the engine stays usable after a reported failure
+    t.load_volume(cfg["image"])
+
+
+def test_ns_hbm_budget_refuses():
+    cfg = P.config1(0.25)
+    s = lss.Segmenter(lss.MODE_NS, hbm_budget_bytes=1 << 20)
+    with pytest.raises(lss.LssError) as e:
+        s.load_volume(cfg["image"])
+    assert e.value.status == 9
+
+
+def test_batch_matches_plain_runs():
+    c3 = P.config3(count=5, scale=0.25)
+    b = lss.Batch(brick=(8, 8, 8), threads_per_brick=256)
+    for v in c3["volumes"]:
+        b.add_volume(v["image"], v["params"], v["spheres"])
+    b.run(1e-3, 5, 300)
+    for i, v in enumerate(c3["volumes"]):
+        s = lss.Segmenter(lss.MODE_NS, brick=(8, 8, 8), threads_per_brick=256)
+        s.load_volume(v["image"])
+        p = v["params"]
+        s.set_parameters(p.target, p.window, p.curvature, p.time_step)
+        s.set_seed_spheres(v["spheres"])
+        it = s.step_until_converged(1e-3, 5, 300)
+        st = b.stats(i)
+        assert st["iterations"] == it, i
+        assert np.array_equal(b.read_phi(i), s.read_phi()), i
+        assert np.array_equal(b.read_mask(i), s.get_saveable_segmentation()), i
