@@ -31,6 +31,7 @@ UNITS = [
     ("ns_engine.cu", []),
     ("engine_host.cu", []),
     ("lss_api.cpp", ["-x", "cu"]),
+    ("compact_api.cu", []),
     ("phantom.cpp", []),
 ]
 

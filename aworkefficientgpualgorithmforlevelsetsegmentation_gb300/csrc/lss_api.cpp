@@ -180,7 +180,9 @@ lss_status lss_unload_volume(lss_engine* e) {
 lss_status lss_set_params(lss_engine* e, const lss_params* p) {
     CHECK_ENGINE(e);
     if (!p) return LSS_ERR_INVALID_ARGUMENT;
-    if (!(p->phi_min < p->phi_max) || p->temporal_threshold < 0 ||
+    // A negative threshold marks every updated voxel as changed (and every
+    // voxel as initially active): the dense all-voxel update.
+    if (!(p->phi_min < p->phi_max) || !(p->window > 0) ||
         (p->neighbourhood != 6 && p->neighbourhood != 26))
         return LSS_ERR_INVALID_ARGUMENT;
     return guard(e, [&] { e->impl->set_params(*p); });

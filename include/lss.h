@@ -279,6 +279,18 @@ lss_status lss_adjoint_run(lss_engine* e, int32_t K, int32_t checkpoint_every,
                            const uint8_t* target_mask, float sigmoid_scale,
                            const float* bias, float* d_bias, lss_grads* out);
 
+/* ---- kernel level --------------------------------------------------------- */
+
+/* ≈ CudppCompact (code/gpuseg/code/src/cuda/Cuda.cpp:699-758) over CUDPP's
+ * cudppCompact: stable compaction of d_src[i] for every i < n with
+ * d_valid[i] != 0 into d_dst (device pointers, caller-owned).  The count is
+ * written to *d_count in device memory.  Its scratch (one status word per
+ * 4096 elements) is taken from the stream-ordered allocator and returned
+ * before the call ends; the call synchronises `stream` (a cudaStream_t, NULL =
+ * the legacy default stream) before returning. */
+lss_status lss_compact_u32(const uint32_t* d_src, const uint32_t* d_valid, uint32_t* d_dst,
+                           uint64_t n, uint64_t* d_count, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -197,7 +197,7 @@ def test_ns_host_fault_injection(monkeypatch):
 
 def test_ns_hbm_budget_refuses():
     cfg = P.config1(0.25)
-    s = lss.Segmenter(lss.MODE_NS, hbm_budget_bytes=1 << 20)
+    s = lss.Segmenter(lss.MODE_NS, hbm_budget_bytes=64 << 10)  # 32^3 needs > 384 KiB
     with pytest.raises(lss.LssError) as e:
         s.load_volume(cfg["image"])
     assert e.value.status == 9
