@@ -70,6 +70,7 @@ SIGNATURES = {
     "lss_set_seed_spheres": (i32, [P, P, i32]),
     "lss_set_phi": (i32, [P, P]),
     "lss_step": (i32, [P, i32, C.POINTER(i32)]),
+    "lss_step_dense": (i32, [P, i32, C.POINTER(C.c_double)]),
     "lss_step_until_converged": (i32, [P, C.POINTER(lss_conv), C.POINTER(i32)]),
     "lss_is_finished": (i32, [P, C.POINTER(i32)]),
     "lss_active_count": (i32, [P, C.POINTER(u64)]),

@@ -67,6 +67,10 @@ class EngineBase {
     virtual void clear_all() = 0;
     virtual void estimate_params(float* t, float* w) = 0;
     virtual void stats(lss_stats* s) = 0;
+    virtual double step_dense(int n) {
+        (void)n;
+        throw Error(LSS_ERR_UNSUPPORTED, "the dense update is available in LSS_MODE_NS only");
+    }
     virtual void adjoint(int K, int every, const uint8_t* target, float scale, const float* bias,
                          float* dbias, lss_grads* out) {
         (void)K; (void)every; (void)target; (void)scale; (void)bias; (void)dbias; (void)out;

@@ -208,6 +208,14 @@ class NsEngine : public EngineBase {
         return it;
     }
 
+    double step_dense(int n) override {
+        require();
+        LSS_REQUIRE(core_->initialized(), LSS_ERR_STATE, "no seed or phi set");
+        last_ms_ = core_->dense_run(n);
+        after_init();
+        return last_ms_;
+    }
+
     bool finished() override { return core_ && active_count() == 0; }
 
     uint64_t active_count() override {

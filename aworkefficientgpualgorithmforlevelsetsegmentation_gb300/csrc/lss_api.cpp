@@ -223,6 +223,15 @@ lss_status lss_step(lss_engine* e, int32_t n, int32_t* done) {
     });
 }
 
+lss_status lss_step_dense(lss_engine* e, int32_t n, double* ms) {
+    CHECK_ENGINE(e);
+    if (n < 0) return LSS_ERR_INVALID_ARGUMENT;
+    return guard(e, [&] {
+        double t = e->impl->step_dense(n);
+        if (ms) *ms = t;
+    });
+}
+
 lss_status lss_step_until_converged(lss_engine* e, const lss_conv* c, int32_t* done) {
     CHECK_ENGINE(e);
     if (!c || c->max_iterations <= 0 || c->patience <= 0) return LSS_ERR_INVALID_ARGUMENT;

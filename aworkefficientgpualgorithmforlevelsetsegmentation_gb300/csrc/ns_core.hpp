@@ -35,6 +35,7 @@ class NsCore {
     void set_phi(int v, const float* phi);
     void fill_phi(int v, float value);
     int run(int max_iters, const lss_conv* conv, float* ms);
+    float dense_run(int iters);
     void read_phi(int v, float* out);
     uint64_t read_active(int v, uint64_t* out, uint64_t cap);
     void estimate(int v, float* t, float* w);

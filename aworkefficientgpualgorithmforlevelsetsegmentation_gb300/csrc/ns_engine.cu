@@ -133,6 +133,30 @@ __global__ void __launch_bounds__(NT) k_ns_emit(NsArgs a, uint32_t p, uint64_t* 
     }
 }
 
+// Dense all-voxel update with the same arithmetic as the sparse engine: the
+// unconditional update the paper compares against (main.tex:523).  Block =
+// 32 x 8 voxels of one plane, marching 8 planes in z; neighbours are read
+// through the read-only cache.
+__global__ void __launch_bounds__(256) k_ns_dense(const NsVol* vols, int v, uint32_t p) {
+    const NsVol& V = vols[v];
+    const int x = blockIdx.x * 32 + threadIdx.x % 32;
+    const int y = blockIdx.y * 8 + threadIdx.x / 32;
+    if (x >= V.nx || y >= V.ny) return;
+    const float* __restrict__ src = V.phi[p];
+    float* __restrict__ dst = V.phi[p ^ 1u];
+    const int z0 = blockIdx.z * 8;
+    for (int z = z0; z < min(z0 + 8, V.nz); ++z) {
+        auto P = [&](int dx, int dy, int dz) {
+            const int xx = min(max(x + dx, 0), V.nx - 1), yy = min(max(y + dy, 0), V.ny - 1),
+                      zz = min(max(z + dz, 0), V.nz - 1);
+            return __ldg(&src[((size_t)zz * V.py + yy) * V.px + xx]);
+        };
+        const size_t k = ((size_t)z * V.py + y) * V.px + x;
+        const float bb = V.bias ? V.bias[k] : 0.0f;
+        dst[k] = ns_update_f32(P, __ldg(&V.img[k]), bb, V);
+    }
+}
+
 // Sum, sum of squares and count of the intensities where phi <= 0.
 __global__ void k_ns_collect(const float* img, const float* phi, int nx, int ny, int nz, int px,
                              int py, double mean, double* acc) {
@@ -167,6 +191,8 @@ struct KernelSet {
     void* build_list;
     void* emit;
     int words;
+    int block;          // threads per block of every kernel of the set
+    size_t warp_smem;   // per-warp shared memory of the warp-per-brick kernel (0: block per brick)
 };
 
 template <int BX, int BY, int BZ, int NT>
@@ -174,19 +200,36 @@ KernelSet kernels_for() {
     using S = Brick<BX, BY, BZ>;
     return KernelSet{(void*)&k_ns_persistent<BX, BY, BZ, NT>, (void*)&k_ns_init_active<BX, BY, BZ, NT>,
                      (void*)&k_ns_build_list<S::WORDS, NT>, (void*)&k_ns_emit<BX, BY, BZ, NT>,
-                     S::WORDS};
+                     S::WORDS, NT, 0};
+}
+
+// Warp per brick, 4 warps per block.
+template <int BX, int BY, int BZ>
+KernelSet kernels_for_warp() {
+    using S = Brick<BX, BY, BZ>;
+    constexpr int NT = 128;
+    return KernelSet{(void*)&k_ns_persistent_warp<BX, BY, BZ, NT>, (void*)&k_ns_init_active<BX, BY, BZ, NT>,
+                     (void*)&k_ns_build_list<S::WORDS, NT>, (void*)&k_ns_emit<BX, BY, BZ, NT>,
+                     S::WORDS, NT, sizeof(WarpSmem<S>)};
 }
 
 }  // namespace
 
 // The instantiated (brick shape, threads per brick) configurations.
+// threads = 32 selects the warp-per-brick kernel (4 warps per block).
 const std::vector<BrickConfig>& brick_configs() {
     static const std::vector<BrickConfig> v = {
-        {8, 8, 8, 256}, {8, 8, 8, 128}, {8, 8, 8, 512}, {8, 8, 4, 128}, {8, 8, 4, 256}, {4, 4, 4, 64}};
+        {8, 8, 8, 32},  {8, 8, 4, 32},  {4, 4, 4, 32},  {8, 8, 8, 256}, {8, 8, 8, 128},
+        {8, 8, 8, 512}, {8, 8, 4, 128}, {8, 8, 4, 256}, {4, 4, 4, 64}};
     return v;
 }
 
 static KernelSet kernels(const BrickConfig& c) {
+    if (c.threads == 32) {
+        if (c.bx == 8 && c.by == 8 && c.bz == 8) return kernels_for_warp<8, 8, 8>();
+        if (c.bx == 8 && c.by == 8 && c.bz == 4) return kernels_for_warp<8, 8, 4>();
+        if (c.bx == 4 && c.by == 4 && c.bz == 4) return kernels_for_warp<4, 4, 4>();
+    }
     if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 256) return kernels_for<8, 8, 8, 256>();
     if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 128) return kernels_for<8, 8, 8, 128>();
     if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 512) return kernels_for<8, 8, 8, 512>();
@@ -309,7 +352,7 @@ void NsCore::configure(const BrickConfig& c) {
     const size_t dyn = dyn_smem();
     int per_sm = 0;
     LSS_CUDA(cudaFuncSetAttribute(ks.persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
-    LSS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ks.persistent, c.threads, dyn));
+    LSS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ks.persistent, ks.block, dyn));
     LSS_REQUIRE(per_sm > 0, LSS_ERR_CUDA, "persistent kernel does not fit on an SM");
     grid_ = owner_->num_sms * per_sm;
     configured_ = true;
@@ -317,8 +360,10 @@ void NsCore::configure(const BrickConfig& c) {
 }
 
 size_t NsCore::dyn_smem() const {
-    const size_t V = vols_.size();
-    return 4 * 4 * ((3 * V + 3) / 4) + 8 * V;
+    const int V = (int)vols_.size();
+    const KernelSet ks = kernels(cfg_);
+    if (!ks.warp_smem) return stop_state_bytes(V);
+    return (stop_state_bytes(V) + 127) / 128 * 128 + 128 + (size_t)(ks.block / 32) * ks.warp_smem;
 }
 
 void NsCore::upload_descriptors() {
@@ -400,8 +445,8 @@ void NsCore::init_active() {
     uint32_t p = parity_;
     void* params[] = {&a, &p};
     const int grid = (int)std::min<uint64_t>(NB_, (uint64_t)owner_->num_sms * 16);
-    LSS_CUDA(cudaLaunchKernel(ks.init_active, dim3(grid), dim3(cfg_.threads), params, 0, st));
-    LSS_CUDA(cudaLaunchKernel(ks.build_list, dim3(std::max(1, owner_->num_sms)), dim3(cfg_.threads), params,
+    LSS_CUDA(cudaLaunchKernel(ks.init_active, dim3(grid), dim3(ks.block), params, 0, st));
+    LSS_CUDA(cudaLaunchKernel(ks.build_list, dim3(std::max(1, owner_->num_sms)), dim3(ks.block), params,
                               0, st));
     std::vector<unsigned long long> n0(vols_.size());
     LSS_CUDA(cudaMemcpyAsync(n0.data(), d_cnt_[parity_], 8 * vols_.size(), cudaMemcpyDeviceToHost, st));
@@ -458,7 +503,7 @@ int NsCore::run(int max_iters, const lss_conv* conv, float* ms) {
     LSS_CUDA(cudaEventCreate(&e1));
     LSS_CUDA(cudaEventRecord(e0, st));
     if (fault_injected("launch")) throw Error(LSS_ERR_INJECTED, "injected launch failure");
-    LSS_CUDA(cudaLaunchCooperativeKernel(ks.persistent, dim3(grid_), dim3(cfg_.threads), params, dyn_smem(),
+    LSS_CUDA(cudaLaunchCooperativeKernel(ks.persistent, dim3(grid_), dim3(ks.block), params, dyn_smem(),
                                          st));
     LSS_CUDA(cudaEventRecord(e1, st));
     LSS_CUDA(cudaEventSynchronize(e1));
@@ -517,7 +562,7 @@ uint64_t NsCore::read_active(int v, uint64_t* out, uint64_t cap) {
     const uint64_t n = s.n_cur;
     if (!out) return n;
     uint64_t* dout = (uint64_t*)arena_.alloc(std::max<uint64_t>(n, 1) * 8);
-    LSS_CUDA(cudaMemsetAsync(d_status_, 0, ((uint64_t)c.nA / cfg_.threads + 2) * 8, owner_->stream));
+    LSS_CUDA(cudaMemsetAsync(d_status_, 0, ((uint64_t)c.nA / kernels(cfg_).block + 2) * 8, owner_->stream));
     LSS_CUDA(cudaMemsetAsync(d_misc_, 0, 4, owner_->stream));
     KernelSet ks = kernels(cfg_);
     NsArgs a = args(parity_, 0, nullptr);
@@ -525,7 +570,7 @@ uint64_t NsCore::read_active(int v, uint64_t* out, uint64_t cap) {
     uint64_t* o = dout;
     uint32_t* tc = d_misc_;
     void* params[] = {&a, &p, &o, &tc};
-    LSS_CUDA(cudaLaunchKernel(ks.emit, dim3(owner_->num_sms * 2), dim3(cfg_.threads), params, 0,
+    LSS_CUDA(cudaLaunchKernel(ks.emit, dim3(owner_->num_sms * 2), dim3(ks.block), params, 0,
                               owner_->stream));
     const uint64_t m = std::min(n, cap);
     if (m) LSS_CUDA(cudaMemcpyAsync(out, dout, m * 8, cudaMemcpyDeviceToHost, owner_->stream));
@@ -552,6 +597,32 @@ void NsCore::estimate(int v, float* t, float* w) {
     arena_.free_last(acc);
     *t = (float)mean;
     *w = (float)std::sqrt(h[1] / (h[2] - 1));
+}
+
+float NsCore::dense_run(int iters) {
+    LSS_REQUIRE(initialized_, LSS_ERR_STATE, "no seed / phi set");
+    cudaStream_t st = owner_->stream;
+    cudaEvent_t e0, e1;
+    LSS_CUDA(cudaEventCreate(&e0));
+    LSS_CUDA(cudaEventCreate(&e1));
+    LSS_CUDA(cudaEventRecord(e0, st));
+    for (int it = 0; it < iters; ++it) {
+        for (int v = 0; v < (int)vols_.size(); ++v) {
+            const VolHost& V = vols_[v];
+            dim3 grid((V.nx + 31) / 32, (V.ny + 7) / 8, (V.nz + 7) / 8);
+            k_ns_dense<<<grid, 256, 0, st>>>(d_vols_, v, parity_);
+        }
+        parity_ ^= 1u;
+    }
+    LSS_CUDA(cudaEventRecord(e1, st));
+    LSS_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    LSS_CUDA(cudaGetLastError());
+    init_active();  // the dense pass leaves no active set: rebuild it from phi
+    return ms;
 }
 
 void NsCore::check_errors() {

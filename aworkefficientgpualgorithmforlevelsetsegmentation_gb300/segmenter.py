@@ -140,6 +140,12 @@ class Segmenter:
 
     step = request_update_segmentation
 
+    def step_dense(self, n: int) -> float:
+        """n dense all-voxel iterations (same arithmetic); returns device ms."""
+        ms = C.c_double()
+        self._chk(self._lib.lss_step_dense(self._h, n, C.byref(ms)))
+        return ms.value
+
     def step_until_converged(self, rel: float = 1e-3, patience: int = 5, max_iterations: int = 2000,
                              abs_threshold: int = 0) -> int:
         c = L.lss_conv(rel, patience, max_iterations, abs_threshold)

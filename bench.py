@@ -237,18 +237,16 @@ def run_ours(args, ws, rank, local):
     assert np.array_equal(m, mask)
     e2e_value = sum_over_ranks(ws, float(e2e_updates)) / (max_over_ranks(ws, e2e_ms) / 1e3)
 
-    # Dense all-voxel GPU update with the same math and the same iteration count.
-    dense = lss.Segmenter(lss.MODE_NS, device=local, brick=(8, 8, 8), threads_per_brick=256)
-    dense.load_volume(cfg["image"])
-    dense.set_parameters(p.target, p.window, p.curvature, p.time_step, alpha_role=p.alpha_role,
-                         temporal_threshold=-1.0, spatial_threshold=-1.0)
-    dense.set_seed_spheres(cfg["spheres"])
-    dense.step(3)
-    dense.step(args.dense_iters)
-    dense_ms_per_it = dense.stats()["last_step_ms"] / args.dense_iters
+    # Dense all-voxel GPU update (same arithmetic, every voxel, no active set)
+    # timed over the same number of iterations the sparse run needed.
+    seg.clear_current_segmentation()
+    seg.set_seed_spheres(cfg["spheres"])
+    seg.step_dense(3)
+    seg.clear_current_segmentation()
+    seg.set_seed_spheres(cfg["spheres"])
+    dense_ms_per_it = seg.step_dense(args.dense_iters) / args.dense_iters
     sparse_ms = ev_ms / args.steps
     dense_ms = dense_ms_per_it * statistics.mean(iters)
-    del dense
 
     peak, peak_kind = measured_peak()
     achieved = BYTES_PER_UPDATE * updates / (kern_ms / 1e3) / 1e9

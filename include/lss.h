@@ -193,6 +193,13 @@ lss_status lss_set_phi(lss_engine* e, const float* phi);
  * finished (IsSegmentationFinished) and no parameter changed. */
 lss_status lss_step(lss_engine* e, int32_t n_iters, int32_t* iters_done);
 
+/* NS: n iterations of the dense all-voxel update with the same arithmetic
+ * (every voxel, no active set): the unconditional update the paper compares
+ * the sparse algorithm against (documentation/papers/hpg2010/latex/
+ * main.tex:523).  *ms (nullable) receives the device time.  The active set is
+ * rebuilt from the resulting phi. */
+lss_status lss_step_dense(lss_engine* e, int32_t n_iters, double* ms);
+
 /* Steps until the stopping rule holds; one device launch in NS mode. */
 lss_status lss_step_until_converged(lss_engine* e, const lss_conv* c, int32_t* iters_done);
 

@@ -14,8 +14,11 @@ pytestmark = pytest.mark.gpu
 def compact_gpu(src, valid):
     import torch
     L = lss.load()
-    s = torch.from_numpy(src.astype(np.uint32).view(np.int32)).cuda()
-    v = torch.from_numpy(valid.astype(np.uint32).view(np.int32)).cuda()
+    pad = max(1, src.size)  # non-null device buffers even for n = 0
+    s = torch.zeros(pad, dtype=torch.int32, device="cuda")
+    v = torch.zeros(pad, dtype=torch.int32, device="cuda")
+    s[: src.size] = torch.from_numpy(src.astype(np.uint32).view(np.int32)).cuda()
+    v[: src.size] = torch.from_numpy(valid.astype(np.uint32).view(np.int32)).cuda()
     d = torch.full((max(1, src.size),), -1, dtype=torch.int32, device="cuda")
     cnt = torch.zeros(1, dtype=torch.int64, device="cuda")
     rc = L.lss_compact_u32(C.c_void_p(s.data_ptr()), C.c_void_p(v.data_ptr()),

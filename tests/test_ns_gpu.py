@@ -37,11 +37,14 @@ def make_oracle(cfg, brick=(8, 8, 8), nbh=26):
     return o
 
 
-@pytest.mark.parametrize("which,scale", [("config1", 0.5), ("config2", 0.25)])
-def test_ns_each_iteration_vs_fp64(which, scale):
+@pytest.mark.parametrize("which,scale,brick,threads", [("config1", 0.5, (8, 8, 8), 256),
+                                                      ("config2", 0.25, (8, 8, 8), 256),
+                                                      ("config2", 0.25, (8, 8, 8), 32),
+                                                      ("config1", 0.5, (4, 4, 4), 32)])
+def test_ns_each_iteration_vs_fp64(which, scale, brick, threads):
     cfg = getattr(P, which)(scale)
-    s = make_gpu(cfg)
-    o = make_oracle(cfg)
+    s = make_gpu(cfg, brick=brick, threads=threads)
+    o = make_oracle(cfg, brick=brick)
     o.set_phi(cfg["phi0"])
     assert np.array_equal(s.active_linear(), o.active()), "initial active set"
     worst = 0.0
@@ -87,7 +90,8 @@ def test_ns_brick_configs_are_voxel_exact():
     cfg = P.config2(0.25)
     ref_phi = ref_act = None
     for (bx, by, bz, t) in [(8, 8, 8, 256), (8, 8, 8, 128), (8, 8, 8, 512), (8, 8, 4, 128),
-                            (8, 8, 4, 256), (4, 4, 4, 64)]:
+                            (8, 8, 4, 256), (4, 4, 4, 64), (8, 8, 8, 32), (8, 8, 4, 32),
+                            (4, 4, 4, 32)]:
         s = make_gpu(cfg, brick=(bx, by, bz), threads=t)
         s.step(30)
         phi = s.read_phi()
