@@ -97,6 +97,7 @@ SIGNATURES = {
     "lss_batch_last_error_string": (C.c_char_p, [P]),
     "lss_adjoint_run": (i32, [P, i32, i32, P, f32, P, P, C.POINTER(lss_grads)]),
     "lss_compact_u32": (i32, [P, P, P, u64, P, P]),
+    "lss_compact_u32_noalloc": (i32, [P, P, P, u64, P, P]),
     "lss_phantom_ellipsoid": (i32, [i32, i32, i32, P, P, f32, f32, f32, u64, P]),
     "lss_phantom_shells": (i32, [i32, i32, i32, i32, P, P, f32, f32, i32, u64, f32, f32, u64, P]),
     "lss_phantom_sdf_spheres": (i32, [i32, i32, i32, P, i32, f32, f32, P]),

@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <mutex>
 #include <string>
 
 #include "common.cuh"
@@ -102,4 +103,82 @@ extern "C" lss_status lss_compact_u32(const uint32_t* d_src, const uint32_t* d_v
     if (s == LSS_OK && cudaStreamSynchronize(st) != cudaSuccess) s = LSS_ERR_CUDA;
     if (s == LSS_OK && err) s = LSS_ERR_TIMEOUT;
     return s;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant.
+//
+// Some callers cannot allocate device memory at the moment they need a
+// compaction: code running inside a CUDA-graph capture that must not add
+// allocation nodes, real-time pipelines whose memory is reserved once at
+// start-up, or hosts whose allocator is owned by another framework.  For
+// them lss_compact_u32_noalloc keeps its scratch in this file-scope device
+// array instead of asking the stream-ordered allocator.  Every GPU that loads
+// the library holds the array (a little over 128 KiB) until the process exits.
+namespace lss {
+
+// Largest n the allocation-free call accepts.
+constexpr uint64_t kNoAllocMaxElements = 1ull << 26;
+constexpr uint64_t kNoAllocStatusWords = kNoAllocMaxElements / kCompactTile + 1;
+
+// Status words, then the tile counter and the error word (one u64).
+static __device__ __align__(256) uint64_t g_noalloc_scratch[kNoAllocStatusWords + 1];
+
+// Device address of the array, looked up once per device with that device
+// current (in host code the symbol is only a host-side stand-in).
+static std::mutex g_noalloc_mu;
+static uint64_t* g_noalloc_addr[64] = {nullptr};
+
+static lss_status noalloc_scratch(uint64_t** out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return LSS_ERR_NO_DEVICE;
+    }
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+            cudaGetLastError();
+            return LSS_ERR_CUDA;
+        }
+        g_noalloc_addr[dev] = (uint64_t*)p;
+    }
+    *out = g_noalloc_addr[dev];
+    return LSS_OK;
+}
+
+}  // namespace lss
+
+extern "C" lss_status lss_compact_u32_noalloc(const uint32_t* d_src, const uint32_t* d_valid,
+                                              uint32_t* d_dst, uint64_t n, uint64_t* d_count,
+                                              void* stream) {
+    if (!d_src || !d_valid || !d_dst || !d_count) return LSS_ERR_INVALID_ARGUMENT;
+    if (n > lss::kNoAllocMaxElements) return LSS_ERR_CAPACITY;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n == 0)
+        return cudaMemsetAsync(d_count, 0, sizeof(uint64_t), st) == cudaSuccess ? LSS_OK : LSS_ERR_CUDA;
+    uint64_t* base = nullptr;
+    lss_status s = lss::noalloc_scratch(&base);
+    if (s != LSS_OK) return s;
+    const uint64_t words = lss::compact_status_words(n);  // <= kNoAllocStatusWords
+    lss::CompactScratch sc;
+    sc.status = base;
+    sc.tile_counter = (uint32_t*)(base + lss::kNoAllocStatusWords);
+    sc.err = sc.tile_counter + 1;
+    // The array keeps the previous call's contents: clear the words this call
+    // reads before writing them, plus the tile counter and the error word.
+    if (cudaMemsetAsync(base, 0, words * 8, st) != cudaSuccess ||
+        cudaMemsetAsync(sc.tile_counter, 0, 8, st) != cudaSuccess ||
+        lss::launch_compact_u32(d_src, d_valid, d_dst, n, d_count, sc, st) != cudaSuccess) {
+        cudaGetLastError();
+        return LSS_ERR_CUDA;
+    }
+    uint32_t err = 0;
+    if (cudaMemcpyAsync(&err, sc.err, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+        cudaGetLastError();
+        return LSS_ERR_CUDA;
+    }
+    return err ? LSS_ERR_TIMEOUT : LSS_OK;
 }

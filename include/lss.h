@@ -298,6 +298,25 @@ lss_status lss_adjoint_run(lss_engine* e, int32_t K, int32_t checkpoint_every,
 lss_status lss_compact_u32(const uint32_t* d_src, const uint32_t* d_valid, uint32_t* d_dst,
                            uint64_t n, uint64_t* d_count, void* stream);
 
+/* Largest n accepted by lss_compact_u32_noalloc. */
+#define LSS_COMPACT_NOALLOC_MAX_ELEMENTS (1ull << 26)
+
+/* lss_compact_u32 for callers that cannot allocate device memory when they
+ * compact: code inside a CUDA-graph capture that must not add allocations,
+ * pipelines whose device memory is reserved once at start-up, hosts whose
+ * allocator belongs to another framework.  No counterpart in the reference
+ * (which allocates through CUDPP's plan).  Same arguments and result as
+ * lss_compact_u32; allocates nothing: its scratch is a fixed device array of
+ * the library (about 128 KiB, held by every GPU that loads the library until
+ * the process exits).  n above LSS_COMPACT_NOALLOC_MAX_ELEMENTS returns
+ * LSS_ERR_CAPACITY without touching the buffers.  The first call on a device
+ * looks the array up on that device (make it before any stream capture).
+ * All calls share the array: calls that overlap on the GPU (other streams,
+ * other threads) race and must be serialised by the caller.  The call
+ * synchronises `stream` before returning. */
+lss_status lss_compact_u32_noalloc(const uint32_t* d_src, const uint32_t* d_valid, uint32_t* d_dst,
+                                   uint64_t n, uint64_t* d_count, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
