@@ -220,9 +220,7 @@ class NsEngine : public EngineBase {
 
     uint64_t active_count() override {
         if (!core_ || !core_->initialized()) return 0;
-        NsVolState s;
-        core_->state(0, &s);
-        return s.n_cur;
+        return core_->read_active(0, nullptr, 0);  // popc over the current masks
     }
 
     uint64_t read_active(uint32_t* out, uint64_t cap, bool packed) override {
@@ -317,10 +315,12 @@ class NsEngine : public EngineBase {
         NsVolState st;
         core_->state(0, &st);
         s->iterations = st.iterations;
-        s->active_count = st.n_cur;
+        s->active_count = core_->read_active(0, nullptr, 0);
         s->initial_active_count = st.n0;
         s->voxel_updates = st.updates;
         s->brick_updates = st.bricks;
+        s->update_ms = core_->last_update_ms();
+        s->barrier_ms = core_->last_barrier_ms();
     }
 
     NsCore& core() { return *core_; }

@@ -1,5 +1,5 @@
 // NsCore: device state of one or many LSS_MODE_NS volumes sharing one global
-// brick space, one set of brick bitmaps/lists and one persistent launch.
+// brick space, one set of brick masks/membership bits and one persistent launch.
 #pragma once
 
 #include <cuda.h>
@@ -50,6 +50,8 @@ class NsCore {
     const BrickConfig& config() const { return cfg_; }
     uint64_t held() const { return arena_.held() + brick_arena_.held(); }
     uint32_t parity() const { return parity_; }
+    double last_update_ms() const { return last_update_ns_ * 1e-6; }
+    double last_barrier_ms() const { return last_barrier_ns_ * 1e-6; }
     uint64_t bricks() const { return NB_; }
     int grid() const { return grid_; }
 
@@ -69,7 +71,7 @@ class NsCore {
    private:
     size_t dyn_smem() const;
     void upload_descriptors();
-    NsArgs args(uint32_t parity0, int max_iters, const lss_conv* conv) const;
+    NsArgs args(uint32_t k0, int max_iters, const lss_conv* conv) const;
 
     EngineBase* owner_;
     DeviceArena arena_;        // volumes (phi, intensities, bias)
@@ -80,17 +82,17 @@ class NsCore {
     uint64_t NB_ = 0;
     uint32_t NW_ = 0;
     int grid_ = 0;
-    uint32_t parity_ = 0;
+    uint32_t parity_ = 0;   // phi buffer holding the current field (= k_total_ & 1)
+    uint32_t k_total_ = 0;  // global iteration index (bits slot k_total_ % 4, count slot % 3)
+    unsigned long long last_update_ns_ = 0, last_barrier_ns_ = 0;
     bool configured_ = false, initialized_ = false;
     NsVol* d_vols_ = nullptr;
     NsVolState* d_vstate_ = nullptr;
     CUtensorMap* d_tmaps_ = nullptr;
     unsigned long long* d_masks_[2] = {nullptr, nullptr};
-    uint32_t* d_bits_[2] = {nullptr, nullptr};
-    unsigned long long* d_cnt_[2] = {nullptr, nullptr};
+    uint32_t* d_bits_[4] = {nullptr, nullptr, nullptr, nullptr};
+    unsigned long long* d_cnt_[3] = {nullptr, nullptr, nullptr};
     uint16_t* d_brick_vol_ = nullptr;
-    uint32_t* d_A_ = nullptr;
-    uint32_t* d_F_ = nullptr;
     uint64_t* d_status_ = nullptr;
     NsCtl* d_ctl_ = nullptr;
     uint32_t* d_misc_ = nullptr;

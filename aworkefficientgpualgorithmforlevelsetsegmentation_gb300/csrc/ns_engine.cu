@@ -70,66 +70,21 @@ __global__ void k_ns_fill(float* p, uint64_t n, float v) {
         p[i] = v;
 }
 
-// phi = min(phi, clamp(|x - c| - r)) over the logical volume.
-__global__ void k_ns_sphere_union(float* phi, int nx, int ny, int nz, int px, int py, float cx,
-                                  float cy, float cz, float r, float lo, float hi) {
-    const uint64_t n = (uint64_t)nx * ny * nz;
+// phi = min(phi, clamp(|x - c| - r)) over the box [b0, b1) of the logical
+// volume (outside it the clamped distance is hi >= phi, so nothing changes).
+__global__ void k_ns_sphere_union(float* phi, int nx, int ny, int nz, int px, int py, int3 b0, int3 b1,
+                                  float cx, float cy, float cz, float r, float lo, float hi) {
+    const int bx = b1.x - b0.x, by = b1.y - b0.y, bz = b1.z - b0.z;
+    const uint64_t n = (uint64_t)bx * by * bz;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x) {
-        const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((uint64_t)nx * ny));
+        const int x = b0.x + (int)(i % bx), y = b0.y + (int)((i / bx) % by),
+                  z = b0.z + (int)(i / ((uint64_t)bx * by));
         const double dx = x - (double)cx, dy = y - (double)cy, dz = z - (double)cz;
         double d = sqrt(dx * dx + dy * dy + dz * dz) - (double)r;
         d = d < lo ? lo : (d > hi ? hi : d);
         float* q = &phi[((uint64_t)z * py + y) * px + x];
         *q = fminf(*q, (float)d);
-    }
-}
-
-// Voxel coordinates of the active list, compacted in brick-major order with a
-// single-pass decoupled lookback over the per-brick counts (tiles of NT bricks).
-template <int BX, int BY, int BZ, int NT>
-__global__ void __launch_bounds__(NT) k_ns_emit(NsArgs a, uint32_t p, uint64_t* out,
-                                               uint32_t* tile_counter) {
-    using S = Brick<BX, BY, BZ>;
-    __shared__ uint32_t s_tile;
-    const uint32_t nA = a.ctl->nA;
-    const uint32_t ntiles = (nA + NT - 1) / NT;
-    for (;;) {
-        if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1u);
-        __syncthreads();
-        const uint32_t tile = s_tile;
-        __syncthreads();
-        if (tile >= ntiles) break;
-        const uint32_t i = tile * NT + threadIdx.x;
-        uint32_t b = 0, cnt = 0;
-        unsigned long long w[S::WORDS];
-        if (i < nA) {
-            b = a.A_list[i];
-            for (int q = 0; q < S::WORDS; ++q) {
-                w[q] = a.masks[p][(size_t)b * S::WORDS + q];
-                cnt += __popcll(w[q]);
-            }
-        }
-        uint64_t total;
-        const uint64_t excl = block_exclusive_sum64(cnt, &total);
-        const uint64_t prefix = tile_exclusive_prefix(a.status, tile, total, &a.ctl->err);
-        if (i < nA) {
-            const NsVol& V = a.vols[a.brick_vol[b]];
-            const uint32_t lb = b - V.brick_base;
-            const int kx = lb % V.nbx, ky = (lb / V.nbx) % V.nby, kz = lb / (V.nbx * V.nby);
-            uint64_t o = prefix + excl;
-            for (int q = 0; q < S::WORDS; ++q) {
-                unsigned long long m = w[q];
-                while (m) {
-                    const int bit = __ffsll(m) - 1;
-                    m &= m - 1;
-                    const int j = q * 64 + bit;
-                    const uint64_t x = kx * S::X + j % S::X, y = ky * S::Y + (j / S::X) % S::Y,
-                                   z = kz * S::Z + j / (S::X * S::Y);
-                    out[o++] = (z * V.ny + y) * V.nx + x;
-                }
-            }
-        }
     }
 }
 
@@ -188,48 +143,28 @@ __global__ void k_ns_collect(const float* img, const float* phi, int nx, int ny,
 struct KernelSet {
     void* persistent;
     void* init_active;
-    void* build_list;
     void* emit;
     int words;
-    int block;          // threads per block of every kernel of the set
-    size_t warp_smem;   // per-warp shared memory of the warp-per-brick kernel (0: block per brick)
+    int block;  // threads per block of every kernel of the set
 };
 
 template <int BX, int BY, int BZ, int NT>
 KernelSet kernels_for() {
     using S = Brick<BX, BY, BZ>;
     return KernelSet{(void*)&k_ns_persistent<BX, BY, BZ, NT>, (void*)&k_ns_init_active<BX, BY, BZ, NT>,
-                     (void*)&k_ns_build_list<S::WORDS, NT>, (void*)&k_ns_emit<BX, BY, BZ, NT>,
-                     S::WORDS, NT, 0};
-}
-
-// Warp per brick, 4 warps per block.
-template <int BX, int BY, int BZ>
-KernelSet kernels_for_warp() {
-    using S = Brick<BX, BY, BZ>;
-    constexpr int NT = 128;
-    return KernelSet{(void*)&k_ns_persistent_warp<BX, BY, BZ, NT>, (void*)&k_ns_init_active<BX, BY, BZ, NT>,
-                     (void*)&k_ns_build_list<S::WORDS, NT>, (void*)&k_ns_emit<BX, BY, BZ, NT>,
-                     S::WORDS, NT, sizeof(WarpSmem<S>)};
+                     (void*)&k_ns_emit<BX, BY, BZ, NT>, S::WORDS, NT};
 }
 
 }  // namespace
 
 // The instantiated (brick shape, threads per brick) configurations.
-// threads = 32 selects the warp-per-brick kernel (4 warps per block).
 const std::vector<BrickConfig>& brick_configs() {
     static const std::vector<BrickConfig> v = {
-        {8, 8, 8, 32},  {8, 8, 4, 32},  {4, 4, 4, 32},  {8, 8, 8, 256}, {8, 8, 8, 128},
-        {8, 8, 8, 512}, {8, 8, 4, 128}, {8, 8, 4, 256}, {4, 4, 4, 64}};
+        {8, 8, 8, 256}, {8, 8, 8, 128}, {8, 8, 8, 512}, {8, 8, 4, 128}, {8, 8, 4, 256}, {4, 4, 4, 64}};
     return v;
 }
 
 static KernelSet kernels(const BrickConfig& c) {
-    if (c.threads == 32) {
-        if (c.bx == 8 && c.by == 8 && c.bz == 8) return kernels_for_warp<8, 8, 8>();
-        if (c.bx == 8 && c.by == 8 && c.bz == 4) return kernels_for_warp<8, 8, 4>();
-        if (c.bx == 4 && c.by == 4 && c.bz == 4) return kernels_for_warp<4, 4, 4>();
-    }
     if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 256) return kernels_for<8, 8, 8, 256>();
     if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 128) return kernels_for<8, 8, 8, 128>();
     if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 512) return kernels_for<8, 8, 8, 512>();
@@ -312,14 +247,10 @@ void NsCore::configure(const BrickConfig& c) {
     d_vols_ = (NsVol*)A(sizeof(NsVol) * vols_.size());
     d_vstate_ = (NsVolState*)A(sizeof(NsVolState) * vols_.size());
     d_tmaps_ = (CUtensorMap*)A(sizeof(CUtensorMap) * 5 * vols_.size());
-    for (int q = 0; q < 2; ++q) {
-        d_masks_[q] = (unsigned long long*)A(NB_ * words_ * 8);
-        d_bits_[q] = (uint32_t*)A((size_t)NW_ * 4);
-        d_cnt_[q] = (unsigned long long*)A(8 * vols_.size());
-    }
+    for (int q = 0; q < 2; ++q) d_masks_[q] = (unsigned long long*)A(NB_ * words_ * 8);
+    for (int q = 0; q < 4; ++q) d_bits_[q] = (uint32_t*)A((size_t)NW_ * 4);
+    for (int q = 0; q < 3; ++q) d_cnt_[q] = (unsigned long long*)A(8 * vols_.size());
     d_brick_vol_ = (uint16_t*)A(NB_ * 2);
-    d_A_ = (uint32_t*)A(NB_ * 4 + 4);
-    d_F_ = (uint32_t*)A(NB_ * 4 + 4);
     d_status_ = (uint64_t*)A((std::max<uint64_t>(NW_, NB_) / 32 + 16) * 8);
     d_ctl_ = (NsCtl*)A(sizeof(NsCtl));
     d_misc_ = (uint32_t*)A(64);
@@ -359,12 +290,7 @@ void NsCore::configure(const BrickConfig& c) {
     owner_->sync();
 }
 
-size_t NsCore::dyn_smem() const {
-    const int V = (int)vols_.size();
-    const KernelSet ks = kernels(cfg_);
-    if (!ks.warp_smem) return stop_state_bytes(V);
-    return (stop_state_bytes(V) + 127) / 128 * 128 + 128 + (size_t)(ks.block / 32) * ks.warp_smem;
-}
+size_t NsCore::dyn_smem() const { return stop_state_bytes((int)vols_.size()); }
 
 void NsCore::upload_descriptors() {
     std::vector<NsVol> d(vols_.size());
@@ -391,26 +317,22 @@ void NsCore::upload_descriptors() {
                                  owner_->stream));
 }
 
-NsArgs NsCore::args(uint32_t parity0, int max_iters, const lss_conv* conv) const {
+NsArgs NsCore::args(uint32_t k0, int max_iters, const lss_conv* conv) const {
     NsArgs a;
     std::memset(&a, 0, sizeof(a));
     a.vols = d_vols_;
     a.vstate = d_vstate_;
     a.nvol = (int32_t)vols_.size();
     a.tmaps = d_tmaps_;
-    for (int q = 0; q < 2; ++q) {
-        a.masks[q] = d_masks_[q];
-        a.bits[q] = d_bits_[q];
-        a.cnt[q] = d_cnt_[q];
-    }
+    for (int q = 0; q < 2; ++q) a.masks[q] = d_masks_[q];
+    for (int q = 0; q < 4; ++q) a.bits[q] = d_bits_[q];
+    for (int q = 0; q < 3; ++q) a.cnt[q] = d_cnt_[q];
     a.brick_vol = d_brick_vol_;
-    a.A_list = d_A_;
-    a.F_list = d_F_;
     a.status = d_status_;
     a.ctl = d_ctl_;
     a.NB = (uint32_t)NB_;
     a.NW = NW_;
-    a.parity0 = parity0;
+    a.k0 = k0;
     a.max_iters = max_iters;
     a.conv_mode = conv ? 1 : 0;
     if (conv) {
@@ -421,7 +343,7 @@ NsArgs NsCore::args(uint32_t parity0, int max_iters, const lss_conv* conv) const
     return a;
 }
 
-// Rebuilds masks, bits and lists of every volume from the current phi (the
+// Rebuilds masks and membership bits of every volume from the current phi (the
 // paper's initial active set, main.tex:217-231).  Both phi buffers are made
 // equal first.
 void NsCore::init_active() {
@@ -429,27 +351,25 @@ void NsCore::init_active() {
     cudaStream_t st = owner_->stream;
     for (VolHost& v : vols_) {
         const uint64_t P = (uint64_t)v.px * v.py * v.pz;
-        float* cur = v.phi[parity_];
-        float* oth = v.phi[parity_ ^ 1];
-        LSS_CUDA(cudaMemcpyAsync(oth, cur, P * 4, cudaMemcpyDeviceToDevice, st));
+        LSS_CUDA(cudaMemcpyAsync(v.phi[parity_ ^ 1], v.phi[parity_], P * 4, cudaMemcpyDeviceToDevice, st));
     }
-    for (int q = 0; q < 2; ++q) {
-        LSS_CUDA(cudaMemsetAsync(d_masks_[q], 0, NB_ * words_ * 8, st));
-        LSS_CUDA(cudaMemsetAsync(d_bits_[q], 0, (size_t)NW_ * 4, st));
-        LSS_CUDA(cudaMemsetAsync(d_cnt_[q], 0, 8 * vols_.size(), st));
-    }
+    for (int q = 0; q < 2; ++q) LSS_CUDA(cudaMemsetAsync(d_masks_[q], 0, NB_ * words_ * 8, st));
+    for (int q = 0; q < 4; ++q) LSS_CUDA(cudaMemsetAsync(d_bits_[q], 0, (size_t)NW_ * 4, st));
+    for (int q = 0; q < 3; ++q) LSS_CUDA(cudaMemsetAsync(d_cnt_[q], 0, 8 * vols_.size(), st));
     LSS_CUDA(cudaMemsetAsync(d_ctl_, 0, sizeof(NsCtl), st));
-    LSS_CUDA(cudaMemsetAsync(d_status_, 0, (NW_ / 64 + 8) * 8, st));
+    // The global iteration index restarts at the phi parity: bits[k%4] holds
+    // A_0 (the other three slots are empty, so A_{-1} is empty too).
+    k_total_ = parity_;
+    const uint32_t s0 = k_total_ % 4u;
     KernelSet ks = kernels(cfg_);
-    NsArgs a = args(parity_, 0, nullptr);
-    uint32_t p = parity_;
-    void* params[] = {&a, &p};
+    NsArgs a = args(k_total_, 0, nullptr);
+    uint32_t p = parity_, sl = s0;
+    void* params[] = {&a, &p, &sl};
     const int grid = (int)std::min<uint64_t>(NB_, (uint64_t)owner_->num_sms * 16);
     LSS_CUDA(cudaLaunchKernel(ks.init_active, dim3(grid), dim3(ks.block), params, 0, st));
-    LSS_CUDA(cudaLaunchKernel(ks.build_list, dim3(std::max(1, owner_->num_sms)), dim3(ks.block), params,
-                              0, st));
     std::vector<unsigned long long> n0(vols_.size());
-    LSS_CUDA(cudaMemcpyAsync(n0.data(), d_cnt_[parity_], 8 * vols_.size(), cudaMemcpyDeviceToHost, st));
+    LSS_CUDA(cudaMemcpyAsync(n0.data(), d_cnt_[0], 8 * vols_.size(), cudaMemcpyDeviceToHost, st));
+    LSS_CUDA(cudaMemsetAsync(d_cnt_[0], 0, 8 * vols_.size(), st));
     owner_->sync();
     std::vector<NsVolState> vs(vols_.size());
     for (size_t i = 0; i < vols_.size(); ++i) {
@@ -468,8 +388,15 @@ void NsCore::init_active() {
 
 void NsCore::sphere_union(int v, float cx, float cy, float cz, float r) {
     VolHost& V = vols_.at(v);
+    // Voxels farther than r + phi_max from the centre keep phi (<= phi_max).
+    const double reach = (double)r + std::max(0.0f, V.p.phi_max) + 1.0;
+    auto lo = [&](double c, int n) { return std::max(0, std::min(n, (int)std::floor(c - reach))); };
+    auto hi = [&](double c, int n) { return std::max(0, std::min(n, (int)std::ceil(c + reach) + 1)); };
+    const int3 b0 = make_int3(lo(cx, V.nx), lo(cy, V.ny), lo(cz, V.nz));
+    const int3 b1 = make_int3(hi(cx, V.nx), hi(cy, V.ny), hi(cz, V.nz));
+    if (b1.x <= b0.x || b1.y <= b0.y || b1.z <= b0.z) return;
     k_ns_sphere_union<<<owner_->num_sms * 4, 256, 0, owner_->stream>>>(
-        V.phi[parity_], V.nx, V.ny, V.nz, V.px, V.py, cx, cy, cz, r, V.p.phi_min, V.p.phi_max);
+        V.phi[parity_], V.nx, V.ny, V.nz, V.px, V.py, b0, b1, cx, cy, cz, r, V.p.phi_min, V.p.phi_max);
     LSS_CUDA(cudaGetLastError());
 }
 
@@ -496,7 +423,7 @@ int NsCore::run(int max_iters, const lss_conv* conv, float* ms) {
     if (max_iters <= 0) return 0;
     cudaStream_t st = owner_->stream;
     KernelSet ks = kernels(cfg_);
-    NsArgs a = args(parity_, max_iters, conv);
+    NsArgs a = args(k_total_, max_iters, conv);
     void* params[] = {&a};
     cudaEvent_t e0, e1;
     LSS_CUDA(cudaEventCreate(&e0));
@@ -519,7 +446,10 @@ int NsCore::run(int max_iters, const lss_conv* conv, float* ms) {
                 "device-side wait gave up (error word " + std::to_string(c.err) + ")");
     std::vector<NsVolState> vs(vols_.size());
     d2h(vs.data(), d_vstate_, vs.size() * sizeof(NsVolState));
-    parity_ = (parity_ + c.iters_run) & 1u;
+    k_total_ += c.iters_run;
+    parity_ = k_total_ & 1u;
+    last_update_ns_ = c.t_phase1_ns;
+    last_barrier_ns_ = c.t_barrier_ns;
     for (size_t i = 0; i < vols_.size(); ++i) vols_[i].iterations = vs[i].iterations;
     return (int)c.iters_run;
 }
@@ -555,28 +485,33 @@ void NsCore::read_phi(int v, float* out) {
 
 uint64_t NsCore::read_active(int v, uint64_t* out, uint64_t cap) {
     LSS_REQUIRE(vols_.size() == 1 && v == 0, LSS_ERR_UNSUPPORTED, "active list of a single volume only");
-    NsCtl c;
-    d2h(&c, d_ctl_, sizeof(c));
-    NsVolState s;
-    state(0, &s);
-    const uint64_t n = s.n_cur;
-    if (!out) return n;
-    uint64_t* dout = (uint64_t*)arena_.alloc(std::max<uint64_t>(n, 1) * 8);
-    LSS_CUDA(cudaMemsetAsync(d_status_, 0, ((uint64_t)c.nA / kernels(cfg_).block + 2) * 8, owner_->stream));
-    LSS_CUDA(cudaMemsetAsync(d_misc_, 0, 4, owner_->stream));
+    LSS_REQUIRE(initialized_, LSS_ERR_STATE, "no seed / phi set");
+    cudaStream_t st = owner_->stream;
     KernelSet ks = kernels(cfg_);
-    NsArgs a = args(parity_, 0, nullptr);
-    uint32_t p = parity_;
-    uint64_t* o = dout;
-    uint32_t* tc = d_misc_;
-    void* params[] = {&a, &p, &o, &tc};
-    LSS_CUDA(cudaLaunchKernel(ks.emit, dim3(owner_->num_sms * 2), dim3(ks.block), params, 0,
-                              owner_->stream));
+    const uint32_t s = k_total_ % 4u;
+    unsigned long long* total = (unsigned long long*)d_misc_;
+    auto emit = [&](uint64_t* dout) {
+        LSS_CUDA(cudaMemsetAsync(d_status_, 0, ((uint64_t)NW_ / ks.block + 2) * 8, st));
+        LSS_CUDA(cudaMemsetAsync(d_misc_, 0, 16, st));
+        LSS_CUDA(cudaMemsetAsync(&d_ctl_->emit_tile, 0, 4, st));
+        NsArgs a = args(k_total_, 0, nullptr);
+        uint32_t p = parity_, sl = s;
+        void* params[] = {&a, &p, &sl, &dout, &total};
+        LSS_CUDA(cudaLaunchKernel(ks.emit, dim3(owner_->num_sms * 2), dim3(ks.block), params, 0, st));
+        unsigned long long n = 0;
+        LSS_CUDA(cudaMemcpyAsync(&n, total, 8, cudaMemcpyDeviceToHost, st));
+        owner_->sync();
+        check_errors();
+        return (uint64_t)n;
+    };
+    const uint64_t n = emit(nullptr);
+    if (!out || n == 0) return n;
+    uint64_t* dout = (uint64_t*)arena_.alloc(n * 8);
+    emit(dout);
     const uint64_t m = std::min(n, cap);
-    if (m) LSS_CUDA(cudaMemcpyAsync(out, dout, m * 8, cudaMemcpyDeviceToHost, owner_->stream));
+    LSS_CUDA(cudaMemcpyAsync(out, dout, m * 8, cudaMemcpyDeviceToHost, st));
     owner_->sync();
     arena_.free_last(dout);
-    check_errors();
     return n;
 }
 

@@ -1,22 +1,27 @@
 // LSS_MODE_NS device code: the persistent bricked iteration kernel and its
 // helpers.  One launch runs many iterations (and, in the batched form, many
-// volumes) with two bounded grid barriers per iteration:
+// volumes) with ONE bounded grid barrier per iteration k:
 //
-//   phase 1  every active brick of A_k: TMA-load the brick's phi with a
-//            one-voxel halo (and its intensities) into shared memory, update
-//            the active voxels (upwind |grad phi|, mean curvature, speed
-//            D = eps - |I - T|), TMA-store the brick into the other phi
-//            buffer, flag changed voxels with warp ballots, dilate the changed
-//            bitmask by the 26- (or 6-) neighbourhood and OR it into the next
-//            masks of the brick and its 26 neighbours; every brick of F_k
-//            (active at k-1, not at k) copies phi across so that both buffers
-//            stay current.
-//   barrier
-//   phase 2  single-pass decoupled-lookback compaction of the brick bitmaps
-//            into the sorted lists A_{k+1} (non-empty next mask) and F_{k+1}
-//            (in A_k, not in A_{k+1}); active voxels of A_{k+1} are counted per
-//            volume (popc of the masks).
-//   barrier  then every block evaluates the stopping rule on the same counts.
+//   every block ranks the bricks of A_k (and of A_{k-1} \ A_k) with a block
+//     prefix sum over the membership words and takes the ranks i, i+G, ...
+//     (block i of G): every block gets ceil(n/G) or floor(n/G) bricks, with
+//     no global list and no atomics;
+//   every owned brick of A_k: TMA-load the brick's phi with a one-voxel halo
+//     (and its intensities) into shared memory, with the next brick's loads
+//     and mask words in flight (double buffered); update the active voxels
+//     (upwind |grad phi|, mean curvature, speed D = eps - |I - T|), TMA-store
+//     the brick into the other phi buffer, flag changed voxels with warp
+//     ballots, dilate the changed bitmask by the 26- (or 6-) neighbourhood and
+//     OR it into the next masks and membership bits of the brick and its 26
+//     neighbours (fire-and-forget reductions);
+//   every owned brick of A_{k-1} that is not in A_k copies phi across, so
+//     both phi buffers stay current;
+//   barrier, then every block evaluates the stopping rule on the same counts.
+//
+// Membership bits, masks and phi are order independent, so results are
+// deterministic.  The ordered (brick-major) voxel list is produced on demand
+// by a single-pass decoupled-lookback compaction over the membership bits
+// (k_ns_emit).
 //
 // The reference keeps one dense list of voxel coordinates and rebuilds it
 // with seven offset buffers, a tag-volume filter and CUDPP compaction per
@@ -61,12 +66,11 @@ struct NsVolState {
 };
 
 struct NsCtl {
-    uint32_t nA, nF;          // lengths of A_k and F_k
     uint32_t err;
     uint32_t bar_count, bar_gen;
-    uint32_t scan_tile;       // dynamic tile counter of the phase-2 compaction
     uint32_t iters_run;       // iterations run by the last launch
-    uint32_t all_done;
+    uint32_t emit_tile;       // tile counter of the voxel-list emission
+    unsigned long long t_phase1_ns, t_barrier_ns;  // block 0's time split
 };
 
 struct NsArgs {
@@ -74,16 +78,14 @@ struct NsArgs {
     NsVolState* vstate;
     int32_t nvol;
     const CUtensorMap* tmaps;
-    unsigned long long* masks[2];  // [NB][WORDS]
-    uint32_t* bits[2];             // [NW]
+    unsigned long long* masks[2];  // [NB][WORDS], by phi parity
+    uint32_t* bits[4];             // [NW] brick membership, by iteration mod 4
     const uint16_t* brick_vol;     // [NB]
-    uint32_t* A_list;
-    uint32_t* F_list;
-    unsigned long long* cnt[2];    // [nvol]
+    unsigned long long* cnt[3];    // [nvol] active voxels updated, by iteration mod 3
     uint64_t* status;              // decoupled-lookback status words
     NsCtl* ctl;
     uint32_t NB, NW;
-    uint32_t parity0;              // phi parity of the launch's first iteration
+    uint32_t k0;                   // global iteration index of the launch's first iteration
     int32_t max_iters;
     int32_t conv_mode;             // 0: exactly max_iters, 1: stopping rule
     double rel;
@@ -99,42 +101,13 @@ struct Brick {
     static constexpr int CHG = VOX / 32;
     static constexpr int TX = BX + 8, TY = BY + 2, TZ = BZ + 2;  // halo tile
     static constexpr int TILE = TX * TY * TZ;
-    static constexpr int EXT = (BX + 2) * (BY + 2) * (BZ + 2);
+    static constexpr int TILE_PAD = (TILE + 31) / 32 * 32;  // 128-byte stride between tiles
+    static constexpr int XY = BX * BY;
     static_assert(VOX % 64 == 0, "brick must hold a multiple of 64 voxels");
     static_assert(BX == 4 || BX == 8, "brick x must be 4 or 8");
+    // Mask words: one z-plane a word (XY == 64) or the whole brick in one word.
+    static_assert(XY == 64 || VOX == 64, "mask word layout");
 };
-
-// Bounded sense-reversing grid barrier (all blocks co-resident: cooperative
-// launch).  Returns false if this block gave up waiting.
-__device__ __forceinline__ bool grid_barrier(NsCtl* ctl, uint32_t& gen, uint32_t nblocks) {
-    __shared__ uint32_t s_ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        s_ok = 1;
-        const uint32_t target = gen + 1;
-        __threadfence();
-        const uint32_t arrived = atomicAdd(&ctl->bar_count, 1u) + 1u;
-        if (arrived == nblocks) {
-            ctl->bar_count = 0;
-            __threadfence();
-            asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(&ctl->bar_gen), "r"(target) : "memory");
-        } else {
-            uint64_t t0 = globaltimer_ns();
-            while (ld_acquire_u32(&ctl->bar_gen) != target) {
-                if (globaltimer_ns() - t0 > kWaitLimitNs) {
-                    set_error(&ctl->err, ERR_BARRIER_TIMEOUT);
-                    s_ok = 0;
-                    break;
-                }
-                __nanosleep(32);
-            }
-        }
-        gen = target;
-        __threadfence();
-    }
-    __syncthreads();
-    return s_ok != 0;
-}
 
 // The spec update of one voxel from the shared-memory halo tile.
 // P(dx,dy,dz) reads the tile around the voxel.  Mirrors ns_update() of the
@@ -178,28 +151,115 @@ __device__ __forceinline__ float ns_update_f32(PF P, float I, float bias, const 
     return fminf(fmaxf(nv, V.lo), V.hi);
 }
 
+// Every TMA destination / source below starts on a 128-byte boundary: the
+// arrays are 128-byte aligned and every per-buffer stride is a multiple of
+// 128 bytes (TILE_PAD floats; VOX floats = 256 B or more).
 template <class S, int NT>
 struct NsSmem {
-    alignas(128) float phi[2][S::TILE];  // halo tiles, double buffered
+    static_assert((S::TILE_PAD * 4) % 128 == 0 && (S::VOX * 4) % 128 == 0, "TMA smem alignment");
+    alignas(128) float phi[2][S::TILE_PAD];  // halo tiles, double buffered
     alignas(128) float img[2][S::VOX];
     alignas(128) float out[2][S::VOX];
-    unsigned long long act[S::WORDS];
-    unsigned long long next[27 * S::WORDS];
+    unsigned long long act[2][S::WORDS];     // the brick's active mask, double buffered
     uint32_t chg[S::CHG];
     alignas(8) uint64_t bar[2];
 };
 
-// Bits of one brick row (BX voxels) of the changed mask.
+// Bit-parallel dilation of a brick's changed mask.  Voxel (lx, ly, lz) is
+// bit j = (lz*Y + ly)*X + lx of the mask (word j/64, bit j%64).  The box
+// (26-neighbour) dilation is separable: x, then y, then z; the part of the
+// result that lands in the neighbour brick at offset (ox, oy, oz) is
+// Z_oz(Y_oy(X_ox(c))), where X_0 dilates within the brick and X_{-1} / X_{+1}
+// move the edge column x = 0 / x = X-1 to the far column of the neighbour
+// (likewise for y and z).  The 6-neighbour dilation is c | X_0 | Y_0 | Z_0 in
+// the brick itself and X_{+-1}, Y_{+-1}, Z_{+-1} in the six face neighbours.
 template <class S>
-__device__ __forceinline__ uint32_t chg_row(const uint32_t* chg, int ly, int lz) {
-    const int off = (lz * S::Y + ly) * S::X;
-    return (chg[off >> 5] >> (off & 31)) & ((1u << S::X) - 1u);
+struct BitGeo {
+    // Bits of a mask word whose voxel satisfies a predicate of (lx, ly, plane).
+    template <class F>
+    static constexpr uint64_t where(F f) {
+        uint64_t m = 0;
+        for (int b = 0; b < 64; ++b)
+            if (f(b % S::X, (b / S::X) % S::Y, b / S::XY)) m |= 1ull << b;
+        return m;
+    }
+    static constexpr uint64_t CX0 = where([](int x, int, int) { return x == 0; });
+    static constexpr uint64_t CXL = where([](int x, int, int) { return x == S::X - 1; });
+    static constexpr uint64_t RY0 = where([](int, int y, int) { return y == 0; });
+    static constexpr uint64_t RYL = where([](int, int y, int) { return y == S::Y - 1; });
+    static constexpr uint64_t PZ0 = where([](int, int, int z) { return z == 0; });
+    static constexpr uint64_t PZL = where([](int, int, int z) { return z == S::Z - 1; });
+};
+
+template <class S>
+__host__ __device__ __forceinline__ uint64_t dil_x(uint64_t v, int o) {
+    using G = BitGeo<S>;
+    if (o == 0) return v | ((v & ~G::CXL) << 1) | ((v & ~G::CX0) >> 1);
+    return o < 0 ? (v & G::CX0) << (S::X - 1) : (v & G::CXL) >> (S::X - 1);
 }
 
 template <class S>
-__device__ __forceinline__ bool chg_bit(const uint32_t* chg, int lx, int ly, int lz) {
-    const int j = (lz * S::Y + ly) * S::X + lx;
-    return (chg[j >> 5] >> (j & 31)) & 1u;
+__host__ __device__ __forceinline__ uint64_t dil_y(uint64_t v, int o) {
+    using G = BitGeo<S>;
+    if (o == 0) return v | ((v & ~G::RYL) << S::X) | ((v & ~G::RY0) >> S::X);
+    return o < 0 ? (v & G::RY0) << (S::X * (S::Y - 1)) : (v & G::RYL) >> (S::X * (S::Y - 1));
+}
+
+// z step over the whole mask (in place).
+template <class S>
+__host__ __device__ __forceinline__ void dil_z(uint64_t (&v)[S::WORDS], int o) {
+    using G = BitGeo<S>;
+    if constexpr (S::WORDS == 1) {
+        constexpr int sh = S::XY * (S::Z - 1);
+        if (o == 0) v[0] = v[0] | ((v[0] & ~G::PZL) << S::XY) | ((v[0] & ~G::PZ0) >> S::XY);
+        else v[0] = o < 0 ? (v[0] & G::PZ0) << sh : (v[0] & G::PZL) >> sh;
+    } else {
+        uint64_t r[S::WORDS];
+#pragma unroll
+        for (int w = 0; w < S::WORDS; ++w) {
+            if (o == 0) r[w] = v[w] | (w > 0 ? v[w - 1] : 0ull) | (w + 1 < S::WORDS ? v[w + 1] : 0ull);
+            else if (o < 0) r[w] = w == S::WORDS - 1 ? v[0] : 0ull;
+            else r[w] = w == 0 ? v[S::WORDS - 1] : 0ull;
+        }
+#pragma unroll
+        for (int w = 0; w < S::WORDS; ++w) v[w] = r[w];
+    }
+}
+
+// The part of the dilated mask m (in place) that lands in the neighbour
+// brick at offset (ox, oy, oz); nbh = 26 or 6.
+template <class S>
+__host__ __device__ __forceinline__ void dilate_slot(uint64_t (&m)[S::WORDS], int ox, int oy, int oz, int nbh) {
+    const int moved = (ox != 0) + (oy != 0) + (oz != 0);
+    if (nbh == 6 && moved > 1) {
+        for (int w = 0; w < S::WORDS; ++w) m[w] = 0ull;
+    } else if (nbh == 6 && moved == 1) {  // face neighbour: one axis moves
+        for (int w = 0; w < S::WORDS; ++w) m[w] = ox ? dil_x<S>(m[w], ox) : (oy ? dil_y<S>(m[w], oy) : m[w]);
+        if (oz) dil_z<S>(m, oz);
+    } else if (nbh == 6) {  // the brick itself: c | X_0 | Y_0 | Z_0
+        uint64_t zz[S::WORDS];
+        for (int w = 0; w < S::WORDS; ++w) zz[w] = m[w];
+        dil_z<S>(zz, 0);
+        for (int w = 0; w < S::WORDS; ++w) m[w] = dil_x<S>(m[w], 0) | dil_y<S>(m[w], 0) | zz[w];
+    } else {
+        for (int w = 0; w < S::WORDS; ++w) m[w] = dil_y<S>(dil_x<S>(m[w], ox), oy);
+        dil_z<S>(m, oz);
+    }
+}
+
+// Voxels of a brick inside the volume when only the first lim_x, lim_y,
+// lim_z voxels of each axis are (the far edge of the volume), for word w.
+template <class S>
+__host__ __device__ __forceinline__ uint64_t inside_mask(int w, int lx, int ly, int lz) {
+    using G = BitGeo<S>;
+    const uint64_t mx = (uint64_t)((1u << lx) - 1u) * G::CX0;
+    uint64_t my;
+    if constexpr (S::XY == 64) my = ly >= S::Y ? ~0ull : (1ull << (S::X * ly)) - 1ull;
+    else my = (uint64_t)((1u << (S::X * ly)) - 1u) * G::where([](int x, int y, int) { return x == 0 && y == 0; });
+    uint64_t mz;
+    if constexpr (S::WORDS == 1) mz = lz >= S::Z ? ~0ull : (1ull << (S::XY * lz)) - 1ull;
+    else mz = w < lz ? ~0ull : 0ull;
+    return mx & my & mz;
 }
 
 // Brick origin of global brick b.
@@ -227,41 +287,51 @@ __device__ __forceinline__ void ns_issue_loads(const NsArgs& a, NsSmem<S, NT>& s
 struct BlockTally {
     uint32_t v = 0xFFFFFFFFu;
     unsigned long long upd = 0, brk = 0;
-    __device__ void add(NsVolState* vs, uint32_t vol, unsigned long long n) {
+    __device__ void add(NsVolState* vs, unsigned long long* cnt, uint32_t vol, unsigned long long n) {
         if (vol != v) {
-            flush(vs);
+            flush(vs, cnt);
             v = vol;
         }
         upd += n;
         brk += 1;
     }
-    __device__ void flush(NsVolState* vs) {
+    __device__ void flush(NsVolState* vs, unsigned long long* cnt) {
         if (v != 0xFFFFFFFFu && brk) {
             atomicAdd(&vs[v].updates, upd);
             atomicAdd(&vs[v].bricks, brk);
+            atomicAdd(&cnt[v], upd);
         }
         upd = brk = 0;
     }
 };
 
-// Phase-1 work on one active brick whose loads were issued into `buf`.
+// Work on one brick of A_k whose loads were issued into `buf`.
+// The brick's mask words -> act[buf] (threads < WORDS), cleared in global
+// memory: the mask array of parity p becomes the accumulator of iteration k+1.
+template <class S, int NT>
+__device__ __forceinline__ void ns_fetch_mask(const NsArgs& a, NsSmem<S, NT>& sm, uint32_t b, uint32_t p,
+                                              int buf) {
+    if (threadIdx.x < S::WORDS) {
+        unsigned long long* cur = a.masks[p] + (size_t)b * S::WORDS;
+        sm.act[buf][threadIdx.x] = cur[threadIdx.x];
+        cur[threadIdx.x] = 0ull;
+    }
+}
+
 template <class S, int NT>
 __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>& sm, uint32_t b,
-                                                 uint32_t p, int buf, uint32_t* mphase,
-                                                 BlockTally& tally) {
+                                                 uint32_t p, uint32_t sn, int buf, uint32_t* mphase,
+                                                 BlockTally& tally, unsigned long long* cnt) {
     const int tid = threadIdx.x;
     const uint32_t v = a.brick_vol[b];
     const NsVol& V = a.vols[v];
     const int3 o = brick_origin<S>(V, b);
     const int x0 = o.x, y0 = o.y, z0 = o.z;
-    unsigned long long* cur = a.masks[p] + (size_t)b * S::WORDS;
-    if (tid < S::WORDS) {
-        sm.act[tid] = cur[tid];
-        cur[tid] = 0ull;
-    }
-    for (int t = tid; t < 27 * S::WORDS; t += NT) sm.next[t] = 0ull;
+    const unsigned long long* act = sm.act[buf];
     if (!mbar_wait(&sm.bar[buf], mphase[buf])) set_error(&a.ctl->err, ERR_TMA_TIMEOUT);
     mphase[buf] ^= 1u;
+    // The store issued from out[buf] two bricks ago must have read its source.
+    if (tid == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
     __syncthreads();
     float* phi = sm.phi[buf];
     // Clamp-to-edge halo where the tile leaves the volume (TMA filled zeros).
@@ -278,12 +348,10 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
         }
         __syncthreads();
     }
-    // The store issued from out[buf] two bricks ago must have read its source.
-    if (tid == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
-    __syncthreads();
     float* out = sm.out[buf];
     constexpr int VPT = (S::VOX + NT - 1) / NT;
     const float* bias = V.bias;
+    bool anyl = false;
 #pragma unroll
     for (int k = 0; k < VPT; ++k) {
         const int j = tid + k * NT;
@@ -293,7 +361,7 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
             const int ti = ((lz + 1) * S::TY + (ly + 1)) * S::TX + (lx + 4);
             const float c = phi[ti];
             float nv = c;
-            if ((sm.act[j >> 6] >> (j & 63)) & 1ull) {
+            if ((act[j >> 6] >> (j & 63)) & 1ull) {
                 auto P = [&](int dx, int dy, int dz) { return phi[ti + (dz * S::TY + dy) * S::TX + dx]; };
                 float bb = 0.0f;
                 if (bias) bb = bias[((size_t)(z0 + lz) * V.py + (y0 + ly)) * V.px + (x0 + lx)];
@@ -303,188 +371,72 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
             out[j] = nv;
         }
         const uint32_t bal = __ballot_sync(0xffffffffu, chg);
+        anyl |= bal != 0u;
         const int word = (tid >> 5) + k * (NT / 32);
         if ((tid & 31) == 0 && word < S::CHG) sm.chg[word] = bal;
     }
     fence_proxy_async_smem();
-    __syncthreads();
+    const int any = __syncthreads_or(anyl ? 1 : 0);
     if (tid == 0) {
         tma_store_3d(&a.tmaps[V.tmap_base + 2 + (p ^ 1u)], x0, y0, z0, out);
         tma_store_commit();
     }
-    // Dilation of the changed mask into the 27 bricks around (and including) b.
-    bool any = false;
-#pragma unroll 1
-    for (int w = 0; w < S::CHG; ++w) any |= sm.chg[w] != 0u;
-    if (any) {
-        const int EX = S::X + 2, EY = S::Y + 2;
-        for (int e = tid; e < S::EXT; e += NT) {
-            const int ex = e % EX - 1, ey = (e / EX) % EY - 1, ez = e / (EX * EY) - 1;
-            const int gx = x0 + ex, gy = y0 + ey, gz = z0 + ez;
-            if (gx < 0 || gy < 0 || gz < 0 || gx >= V.nx || gy >= V.ny || gz >= V.nz) continue;
+    // Dilation of the changed mask into the 27 bricks around (and including)
+    // b: lane L of warp 0 computes the part for neighbour L and ORs it into
+    // the next masks and membership bits (reductions, no round trip).
+    if (any && tid < 27) {
+        const int ox = tid % 3 - 1, oy = (tid / 3) % 3 - 1, oz = tid / 9 - 1;
+        const int bx = x0 / S::X + ox, by = y0 / S::Y + oy, bz = z0 / S::Z + oz;
+        // Voxels of the neighbour inside the volume along each axis (bricks
+        // in the padding beyond the volume hold none).
+        const int lx = V.nx - bx * S::X, ly = V.ny - by * S::Y, lz = V.nz - bz * S::Z;
+        const bool six_skip = V.nbh == 6 && (ox != 0) + (oy != 0) + (oz != 0) > 1;
+        if (!six_skip && bx >= 0 && by >= 0 && bz >= 0 && lx > 0 && ly > 0 && lz > 0) {
+            uint64_t m[S::WORDS];
+#pragma unroll
+            for (int w = 0; w < S::WORDS; ++w)
+                m[w] = (uint64_t)sm.chg[2 * w] | ((uint64_t)sm.chg[2 * w + 1] << 32);
+            dilate_slot<S>(m, ox, oy, oz, V.nbh);
+            const bool clip = lx < S::X || ly < S::Y || lz < S::Z;
+            const uint32_t nb = b + (int32_t)((oz * V.nby + oy) * V.nbx + ox);
             bool hit = false;
-            if (V.nbh == 26) {
-                const int lo = max(ex - 1, 0), hi = min(ex + 1, S::X - 1);
-                if (lo <= hi) {
-                    const uint32_t m = ((1u << (hi - lo + 1)) - 1u) << lo;
-                    for (int dz = -1; dz <= 1 && !hit; ++dz) {
-                        const int z = ez + dz;
-                        if (z < 0 || z >= S::Z) continue;
-                        for (int dy = -1; dy <= 1; ++dy) {
-                            const int y = ey + dy;
-                            if (y < 0 || y >= S::Y) continue;
-                            if (chg_row<S>(sm.chg, y, z) & m) { hit = true; break; }
-                        }
-                    }
-                }
-            } else {
-                const bool in = ex >= 0 && ex < S::X && ey >= 0 && ey < S::Y && ez >= 0 && ez < S::Z;
-                if (in && chg_bit<S>(sm.chg, ex, ey, ez)) hit = true;
-                const int nb[6][3] = {{-1, 0, 0}, {1, 0, 0}, {0, -1, 0}, {0, 1, 0}, {0, 0, -1}, {0, 0, 1}};
-                for (int q = 0; q < 6 && !hit; ++q) {
-                    const int x = ex + nb[q][0], y = ey + nb[q][1], z = ez + nb[q][2];
-                    if (x >= 0 && x < S::X && y >= 0 && y < S::Y && z >= 0 && z < S::Z &&
-                        chg_bit<S>(sm.chg, x, y, z))
-                        hit = true;
+#pragma unroll
+            for (int w = 0; w < S::WORDS; ++w) {
+                uint64_t x = m[w];
+                if (clip) x &= inside_mask<S>(w, min(lx, S::X), min(ly, S::Y), min(lz, S::Z));
+                if (x) {
+                    atomicOr(&a.masks[p ^ 1u][(size_t)nb * S::WORDS + w], (unsigned long long)x);
+                    hit = true;
                 }
             }
-            if (!hit) continue;
-            const int ox = ex < 0 ? -1 : (ex >= S::X ? 1 : 0);
-            const int oy = ey < 0 ? -1 : (ey >= S::Y ? 1 : 0);
-            const int oz = ez < 0 ? -1 : (ez >= S::Z ? 1 : 0);
-            const int lx = ex - ox * S::X, ly = ey - oy * S::Y, lz = ez - oz * S::Z;
-            const int jj = (lz * S::Y + ly) * S::X + lx;
-            const int slot = (oz + 1) * 9 + (oy + 1) * 3 + (ox + 1);
-            atomicOr(&sm.next[slot * S::WORDS + (jj >> 6)], 1ull << (jj & 63));
-        }
-        __syncthreads();
-        for (int t = tid; t < 27 * S::WORDS; t += NT) {
-            const unsigned long long w = sm.next[t];
-            if (!w) continue;
-            const int slot = t / S::WORDS, word = t % S::WORDS;
-            const int ox = slot % 3 - 1, oy = (slot / 3) % 3 - 1, oz = slot / 9 - 1;
-            const uint32_t nb = b + (int32_t)((oz * V.nby + oy) * V.nbx + ox);
-            atomicOr(&a.masks[p ^ 1u][(size_t)nb * S::WORDS + word], w);
-            uint32_t* bw = &a.bits[p ^ 1u][nb >> 5];
-            const uint32_t bit = 1u << (nb & 31);
-            if (!(*(volatile uint32_t*)bw & bit)) atomicOr(bw, bit);
+            if (hit) atomicOr(&a.bits[sn][nb >> 5], 1u << (nb & 31));
         }
     }
     if (tid == 0) {
         unsigned long long n = 0;
-        for (int w = 0; w < S::WORDS; ++w) n += __popcll(sm.act[w]);
-        tally.add(a.vstate, v, n);
+        for (int w = 0; w < S::WORDS; ++w) n += __popcll(act[w]);
+        tally.add(a.vstate, cnt, v, n);
     }
     __syncthreads();
 }
 
-// Phase-1 work on one brick of F_k: phi[p] -> phi[p^1].
+// A brick of A_{k-1} not in A_k: phi[p] -> phi[p^1].
 template <class S, int NT>
 __device__ __forceinline__ void ns_flush_brick(const NsArgs& a, uint32_t b, uint32_t p) {
     const NsVol& V = a.vols[a.brick_vol[b]];
-    const uint32_t lb = b - V.brick_base;
-    const int kx = lb % V.nbx, ky = (lb / V.nbx) % V.nby, kz = lb / (V.nbx * V.nby);
+    const int3 o = brick_origin<S>(V, b);
     const float* src = V.phi[p];
     float* dst = V.phi[p ^ 1u];
     constexpr int Q = S::X / 4;  // float4 per row
     for (int t = threadIdx.x; t < S::Y * S::Z * Q; t += NT) {
         const int q = t % Q, ly = (t / Q) % S::Y, lz = t / (Q * S::Y);
-        const size_t off = ((size_t)(kz * S::Z + lz) * V.py + (ky * S::Y + ly)) * V.px + kx * S::X + 4 * q;
+        const size_t off = ((size_t)(o.z + lz) * V.py + (o.y + ly)) * V.px + o.x + 4 * q;
         *reinterpret_cast<float4*>(dst + off) = *reinterpret_cast<const float4*>(src + off);
     }
 }
 
-// Phase 2 (and list construction at initialisation): compaction of the brick
-// bitmaps.  next: bricks with a non-empty next mask (-> A); cur (nullable):
-// bricks of A_k (cur & ~next -> F, and cur is cleared).  done (nullable)
-// drops bricks of finished volumes.  Counts the voxels of A per volume into
-// cnt.  The last tile publishes the list lengths.
-template <int WORDS, int NT>
-__device__ __forceinline__ void ns_scan(const NsArgs& a, uint32_t* next, uint32_t* cur,
-                                        const unsigned long long* nmask, unsigned long long* cnt,
-                                        const int32_t* done) {
-    __shared__ uint32_t s_tile;
-    const uint32_t ntiles = (a.NW + NT - 1) / NT;
-    constexpr uint64_t M31 = (1ull << 31) - 1;
-    for (;;) {
-        if (threadIdx.x == 0) s_tile = atomicAdd(&a.ctl->scan_tile, 1u);
-        __syncthreads();
-        const uint32_t tile = s_tile;
-        __syncthreads();
-        if (tile >= ntiles) break;
-        const uint32_t w = tile * NT + threadIdx.x;
-        uint32_t an = 0, c = 0;
-        if (w < a.NW) {
-            an = next[w];
-            if (cur) c = cur[w];
-            if (done && (an | c)) {
-                uint32_t all = an | c;
-                while (all) {
-                    const int bit = __ffs(all) - 1;
-                    all &= all - 1;
-                    if (done[a.brick_vol[w * 32 + bit]]) {
-                        an &= ~(1u << bit);
-                        c &= ~(1u << bit);
-                    }
-                }
-            }
-        }
-        const uint32_t fb = c & ~an;
-        const uint64_t val = ((uint64_t)__popc(an) << 31) | (uint64_t)__popc(fb);
-        uint64_t total;
-        const uint64_t excl = block_exclusive_sum64(val, &total);
-        const uint64_t prefix = tile_exclusive_prefix(a.status, tile, total, &a.ctl->err);
-        const uint32_t a0 = (uint32_t)(prefix >> 31);  // this tile's first A position
-        uint32_t pa = a0 + (uint32_t)(excl >> 31);
-        uint32_t pf = (uint32_t)((prefix & M31) + (excl & M31));
-        uint32_t m = an;
-        while (m) {
-            const int bit = __ffs(m) - 1;
-            m &= m - 1;
-            a.A_list[pa++] = w * 32 + bit;
-        }
-        m = fb;
-        while (m) {
-            const int bit = __ffs(m) - 1;
-            m &= m - 1;
-            a.F_list[pf++] = w * 32 + bit;
-        }
-        if (cur && w < a.NW) cur[w] = 0u;
-        if (tile == ntiles - 1 && threadIdx.x == 0) {
-            const uint64_t t = prefix + total;
-            a.ctl->nA = (uint32_t)(t >> 31);
-            a.ctl->nF = (uint32_t)(t & M31);
-        }
-        // Voxel count of this tile's A bricks, spread over the block; one
-        // atomic per warp and volume run.
-        __syncthreads();
-        const uint32_t a1 = a0 + (uint32_t)(total >> 31);
-        uint32_t vol = 0xFFFFFFFFu;
-        unsigned long long sum = 0;
-        for (uint32_t i = a0 + threadIdx.x; i < a1; i += NT) {
-            const uint32_t bk = a.A_list[i];
-            const uint32_t bv = a.brick_vol[bk];
-            if (bv != vol) {
-                if (sum) atomicAdd(&cnt[vol], sum);
-                vol = bv;
-                sum = 0;
-            }
-            for (int q = 0; q < WORDS; ++q) sum += __popcll(nmask[(size_t)bk * WORDS + q]);
-        }
-        const uint32_t v0 = __reduce_min_sync(0xffffffffu, sum ? vol : 0xFFFFFFFFu);
-        const bool uniform = __all_sync(0xffffffffu, vol == v0 || sum == 0);
-        if (uniform) {
-            for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
-            if ((threadIdx.x & 31) == 0 && sum) atomicAdd(&cnt[v0], sum);
-        } else if (sum) {
-            atomicAdd(&cnt[vol], sum);
-        }
-        __syncthreads();
-    }
-}
-
 // Per-volume stopping state kept identically by every block (dynamic shared
-// memory): done, streak, stop iteration, current count.
+// memory): done, streak, stop iteration, last count.
 struct StopState {
     int32_t* done;
     int32_t* streak;
@@ -505,11 +457,31 @@ __device__ __forceinline__ StopState stop_state(int32_t* base, int nvol) {
     return s;
 }
 
-template <int NT>
-__device__ __forceinline__ void ns_begin(const NsArgs& a, StopState& ss, uint32_t* s_gen) {
+// The persistent kernel: one block per brick at a time, NT threads.
+//
+// Slots at iteration k: membership bits B[k%4] = A_k, B[(k+1)%4] = A_{k+1}
+// (being built), B[(k+3)%4] = A_{k-1}, B[(k+2)%4] cleared for reuse; voxel
+// counts cnt[k%3].  Stopping rule after iteration k, per volume: n_k = active
+// voxels updated at k; streak = consecutive iterations with n_k < rel * n0;
+// stop when streak >= patience, n_k <= abs_thr, or the budget is used.
+constexpr uint32_t kNoBrick = 0xFFFFFFFFu;  // a brick of a finished volume
+
+// At least 1024 resident threads per SM: 64 registers a thread at most.
+template <int BX, int BY, int BZ, int NT>
+__global__ void __launch_bounds__(NT, 1024 / NT) k_ns_persistent(NsArgs a) {
+    using S = Brick<BX, BY, BZ>;
+    __shared__ NsSmem<S, NT> sm;
+    __shared__ uint32_t s_gen;
+    __shared__ int32_t s_live;
+    __shared__ uint32_t s_work[NT], s_flush[NT];
+    extern __shared__ int32_t s_dyn[];
+    StopState ss = stop_state(s_dyn, a.nvol);
     const int tid = threadIdx.x;
+    const uint32_t G = gridDim.x;
     if (tid == 0) {
-        *s_gen = ld_acquire_u32(&a.ctl->bar_gen);
+        mbar_init(&sm.bar[0], 1);
+        mbar_init(&sm.bar[1], 1);
+        s_gen = ld_acquire_u32(&a.ctl->bar_gen);
         for (int v = 0; v < a.nvol; ++v)
             for (int m = 0; m < 5; ++m) tmap_acquire(&a.tmaps[a.vols[v].tmap_base + m]);
     }
@@ -517,360 +489,187 @@ __device__ __forceinline__ void ns_begin(const NsArgs& a, StopState& ss, uint32_
         ss.done[v] = 0;
         ss.streak[v] = 0;
         ss.stop[v] = -1;
-        ss.n[v] = a.vstate[v].n_cur;
+        ss.n[v] = 0;
     }
-}
-
-// Start of an iteration (block 0): clear this iteration's count slot, the
-// compaction status words and the tile counter.
-template <int NT>
-__device__ __forceinline__ void ns_iteration_prologue(const NsArgs& a, uint32_t p) {
-    if (blockIdx.x != 0) return;
-    const int tid = threadIdx.x;
-    for (int v = tid; v < a.nvol; v += NT) a.cnt[p ^ 1u][v] = 0ull;
-    const uint32_t ntiles = (a.NW + NT - 1) / NT;
-    for (uint32_t t = tid; t < ntiles; t += NT) a.status[t] = 0ull;
-    if (tid == 0) a.ctl->scan_tile = 0u;
-}
-
-// After phase 1: barrier, phase-2 compaction, barrier, stopping rule.
-// Returns false when the loop must end (*it_out then holds the iterations run).
-template <int WORDS, int NT>
-__device__ __forceinline__ bool ns_iteration_epilogue(const NsArgs& a, StopState& ss, uint32_t& gen,
-                                                      uint32_t p, int it, int* it_out) {
-    const int tid = threadIdx.x;
-    const uint32_t G = gridDim.x;
-    *it_out = it;
-    __syncthreads();
-    if (!grid_barrier(a.ctl, gen, G)) return false;
-    ns_scan<WORDS, NT>(a, a.bits[p ^ 1u], a.bits[p], a.masks[p ^ 1u], a.cnt[p ^ 1u],
-                       a.nvol > 1 ? ss.done : nullptr);
-    if (!grid_barrier(a.ctl, gen, G)) return false;
-    if (tid == 0) asm volatile("fence.proxy.async.global;" ::: "memory");
-    if (*(volatile uint32_t*)&a.ctl->err) return false;
-    __shared__ int32_t s_live;
-    if (tid == 0) s_live = 0;
-    __syncthreads();
-    for (int v = tid; v < a.nvol; v += NT) {
-        if (ss.done[v]) continue;
-        const unsigned long long n = *(volatile unsigned long long*)&a.cnt[p ^ 1u][v];
-        ss.n[v] = n;
-        bool stop;
-        if (a.conv_mode) {
-            const unsigned long long n0 = a.vstate[v].n0;
-            ss.streak[v] = ((double)n < a.rel * (double)n0) ? ss.streak[v] + 1 : 0;
-            stop = ss.streak[v] >= a.patience || n <= a.abs_thr || it + 1 >= a.max_iters;
-        } else {
-            stop = it + 1 >= a.max_iters;
-        }
-        if (stop) {
-            ss.done[v] = 1;
-            ss.stop[v] = it;
-        } else {
-            atomicAdd(&s_live, 1);
-        }
-    }
-    __syncthreads();
-    *it_out = it + 1;
-    return s_live != 0;
-}
-
-template <int NT>
-__device__ __forceinline__ void ns_finish(const NsArgs& a, const StopState& ss, int it) {
-    if (blockIdx.x != 0) return;
-    const int tid = threadIdx.x;
-    for (int v = tid; v < a.nvol; v += NT) {
-        NsVolState& st = a.vstate[v];
-        const int ran = ss.stop[v] >= 0 ? ss.stop[v] + 1 : it;
-        st.iterations += (unsigned long long)ran;
-        st.parity = (int32_t)((a.parity0 + (uint32_t)ran) & 1u);
-        st.n_cur = ss.n[v];
-        st.streak = ss.streak[v];
-        st.done = a.conv_mode ? ss.done[v] : 0;
-    }
-    if (tid == 0) a.ctl->iters_run = (uint32_t)it;
-}
-
-// One block per brick (NT threads per brick), loads double buffered.
-template <int BX, int BY, int BZ, int NT>
-__global__ void __launch_bounds__(NT) k_ns_persistent(NsArgs a) {
-    using S = Brick<BX, BY, BZ>;
-    __shared__ NsSmem<S, NT> sm;
-    extern __shared__ int32_t s_dyn[];
-    StopState ss = stop_state(s_dyn, a.nvol);
-    const int tid = threadIdx.x;
-    const uint32_t G = gridDim.x;
-    __shared__ uint32_t s_gen;
-    if (tid == 0) {
-        mbar_init(&sm.bar[0], 1);
-        mbar_init(&sm.bar[1], 1);
-    }
-    ns_begin<NT>(a, ss, &s_gen);
     __syncthreads();
     uint32_t gen = s_gen;
     uint32_t mphase[2] = {0u, 0u};
-    int it = 0, ran = 0;
-    for (; it < a.max_iters; ++it) {
-        const uint32_t p = (a.parity0 + (uint32_t)it) & 1u;
-        const uint32_t nA = *(volatile uint32_t*)&a.ctl->nA;
-        const uint32_t nF = *(volatile uint32_t*)&a.ctl->nF;
-        ns_iteration_prologue<NT>(a, p);
+    int ran = 0;
+    uint64_t t0 = 0, t1 = 0;
+    int buf = 0;
+    for (int it = 0; it < a.max_iters; ++it) {
+        const uint32_t k = a.k0 + (uint32_t)it;
+        const uint32_t p = k & 1u, c3 = k % 3u, c3n = (k + 1u) % 3u;
+        const uint32_t* cur = a.bits[k % 4u];
+        const uint32_t* prev = a.bits[(k + 3u) % 4u];
+        const uint32_t sn = (k + 1u) % 4u, sz = (k + 2u) % 4u;
+        if (blockIdx.x == 0 && tid == 0) t0 = globaltimer_ns();
+        if (blockIdx.x == 0)
+            for (int v = tid; v < a.nvol; v += NT) a.cnt[c3n][v] = 0ull;
         BlockTally tally;
-        int buf = 0;
-        if (tid == 0 && blockIdx.x < nA) ns_issue_loads<S, NT>(a, sm, a.A_list[blockIdx.x], p, 0);
-        for (uint32_t w = blockIdx.x; w < nA; w += G) {
-            const uint32_t b = a.A_list[w];
-            if (tid == 0 && w + G < nA) ns_issue_loads<S, NT>(a, sm, a.A_list[w + G], p, buf ^ 1);
-            if (!ss.done[a.brick_vol[b]]) {
-                ns_process_brick<S, NT>(a, sm, b, p, buf, mphase, tally);
-            } else {
-                if (!mbar_wait(&sm.bar[buf], mphase[buf])) set_error(&a.ctl->err, ERR_TMA_TIMEOUT);
-                mphase[buf] ^= 1u;
-                __syncthreads();
+        // Ranks of the bricks to update (A_k) and to flush (A_{k-1} \ A_k):
+        // thread t counts the words t, t+NT, ...; ranks follow (thread, word).
+        uint32_t ca = 0, cf = 0;
+        for (uint32_t w = tid; w < a.NW; w += NT) {
+            const uint32_t c = cur[w];
+            ca += __popc(c);
+            cf += __popc(prev[w] & ~c);
+        }
+        uint64_t tot;
+        const uint64_t ex = block_exclusive_sum64(((uint64_t)cf << 32) | ca, &tot);
+        const uint32_t na = (uint32_t)tot, nfl = (uint32_t)(tot >> 32);
+        // Block i takes the ranks i, i+G, i+2G, ... of both kinds.
+        const uint32_t bi = blockIdx.x;
+        const uint32_t mya = na > bi ? (na - bi + G - 1) / G : 0u;
+        const uint32_t myf = nfl > bi ? (nfl - bi + G - 1) / G : 0u;
+        for (uint32_t c0 = 0; c0 < mya || c0 < myf; c0 += NT) {
+            // Chunk c0: this block's j-th brick for j in [c0, c0 + NT).
+            const uint32_t nw = min(mya - min(mya, c0), (uint32_t)NT);
+            const uint32_t nf = min(myf - min(myf, c0), (uint32_t)NT);
+            {
+                const uint32_t lo = bi + c0 * G;
+                const uint32_t hia = bi + (c0 + nw) * G, hif = bi + (c0 + nf) * G;
+                uint32_t ra = (uint32_t)ex, rf = (uint32_t)(ex >> 32);
+                for (uint32_t w = tid; w < a.NW; w += NT) {
+                    const uint32_t c = cur[w], f = prev[w] & ~c;
+                    const uint32_t pc = __popc(c), pf = __popc(f);
+                    // Ranks q of [ra, ra + pc) with q = bi (mod G) and q in [lo, hia).
+                    for (int kind = 0; kind < 2; ++kind) {
+                        const uint32_t r = kind ? rf : ra, n = kind ? pf : pc, hi = kind ? hif : hia;
+                        const uint32_t m0 = kind ? f : c;
+                        uint32_t q = max(r, lo);
+                        q = bi + (q - bi + G - 1) / G * G;
+                        for (; q < r + n && q < hi; q += G) {
+                            uint32_t m = m0;
+                            for (uint32_t s2 = q - r; s2; --s2) m &= m - 1u;
+                            const uint32_t b = w * 32u + (uint32_t)(__ffs(m) - 1);
+                            const uint32_t slot = (q - bi) / G - c0;
+                            const uint32_t e = ss.done[a.brick_vol[b]] ? kNoBrick : b;
+                            if (kind) s_flush[slot] = e; else s_work[slot] = e;
+                        }
+                    }
+                    ra += pc;
+                    rf += pf;
+                }
             }
-            buf ^= 1;
+            __syncthreads();
+            uint32_t q = 0;
+            while (q < nw && s_work[q] == kNoBrick) ++q;
+            if (q < nw) {
+                if (tid == 0) ns_issue_loads<S, NT>(a, sm, s_work[q], p, buf);
+                ns_fetch_mask<S, NT>(a, sm, s_work[q], p, buf);
+            }
+            while (q < nw) {
+                uint32_t q2 = q + 1;
+                while (q2 < nw && s_work[q2] == kNoBrick) ++q2;
+                if (q2 < nw) {
+                    if (tid == 0) ns_issue_loads<S, NT>(a, sm, s_work[q2], p, buf ^ 1);
+                    ns_fetch_mask<S, NT>(a, sm, s_work[q2], p, buf ^ 1);
+                }
+                ns_process_brick<S, NT>(a, sm, s_work[q], p, sn, buf, mphase, tally, a.cnt[c3]);
+                buf ^= 1;
+                q = q2;
+            }
+            for (uint32_t r = 0; r < nf; ++r)
+                if (s_flush[r] != kNoBrick) ns_flush_brick<S, NT>(a, s_flush[r], p);
+            __syncthreads();
         }
-        if (tid == 0) tally.flush(a.vstate);
-        for (uint32_t w = blockIdx.x; w < nF; w += G) {
-            const uint32_t b = a.F_list[w];
-            if (!ss.done[a.brick_vol[b]]) ns_flush_brick<S, NT>(a, b, p);
-        }
+        if (tid == 0) tally.flush(a.vstate, a.cnt[c3]);
+        for (uint32_t w = blockIdx.x * NT + tid; w < a.NW; w += G * NT) a.bits[sz][w] = 0u;
         if (tid == 0) {
             tma_store_wait_all();
             asm volatile("fence.proxy.async.global;" ::: "memory");
         }
-        if (!ns_iteration_epilogue<S::WORDS, NT>(a, ss, gen, p, it, &ran)) break;
-    }
-    if (it == a.max_iters) ran = it;
-    ns_finish<NT>(a, ss, ran);
-}
-
-// ---------------------------------------------------------------------------
-// One warp per brick: each warp owns a shared-memory slice and an mbarrier and
-// synchronises with __syncwarp only, so an SM keeps as many bricks in flight
-// as it holds warps.
-template <class S>
-struct WarpSmem {
-    alignas(128) float phi[S::TILE];
-    alignas(128) float img[S::VOX];
-    alignas(128) float out[S::VOX];
-    unsigned long long act[S::WORDS];
-    unsigned long long next[27 * S::WORDS];
-    uint32_t chg[S::CHG];
-    alignas(8) uint64_t bar;
-};
-
-template <class S>
-__device__ __forceinline__ void ns_process_brick_warp(const NsArgs& a, WarpSmem<S>& sm, uint32_t b,
-                                                      uint32_t p, uint32_t& mphase,
-                                                      BlockTally& tally) {
-    const int lane = threadIdx.x & 31;
-    const uint32_t v = a.brick_vol[b];
-    const NsVol& V = a.vols[v];
-    const int3 o = brick_origin<S>(V, b);
-    const int x0 = o.x, y0 = o.y, z0 = o.z;
-    unsigned long long* cur = a.masks[p] + (size_t)b * S::WORDS;
-    if (lane == 0) {
-        // The previous brick's store must have read its source before the
-        // update overwrites it.
-        asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-        mbar_expect_tx(&sm.bar, (uint32_t)(S::TILE + S::VOX) * 4u);
-        tma_load_3d(sm.phi, &a.tmaps[V.tmap_base + p], x0 - 4, y0 - 1, z0 - 1, &sm.bar);
-        tma_load_3d(sm.img, &a.tmaps[V.tmap_base + 4], x0, y0, z0, &sm.bar);
-    }
-    for (int t = lane; t < S::WORDS; t += 32) {
-        sm.act[t] = cur[t];
-        cur[t] = 0ull;
-    }
-    for (int t = lane; t < 27 * S::WORDS; t += 32) sm.next[t] = 0ull;
-    if (!mbar_wait(&sm.bar, mphase)) set_error(&a.ctl->err, ERR_TMA_TIMEOUT);
-    mphase ^= 1u;
-    __syncwarp();
-    float* phi = sm.phi;
-    const bool edge = x0 < 4 || y0 < 1 || z0 < 1 || x0 + S::X + 4 > V.nx || y0 + S::Y + 1 > V.ny ||
-                      z0 + S::Z + 1 > V.nz;
-    if (edge) {
-        for (int t = lane; t < S::TILE; t += 32) {
-            const int tx = t % S::TX, ty = (t / S::TX) % S::TY, tz = t / (S::TX * S::TY);
-            const int gx = x0 - 4 + tx, gy = y0 - 1 + ty, gz = z0 - 1 + tz;
-            const int cx = min(max(gx, 0), V.nx - 1), cy = min(max(gy, 0), V.ny - 1),
-                      cz = min(max(gz, 0), V.nz - 1);
-            if (cx != gx || cy != gy || cz != gz)
-                phi[t] = phi[((cz - z0 + 1) * S::TY + (cy - y0 + 1)) * S::TX + (cx - x0 + 4)];
-        }
-        __syncwarp();
-    }
-    const float* bias = V.bias;
-    bool any = false;
-#pragma unroll 2
-    for (int k = 0; k < S::CHG; ++k) {
-        const int j = lane + 32 * k;
-        const int lx = j % S::X, ly = (j / S::X) % S::Y, lz = j / (S::X * S::Y);
-        const int ti = ((lz + 1) * S::TY + (ly + 1)) * S::TX + (lx + 4);
-        const float c = phi[ti];
-        float nv = c;
-        bool chg = false;
-        if ((sm.act[j >> 6] >> (j & 63)) & 1ull) {
-            auto P = [&](int dx, int dy, int dz) { return phi[ti + (dz * S::TY + dy) * S::TX + dx]; };
-            float bb = 0.0f;
-            if (bias) bb = bias[((size_t)(z0 + lz) * V.py + (y0 + ly)) * V.px + (x0 + lx)];
-            nv = ns_update_f32(P, sm.img[j], bb, V);
-            chg = fabsf(nv - c) > V.thr_t;
-        }
-        sm.out[j] = nv;
-        const uint32_t bal = __ballot_sync(0xffffffffu, chg);
-        any |= bal != 0u;
-        if (lane == 0) sm.chg[k] = bal;
-    }
-    fence_proxy_async_smem();
-    __syncwarp();
-    if (lane == 0) {
-        tma_store_3d(&a.tmaps[V.tmap_base + 2 + (p ^ 1u)], x0, y0, z0, sm.out);
-        tma_store_commit();
-    }
-    if (any) {
-        const int EX = S::X + 2, EY = S::Y + 2;
-        for (int e = lane; e < S::EXT; e += 32) {
-            const int ex = e % EX - 1, ey = (e / EX) % EY - 1, ez = e / (EX * EY) - 1;
-            const int gx = x0 + ex, gy = y0 + ey, gz = z0 + ez;
-            if (gx < 0 || gy < 0 || gz < 0 || gx >= V.nx || gy >= V.ny || gz >= V.nz) continue;
-            bool hit = false;
-            if (V.nbh == 26) {
-                const int lo = max(ex - 1, 0), hi = min(ex + 1, S::X - 1);
-                if (lo <= hi) {
-                    const uint32_t m = ((1u << (hi - lo + 1)) - 1u) << lo;
-                    for (int dz = -1; dz <= 1 && !hit; ++dz) {
-                        const int z = ez + dz;
-                        if (z < 0 || z >= S::Z) continue;
-                        for (int dy = -1; dy <= 1; ++dy) {
-                            const int y = ey + dy;
-                            if (y < 0 || y >= S::Y) continue;
-                            if (chg_row<S>(sm.chg, y, z) & m) { hit = true; break; }
-                        }
-                    }
-                }
+        if (blockIdx.x == 0 && tid == 0) t1 = globaltimer_ns();
+        __syncthreads();
+        if (tid == 0) {
+            const uint32_t target = gen + 1;
+            __threadfence();
+            const uint32_t arrived = atomicAdd(&a.ctl->bar_count, 1u) + 1u;
+            if (arrived == G) {
+                a.ctl->bar_count = 0;
+                __threadfence();
+                asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(&a.ctl->bar_gen), "r"(target) : "memory");
             } else {
-                const bool in = ex >= 0 && ex < S::X && ey >= 0 && ey < S::Y && ez >= 0 && ez < S::Z;
-                if (in && chg_bit<S>(sm.chg, ex, ey, ez)) hit = true;
-                const int nb[6][3] = {{-1, 0, 0}, {1, 0, 0}, {0, -1, 0}, {0, 1, 0}, {0, 0, -1}, {0, 0, 1}};
-                for (int q = 0; q < 6 && !hit; ++q) {
-                    const int x = ex + nb[q][0], y = ey + nb[q][1], z = ez + nb[q][2];
-                    if (x >= 0 && x < S::X && y >= 0 && y < S::Y && z >= 0 && z < S::Z &&
-                        chg_bit<S>(sm.chg, x, y, z))
-                        hit = true;
+                const uint64_t w0 = globaltimer_ns();
+                uint32_t ns = 16;
+                while (ld_acquire_u32(&a.ctl->bar_gen) != target) {
+                    if (globaltimer_ns() - w0 > kWaitLimitNs) {
+                        set_error(&a.ctl->err, ERR_BARRIER_TIMEOUT);
+                        break;
+                    }
+                    __nanosleep(ns);
+                    if (ns < 256) ns <<= 1;
                 }
             }
-            if (!hit) continue;
-            const int ox = ex < 0 ? -1 : (ex >= S::X ? 1 : 0);
-            const int oy = ey < 0 ? -1 : (ey >= S::Y ? 1 : 0);
-            const int oz = ez < 0 ? -1 : (ez >= S::Z ? 1 : 0);
-            const int lx = ex - ox * S::X, ly = ey - oy * S::Y, lz = ez - oz * S::Z;
-            const int jj = (lz * S::Y + ly) * S::X + lx;
-            const int slot = (oz + 1) * 9 + (oy + 1) * 3 + (ox + 1);
-            atomicOr(&sm.next[slot * S::WORDS + (jj >> 6)], 1ull << (jj & 63));
-        }
-        __syncwarp();
-        for (int t = lane; t < 27 * S::WORDS; t += 32) {
-            const unsigned long long w = sm.next[t];
-            if (!w) continue;
-            const int slot = t / S::WORDS, word = t % S::WORDS;
-            const int ox = slot % 3 - 1, oy = (slot / 3) % 3 - 1, oz = slot / 9 - 1;
-            const uint32_t nb = b + (int32_t)((oz * V.nby + oy) * V.nbx + ox);
-            atomicOr(&a.masks[p ^ 1u][(size_t)nb * S::WORDS + word], w);
-            atomicOr(&a.bits[p ^ 1u][nb >> 5], 1u << (nb & 31));
-        }
-    }
-    if (lane == 0) {
-        unsigned long long n = 0;
-        for (int w = 0; w < S::WORDS; ++w) n += __popcll(sm.act[w]);
-        tally.add(a.vstate, v, n);
-    }
-    __syncwarp();
-}
-
-template <class S>
-__device__ __forceinline__ void ns_flush_brick_warp(const NsArgs& a, uint32_t b, uint32_t p) {
-    const NsVol& V = a.vols[a.brick_vol[b]];
-    const int3 o = brick_origin<S>(V, b);
-    const float* src = V.phi[p];
-    float* dst = V.phi[p ^ 1u];
-    constexpr int Q = S::X / 4;
-    for (int t = threadIdx.x & 31; t < S::Y * S::Z * Q; t += 32) {
-        const int q = t % Q, ly = (t / Q) % S::Y, lz = t / (Q * S::Y);
-        const size_t off = ((size_t)(o.z + lz) * V.py + (o.y + ly)) * V.px + o.x + 4 * q;
-        *reinterpret_cast<float4*>(dst + off) = *reinterpret_cast<const float4*>(src + off);
-    }
-}
-
-template <class S>
-__host__ __device__ constexpr size_t warp_smem_offset(int nvol) {
-    return (stop_state_bytes(nvol) + 127) / 128 * 128 + 128;  // + slack for base alignment
-}
-
-// NT/32 warps per block, one brick per warp at a time.
-template <int BX, int BY, int BZ, int NT>
-__global__ void __launch_bounds__(NT) k_ns_persistent_warp(NsArgs a) {
-    using S = Brick<BX, BY, BZ>;
-    constexpr int W = NT / 32;
-    extern __shared__ __align__(128) unsigned char s_raw[];
-    StopState ss = stop_state(reinterpret_cast<int32_t*>(s_raw), a.nvol);
-    uintptr_t wb = reinterpret_cast<uintptr_t>(s_raw) + (stop_state_bytes(a.nvol) + 127) / 128 * 128;
-    wb = (wb + 127) & ~(uintptr_t)127;
-    WarpSmem<S>* wsm = reinterpret_cast<WarpSmem<S>*>(wb);
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    WarpSmem<S>& sm = wsm[warp];
-    const uint32_t GW = gridDim.x * W;
-    const uint32_t gw = blockIdx.x * W + warp;
-    __shared__ uint32_t s_gen;
-    if (lane == 0) mbar_init(&sm.bar, 1);
-    ns_begin<NT>(a, ss, &s_gen);
-    __syncthreads();
-    uint32_t gen = s_gen;
-    uint32_t mphase = 0;
-    int it = 0, ran = 0;
-    for (; it < a.max_iters; ++it) {
-        const uint32_t p = (a.parity0 + (uint32_t)it) & 1u;
-        const uint32_t nA = *(volatile uint32_t*)&a.ctl->nA;
-        const uint32_t nF = *(volatile uint32_t*)&a.ctl->nF;
-        ns_iteration_prologue<NT>(a, p);
-        BlockTally tally;
-        for (uint32_t w = gw; w < nA; w += GW) {
-            const uint32_t b = a.A_list[w];
-            if (!ss.done[a.brick_vol[b]]) ns_process_brick_warp<S>(a, sm, b, p, mphase, tally);
-        }
-        if (lane == 0) tally.flush(a.vstate);
-        for (uint32_t w = gw; w < nF; w += GW) {
-            const uint32_t b = a.F_list[w];
-            if (!ss.done[a.brick_vol[b]]) ns_flush_brick_warp<S>(a, b, p);
-        }
-        if (lane == 0) {
-            tma_store_wait_all();
+            gen = target;
             asm volatile("fence.proxy.async.global;" ::: "memory");
+            if (blockIdx.x == 0) {
+                const uint64_t t2 = globaltimer_ns();
+                a.ctl->t_phase1_ns += t1 - t0;
+                a.ctl->t_barrier_ns += t2 - t1;
+            }
         }
-        if (!ns_iteration_epilogue<S::WORDS, NT>(a, ss, gen, p, it, &ran)) break;
+        __syncthreads();
+        if (*(volatile uint32_t*)&a.ctl->err) { ran = it; break; }
+        // Stopping rule, evaluated identically by every block.
+        if (tid == 0) s_live = 0;
+        __syncthreads();
+        for (int v = tid; v < a.nvol; v += NT) {
+            if (ss.done[v]) continue;
+            const unsigned long long n = *(volatile unsigned long long*)&a.cnt[c3][v];
+            ss.n[v] = n;
+            bool stop;
+            if (a.conv_mode) {
+                const unsigned long long n0 = a.vstate[v].n0;
+                ss.streak[v] = ((double)n < a.rel * (double)n0) ? ss.streak[v] + 1 : 0;
+                stop = ss.streak[v] >= a.patience || n <= a.abs_thr || it + 1 >= a.max_iters;
+            } else {
+                stop = it + 1 >= a.max_iters;
+            }
+            if (stop) {
+                ss.done[v] = 1;
+                ss.stop[v] = it;
+            } else {
+                atomicAdd(&s_live, 1);
+            }
+        }
+        __syncthreads();
+        ran = it + 1;
+        if (s_live == 0) break;
     }
-    if (it == a.max_iters) ran = it;
-    ns_finish<NT>(a, ss, ran);
+    if (blockIdx.x == 0) {
+        for (int v = tid; v < a.nvol; v += NT) {
+            NsVolState& st = a.vstate[v];
+            const int r = ss.stop[v] >= 0 ? ss.stop[v] + 1 : ran;
+            st.iterations += (unsigned long long)r;
+            st.parity = (int32_t)((a.k0 + (uint32_t)r) & 1u);
+            st.n_cur = ss.n[v];
+            st.streak = ss.streak[v];
+            st.done = a.conv_mode ? ss.done[v] : 0;
+        }
+        if (tid == 0) a.ctl->iters_run = (uint32_t)ran;
+    }
 }
 
 // Initial active set of every brick: voxels whose 6-neighbours differ by more
-// than thr_s (clamped coordinates), one block per brick.
+// than thr_s (clamped coordinates), one block per brick; bricks with a
+// non-empty mask get their membership bit in bits[s].  Counts land in cnt[0].
 template <int BX, int BY, int BZ, int NT>
-__global__ void __launch_bounds__(NT) k_ns_init_active(NsArgs a, uint32_t p) {
+__global__ void __launch_bounds__(NT) k_ns_init_active(NsArgs a, uint32_t p, uint32_t s) {
     using S = Brick<BX, BY, BZ>;
     __shared__ uint32_t s_w[S::CHG];
     for (uint32_t b = blockIdx.x; b < a.NB; b += gridDim.x) {
-        const NsVol& V = a.vols[a.brick_vol[b]];
-        const uint32_t lb = b - V.brick_base;
-        const int kx = lb % V.nbx, ky = (lb / V.nbx) % V.nby, kz = lb / (V.nbx * V.nby);
+        const uint32_t v = a.brick_vol[b];
+        const NsVol& V = a.vols[v];
+        const int3 o = brick_origin<S>(V, b);
         const float* ph = V.phi[p];
         constexpr int VPT = (S::VOX + NT - 1) / NT;
         for (int k = 0; k < VPT; ++k) {
             const int j = threadIdx.x + k * NT;
             bool act = false;
             if (j < S::VOX) {
-                const int x = kx * S::X + j % S::X, y = ky * S::Y + (j / S::X) % S::Y,
-                          z = kz * S::Z + j / (S::X * S::Y);
+                const int x = o.x + j % S::X, y = o.y + (j / S::X) % S::Y, z = o.z + j / (S::X * S::Y);
                 if (x < V.nx && y < V.ny && z < V.nz) {
                     auto at = [&](int xx, int yy, int zz) {
                         xx = min(max(xx, 0), V.nx - 1);
@@ -893,20 +692,70 @@ __global__ void __launch_bounds__(NT) k_ns_init_active(NsArgs a, uint32_t p) {
             if ((threadIdx.x & 31) == 0 && word < S::CHG) s_w[word] = bal;
         }
         __syncthreads();
-        if (threadIdx.x < S::WORDS) {
-            const unsigned long long w =
-                (unsigned long long)s_w[2 * threadIdx.x] | ((unsigned long long)s_w[2 * threadIdx.x + 1] << 32);
-            a.masks[p][(size_t)b * S::WORDS + threadIdx.x] = w;
-            if (w) atomicOr(&a.bits[p][b >> 5], 1u << (b & 31));
+        if (threadIdx.x == 0) {
+            unsigned long long n = 0;
+            for (int q = 0; q < S::WORDS; ++q) {
+                const unsigned long long w =
+                    (unsigned long long)s_w[2 * q] | ((unsigned long long)s_w[2 * q + 1] << 32);
+                a.masks[p][(size_t)b * S::WORDS + q] = w;
+                n += __popcll(w);
+            }
+            if (n) {
+                atomicOr(&a.bits[s][b >> 5], 1u << (b & 31));
+                atomicAdd(&a.cnt[0][v], n);
+            }
         }
         __syncthreads();
     }
 }
 
-// List construction from bits[p] (no F list, bits kept).
-template <int WORDS, int NT>
-__global__ void __launch_bounds__(NT) k_ns_build_list(NsArgs a, uint32_t p) {
-    ns_scan<WORDS, NT>(a, a.bits[p], nullptr, a.masks[p], a.cnt[p], nullptr);
+// The active voxels of the current set in brick-major order: a single-pass
+// decoupled-lookback compaction over the membership bits of slot s (tiles of
+// NT bit words = 32*NT bricks); per brick the voxel count is popc of its
+// mask.  Writes volume-local linear indices (x + nx*(y + ny*z)) and, from the
+// last tile, the total count.
+template <int BX, int BY, int BZ, int NT>
+__global__ void __launch_bounds__(NT) k_ns_emit(NsArgs a, uint32_t p, uint32_t s, uint64_t* out,
+                                               unsigned long long* total_out) {
+    using S = Brick<BX, BY, BZ>;
+    __shared__ uint32_t s_tile;
+    const uint32_t ntiles = (a.NW + NT - 1) / NT;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(&a.ctl->emit_tile, 1u);
+        __syncthreads();
+        const uint32_t tile = s_tile;
+        __syncthreads();
+        if (tile >= ntiles) break;
+        const uint32_t w = tile * NT + threadIdx.x;
+        const uint32_t bw = w < a.NW ? a.bits[s][w] : 0u;
+        unsigned long long cnt = 0;
+        for (uint32_t m = bw; m; m &= m - 1) {
+            const uint32_t b = w * 32 + (__ffs(m) - 1);
+            for (int q = 0; q < S::WORDS; ++q) cnt += __popcll(a.masks[p][(size_t)b * S::WORDS + q]);
+        }
+        uint64_t total;
+        const uint64_t excl = block_exclusive_sum64(cnt, &total);
+        const uint64_t prefix = tile_exclusive_prefix(a.status, tile, total, &a.ctl->err);
+        uint64_t o = prefix + excl;
+        for (uint32_t m = bw; m; m &= m - 1) {
+            const uint32_t b = w * 32 + (__ffs(m) - 1);
+            const NsVol& V = a.vols[a.brick_vol[b]];
+            const int3 og = brick_origin<S>(V, b);
+            for (int q = 0; q < S::WORDS; ++q) {
+                unsigned long long mm = a.masks[p][(size_t)b * S::WORDS + q];
+                while (mm) {
+                    const int bit = __ffsll(mm) - 1;
+                    mm &= mm - 1;
+                    const int j = q * 64 + bit;
+                    const uint64_t x = og.x + j % S::X, y = og.y + (j / S::X) % S::Y,
+                                   z = og.z + j / (S::X * S::Y);
+                    if (out) out[o] = (z * V.ny + y) * V.nx + x;
+                    ++o;
+                }
+            }
+        }
+        if (tile == ntiles - 1 && threadIdx.x == 0) *total_out = prefix + total;
+    }
 }
 
 }  // namespace lss

@@ -265,6 +265,7 @@ def run_ours(args, ws, rank, local):
                        "iterations_to_converge": iters[-1],
                        "converge_ms": sparse_ms,
                        "brick": [st["brick_x"], st["brick_y"], st["brick_z"]],
+                       "block0_update_ms": st["update_ms"], "block0_barrier_ms": st["barrier_ms"],
                        "threads_per_brick": st["threads_per_brick"],
                        "l2": "flushed between steps (256 MiB write); volume 192 MiB > L2",
                        "parallelism": "replicas" if ws > 1 else "single"},
@@ -294,7 +295,7 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--brick", type=int, nargs=3, default=None)
     ap.add_argument("--threads", type=int, default=0)
-    ap.add_argument("--ref-iters", type=int, default=40)
+    ap.add_argument("--ref-iters", type=int, default=150)
     ap.add_argument("--dense-iters", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

@@ -126,6 +126,9 @@ typedef struct lss_stats {
     uint32_t brick_x, brick_y, brick_z, threads_per_brick;
     int32_t  mode;
     int32_t  error_flags;          /* device-side error word (timeouts, bounds)      */
+    double   update_ms;            /* NS: time of the last launch's block 0 in brick
+                                      work (updates, flushes) ...                    */
+    double   barrier_ms;           /* ... and waiting at the grid barrier            */
 } lss_stats;
 
 /* ---- construction / teardown ------------------------------------------ */

@@ -172,17 +172,19 @@ uint64_t ons_step(void* h, int k) {
     return o->active.size();
 }
 
-// Runs to the stopping rule: n < rel*n0 for `patience` consecutive
-// iterations, n <= abs_thr, or max_it; returns the iterations run.
+// Runs to the stopping rule, evaluated after each iteration on n_k, the
+// number of active voxels that iteration updated: stop once n_k < rel*n0 for
+// `patience` consecutive iterations, once n_k <= abs_thr, or after max_it
+// iterations.  Returns the iterations run.
 int ons_run(void* h, double rel, int patience, int max_it, uint64_t abs_thr) {
     NsOracle* o = (NsOracle*)h;
     int streak = 0, it = 0;
     while (it < max_it) {
-        if (o->active.size() <= abs_thr) break;
-        size_t n = o->step();
+        const size_t n = o->active.size();
+        o->step();
         ++it;
         if ((double)n < rel * (double)o->n0) ++streak; else streak = 0;
-        if (streak >= patience) break;
+        if (streak >= patience || n <= abs_thr) break;
     }
     return it;
 }
