@@ -309,6 +309,9 @@ void NsCore::upload_descriptors() {
         o.lo = v.p.phi_min; o.hi = v.p.phi_max;
         o.thr_t = v.p.temporal_threshold; o.thr_s = v.p.spatial_threshold;
         o.alpha_data = v.p.alpha_role == LSS_ALPHA_CURVATURE ? 0 : 1;
+        o.inv_eps = 1.0f / v.p.window;
+        o.wc = o.alpha_data ? 1.0f - v.p.curvature : v.p.curvature;
+        o.wd = 1.0f - o.wc;
         o.nbh = v.p.neighbourhood == 6 ? 6 : 26;
         o.tmap_base = (uint32_t)(5 * i);
     }

@@ -53,7 +53,9 @@ struct NsVol {
     int32_t alpha_data;     // 1: alpha weights the data term, 0: the curvature term
     int32_t nbh;            // 26 or 6
     uint32_t tmap_base;     // 5 maps: phi0 halo-load, phi1 halo-load, phi0 store, phi1 store, img
-    int32_t pad;
+    float inv_eps;          // 1 / eps
+    float wc, wd;           // curvature and data weights (from alpha and alpha_data)
+    int32_t pad[2];
 };
 
 struct NsVolState {
@@ -65,12 +67,26 @@ struct NsVolState {
     int32_t streak, done, parity, pad;
 };
 
+// Grid-barrier words.  Arrival: blocks arrived (low 16 bits) + voxel updates
+// of the iteration summed over the blocks (high 48 bits), so the last block
+// to arrive knows the iteration's count without another memory round trip.
+// Release (own 128-byte line, polled): generation (low 32 bits) | streak of
+// the stopping rule (bits 32..47) | stop flag (bit 48).
+constexpr int kArriveShift = 16;
+constexpr uint64_t kArriveMask = (1ull << kArriveShift) - 1ull;
+constexpr int kRelStreakShift = 32;
+constexpr uint64_t kRelStop = 1ull << 48;
+
 struct NsCtl {
+    unsigned long long bar_arrive;
+    unsigned long long n_last;  // updates of the last iteration (one-volume path)
     uint32_t err;
-    uint32_t bar_count, bar_gen;
-    uint32_t iters_run;       // iterations run by the last launch
-    uint32_t emit_tile;       // tile counter of the voxel-list emission
+    uint32_t iters_run;         // iterations run by the last launch
+    uint32_t emit_tile;         // tile counter of the voxel-list emission
+    uint32_t pad;
     unsigned long long t_phase1_ns, t_barrier_ns;  // block 0's time split
+    alignas(128) unsigned long long bar_release;
+    unsigned long long pad2[15];
 };
 
 struct NsArgs {
@@ -129,13 +145,12 @@ __device__ __forceinline__ float ns_update_f32(PF P, float I, float bias, const 
         const float num = fxx * (cy * cy + cz * cz) + fyy * (cx * cx + cz * cz) +
                           fzz * (cx * cx + cy * cy) -
                           2.0f * (cx * cy * fxy + cx * cz * fxz + cy * cz * fyz);
-        curv = num / g2;
+        curv = __fdividef(num, g2);  // g2 in (1e-12, 48]: within 2 ulp
     }
-    float D = (V.eps - fabsf(I - V.T)) / V.eps;
+    float D = (V.eps - fabsf(I - V.T)) * V.inv_eps;
     D = fminf(fmaxf(D, -1.0f), 1.0f) + bias;
-    const float wc = V.alpha_data ? 1.0f - V.alpha : V.alpha;
-    const float wd = 1.0f - wc;
-    const float F = wd * D;
+    const float wc = V.wc;
+    const float F = V.wd * D;
     const float dxm = c - xm, dxp = xp - c, dym = c - ym, dyp = yp - c, dzm = c - zm, dzp = zp - c;
     float g;
     if (F > 0.0f) {
@@ -161,7 +176,9 @@ struct NsSmem {
     alignas(128) float img[2][S::VOX];
     alignas(128) float out[2][S::VOX];
     unsigned long long act[2][S::WORDS];     // the brick's active mask, double buffered
-    uint32_t chg[S::CHG];
+    uint32_t chg[S::CHG];                    // changed voxels of the brick (bits)
+    uint16_t list[S::VOX];                   // active voxels of the brick, compacted
+    uint8_t chgb[S::VOX];                    // changed voxels of the brick (bytes)
     alignas(8) uint64_t bar[2];
 };
 
@@ -194,15 +211,17 @@ struct BitGeo {
 template <class S>
 __host__ __device__ __forceinline__ uint64_t dil_x(uint64_t v, int o) {
     using G = BitGeo<S>;
-    if (o == 0) return v | ((v & ~G::CXL) << 1) | ((v & ~G::CX0) >> 1);
-    return o < 0 ? (v & G::CX0) << (S::X - 1) : (v & G::CXL) >> (S::X - 1);
+    const uint64_t d0 = v | ((v & ~G::CXL) << 1) | ((v & ~G::CX0) >> 1);
+    const uint64_t dm = (v & G::CX0) << (S::X - 1), dp = (v & G::CXL) >> (S::X - 1);
+    return o == 0 ? d0 : (o < 0 ? dm : dp);
 }
 
 template <class S>
 __host__ __device__ __forceinline__ uint64_t dil_y(uint64_t v, int o) {
     using G = BitGeo<S>;
-    if (o == 0) return v | ((v & ~G::RYL) << S::X) | ((v & ~G::RY0) >> S::X);
-    return o < 0 ? (v & G::RY0) << (S::X * (S::Y - 1)) : (v & G::RYL) >> (S::X * (S::Y - 1));
+    const uint64_t d0 = v | ((v & ~G::RYL) << S::X) | ((v & ~G::RY0) >> S::X);
+    const uint64_t dm = (v & G::RY0) << (S::X * (S::Y - 1)), dp = (v & G::RYL) >> (S::X * (S::Y - 1));
+    return o == 0 ? d0 : (o < 0 ? dm : dp);
 }
 
 // z step over the whole mask (in place).
@@ -247,6 +266,40 @@ __host__ __device__ __forceinline__ void dilate_slot(uint64_t (&m)[S::WORDS], in
     }
 }
 
+// Word w of dilate_slot's result, from the changed mask given as 32-bit
+// words (chg[2q] | chg[2q+1] << 32 is mask word q).  With one z-plane a word,
+// word w of the neighbour depends on planes w-1, w, w+1 only, so the 27 x
+// WORDS words are computed by independent threads.
+template <class S>
+__host__ __device__ __forceinline__ uint64_t dilate_word(const uint32_t* chg, int ox, int oy, int oz, int w,
+                                                         int nbh) {
+    auto W = [&](int q) -> uint64_t { return (uint64_t)chg[2 * q] | ((uint64_t)chg[2 * q + 1] << 32); };
+    if constexpr (S::WORDS == 1) {
+        uint64_t m[1] = {W(0)};
+        dilate_slot<S>(m, ox, oy, oz, nbh);
+        return m[0];
+    } else {
+        if (nbh == 6) {
+            if ((ox != 0) + (oy != 0) + (oz != 0) > 1) return 0ull;
+            if (oz) return oz < 0 ? (w == S::WORDS - 1 ? W(0) : 0ull) : (w == 0 ? W(S::WORDS - 1) : 0ull);
+            const uint64_t c = W(w);
+            if (ox) return dil_x<S>(c, ox);
+            if (oy) return dil_y<S>(c, oy);
+            uint64_t r = dil_x<S>(c, 0) | dil_y<S>(c, 0);
+            if (w > 0) r |= W(w - 1);
+            if (w + 1 < S::WORDS) r |= W(w + 1);
+            return r;
+        }
+        auto xy = [&](uint64_t c) { return dil_y<S>(dil_x<S>(c, ox), oy); };
+        if (oz < 0) return w == S::WORDS - 1 ? xy(W(0)) : 0ull;
+        if (oz > 0) return w == 0 ? xy(W(S::WORDS - 1)) : 0ull;
+        uint64_t r = xy(W(w));
+        if (w > 0) r |= xy(W(w - 1));
+        if (w + 1 < S::WORDS) r |= xy(W(w + 1));
+        return r;
+    }
+}
+
 // Voxels of a brick inside the volume when only the first lim_x, lim_y,
 // lim_z voxels of each axis are (the far edge of the volume), for word w.
 template <class S>
@@ -274,8 +327,8 @@ __device__ __forceinline__ int3 brick_origin(const NsVol& V, uint32_t b) {
 // into buffer `buf` (thread 0 only).
 template <class S, int NT>
 __device__ __forceinline__ void ns_issue_loads(const NsArgs& a, NsSmem<S, NT>& sm, uint32_t b,
-                                               uint32_t p, int buf) {
-    const NsVol& V = a.vols[a.brick_vol[b]];
+                                               uint32_t p, int buf, const NsVol* vone) {
+    const NsVol& V = vone ? *vone : a.vols[a.brick_vol[b]];
     const int3 o = brick_origin<S>(V, b);
     mbar_expect_tx(&sm.bar[buf], (uint32_t)(S::TILE + S::VOX) * 4u);
     tma_load_3d(sm.phi[buf], &a.tmaps[V.tmap_base + p], o.x - 4, o.y - 1, o.z - 1, &sm.bar[buf]);
@@ -284,9 +337,11 @@ __device__ __forceinline__ void ns_issue_loads(const NsArgs& a, NsSmem<S, NT>& s
 
 // Per-block running totals of updated voxels and bricks of one volume,
 // flushed with one atomic each when the volume changes or the phase ends.
+// `iter` sums the block's updates over all volumes of the iteration.  cnt
+// may be null (one volume: the count travels with the barrier arrival).
 struct BlockTally {
     uint32_t v = 0xFFFFFFFFu;
-    unsigned long long upd = 0, brk = 0;
+    unsigned long long upd = 0, brk = 0, iter = 0;
     __device__ void add(NsVolState* vs, unsigned long long* cnt, uint32_t vol, unsigned long long n) {
         if (vol != v) {
             flush(vs, cnt);
@@ -294,12 +349,13 @@ struct BlockTally {
         }
         upd += n;
         brk += 1;
+        iter += n;
     }
     __device__ void flush(NsVolState* vs, unsigned long long* cnt) {
         if (v != 0xFFFFFFFFu && brk) {
             atomicAdd(&vs[v].updates, upd);
             atomicAdd(&vs[v].bricks, brk);
-            atomicAdd(&cnt[v], upd);
+            if (cnt) atomicAdd(&cnt[v], upd);
         }
         upd = brk = 0;
     }
@@ -318,13 +374,16 @@ __device__ __forceinline__ void ns_fetch_mask(const NsArgs& a, NsSmem<S, NT>& sm
     }
 }
 
+// vone: the volume descriptor in shared memory when the launch has one
+// volume (else null: descriptors are read per brick).
 template <class S, int NT>
 __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>& sm, uint32_t b,
                                                  uint32_t p, uint32_t sn, int buf, uint32_t* mphase,
-                                                 BlockTally& tally, unsigned long long* cnt) {
+                                                 BlockTally& tally, unsigned long long* cnt,
+                                                 const NsVol* vone) {
     const int tid = threadIdx.x;
-    const uint32_t v = a.brick_vol[b];
-    const NsVol& V = a.vols[v];
+    const uint32_t v = vone ? 0u : a.brick_vol[b];
+    const NsVol& V = vone ? *vone : a.vols[v];
     const int3 o = brick_origin<S>(V, b);
     const int x0 = o.x, y0 = o.y, z0 = o.z;
     const unsigned long long* act = sm.act[buf];
@@ -349,81 +408,106 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
         __syncthreads();
     }
     float* out = sm.out[buf];
+    auto tile_index = [](int j) {
+        const int lx = j % S::X, ly = (j / S::X) % S::Y, lz = j / (S::X * S::Y);
+        return ((lz + 1) * S::TY + (ly + 1)) * S::TX + (lx + 4);
+    };
+    // Pass 1: copy the brick (inactive voxels keep phi) and compact the active
+    // voxels, ranked in brick order, into list[].
+    uint32_t nact = 0;
+#pragma unroll
+    for (int w = 0; w < S::WORDS; ++w) nact += __popcll(act[w]);
     constexpr int VPT = (S::VOX + NT - 1) / NT;
+#pragma unroll
+    for (int k = 0; k < VPT; ++k) {
+        const int j = tid + k * NT;
+        if (j < S::VOX) {
+            out[j] = phi[tile_index(j)];
+            sm.chgb[j] = 0;
+            const int w = j >> 6, bit = j & 63;
+            const uint64_t aw = act[w];
+            if ((aw >> bit) & 1ull) {
+                uint32_t r = __popcll(aw & ((1ull << bit) - 1ull));
+                for (int q = 0; q < w; ++q) r += __popcll(act[q]);
+                sm.list[r] = (uint16_t)j;
+            }
+        }
+    }
+    __syncthreads();
+    // Pass 2: update the active voxels, densely packed over the threads.
     const float* bias = V.bias;
+    for (uint32_t i = tid; i < nact; i += NT) {
+        const int j = sm.list[i];
+        const int ti = tile_index(j);
+        auto P = [&](int dx, int dy, int dz) { return phi[ti + (dz * S::TY + dy) * S::TX + dx]; };
+        float bb = 0.0f;
+        if (bias) {
+            const int lx = j % S::X, ly = (j / S::X) % S::Y, lz = j / (S::X * S::Y);
+            bb = bias[((size_t)(z0 + lz) * V.py + (y0 + ly)) * V.px + (x0 + lx)];
+        }
+        const float c = phi[ti];
+        const float nv = ns_update_f32(P, sm.img[buf][j], bb, V);
+        out[j] = nv;
+        sm.chgb[j] = fabsf(nv - c) > V.thr_t;
+    }
+    fence_proxy_async_smem();
+    __syncthreads();
+    // Pass 3: changed bytes -> bit words (warp ballots).
     bool anyl = false;
 #pragma unroll
     for (int k = 0; k < VPT; ++k) {
         const int j = tid + k * NT;
-        bool chg = false;
-        if (j < S::VOX) {
-            const int lx = j % S::X, ly = (j / S::X) % S::Y, lz = j / (S::X * S::Y);
-            const int ti = ((lz + 1) * S::TY + (ly + 1)) * S::TX + (lx + 4);
-            const float c = phi[ti];
-            float nv = c;
-            if ((act[j >> 6] >> (j & 63)) & 1ull) {
-                auto P = [&](int dx, int dy, int dz) { return phi[ti + (dz * S::TY + dy) * S::TX + dx]; };
-                float bb = 0.0f;
-                if (bias) bb = bias[((size_t)(z0 + lz) * V.py + (y0 + ly)) * V.px + (x0 + lx)];
-                nv = ns_update_f32(P, sm.img[buf][j], bb, V);
-                chg = fabsf(nv - c) > V.thr_t;
-            }
-            out[j] = nv;
-        }
-        const uint32_t bal = __ballot_sync(0xffffffffu, chg);
+        const uint32_t bal = __ballot_sync(0xffffffffu, j < S::VOX && sm.chgb[j]);
         anyl |= bal != 0u;
         const int word = (tid >> 5) + k * (NT / 32);
         if ((tid & 31) == 0 && word < S::CHG) sm.chg[word] = bal;
     }
-    fence_proxy_async_smem();
     const int any = __syncthreads_or(anyl ? 1 : 0);
     if (tid == 0) {
         tma_store_3d(&a.tmaps[V.tmap_base + 2 + (p ^ 1u)], x0, y0, z0, out);
         tma_store_commit();
+        tally.add(a.vstate, cnt, v, nact);
     }
     // Dilation of the changed mask into the 27 bricks around (and including)
-    // b: lane L of warp 0 computes the part for neighbour L and ORs it into
-    // the next masks and membership bits (reductions, no round trip).
-    if (any && tid < 27) {
-        const int ox = tid % 3 - 1, oy = (tid / 3) % 3 - 1, oz = tid / 9 - 1;
-        const int bx = x0 / S::X + ox, by = y0 / S::Y + oy, bz = z0 / S::Z + oz;
-        // Voxels of the neighbour inside the volume along each axis (bricks
-        // in the padding beyond the volume hold none).
-        const int lx = V.nx - bx * S::X, ly = V.ny - by * S::Y, lz = V.nz - bz * S::Z;
-        const bool six_skip = V.nbh == 6 && (ox != 0) + (oy != 0) + (oz != 0) > 1;
-        if (!six_skip && bx >= 0 && by >= 0 && bz >= 0 && lx > 0 && ly > 0 && lz > 0) {
-            uint64_t m[S::WORDS];
+    // b: thread t computes word t % WORDS of neighbour t / WORDS and ORs it
+    // into the next masks; one thread per neighbour sets its membership bit
+    // (reductions, no round trip).
+    if (any) {
+        constexpr int ROUNDS = (27 * S::WORDS + NT - 1) / NT;
 #pragma unroll
-            for (int w = 0; w < S::WORDS; ++w)
-                m[w] = (uint64_t)sm.chg[2 * w] | ((uint64_t)sm.chg[2 * w + 1] << 32);
-            dilate_slot<S>(m, ox, oy, oz, V.nbh);
-            const bool clip = lx < S::X || ly < S::Y || lz < S::Z;
-            const uint32_t nb = b + (int32_t)((oz * V.nby + oy) * V.nbx + ox);
-            bool hit = false;
-#pragma unroll
-            for (int w = 0; w < S::WORDS; ++w) {
-                uint64_t x = m[w];
-                if (clip) x &= inside_mask<S>(w, min(lx, S::X), min(ly, S::Y), min(lz, S::Z));
-                if (x) {
-                    atomicOr(&a.masks[p ^ 1u][(size_t)nb * S::WORDS + w], (unsigned long long)x);
-                    hit = true;
+        for (int r = 0; r < ROUNDS; ++r) {
+            const int t = tid + r * NT;
+            const int slot = t / S::WORDS, w = t % S::WORDS;
+            uint64_t x = 0ull;
+            uint32_t nb = 0;
+            if (slot < 27) {
+                const int ox = slot % 3 - 1, oy = (slot / 3) % 3 - 1, oz = slot / 9 - 1;
+                const int bx = x0 / S::X + ox, by = y0 / S::Y + oy, bz = z0 / S::Z + oz;
+                // Voxels of the neighbour inside the volume along each axis
+                // (bricks in the padding beyond the volume hold none).
+                const int lx = V.nx - bx * S::X, ly = V.ny - by * S::Y, lz = V.nz - bz * S::Z;
+                if (bx >= 0 && by >= 0 && bz >= 0 && lx > 0 && ly > 0 && lz > 0) {
+                    x = dilate_word<S>(sm.chg, ox, oy, oz, w, V.nbh);
+                    if (lx < S::X || ly < S::Y || lz < S::Z)
+                        x &= inside_mask<S>(w, min(lx, S::X), min(ly, S::Y), min(lz, S::Z));
+                    nb = b + (int32_t)((oz * V.nby + oy) * V.nbx + ox);
+                    if (x) atomicOr(&a.masks[p ^ 1u][(size_t)nb * S::WORDS + w], (unsigned long long)x);
                 }
             }
-            if (hit) atomicOr(&a.bits[sn][nb >> 5], 1u << (nb & 31));
+            // The WORDS threads of a neighbour are adjacent lanes of one warp.
+            const uint32_t bal = __ballot_sync(0xffffffffu, x != 0ull);
+            const int lane = tid & 31, g0 = lane & ~(S::WORDS - 1);
+            const uint32_t gmask = (S::WORDS >= 32 ? 0xffffffffu : ((1u << S::WORDS) - 1u)) << g0;
+            if (lane == g0 && (bal & gmask)) atomicOr(&a.bits[sn][nb >> 5], 1u << (nb & 31));
         }
-    }
-    if (tid == 0) {
-        unsigned long long n = 0;
-        for (int w = 0; w < S::WORDS; ++w) n += __popcll(act[w]);
-        tally.add(a.vstate, cnt, v, n);
     }
     __syncthreads();
 }
 
 // A brick of A_{k-1} not in A_k: phi[p] -> phi[p^1].
 template <class S, int NT>
-__device__ __forceinline__ void ns_flush_brick(const NsArgs& a, uint32_t b, uint32_t p) {
-    const NsVol& V = a.vols[a.brick_vol[b]];
+__device__ __forceinline__ void ns_flush_brick(const NsArgs& a, uint32_t b, uint32_t p, const NsVol* vone) {
+    const NsVol& V = vone ? *vone : a.vols[a.brick_vol[b]];
     const int3 o = brick_origin<S>(V, b);
     const float* src = V.phi[p];
     float* dst = V.phi[p ^ 1u];
@@ -465,15 +549,19 @@ __device__ __forceinline__ StopState stop_state(int32_t* base, int nvol) {
 // voxels updated at k; streak = consecutive iterations with n_k < rel * n0;
 // stop when streak >= patience, n_k <= abs_thr, or the budget is used.
 constexpr uint32_t kNoBrick = 0xFFFFFFFFu;  // a brick of a finished volume
+constexpr int kScanCache = 4;               // membership words per thread kept in shared memory
 
 // At least 1024 resident threads per SM: 64 registers a thread at most.
 template <int BX, int BY, int BZ, int NT>
 __global__ void __launch_bounds__(NT, 1024 / NT) k_ns_persistent(NsArgs a) {
     using S = Brick<BX, BY, BZ>;
     __shared__ NsSmem<S, NT> sm;
-    __shared__ uint32_t s_gen;
+    __shared__ NsVol s_vol;  // the descriptor of a one-volume launch
+    __shared__ uint32_t s_gen, s_abort;
+    __shared__ unsigned long long s_rel, s_n0;
     __shared__ int32_t s_live;
     __shared__ uint32_t s_work[NT], s_flush[NT];
+    __shared__ uint2 s_scan[kScanCache][NT];  // (A_k word, A_{k-1} \ A_k word) per thread
     extern __shared__ int32_t s_dyn[];
     StopState ss = stop_state(s_dyn, a.nvol);
     const int tid = threadIdx.x;
@@ -481,7 +569,10 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_ns_persistent(NsArgs a) {
     if (tid == 0) {
         mbar_init(&sm.bar[0], 1);
         mbar_init(&sm.bar[1], 1);
-        s_gen = ld_acquire_u32(&a.ctl->bar_gen);
+        s_gen = (uint32_t)ld_acquire_u64((const uint64_t*)&a.ctl->bar_release);
+        s_abort = 0;
+        s_n0 = a.vstate[0].n0;
+        if (a.nvol == 1) s_vol = a.vols[0];
         for (int v = 0; v < a.nvol; ++v)
             for (int m = 0; m < 5; ++m) tmap_acquire(&a.tmaps[a.vols[v].tmap_base + m]);
     }
@@ -493,6 +584,11 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_ns_persistent(NsArgs a) {
     }
     __syncthreads();
     uint32_t gen = s_gen;
+    const bool one = a.nvol == 1;  // one volume: the stopping rule rides on the barrier
+    const NsVol* vone = one ? &s_vol : nullptr;
+    const unsigned long long n0 = s_n0;
+    uint32_t streak = 0;
+    const uint32_t patience = (uint32_t)min(max(a.patience, 0), 0xFFFF);
     uint32_t mphase[2] = {0u, 0u};
     int ran = 0;
     uint64_t t0 = 0, t1 = 0;
@@ -509,8 +605,18 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_ns_persistent(NsArgs a) {
         BlockTally tally;
         // Ranks of the bricks to update (A_k) and to flush (A_{k-1} \ A_k):
         // thread t counts the words t, t+NT, ...; ranks follow (thread, word).
+        // The first kScanCache words of each thread are kept in shared memory.
         uint32_t ca = 0, cf = 0;
-        for (uint32_t w = tid; w < a.NW; w += NT) {
+#pragma unroll
+        for (int m = 0; m < kScanCache; ++m) {
+            const uint32_t w = tid + (uint32_t)m * NT;
+            const uint32_t c = w < a.NW ? cur[w] : 0u;
+            const uint32_t f = w < a.NW ? prev[w] & ~c : 0u;
+            s_scan[m][tid] = make_uint2(c, f);
+            ca += __popc(c);
+            cf += __popc(f);
+        }
+        for (uint32_t w = tid + kScanCache * NT; w < a.NW; w += NT) {
             const uint32_t c = cur[w];
             ca += __popc(c);
             cf += __popc(prev[w] & ~c);
@@ -530,51 +636,62 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_ns_persistent(NsArgs a) {
                 const uint32_t lo = bi + c0 * G;
                 const uint32_t hia = bi + (c0 + nw) * G, hif = bi + (c0 + nf) * G;
                 uint32_t ra = (uint32_t)ex, rf = (uint32_t)(ex >> 32);
-                for (uint32_t w = tid; w < a.NW; w += NT) {
-                    const uint32_t c = cur[w], f = prev[w] & ~c;
-                    const uint32_t pc = __popc(c), pf = __popc(f);
-                    // Ranks q of [ra, ra + pc) with q = bi (mod G) and q in [lo, hia).
-                    for (int kind = 0; kind < 2; ++kind) {
-                        const uint32_t r = kind ? rf : ra, n = kind ? pf : pc, hi = kind ? hif : hia;
-                        const uint32_t m0 = kind ? f : c;
-                        uint32_t q = max(r, lo);
-                        q = bi + (q - bi + G - 1) / G * G;
-                        for (; q < r + n && q < hi; q += G) {
-                            uint32_t m = m0;
-                            for (uint32_t s2 = q - r; s2; --s2) m &= m - 1u;
-                            const uint32_t b = w * 32u + (uint32_t)(__ffs(m) - 1);
-                            const uint32_t slot = (q - bi) / G - c0;
-                            const uint32_t e = ss.done[a.brick_vol[b]] ? kNoBrick : b;
-                            if (kind) s_flush[slot] = e; else s_work[slot] = e;
-                        }
+                // Ranks q of [r, r + popc(m0)) with q = bi (mod G), q in [lo, hi).
+                auto visit = [&](uint32_t w, uint32_t m0, uint32_t r, uint32_t hi, uint32_t* out) {
+                    const uint32_t n = __popc(m0);
+                    uint32_t q = max(r, lo);
+                    q = bi + (q - bi + G - 1) / G * G;
+                    for (; q < r + n && q < hi; q += G) {
+                        uint32_t m = m0;
+                        for (uint32_t s2 = q - r; s2; --s2) m &= m - 1u;
+                        const uint32_t b = w * 32u + (uint32_t)(__ffs(m) - 1);
+                        out[(q - bi) / G - c0] = (!one && ss.done[a.brick_vol[b]]) ? kNoBrick : b;
                     }
-                    ra += pc;
-                    rf += pf;
+                };
+                for (int m = 0; m < kScanCache; ++m) {
+                    const uint32_t w = tid + (uint32_t)m * NT;
+                    const uint2 cf2 = s_scan[m][tid];
+                    if (cf2.x) visit(w, cf2.x, ra, hia, s_work);
+                    if (cf2.y) visit(w, cf2.y, rf, hif, s_flush);
+                    ra += __popc(cf2.x);
+                    rf += __popc(cf2.y);
+                }
+                for (uint32_t w = tid + kScanCache * NT; w < a.NW; w += NT) {
+                    const uint32_t c = cur[w], f = prev[w] & ~c;
+                    if (c) visit(w, c, ra, hia, s_work);
+                    if (f) visit(w, f, rf, hif, s_flush);
+                    ra += __popc(c);
+                    rf += __popc(f);
                 }
             }
             __syncthreads();
             uint32_t q = 0;
             while (q < nw && s_work[q] == kNoBrick) ++q;
             if (q < nw) {
-                if (tid == 0) ns_issue_loads<S, NT>(a, sm, s_work[q], p, buf);
+                if (tid == 0) ns_issue_loads<S, NT>(a, sm, s_work[q], p, buf, vone);
                 ns_fetch_mask<S, NT>(a, sm, s_work[q], p, buf);
             }
             while (q < nw) {
                 uint32_t q2 = q + 1;
                 while (q2 < nw && s_work[q2] == kNoBrick) ++q2;
                 if (q2 < nw) {
-                    if (tid == 0) ns_issue_loads<S, NT>(a, sm, s_work[q2], p, buf ^ 1);
+                    if (tid == 0) ns_issue_loads<S, NT>(a, sm, s_work[q2], p, buf ^ 1, vone);
                     ns_fetch_mask<S, NT>(a, sm, s_work[q2], p, buf ^ 1);
                 }
-                ns_process_brick<S, NT>(a, sm, s_work[q], p, sn, buf, mphase, tally, a.cnt[c3]);
+                ns_process_brick<S, NT>(a, sm, s_work[q], p, sn, buf, mphase, tally,
+                                        one ? nullptr : a.cnt[c3], vone);
                 buf ^= 1;
                 q = q2;
             }
             for (uint32_t r = 0; r < nf; ++r)
-                if (s_flush[r] != kNoBrick) ns_flush_brick<S, NT>(a, s_flush[r], p);
+                if (s_flush[r] != kNoBrick) ns_flush_brick<S, NT>(a, s_flush[r], p, vone);
             __syncthreads();
         }
-        if (tid == 0) tally.flush(a.vstate, a.cnt[c3]);
+        unsigned long long mine = 0;
+        if (tid == 0) {
+            mine = tally.iter;
+            tally.flush(a.vstate, one ? nullptr : a.cnt[c3]);
+        }
         for (uint32_t w = blockIdx.x * NT + tid; w < a.NW; w += G * NT) a.bits[sz][w] = 0u;
         if (tid == 0) {
             tma_store_wait_all();
@@ -585,23 +702,40 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_ns_persistent(NsArgs a) {
         if (tid == 0) {
             const uint32_t target = gen + 1;
             __threadfence();
-            const uint32_t arrived = atomicAdd(&a.ctl->bar_count, 1u) + 1u;
-            if (arrived == G) {
-                a.ctl->bar_count = 0;
-                __threadfence();
-                asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(&a.ctl->bar_gen), "r"(target) : "memory");
+            const unsigned long long old = atomicAdd(&a.ctl->bar_arrive, (mine << kArriveShift) | 1ull);
+            unsigned long long rel;
+            if ((old & kArriveMask) == G - 1) {
+                // Last to arrive: evaluate the one-volume stopping rule, release.
+                a.ctl->bar_arrive = 0ull;
+                uint32_t st = streak;
+                bool stop = it + 1 >= a.max_iters;
+                if (one) {
+                    const unsigned long long n = (old >> kArriveShift) + mine;
+                    a.ctl->n_last = n;
+                    if (a.conv_mode) {
+                        st = ((double)n < a.rel * (double)n0) ? min(st + 1u, 0xFFFFu) : 0u;
+                        stop = stop || st >= patience || n <= a.abs_thr;
+                    }
+                }
+                rel = (unsigned long long)target | ((unsigned long long)st << kRelStreakShift) |
+                      (stop ? kRelStop : 0ull);
+                st_release_u64((uint64_t*)&a.ctl->bar_release, rel);  // orders the stores above
             } else {
                 const uint64_t w0 = globaltimer_ns();
                 uint32_t ns = 16;
-                while (ld_acquire_u32(&a.ctl->bar_gen) != target) {
+                for (;;) {
+                    rel = ld_acquire_u64((const uint64_t*)&a.ctl->bar_release);
+                    if ((uint32_t)rel == target) break;
                     if (globaltimer_ns() - w0 > kWaitLimitNs) {
                         set_error(&a.ctl->err, ERR_BARRIER_TIMEOUT);
+                        s_abort = 1;
                         break;
                     }
                     __nanosleep(ns);
-                    if (ns < 256) ns <<= 1;
+                    if (ns < 64) ns <<= 1;
                 }
             }
+            s_rel = rel;
             gen = target;
             asm volatile("fence.proxy.async.global;" ::: "memory");
             if (blockIdx.x == 0) {
@@ -611,7 +745,22 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_ns_persistent(NsArgs a) {
             }
         }
         __syncthreads();
-        if (*(volatile uint32_t*)&a.ctl->err) { ran = it; break; }
+        // A block that gave up leaves; the others then give up at the next
+        // barrier (bounded), so every block ends.
+        if (s_abort) { ran = it; break; }
+        if (one) {
+            const unsigned long long rel = s_rel;
+            streak = (uint32_t)(rel >> kRelStreakShift) & 0xFFFFu;
+            ran = it + 1;
+            if (rel & kRelStop) {
+                if (tid == 0) {
+                    ss.done[0] = 1;
+                    ss.stop[0] = it;
+                }
+                break;
+            }
+            continue;
+        }
         // Stopping rule, evaluated identically by every block.
         if (tid == 0) s_live = 0;
         __syncthreads();
@@ -638,6 +787,12 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_ns_persistent(NsArgs a) {
         ran = it + 1;
         if (s_live == 0) break;
     }
+    __syncthreads();
+    if (one && tid == 0) {
+        ss.n[0] = *(volatile unsigned long long*)&a.ctl->n_last;
+        ss.streak[0] = (int32_t)streak;
+    }
+    __syncthreads();
     if (blockIdx.x == 0) {
         for (int v = tid; v < a.nvol; v += NT) {
             NsVolState& st = a.vstate[v];
