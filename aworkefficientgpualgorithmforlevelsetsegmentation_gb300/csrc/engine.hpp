@@ -48,6 +48,7 @@ class EngineBase {
     std::string last_error;
     int device = 0;
     int num_sms = 0;
+    uint64_t launches = 0;  // kernels launched by this engine (graph launches count their kernels)
 
     virtual void load_volume(const void* data, int nx, int ny, int nz, int dtype, float aniso) = 0;
     virtual void unload_volume() = 0;

@@ -82,23 +82,40 @@ void EngineBase::sync() {
 static std::mutex g_tune_mu;
 static std::map<std::tuple<int, int, int, int>, BrickConfig> g_tune_cache;
 
+static bool same_config(const BrickConfig& a, const BrickConfig& b) {
+    return a.bx == b.bx && a.by == b.by && a.bz == b.bz && a.threads == b.threads;
+}
+
 static BrickConfig autotune(NsCore& core, EngineBase* owner, int iters) {
     auto& vols = core.vols();
     uint64_t vox = 0;
     for (auto& v : vols) vox += (uint64_t)v.nx * v.ny * v.nz;
     auto key = std::make_tuple((int)vols.size(), (int)std::log2((double)vox + 1), vols[0].nx / 64,
                                vols[0].nz / 64);
+    // Save the seeded phi of every volume.
+    auto save = [&]() {
+        std::vector<std::vector<float>> saved(vols.size());
+        for (size_t i = 0; i < vols.size(); ++i) {
+            saved[i].resize((size_t)vols[i].nx * vols[i].ny * vols[i].nz);
+            core.read_phi((int)i, saved[i].data());
+        }
+        return saved;
+    };
     {
         std::lock_guard<std::mutex> g(g_tune_mu);
         auto it = g_tune_cache.find(key);
-        if (it != g_tune_cache.end()) return it->second;
+        if (it != g_tune_cache.end()) {
+            const BrickConfig c = it->second;
+            if (!same_config(c, core.config())) {  // apply the cached choice
+                auto saved = save();
+                core.configure(c);
+                for (size_t i = 0; i < vols.size(); ++i) core.set_phi((int)i, saved[i].data());
+                core.init_active();
+            }
+            return c;
+        }
     }
-    // Save the seeded phi of every volume.
-    std::vector<std::vector<float>> saved(vols.size());
-    for (size_t i = 0; i < vols.size(); ++i) {
-        saved[i].resize((size_t)vols[i].nx * vols[i].ny * vols[i].nz);
-        core.read_phi((int)i, saved[i].data());
-    }
+    std::vector<std::vector<float>> saved = save();
     BrickConfig best = brick_configs()[0];
     float best_ms = 1e30f;
     for (const BrickConfig& c : brick_configs()) {
@@ -199,7 +216,7 @@ class NsEngine : public EngineBase {
             after_init();
         }
         if (!tuned_) {
-            autotune(*core_, this, 16);
+            autotune(*core_, this, 256);
             tuned_ = true;
         }
         float ms = 0;
@@ -304,6 +321,7 @@ class NsEngine : public EngineBase {
     void stats(lss_stats* s) override {
         std::memset(s, 0, sizeof(*s));
         s->mode = LSS_MODE_NS;
+        s->kernel_launches = launches;
         if (!core_) return;
         const auto& v = core_->vols()[0];
         s->padded_x = v.px; s->padded_y = v.py; s->padded_z = v.pz;
@@ -387,7 +405,7 @@ class BatchEngine : public EngineBase {
             for (size_t k = 0; k + 3 < seeds_[v].size(); k += 4)
                 core_.sphere_union(v, seeds_[v][k], seeds_[v][k + 1], seeds_[v][k + 2], seeds_[v][k + 3]);
         core_.init_active();
-        if (cfg.brick_x <= 0) autotune(core_, this, 12);
+        if (cfg.brick_x <= 0) autotune(core_, this, 32);
         float ms = 0;
         lss_conv cv = conv ? *conv : lss_conv{0.0, 1, 1000, 0};
         int it = core_.run(cv.max_iterations, &cv, &ms);
@@ -408,6 +426,7 @@ class BatchEngine : public EngineBase {
     void stats_v(int v, lss_stats* s) {
         std::memset(s, 0, sizeof(*s));
         s->mode = LSS_MODE_NS;
+        s->kernel_launches = launches;
         const auto& V = core_.vols().at(v);
         s->padded_x = V.px; s->padded_y = V.py; s->padded_z = V.pz;
         s->brick_x = core_.config().bx; s->brick_y = core_.config().by; s->brick_z = core_.config().bz;

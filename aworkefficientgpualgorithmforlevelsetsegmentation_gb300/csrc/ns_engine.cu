@@ -196,8 +196,11 @@ int NsCore::add_volume(const float* data, int nx, int ny, int nz, const lss_para
     float* tmp = (float*)arena_.alloc((uint64_t)nx * ny * nz * 4);
     LSS_CUDA(cudaMemcpyAsync(tmp, data, (uint64_t)nx * ny * nz * 4, cudaMemcpyHostToDevice, st));
     k_ns_scatter<<<owner_->num_sms * 4, 256, 0, st>>>(v.img, tmp, nx, ny, nz, v.px, v.py);
+    ++owner_->launches;
     k_ns_fill<<<owner_->num_sms * 4, 256, 0, st>>>(v.phi[0], P, p.phi_max);
+    ++owner_->launches;
     k_ns_fill<<<owner_->num_sms * 4, 256, 0, st>>>(v.phi[1], P, p.phi_max);
+    ++owner_->launches;
     LSS_CUDA(cudaGetLastError());
     owner_->sync();
     arena_.free_last(tmp);
@@ -220,6 +223,7 @@ void NsCore::set_bias(int v, const float* bias) {
                                  owner_->stream));
         k_ns_scatter<<<owner_->num_sms * 4, 256, 0, owner_->stream>>>(V.bias_buf, tmp, V.nx, V.ny, V.nz,
                                                                      V.px, V.py);
+        ++owner_->launches;
         owner_->sync();
         arena_.free_last(tmp);
         V.bias = V.bias_buf;
@@ -370,6 +374,7 @@ void NsCore::init_active() {
     void* params[] = {&a, &p, &sl};
     const int grid = (int)std::min<uint64_t>(NB_, (uint64_t)owner_->num_sms * 16);
     LSS_CUDA(cudaLaunchKernel(ks.init_active, dim3(grid), dim3(ks.block), params, 0, st));
+    ++owner_->launches;
     std::vector<unsigned long long> n0(vols_.size());
     LSS_CUDA(cudaMemcpyAsync(n0.data(), d_cnt_[0], 8 * vols_.size(), cudaMemcpyDeviceToHost, st));
     LSS_CUDA(cudaMemsetAsync(d_cnt_[0], 0, 8 * vols_.size(), st));
@@ -400,6 +405,7 @@ void NsCore::sphere_union(int v, float cx, float cy, float cz, float r) {
     if (b1.x <= b0.x || b1.y <= b0.y || b1.z <= b0.z) return;
     k_ns_sphere_union<<<owner_->num_sms * 4, 256, 0, owner_->stream>>>(
         V.phi[parity_], V.nx, V.ny, V.nz, V.px, V.py, b0, b1, cx, cy, cz, r, V.p.phi_min, V.p.phi_max);
+    ++owner_->launches;
     LSS_CUDA(cudaGetLastError());
 }
 
@@ -410,6 +416,7 @@ void NsCore::set_phi(int v, const float* phi) {
                              owner_->stream));
     k_ns_scatter<<<owner_->num_sms * 4, 256, 0, owner_->stream>>>(V.phi[parity_], tmp, V.nx, V.ny, V.nz,
                                                                  V.px, V.py);
+    ++owner_->launches;
     owner_->sync();
     arena_.free_last(tmp);
 }
@@ -418,6 +425,7 @@ void NsCore::fill_phi(int v, float value) {
     VolHost& V = vols_.at(v);
     k_ns_fill<<<owner_->num_sms * 4, 256, 0, owner_->stream>>>(V.phi[parity_], (uint64_t)V.px * V.py * V.pz,
                                                               value);
+    ++owner_->launches;
     LSS_CUDA(cudaGetLastError());
 }
 
@@ -435,6 +443,7 @@ int NsCore::run(int max_iters, const lss_conv* conv, float* ms) {
     if (fault_injected("launch")) throw Error(LSS_ERR_INJECTED, "injected launch failure");
     LSS_CUDA(cudaLaunchCooperativeKernel(ks.persistent, dim3(grid_), dim3(ks.block), params, dyn_smem(),
                                          st));
+    ++owner_->launches;
     LSS_CUDA(cudaEventRecord(e1, st));
     LSS_CUDA(cudaEventSynchronize(e1));
     float t = 0;
@@ -480,6 +489,7 @@ void NsCore::read_phi(int v, float* out) {
     float* tmp = (float*)arena_.alloc((uint64_t)V.nx * V.ny * V.nz * 4);
     k_ns_gather<<<owner_->num_sms * 4, 256, 0, owner_->stream>>>(tmp, V.phi[p], V.nx, V.ny, V.nz, V.px,
                                                                 V.py);
+    ++owner_->launches;
     LSS_CUDA(cudaMemcpyAsync(out, tmp, (uint64_t)V.nx * V.ny * V.nz * 4, cudaMemcpyDeviceToHost,
                              owner_->stream));
     owner_->sync();
@@ -501,6 +511,7 @@ uint64_t NsCore::read_active(int v, uint64_t* out, uint64_t cap) {
         uint32_t p = parity_, sl = s;
         void* params[] = {&a, &p, &sl, &dout, &total};
         LSS_CUDA(cudaLaunchKernel(ks.emit, dim3(owner_->num_sms * 2), dim3(ks.block), params, 0, st));
+        ++owner_->launches;
         unsigned long long n = 0;
         LSS_CUDA(cudaMemcpyAsync(&n, total, 8, cudaMemcpyDeviceToHost, st));
         owner_->sync();
@@ -527,6 +538,7 @@ void NsCore::estimate(int v, float* t, float* w) {
         LSS_CUDA(cudaMemsetAsync(acc, 0, 24, owner_->stream));
         k_ns_collect<<<owner_->num_sms * 4, 256, 0, owner_->stream>>>(V.img, V.phi[parity_], V.nx, V.ny,
                                                                      V.nz, V.px, V.py, mean, acc);
+        ++owner_->launches;
         LSS_CUDA(cudaMemcpyAsync(h, acc, 24, cudaMemcpyDeviceToHost, owner_->stream));
         owner_->sync();
         LSS_REQUIRE(h[2] >= 2, LSS_ERR_STATE, "fewer than two segmented voxels");
@@ -549,6 +561,7 @@ float NsCore::dense_run(int iters) {
             const VolHost& V = vols_[v];
             dim3 grid((V.nx + 31) / 32, (V.ny + 7) / 8, (V.nz + 7) / 8);
             k_ns_dense<<<grid, 256, 0, st>>>(d_vols_, v, parity_);
+            ++owner_->launches;
         }
         parity_ ^= 1u;
     }

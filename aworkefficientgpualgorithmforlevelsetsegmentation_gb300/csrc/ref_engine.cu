@@ -574,6 +574,7 @@ class RefEngine : public EngineBase {
         for (int k = 0; k < 2; ++k) {
             k_ref_init_level_set<<<blocks(), kThreads, 0, stream>>>(wr_, export_, rd_, d_, seed,
                                                                    rr, aniso_);
+            ++launches;
             swap();
         }
         rebuild_dense();
@@ -607,9 +608,13 @@ class RefEngine : public EngineBase {
 
     void rebuild_dense() {
         k_ref_init_active<<<blocks(), kThreads, 0, stream>>>(valid_, rd_, d_);
+        ++launches;
         k_ref_coord_init<<<blocks(), kThreads, 0, stream>>>(coord_, d_, ctl_, 1);
+        ++launches;
         k_ref_plan<<<1, kThreads, 0, stream>>>(ctl_, status_, (uint32_t)N_, 1, 0);
+        ++launches;
         k_ref_compact<<<blocks(), kThreads, 0, stream>>>(coord_, valid_, active_, ctl_, status_);
+        ++launches;
         LSS_CUDA(cudaGetLastError());
     }
 
@@ -638,22 +643,34 @@ class RefEngine : public EngineBase {
             case LSS_S32: LSS_REF_UPD(int32_t); break;
 #undef LSS_REF_UPD
         }
+        ++launches;
         swap();
         k_ref_plan<<<1, kThreads, 0, stream>>>(ctl_, status_, (uint32_t)N_, reinit ? 1 : 0, 1);
+        ++launches;
         if (reinit) {
             k_ref_init_active<<<B, kThreads, 0, stream>>>(valid_, rd_, d_);
+            ++launches;
             k_ref_coord_init<<<B, kThreads, 0, stream>>>(coord_, d_, ctl_, 0);
+            ++launches;
         } else {
             const int q = cfg.ref_quirk_i3 ? 1 : 0;
             k_ref_output<<<B, kThreads, 0, stream>>>(coord_, valid_, rd_, tag_, active_, d_, ctl_, q);
+            ++launches;
             k_ref_clear_tag<<<B, kThreads, 0, stream>>>(tag_, active_, d_, ctl_);
+            ++launches;
             k_ref_filter0<<<B, kThreads, 0, stream>>>(coord_, valid_, tag_, d_, ctl_);
-            for (int e = 1; e < 7; ++e)
+            ++launches;
+            for (int e = 1; e < 7; ++e) {
                 k_ref_filter<<<B, kThreads, 0, stream>>>(coord_, valid_, tag_, d_, ctl_, e);
+                ++launches;
+            }
             k_ref_coord_init<<<B, kThreads, 0, stream>>>(coord_, d_, ctl_, 0);
+            ++launches;
             k_ref_scatter<<<B, kThreads, 0, stream>>>(valid_, rd_, tag_, active_, d_, ctl_, q);
+            ++launches;
         }
         k_ref_compact<<<B, kThreads, 0, stream>>>(coord_, valid_, active_, ctl_, status_);
+        ++launches;
     }
 
     // A graph of one normal iteration for each buffer parity.
@@ -675,7 +692,10 @@ class RefEngine : public EngineBase {
             cudaGraph_t g;
             int8_t* rd0 = rd_;
             LSS_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+            const uint64_t l0 = launches;
             enqueue_iteration(false);
+            graph_kernels_[parity] = launches - l0;  // captured, not launched
+            launches = l0;
             LSS_CUDA(cudaStreamEndCapture(stream, &g));
             rd_ = rd0;
             wr_ = rd0 == phiX_ ? phiY_ : phiX_;
@@ -683,6 +703,7 @@ class RefEngine : public EngineBase {
             cudaGraphDestroy(g);
         }
         LSS_CUDA(cudaGraphLaunch(graphs_[parity], stream));
+        launches += graph_kernels_[parity];
         swap();
     }
 
@@ -775,6 +796,7 @@ class RefEngine : public EngineBase {
         require_loaded();
         LSS_CUDA(cudaMemcpyAsync(tag_, export_, N_, cudaMemcpyDeviceToDevice, stream));
         k_ref_add_level_set<<<blocks(), kThreads, 0, stream>>>(tag_, frozen_, N_);
+        ++launches;
         std::vector<uint8_t> h(N_);
         LSS_CUDA(cudaMemcpyAsync(h.data(), tag_, N_, cudaMemcpyDeviceToHost, stream));
         LSS_CUDA(cudaMemsetAsync(tag_, 0, N_, stream));
@@ -802,6 +824,7 @@ class RefEngine : public EngineBase {
         if (!scratch_) scratch_ = (uint8_t*)arena_.alloc(N_);
         LSS_CUDA(cudaMemsetAsync(scratch_, 0, N_, stream));
         k_ref_export_active<<<blocks(), kThreads, 0, stream>>>(scratch_, active_, d_, ctl_);
+        ++launches;
         std::vector<uint8_t> h(N_);
         LSS_CUDA(cudaMemcpyAsync(h.data(), scratch_, N_, cudaMemcpyDeviceToHost, stream));
         sync();
@@ -814,6 +837,7 @@ class RefEngine : public EngineBase {
     void freeze() override {
         require_loaded();
         k_ref_add_level_set<<<blocks(), kThreads, 0, stream>>>(frozen_, export_, N_);
+        ++launches;
         sync();
     }
 
@@ -844,7 +868,8 @@ class RefEngine : public EngineBase {
         for (int pass = 0; pass < 2; ++pass) {
             LSS_CUDA(cudaMemsetAsync(acc_, 0, 3 * sizeof(double), stream));
             switch (dtype_) {
-#define LSS_COL(TY) k_ref_collect<TY><<<blocks(), kThreads, 0, stream>>>(src_, export_, N_, mean, acc_)
+#define LSS_COL(TY) \
+    k_ref_collect<TY><<<blocks(), kThreads, 0, stream>>>(src_, export_, N_, mean, acc_), ++launches
                 case LSS_U8: LSS_COL(uint8_t); break;
                 case LSS_S8: LSS_COL(int8_t); break;
                 case LSS_U16: LSS_COL(uint16_t); break;
@@ -867,6 +892,7 @@ class RefEngine : public EngineBase {
     void stats(lss_stats* s) override {
         std::memset(s, 0, sizeof(*s));
         s->mode = LSS_MODE_REF;
+        s->kernel_launches = launches;
         if (!loaded_) return;
         RefCtl c;
         LSS_CUDA(cudaMemcpyAsync(&c, ctl_, sizeof(c), cudaMemcpyDeviceToHost, stream));
@@ -923,6 +949,7 @@ class RefEngine : public EngineBase {
     double last_ms_ = 0;
     GraphKey gkey_;
     cudaGraphExec_t graphs_[2] = {nullptr, nullptr};
+    uint64_t graph_kernels_[2] = {0, 0};  // kernels of each graph
 };
 
 }  // namespace

@@ -62,7 +62,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -195,6 +195,10 @@ def run_ours(args, ws, rank, local):
     torch.cuda.synchronize()
     barrier(ws)
     ev_ms, kern_ms, updates, iters = 0.0, 0.0, 0, []
+    # Kernel launches of the library inside the timed steps: the counter is
+    # read at the start of each stats call, and every stats call itself
+    # launches one kernel (the active-count readback) afterwards.
+    launches0 = seg.stats()["kernel_launches"]
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
             flush.fill_(1)  # L2 flush between timed steps (outside the events)
@@ -210,6 +214,7 @@ def run_ours(args, ws, rank, local):
             kern_ms += st["last_step_ms"]
             updates += st["voxel_updates"]
             iters.append(it)
+    launches_steps = st["kernel_launches"] - launches0 - args.steps
     torch.cuda.synchronize()
     barrier(ws)
     t_max = max_over_ranks(ws, ev_ms)
@@ -250,7 +255,6 @@ def run_ours(args, ws, rank, local):
 
     peak, peak_kind = measured_peak()
     achieved = BYTES_PER_UPDATE * updates / (kern_ms / 1e3) / 1e9
-    launches_per_step = 8
     if rank == 0:
         cpu_u, cpu_t = (None, None)
         if not args.no_cpu:
@@ -280,7 +284,7 @@ def run_ours(args, ws, rank, local):
             "e2e": {"value": e2e_value, "unit": "voxel_updates/s",
                     "h2d_bytes_per_step": int(img.nbytes),
                     "d2h_bytes_per_step": int(mask.nbytes)},
-            "gpu_launches": launches_per_step * args.steps,
+            "gpu_launches": int(launches_steps),
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)
@@ -289,7 +293,7 @@ def run_ours(args, ws, rank, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--scale", type=float, default=1.0)

@@ -129,6 +129,8 @@ typedef struct lss_stats {
     double   update_ms;            /* NS: time of the last launch's block 0 in brick
                                       work (updates, flushes) ...                    */
     double   barrier_ms;           /* ... and waiting at the grid barrier            */
+    uint64_t kernel_launches;      /* kernels launched by the engine so far (read
+                                      before the stats call's own readback)          */
 } lss_stats;
 
 /* ---- construction / teardown ------------------------------------------ */
