@@ -145,22 +145,34 @@ struct KernelSet {
     void* init_active;
     void* emit;
     int words;
-    int block;  // threads per block of every kernel of the set
+    int block;          // threads per block of the init / emit kernels
+    int pblock;         // threads per block of the persistent kernel
+    size_t smem_fixed;  // dynamic shared memory of the persistent kernel, without the stopping state
 };
 
 template <int BX, int BY, int BZ, int NT>
 KernelSet kernels_for() {
     using S = Brick<BX, BY, BZ>;
     return KernelSet{(void*)&k_ns_persistent<BX, BY, BZ, NT>, (void*)&k_ns_init_active<BX, BY, BZ, NT>,
-                     (void*)&k_ns_emit<BX, BY, BZ, NT>, S::WORDS, NT};
+                     (void*)&k_ns_emit<BX, BY, BZ, NT>, S::WORDS, NT, NT, 0};
+}
+
+// Warp per brick, W warps in the one block per SM.
+template <int BX, int BY, int BZ, int W, int NT>
+KernelSet warp_kernels_for() {
+    using S = Brick<BX, BY, BZ>;
+    return KernelSet{(void*)&k_ns_warp<BX, BY, BZ, W>, (void*)&k_ns_init_active<BX, BY, BZ, NT>,
+                     (void*)&k_ns_emit<BX, BY, BZ, NT>, S::WORDS, NT, W * 32, warp_smem_fixed<S, W>()};
 }
 
 }  // namespace
 
-// The instantiated (brick shape, threads per brick) configurations.
+// The instantiated (brick shape, threads per brick) configurations; 32
+// threads per brick = one warp per brick (k_ns_warp).
 const std::vector<BrickConfig>& brick_configs() {
     static const std::vector<BrickConfig> v = {
-        {8, 8, 8, 256}, {8, 8, 8, 128}, {8, 8, 8, 512}, {8, 8, 4, 128}, {8, 8, 4, 256}, {4, 4, 4, 64}};
+        {8, 8, 8, 256}, {8, 8, 8, 128}, {8, 8, 8, 512}, {8, 8, 4, 128}, {8, 8, 4, 256}, {4, 4, 4, 64},
+        {8, 8, 4, 32},  {8, 8, 8, 32},  {4, 4, 4, 32}};
     return v;
 }
 
@@ -171,6 +183,9 @@ static KernelSet kernels(const BrickConfig& c) {
     if (c.bx == 8 && c.by == 8 && c.bz == 4 && c.threads == 128) return kernels_for<8, 8, 4, 128>();
     if (c.bx == 8 && c.by == 8 && c.bz == 4 && c.threads == 256) return kernels_for<8, 8, 4, 256>();
     if (c.bx == 4 && c.by == 4 && c.bz == 4 && c.threads == 64) return kernels_for<4, 4, 4, 64>();
+    if (c.bx == 8 && c.by == 8 && c.bz == 4 && c.threads == 32) return warp_kernels_for<8, 8, 4, 16, 256>();
+    if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 32) return warp_kernels_for<8, 8, 8, 16, 256>();
+    if (c.bx == 4 && c.by == 4 && c.bz == 4 && c.threads == 32) return warp_kernels_for<4, 4, 4, 32, 64>();
     throw Error(LSS_ERR_UNSUPPORTED, "unsupported brick configuration");
 }
 
@@ -287,14 +302,16 @@ void NsCore::configure(const BrickConfig& c) {
     const size_t dyn = dyn_smem();
     int per_sm = 0;
     LSS_CUDA(cudaFuncSetAttribute(ks.persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
-    LSS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ks.persistent, ks.block, dyn));
+    LSS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ks.persistent, ks.pblock, dyn));
     LSS_REQUIRE(per_sm > 0, LSS_ERR_CUDA, "persistent kernel does not fit on an SM");
     grid_ = owner_->num_sms * per_sm;
     configured_ = true;
     owner_->sync();
 }
 
-size_t NsCore::dyn_smem() const { return stop_state_bytes((int)vols_.size()); }
+size_t NsCore::dyn_smem() const {
+    return kernels(cfg_).smem_fixed + stop_state_bytes((int)vols_.size());
+}
 
 void NsCore::upload_descriptors() {
     std::vector<NsVol> d(vols_.size());
@@ -441,7 +458,7 @@ int NsCore::run(int max_iters, const lss_conv* conv, float* ms) {
     LSS_CUDA(cudaEventCreate(&e1));
     LSS_CUDA(cudaEventRecord(e0, st));
     if (fault_injected("launch")) throw Error(LSS_ERR_INJECTED, "injected launch failure");
-    LSS_CUDA(cudaLaunchCooperativeKernel(ks.persistent, dim3(grid_), dim3(ks.block), params, dyn_smem(),
+    LSS_CUDA(cudaLaunchCooperativeKernel(ks.persistent, dim3(grid_), dim3(ks.pblock), params, dyn_smem(),
                                          st));
     ++owner_->launches;
     LSS_CUDA(cudaEventRecord(e1, st));

@@ -127,42 +127,56 @@ struct Brick {
 
 // The spec update of one voxel from the shared-memory halo tile.
 // P(dx,dy,dz) reads the tile around the voxel.  Mirrors ns_update() of the
-// FP64 oracle in fp32.
+// FP64 oracle in fp32.  Every operation is an explicit round-to-nearest
+// intrinsic (no contraction or reassociation left to the compiler), so the
+// result is the same bit for bit in every kernel that inlines it.
 template <class PF>
 __device__ __forceinline__ float ns_update_f32(PF P, float I, float bias, const NsVol& V) {
     const float c = P(0, 0, 0);
     const float xm = P(-1, 0, 0), xp = P(1, 0, 0);
     const float ym = P(0, -1, 0), yp = P(0, 1, 0);
     const float zm = P(0, 0, -1), zp = P(0, 0, 1);
-    const float cx = (xp - xm) * 0.5f, cy = (yp - ym) * 0.5f, cz = (zp - zm) * 0.5f;
-    const float fxx = xp - 2.0f * c + xm, fyy = yp - 2.0f * c + ym, fzz = zp - 2.0f * c + zm;
-    const float fxy = (P(1, 1, 0) - P(1, -1, 0) - P(-1, 1, 0) + P(-1, -1, 0)) * 0.25f;
-    const float fxz = (P(1, 0, 1) - P(1, 0, -1) - P(-1, 0, 1) + P(-1, 0, -1)) * 0.25f;
-    const float fyz = (P(0, 1, 1) - P(0, 1, -1) - P(0, -1, 1) + P(0, -1, -1)) * 0.25f;
-    const float g2 = cx * cx + cy * cy + cz * cz;
+    const float cx = __fmul_rn(__fsub_rn(xp, xm), 0.5f);
+    const float cy = __fmul_rn(__fsub_rn(yp, ym), 0.5f);
+    const float cz = __fmul_rn(__fsub_rn(zp, zm), 0.5f);
+    const float c2 = __fmul_rn(2.0f, c);
+    const float fxx = __fadd_rn(__fsub_rn(xp, c2), xm);
+    const float fyy = __fadd_rn(__fsub_rn(yp, c2), ym);
+    const float fzz = __fadd_rn(__fsub_rn(zp, c2), zm);
+    auto cross = [&](float pp, float pm, float mp, float mm) {
+        return __fmul_rn(__fadd_rn(__fsub_rn(__fsub_rn(pp, pm), mp), mm), 0.25f);
+    };
+    const float fxy = cross(P(1, 1, 0), P(1, -1, 0), P(-1, 1, 0), P(-1, -1, 0));
+    const float fxz = cross(P(1, 0, 1), P(1, 0, -1), P(-1, 0, 1), P(-1, 0, -1));
+    const float fyz = cross(P(0, 1, 1), P(0, 1, -1), P(0, -1, 1), P(0, -1, -1));
+    const float xx = __fmul_rn(cx, cx), yy = __fmul_rn(cy, cy), zz = __fmul_rn(cz, cz);
+    const float g2 = __fadd_rn(__fadd_rn(xx, yy), zz);
     float curv = 0.0f;
     if (g2 > 1e-12f) {
-        const float num = fxx * (cy * cy + cz * cz) + fyy * (cx * cx + cz * cz) +
-                          fzz * (cx * cx + cy * cy) -
-                          2.0f * (cx * cy * fxy + cx * cz * fxz + cy * cz * fyz);
+        const float t = __fmaf_rn(fzz, __fadd_rn(xx, yy),
+                                  __fmaf_rn(fyy, __fadd_rn(xx, zz), __fmul_rn(fxx, __fadd_rn(yy, zz))));
+        const float x = __fmaf_rn(__fmul_rn(cy, cz), fyz,
+                                  __fmaf_rn(__fmul_rn(cx, cz), fxz, __fmul_rn(__fmul_rn(cx, cy), fxy)));
+        const float num = __fmaf_rn(-2.0f, x, t);
         curv = __fdividef(num, g2);  // g2 in (1e-12, 48]: within 2 ulp
     }
-    float D = (V.eps - fabsf(I - V.T)) * V.inv_eps;
-    D = fminf(fmaxf(D, -1.0f), 1.0f) + bias;
-    const float wc = V.wc;
-    const float F = V.wd * D;
-    const float dxm = c - xm, dxp = xp - c, dym = c - ym, dyp = yp - c, dzm = c - zm, dzp = zp - c;
-    float g;
+    float D = __fmul_rn(__fsub_rn(V.eps, fabsf(__fsub_rn(I, V.T))), V.inv_eps);
+    D = __fadd_rn(fminf(fmaxf(D, -1.0f), 1.0f), bias);
+    const float F = __fmul_rn(V.wd, D);
+    const float dxm = __fsub_rn(c, xm), dxp = __fsub_rn(xp, c), dym = __fsub_rn(c, ym),
+                dyp = __fsub_rn(yp, c), dzm = __fsub_rn(c, zm), dzp = __fsub_rn(zp, c);
+    float a, b, e, f, h, k;
     if (F > 0.0f) {
-        const float a = fmaxf(dxm, 0.0f), b = fminf(dxp, 0.0f), e = fmaxf(dym, 0.0f),
-                    f = fminf(dyp, 0.0f), h = fmaxf(dzm, 0.0f), k = fminf(dzp, 0.0f);
-        g = sqrtf(a * a + b * b + e * e + f * f + h * h + k * k);
+        a = fmaxf(dxm, 0.0f); b = fminf(dxp, 0.0f); e = fmaxf(dym, 0.0f);
+        f = fminf(dyp, 0.0f); h = fmaxf(dzm, 0.0f); k = fminf(dzp, 0.0f);
     } else {
-        const float a = fminf(dxm, 0.0f), b = fmaxf(dxp, 0.0f), e = fminf(dym, 0.0f),
-                    f = fmaxf(dyp, 0.0f), h = fminf(dzm, 0.0f), k = fmaxf(dzp, 0.0f);
-        g = sqrtf(a * a + b * b + e * e + f * f + h * h + k * k);
+        a = fminf(dxm, 0.0f); b = fmaxf(dxp, 0.0f); e = fminf(dym, 0.0f);
+        f = fmaxf(dyp, 0.0f); h = fminf(dzm, 0.0f); k = fmaxf(dzp, 0.0f);
     }
-    float nv = c + V.dt * (wc * curv - F * g);
+    const float s2 = __fmaf_rn(k, k, __fmaf_rn(h, h, __fmaf_rn(f, f, __fmaf_rn(e, e,
+                               __fmaf_rn(b, b, __fmul_rn(a, a))))));
+    const float g = __fsqrt_rn(s2);
+    const float nv = __fmaf_rn(V.dt, __fsub_rn(__fmul_rn(V.wc, curv), __fmul_rn(F, g)), c);
     return fminf(fmaxf(nv, V.lo), V.hi);
 }
 
@@ -505,14 +519,16 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
 }
 
 // A brick of A_{k-1} not in A_k: phi[p] -> phi[p^1].
-template <class S, int NT>
-__device__ __forceinline__ void ns_flush_brick(const NsArgs& a, uint32_t b, uint32_t p, const NsVol* vone) {
+// Threads t0, t0 + stride, ... copy.
+template <class S>
+__device__ __forceinline__ void ns_flush_brick(const NsArgs& a, uint32_t b, uint32_t p, const NsVol* vone,
+                                               int t0, int stride) {
     const NsVol& V = vone ? *vone : a.vols[a.brick_vol[b]];
     const int3 o = brick_origin<S>(V, b);
     const float* src = V.phi[p];
     float* dst = V.phi[p ^ 1u];
     constexpr int Q = S::X / 4;  // float4 per row
-    for (int t = threadIdx.x; t < S::Y * S::Z * Q; t += NT) {
+    for (int t = t0; t < S::Y * S::Z * Q; t += stride) {
         const int q = t % Q, ly = (t / Q) % S::Y, lz = t / (Q * S::Y);
         const size_t off = ((size_t)(o.z + lz) * V.py + (o.y + ly)) * V.px + o.x + 4 * q;
         *reinterpret_cast<float4*>(dst + off) = *reinterpret_cast<const float4*>(src + off);
@@ -541,38 +557,47 @@ __device__ __forceinline__ StopState stop_state(int32_t* base, int nvol) {
     return s;
 }
 
-// The persistent kernel: one block per brick at a time, NT threads.
-//
+constexpr uint32_t kNoBrick = 0xFFFFFFFFu;  // a brick of a finished volume
+constexpr int kScanCache = 4;               // membership words per thread kept in shared memory
+
+// Shared state of the iteration driver (static shared memory).
+template <int NT>
+struct IterShared {
+    NsVol vol;                     // the descriptor of a one-volume launch
+    uint32_t gen, abort;
+    unsigned long long rel, n0, upd;
+    int32_t live;
+    uint32_t work[NT], flush[NT];  // this block's bricks of the chunk
+    uint2 scan[kScanCache][NT];    // (A_k word, A_{k-1} \ A_k word) per thread
+};
+
+// The iteration driver shared by the persistent kernels.  Per iteration k:
+//   every block ranks the bricks of A_k (and of A_{k-1} \ A_k) with a block
+//     prefix sum over the membership words and takes the ranks i, i+G, ...
+//     (block i of G): every block gets ceil(n/G) or floor(n/G) bricks, with
+//     no global list and no atomics;
+//   Proc::chunk updates the block's bricks of A_k and copies its bricks of
+//     A_{k-1} \ A_k across (phi[p] -> phi[p^1]), so both buffers stay current;
+//   Proc::finish closes the iteration (tallies, TMA stores complete);
+//   one bounded grid barrier; its arrival word carries the block's voxel
+//     updates, so the last block to arrive evaluates the one-volume stopping
+//     rule and releases the others with the decision in the release word
+//     (several volumes: every block evaluates the rule on the same counts).
 // Slots at iteration k: membership bits B[k%4] = A_k, B[(k+1)%4] = A_{k+1}
 // (being built), B[(k+3)%4] = A_{k-1}, B[(k+2)%4] cleared for reuse; voxel
 // counts cnt[k%3].  Stopping rule after iteration k, per volume: n_k = active
 // voxels updated at k; streak = consecutive iterations with n_k < rel * n0;
 // stop when streak >= patience, n_k <= abs_thr, or the budget is used.
-constexpr uint32_t kNoBrick = 0xFFFFFFFFu;  // a brick of a finished volume
-constexpr int kScanCache = 4;               // membership words per thread kept in shared memory
-
-// At least 1024 resident threads per SM: 64 registers a thread at most.
-template <int BX, int BY, int BZ, int NT>
-__global__ void __launch_bounds__(NT, 1024 / NT) k_ns_persistent(NsArgs a) {
-    using S = Brick<BX, BY, BZ>;
-    __shared__ NsSmem<S, NT> sm;
-    __shared__ NsVol s_vol;  // the descriptor of a one-volume launch
-    __shared__ uint32_t s_gen, s_abort;
-    __shared__ unsigned long long s_rel, s_n0;
-    __shared__ int32_t s_live;
-    __shared__ uint32_t s_work[NT], s_flush[NT];
-    __shared__ uint2 s_scan[kScanCache][NT];  // (A_k word, A_{k-1} \ A_k word) per thread
-    extern __shared__ int32_t s_dyn[];
-    StopState ss = stop_state(s_dyn, a.nvol);
+template <int NT, class Proc>
+__device__ __forceinline__ void ns_drive(const NsArgs& a, IterShared<NT>& sh, StopState ss, Proc& proc) {
     const int tid = threadIdx.x;
     const uint32_t G = gridDim.x;
     if (tid == 0) {
-        mbar_init(&sm.bar[0], 1);
-        mbar_init(&sm.bar[1], 1);
-        s_gen = (uint32_t)ld_acquire_u64((const uint64_t*)&a.ctl->bar_release);
-        s_abort = 0;
-        s_n0 = a.vstate[0].n0;
-        if (a.nvol == 1) s_vol = a.vols[0];
+        sh.gen = (uint32_t)ld_acquire_u64((const uint64_t*)&a.ctl->bar_release);
+        sh.abort = 0;
+        sh.upd = 0;
+        sh.n0 = a.vstate[0].n0;
+        if (a.nvol == 1) sh.vol = a.vols[0];
         for (int v = 0; v < a.nvol; ++v)
             for (int m = 0; m < 5; ++m) tmap_acquire(&a.tmaps[a.vols[v].tmap_base + m]);
     }
@@ -582,37 +607,36 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_ns_persistent(NsArgs a) {
         ss.stop[v] = -1;
         ss.n[v] = 0;
     }
+    proc.init();
     __syncthreads();
-    uint32_t gen = s_gen;
+    uint32_t gen = sh.gen;
     const bool one = a.nvol == 1;  // one volume: the stopping rule rides on the barrier
-    const NsVol* vone = one ? &s_vol : nullptr;
-    const unsigned long long n0 = s_n0;
+    const NsVol* vone = one ? &sh.vol : nullptr;
+    const unsigned long long n0 = sh.n0;
     uint32_t streak = 0;
     const uint32_t patience = (uint32_t)min(max(a.patience, 0), 0xFFFF);
-    uint32_t mphase[2] = {0u, 0u};
     int ran = 0;
     uint64_t t0 = 0, t1 = 0;
-    int buf = 0;
     for (int it = 0; it < a.max_iters; ++it) {
         const uint32_t k = a.k0 + (uint32_t)it;
         const uint32_t p = k & 1u, c3 = k % 3u, c3n = (k + 1u) % 3u;
         const uint32_t* cur = a.bits[k % 4u];
         const uint32_t* prev = a.bits[(k + 3u) % 4u];
         const uint32_t sn = (k + 1u) % 4u, sz = (k + 2u) % 4u;
+        unsigned long long* cnt = one ? nullptr : a.cnt[c3];
         if (blockIdx.x == 0 && tid == 0) t0 = globaltimer_ns();
         if (blockIdx.x == 0)
             for (int v = tid; v < a.nvol; v += NT) a.cnt[c3n][v] = 0ull;
-        BlockTally tally;
-        // Ranks of the bricks to update (A_k) and to flush (A_{k-1} \ A_k):
-        // thread t counts the words t, t+NT, ...; ranks follow (thread, word).
-        // The first kScanCache words of each thread are kept in shared memory.
+        // Ranks: thread t counts the words t, t+NT, ...; ranks follow (thread,
+        // word).  The first kScanCache words of each thread stay in shared
+        // memory for the second pass.
         uint32_t ca = 0, cf = 0;
 #pragma unroll
         for (int m = 0; m < kScanCache; ++m) {
             const uint32_t w = tid + (uint32_t)m * NT;
             const uint32_t c = w < a.NW ? cur[w] : 0u;
             const uint32_t f = w < a.NW ? prev[w] & ~c : 0u;
-            s_scan[m][tid] = make_uint2(c, f);
+            sh.scan[m][tid] = make_uint2(c, f);
             ca += __popc(c);
             cf += __popc(f);
         }
@@ -650,56 +674,30 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_ns_persistent(NsArgs a) {
                 };
                 for (int m = 0; m < kScanCache; ++m) {
                     const uint32_t w = tid + (uint32_t)m * NT;
-                    const uint2 cf2 = s_scan[m][tid];
-                    if (cf2.x) visit(w, cf2.x, ra, hia, s_work);
-                    if (cf2.y) visit(w, cf2.y, rf, hif, s_flush);
+                    const uint2 cf2 = sh.scan[m][tid];
+                    if (cf2.x) visit(w, cf2.x, ra, hia, sh.work);
+                    if (cf2.y) visit(w, cf2.y, rf, hif, sh.flush);
                     ra += __popc(cf2.x);
                     rf += __popc(cf2.y);
                 }
                 for (uint32_t w = tid + kScanCache * NT; w < a.NW; w += NT) {
                     const uint32_t c = cur[w], f = prev[w] & ~c;
-                    if (c) visit(w, c, ra, hia, s_work);
-                    if (f) visit(w, f, rf, hif, s_flush);
+                    if (c) visit(w, c, ra, hia, sh.work);
+                    if (f) visit(w, f, rf, hif, sh.flush);
                     ra += __popc(c);
                     rf += __popc(f);
                 }
             }
             __syncthreads();
-            uint32_t q = 0;
-            while (q < nw && s_work[q] == kNoBrick) ++q;
-            if (q < nw) {
-                if (tid == 0) ns_issue_loads<S, NT>(a, sm, s_work[q], p, buf, vone);
-                ns_fetch_mask<S, NT>(a, sm, s_work[q], p, buf);
-            }
-            while (q < nw) {
-                uint32_t q2 = q + 1;
-                while (q2 < nw && s_work[q2] == kNoBrick) ++q2;
-                if (q2 < nw) {
-                    if (tid == 0) ns_issue_loads<S, NT>(a, sm, s_work[q2], p, buf ^ 1, vone);
-                    ns_fetch_mask<S, NT>(a, sm, s_work[q2], p, buf ^ 1);
-                }
-                ns_process_brick<S, NT>(a, sm, s_work[q], p, sn, buf, mphase, tally,
-                                        one ? nullptr : a.cnt[c3], vone);
-                buf ^= 1;
-                q = q2;
-            }
-            for (uint32_t r = 0; r < nf; ++r)
-                if (s_flush[r] != kNoBrick) ns_flush_brick<S, NT>(a, s_flush[r], p, vone);
-            __syncthreads();
+            proc.chunk(a, sh, nw, nf, p, sn, cnt, vone);  // ends with a block barrier
         }
-        unsigned long long mine = 0;
-        if (tid == 0) {
-            mine = tally.iter;
-            tally.flush(a.vstate, one ? nullptr : a.cnt[c3]);
-        }
+        proc.finish(a, sh, cnt);
         for (uint32_t w = blockIdx.x * NT + tid; w < a.NW; w += G * NT) a.bits[sz][w] = 0u;
-        if (tid == 0) {
-            tma_store_wait_all();
-            asm volatile("fence.proxy.async.global;" ::: "memory");
-        }
         if (blockIdx.x == 0 && tid == 0) t1 = globaltimer_ns();
         __syncthreads();
         if (tid == 0) {
+            const unsigned long long mine = sh.upd;
+            sh.upd = 0;
             const uint32_t target = gen + 1;
             __threadfence();
             const unsigned long long old = atomicAdd(&a.ctl->bar_arrive, (mine << kArriveShift) | 1ull);
@@ -728,14 +726,14 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_ns_persistent(NsArgs a) {
                     if ((uint32_t)rel == target) break;
                     if (globaltimer_ns() - w0 > kWaitLimitNs) {
                         set_error(&a.ctl->err, ERR_BARRIER_TIMEOUT);
-                        s_abort = 1;
+                        sh.abort = 1;
                         break;
                     }
                     __nanosleep(ns);
                     if (ns < 64) ns <<= 1;
                 }
             }
-            s_rel = rel;
+            sh.rel = rel;
             gen = target;
             asm volatile("fence.proxy.async.global;" ::: "memory");
             if (blockIdx.x == 0) {
@@ -747,9 +745,9 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_ns_persistent(NsArgs a) {
         __syncthreads();
         // A block that gave up leaves; the others then give up at the next
         // barrier (bounded), so every block ends.
-        if (s_abort) { ran = it; break; }
+        if (sh.abort) { ran = it; break; }
         if (one) {
-            const unsigned long long rel = s_rel;
+            const unsigned long long rel = sh.rel;
             streak = (uint32_t)(rel >> kRelStreakShift) & 0xFFFFu;
             ran = it + 1;
             if (rel & kRelStop) {
@@ -762,7 +760,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_ns_persistent(NsArgs a) {
             continue;
         }
         // Stopping rule, evaluated identically by every block.
-        if (tid == 0) s_live = 0;
+        if (tid == 0) sh.live = 0;
         __syncthreads();
         for (int v = tid; v < a.nvol; v += NT) {
             if (ss.done[v]) continue;
@@ -770,8 +768,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_ns_persistent(NsArgs a) {
             ss.n[v] = n;
             bool stop;
             if (a.conv_mode) {
-                const unsigned long long n0 = a.vstate[v].n0;
-                ss.streak[v] = ((double)n < a.rel * (double)n0) ? ss.streak[v] + 1 : 0;
+                const unsigned long long nv0 = a.vstate[v].n0;
+                ss.streak[v] = ((double)n < a.rel * (double)nv0) ? ss.streak[v] + 1 : 0;
                 stop = ss.streak[v] >= a.patience || n <= a.abs_thr || it + 1 >= a.max_iters;
             } else {
                 stop = it + 1 >= a.max_iters;
@@ -780,12 +778,12 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_ns_persistent(NsArgs a) {
                 ss.done[v] = 1;
                 ss.stop[v] = it;
             } else {
-                atomicAdd(&s_live, 1);
+                atomicAdd(&sh.live, 1);
             }
         }
         __syncthreads();
         ran = it + 1;
-        if (s_live == 0) break;
+        if (sh.live == 0) break;
     }
     __syncthreads();
     if (one && tid == 0) {
@@ -805,6 +803,260 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_ns_persistent(NsArgs a) {
         }
         if (tid == 0) a.ctl->iters_run = (uint32_t)ran;
     }
+}
+
+// Block-per-brick processing: all NT threads of the block work on one brick
+// at a time (the next brick's loads in flight).
+template <class S, int NT>
+struct BlockProc {
+    NsSmem<S, NT>& sm;
+    uint32_t mphase[2];
+    int buf;
+    BlockTally tally;  // thread 0
+    __device__ explicit BlockProc(NsSmem<S, NT>& s) : sm(s), mphase{0u, 0u}, buf(0) {}
+    __device__ void init() {
+        if (threadIdx.x == 0) {
+            mbar_init(&sm.bar[0], 1);
+            mbar_init(&sm.bar[1], 1);
+        }
+    }
+    __device__ void chunk(const NsArgs& a, IterShared<NT>& sh, uint32_t nw, uint32_t nf, uint32_t p,
+                          uint32_t sn, unsigned long long* cnt, const NsVol* vone) {
+        const int tid = threadIdx.x;
+        uint32_t q = 0;
+        while (q < nw && sh.work[q] == kNoBrick) ++q;
+        if (q < nw) {
+            if (tid == 0) ns_issue_loads<S, NT>(a, sm, sh.work[q], p, buf, vone);
+            ns_fetch_mask<S, NT>(a, sm, sh.work[q], p, buf);
+        }
+        while (q < nw) {
+            uint32_t q2 = q + 1;
+            while (q2 < nw && sh.work[q2] == kNoBrick) ++q2;
+            if (q2 < nw) {
+                if (tid == 0) ns_issue_loads<S, NT>(a, sm, sh.work[q2], p, buf ^ 1, vone);
+                ns_fetch_mask<S, NT>(a, sm, sh.work[q2], p, buf ^ 1);
+            }
+            ns_process_brick<S, NT>(a, sm, sh.work[q], p, sn, buf, mphase, tally, cnt, vone);
+            buf ^= 1;
+            q = q2;
+        }
+        for (uint32_t r = 0; r < nf; ++r)
+            if (sh.flush[r] != kNoBrick) ns_flush_brick<S>(a, sh.flush[r], p, vone, tid, NT);
+        __syncthreads();
+    }
+    __device__ void finish(const NsArgs& a, IterShared<NT>& sh, unsigned long long* cnt) {
+        if (threadIdx.x == 0) {
+            sh.upd = tally.iter;
+            tally.flush(a.vstate, cnt);
+            tally = BlockTally();
+            tma_store_wait_all();
+            asm volatile("fence.proxy.async.global;" ::: "memory");
+        }
+    }
+};
+
+// The persistent kernel, block per brick.  At least 1024 resident threads per
+// SM: 64 registers a thread at most.
+template <int BX, int BY, int BZ, int NT>
+__global__ void __launch_bounds__(NT, 1024 / NT) k_ns_persistent(NsArgs a) {
+    using S = Brick<BX, BY, BZ>;
+    __shared__ NsSmem<S, NT> sm;
+    __shared__ IterShared<NT> sh;
+    extern __shared__ int32_t s_dyn[];
+    BlockProc<S, NT> proc(sm);
+    ns_drive<NT>(a, sh, stop_state(s_dyn, a.nvol), proc);
+}
+
+// ---------------------------------------------------------------------------
+// Warp per brick: one block per SM, W warps, every warp updates its own
+// bricks with warp-level synchronisation only (no block barrier inside the
+// brick work), so up to W bricks per SM are in flight at once and the grid
+// barrier has one participant per SM.
+
+template <class S>
+struct WarpSlot {
+    static_assert((S::TILE_PAD * 4) % 128 == 0 && (S::VOX * 4) % 128 == 0, "TMA smem alignment");
+    alignas(128) float phi[S::TILE_PAD];  // halo tile of phi
+    alignas(128) float img[S::VOX];
+    alignas(128) float out[S::VOX];
+    unsigned long long act[S::WORDS];
+    uint32_t chg[S::CHG];
+    uint16_t list[S::VOX];
+    uint8_t chgb[S::VOX];
+    alignas(8) uint64_t bar;
+};
+
+// One brick of A_k by one warp: TMA load (lane 0) + mask fetch, pass 1 (copy,
+// ballot-prefix compaction of the active voxels), pass 2 (update), pass 3
+// (changed bytes -> ballot words), TMA store (lane 0), dilation into the 27
+// neighbours (one mask word per lane and round; one lane per neighbour sets
+// its membership bit).
+template <class S>
+__device__ __forceinline__ void ns_warp_brick(const NsArgs& a, WarpSlot<S>& sl, uint32_t b, uint32_t p,
+                                              uint32_t sn, uint32_t& phase, BlockTally& tally,
+                                              unsigned long long* cnt, const NsVol* vone) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t v = vone ? 0u : a.brick_vol[b];
+    const NsVol& V = vone ? *vone : a.vols[v];
+    const int3 o = brick_origin<S>(V, b);
+    if (lane < S::WORDS) {
+        unsigned long long* mp = a.masks[p] + (size_t)b * S::WORDS + lane;
+        sl.act[lane] = *mp;
+        *mp = 0ull;  // the mask array of parity p becomes the accumulator of iteration k+1
+    }
+    if (lane == 0) {
+        asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");  // this warp's last store read out[]
+        fence_proxy_async_smem();  // the warp's generic reads of the slot before the async writes
+        mbar_expect_tx(&sl.bar, (uint32_t)(S::TILE + S::VOX) * 4u);
+        tma_load_3d(sl.phi, &a.tmaps[V.tmap_base + p], o.x - 4, o.y - 1, o.z - 1, &sl.bar);
+        tma_load_3d(sl.img, &a.tmaps[V.tmap_base + 4], o.x, o.y, o.z, &sl.bar);
+    }
+    __syncwarp();
+    if (!mbar_wait(&sl.bar, phase)) set_error(&a.ctl->err, ERR_TMA_TIMEOUT);
+    phase ^= 1u;
+    float* phi = sl.phi;
+    // Clamp-to-edge halo where the tile leaves the volume (TMA filled zeros).
+    if (o.x < 4 || o.y < 1 || o.z < 1 || o.x + S::X + 4 > V.nx || o.y + S::Y + 1 > V.ny ||
+        o.z + S::Z + 1 > V.nz) {
+        for (int t = lane; t < S::TILE; t += 32) {
+            const int tx = t % S::TX, ty = (t / S::TX) % S::TY, tz = t / (S::TX * S::TY);
+            const int gx = o.x - 4 + tx, gy = o.y - 1 + ty, gz = o.z - 1 + tz;
+            const int cx = min(max(gx, 0), V.nx - 1), cy = min(max(gy, 0), V.ny - 1),
+                      cz = min(max(gz, 0), V.nz - 1);
+            if (cx != gx || cy != gy || cz != gz)
+                phi[t] = phi[((cz - o.z + 1) * S::TY + (cy - o.y + 1)) * S::TX + (cx - o.x + 4)];
+        }
+        __syncwarp();
+    }
+    auto tile_index = [](int j) {
+        const int lx = j % S::X, ly = (j / S::X) % S::Y, lz = j / (S::X * S::Y);
+        return ((lz + 1) * S::TY + (ly + 1)) * S::TX + (lx + 4);
+    };
+    const uint32_t lt = (1u << lane) - 1u;
+    // pass 1
+    uint32_t nact = 0;
+#pragma unroll 4
+    for (int g = 0; g < S::VOX / 32; ++g) {
+        const int j = lane + 32 * g;
+        sl.out[j] = phi[tile_index(j)];
+        sl.chgb[j] = 0;
+        const bool act = (sl.act[j >> 6] >> (j & 63)) & 1ull;
+        const uint32_t bal = __ballot_sync(0xffffffffu, act);
+        if (act) sl.list[nact + __popc(bal & lt)] = (uint16_t)j;
+        nact += __popc(bal);
+    }
+    __syncwarp();
+    // pass 2
+    for (uint32_t i = lane; i < nact; i += 32) {
+        const int j = sl.list[i];
+        const int ti = tile_index(j);
+        auto P = [&](int dx, int dy, int dz) { return phi[ti + (dz * S::TY + dy) * S::TX + dx]; };
+        float bb = 0.0f;
+        if (V.bias) {
+            const int lx = j % S::X, ly = (j / S::X) % S::Y, lz = j / (S::X * S::Y);
+            bb = V.bias[((size_t)(o.z + lz) * V.py + (o.y + ly)) * V.px + (o.x + lx)];
+        }
+        const float c = phi[ti];
+        const float nv = ns_update_f32(P, sl.img[j], bb, V);
+        sl.out[j] = nv;
+        sl.chgb[j] = fabsf(nv - c) > V.thr_t;
+    }
+    fence_proxy_async_smem();
+    __syncwarp();
+    // pass 3
+    bool any = false;
+#pragma unroll 4
+    for (int g = 0; g < S::VOX / 32; ++g) {
+        const uint32_t bal = __ballot_sync(0xffffffffu, sl.chgb[lane + 32 * g] != 0);
+        if (lane == 0) sl.chg[g] = bal;
+        any |= bal != 0u;
+    }
+    __syncwarp();
+    if (lane == 0) {
+        tma_store_3d(&a.tmaps[V.tmap_base + 2 + (p ^ 1u)], o.x, o.y, o.z, sl.out);
+        tma_store_commit();
+        tally.add(a.vstate, cnt, v, nact);
+    }
+    if (any) {
+        constexpr int ROUNDS = (27 * S::WORDS + 31) / 32;
+#pragma unroll
+        for (int r = 0; r < ROUNDS; ++r) {
+            const int t = lane + r * 32;
+            const int slot = t / S::WORDS, w = t % S::WORDS;
+            uint64_t x = 0ull;
+            uint32_t nb = 0;
+            if (slot < 27) {
+                const int ox = slot % 3 - 1, oy = (slot / 3) % 3 - 1, oz = slot / 9 - 1;
+                const int bx = o.x / S::X + ox, by = o.y / S::Y + oy, bz = o.z / S::Z + oz;
+                // Voxels of the neighbour inside the volume along each axis
+                // (bricks in the padding beyond the volume hold none).
+                const int lx = V.nx - bx * S::X, ly = V.ny - by * S::Y, lz = V.nz - bz * S::Z;
+                if (bx >= 0 && by >= 0 && bz >= 0 && lx > 0 && ly > 0 && lz > 0) {
+                    x = dilate_word<S>(sl.chg, ox, oy, oz, w, V.nbh);
+                    if (lx < S::X || ly < S::Y || lz < S::Z)
+                        x &= inside_mask<S>(w, min(lx, S::X), min(ly, S::Y), min(lz, S::Z));
+                    nb = b + (int32_t)((oz * V.nby + oy) * V.nbx + ox);
+                    if (x) atomicOr(&a.masks[p ^ 1u][(size_t)nb * S::WORDS + w], (unsigned long long)x);
+                }
+            }
+            // The WORDS lanes of a neighbour are adjacent lanes.
+            const uint32_t bal = __ballot_sync(0xffffffffu, x != 0ull);
+            const int g0 = lane & ~(S::WORDS - 1);
+            const uint32_t gmask = (S::WORDS >= 32 ? 0xffffffffu : ((1u << S::WORDS) - 1u)) << g0;
+            if (lane == g0 && (bal & gmask)) atomicOr(&a.bits[sn][nb >> 5], 1u << (nb & 31));
+        }
+    }
+    __syncwarp();
+}
+
+template <class S, int W>
+struct WarpProc {
+    static constexpr int NT = W * 32;
+    WarpSlot<S>* slots;
+    uint32_t phase;    // this warp's load barrier phase
+    BlockTally tally;  // lane 0 of every warp
+    __device__ explicit WarpProc(WarpSlot<S>* s) : slots(s), phase(0u) {}
+    __device__ void init() {
+        if ((threadIdx.x & 31) == 0) mbar_init(&slots[threadIdx.x >> 5].bar, 1);
+    }
+    __device__ void chunk(const NsArgs& a, IterShared<NT>& sh, uint32_t nw, uint32_t nf, uint32_t p,
+                          uint32_t sn, unsigned long long* cnt, const NsVol* vone) {
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        WarpSlot<S>& sl = slots[warp];
+        for (uint32_t q = warp; q < nw; q += W)
+            if (sh.work[q] != kNoBrick) ns_warp_brick<S>(a, sl, sh.work[q], p, sn, phase, tally, cnt, vone);
+        for (uint32_t q = warp; q < nf; q += W)
+            if (sh.flush[q] != kNoBrick) ns_flush_brick<S>(a, sh.flush[q], p, vone, lane, 32);
+        __syncthreads();
+    }
+    __device__ void finish(const NsArgs& a, IterShared<NT>& sh, unsigned long long* cnt) {
+        if ((threadIdx.x & 31) == 0) {
+            if (tally.iter) atomicAdd(&sh.upd, tally.iter);
+            tally.flush(a.vstate, cnt);
+            tally = BlockTally();
+            tma_store_wait_all();
+            asm volatile("fence.proxy.async.global;" ::: "memory");
+        }
+    }
+};
+
+// Dynamic shared memory of the warp kernel: 128 bytes of alignment slack, the
+// W warp slots, then the stopping state.
+template <class S, int W>
+__host__ __device__ constexpr size_t warp_smem_fixed() {
+    return 128 + (size_t)W * sizeof(WarpSlot<S>);
+}
+
+template <int BX, int BY, int BZ, int W>
+__global__ void __launch_bounds__(W * 32, 1) k_ns_warp(NsArgs a) {
+    using S = Brick<BX, BY, BZ>;
+    __shared__ IterShared<W * 32> sh;
+    extern __shared__ unsigned char s_dyn_raw[];
+    unsigned char* dyn = s_dyn_raw + ((128u - (smem_addr(s_dyn_raw) & 127u)) & 127u);
+    WarpSlot<S>* slots = reinterpret_cast<WarpSlot<S>*>(dyn);
+    int32_t* state = reinterpret_cast<int32_t*>(s_dyn_raw + warp_smem_fixed<S, W>());
+    WarpProc<S, W> proc(slots);
+    ns_drive<W * 32>(a, sh, stop_state(state, a.nvol), proc);
 }
 
 // Initial active set of every brick: voxels whose 6-neighbours differ by more
