@@ -32,6 +32,7 @@ UNITS = [
     ("engine_host.cu", []),
     ("lss_api.cpp", ["-x", "cu"]),
     ("compact_api.cu", []),
+    ("ns_adjoint.cu", []),
     ("phantom.cpp", []),
 ]
 

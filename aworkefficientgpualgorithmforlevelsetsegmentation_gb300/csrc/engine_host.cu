@@ -225,6 +225,17 @@ class NsEngine : public EngineBase {
         return it;
     }
 
+    void adjoint(int K, int every, const uint8_t* target, float scale, const float* bias, float* dbias,
+                 lss_grads* out) override {
+        require();
+        LSS_REQUIRE(core_->initialized(), LSS_ERR_STATE, "no seed or phi set");
+        if (pending_reinit_) {
+            core_->init_active();
+            after_init();
+        }
+        ns_adjoint(*core_, K, every, target, scale, bias, dbias, out);
+    }
+
     double step_dense(int n) override {
         require();
         LSS_REQUIRE(core_->initialized(), LSS_ERR_STATE, "no seed or phi set");

@@ -21,6 +21,11 @@ struct BrickConfig {
 
 const std::vector<BrickConfig>& brick_configs();
 
+class NsCore;
+// The differentiation form (csrc/ns_adjoint.cu).
+void ns_adjoint(NsCore& core, int K, int every, const uint8_t* target, float tau, const float* bias,
+                float* dbias, lss_grads* out);
+
 class NsCore {
    public:
     NsCore(EngineBase* owner, uint64_t budget);
@@ -54,6 +59,11 @@ class NsCore {
     double last_barrier_ms() const { return last_barrier_ns_ * 1e-6; }
     uint64_t bricks() const { return NB_; }
     int grid() const { return grid_; }
+    int words() const { return words_; }
+    uint64_t budget_left() const { return arena_.budget_left(); }
+    const unsigned long long* masks(uint32_t parity) const { return d_masks_[parity & 1u]; }
+    NsVol descriptor(int v) const;  // host copy of the device descriptor of volume v
+    EngineBase* owner() const { return owner_; }
 
     struct VolHost {
         int nx = 0, ny = 0, nz = 0, px = 0, py = 0, pz = 0, nbx = 0, nby = 0, nbz = 0;

@@ -313,29 +313,32 @@ size_t NsCore::dyn_smem() const {
     return kernels(cfg_).smem_fixed + stop_state_bytes((int)vols_.size());
 }
 
+NsVol NsCore::descriptor(int i) const {
+    const VolHost& v = vols_.at(i);
+    NsVol o;
+    std::memset(&o, 0, sizeof(o));
+    o.nx = v.nx; o.ny = v.ny; o.nz = v.nz;
+    o.px = v.px; o.py = v.py; o.pz = v.pz;
+    o.nbx = v.nbx; o.nby = v.nby; o.nbz = v.nbz;
+    o.brick_base = v.brick_base;
+    o.phi[0] = v.phi[0]; o.phi[1] = v.phi[1];
+    o.img = v.img;
+    o.bias = v.bias;
+    o.T = v.p.target; o.eps = v.p.window; o.alpha = v.p.curvature; o.dt = v.p.time_step;
+    o.lo = v.p.phi_min; o.hi = v.p.phi_max;
+    o.thr_t = v.p.temporal_threshold; o.thr_s = v.p.spatial_threshold;
+    o.alpha_data = v.p.alpha_role == LSS_ALPHA_CURVATURE ? 0 : 1;
+    o.inv_eps = 1.0f / v.p.window;
+    o.wc = o.alpha_data ? 1.0f - v.p.curvature : v.p.curvature;
+    o.wd = 1.0f - o.wc;
+    o.nbh = v.p.neighbourhood == 6 ? 6 : 26;
+    o.tmap_base = (uint32_t)(5 * i);
+    return o;
+}
+
 void NsCore::upload_descriptors() {
     std::vector<NsVol> d(vols_.size());
-    for (size_t i = 0; i < vols_.size(); ++i) {
-        const VolHost& v = vols_[i];
-        NsVol& o = d[i];
-        std::memset(&o, 0, sizeof(o));
-        o.nx = v.nx; o.ny = v.ny; o.nz = v.nz;
-        o.px = v.px; o.py = v.py; o.pz = v.pz;
-        o.nbx = v.nbx; o.nby = v.nby; o.nbz = v.nbz;
-        o.brick_base = v.brick_base;
-        o.phi[0] = v.phi[0]; o.phi[1] = v.phi[1];
-        o.img = v.img;
-        o.bias = v.bias;
-        o.T = v.p.target; o.eps = v.p.window; o.alpha = v.p.curvature; o.dt = v.p.time_step;
-        o.lo = v.p.phi_min; o.hi = v.p.phi_max;
-        o.thr_t = v.p.temporal_threshold; o.thr_s = v.p.spatial_threshold;
-        o.alpha_data = v.p.alpha_role == LSS_ALPHA_CURVATURE ? 0 : 1;
-        o.inv_eps = 1.0f / v.p.window;
-        o.wc = o.alpha_data ? 1.0f - v.p.curvature : v.p.curvature;
-        o.wd = 1.0f - o.wc;
-        o.nbh = v.p.neighbourhood == 6 ? 6 : 26;
-        o.tmap_base = (uint32_t)(5 * i);
-    }
+    for (size_t i = 0; i < vols_.size(); ++i) d[i] = descriptor((int)i);
     if (d_vols_)
         LSS_CUDA(cudaMemcpyAsync(d_vols_, d.data(), d.size() * sizeof(NsVol), cudaMemcpyHostToDevice,
                                  owner_->stream));

@@ -32,7 +32,7 @@ def _stale(out: str, srcs: list[str]) -> bool:
 
 def build(force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    srcs = [os.path.join(HERE, f) for f in ("lss_oracle.cpp", "ref_model.hpp", "ns_model.hpp")]
+    srcs = [os.path.join(HERE, f) for f in ("lss_oracle.cpp", "ref_model.hpp", "ns_model.hpp", "ns_adjoint.hpp")]
     if force or _stale(LIB, srcs):
         cmd = ["g++", *CXXFLAGS, "-I", HERE, srcs[0], "-o", LIB + ".tmp"]
         subprocess.run(cmd, check=True)

@@ -12,6 +12,7 @@
 #ifdef LSS_ORACLE_REFERENCE_KERNELS
 #include "ref_shim/ref_backend.hpp"
 #endif
+#include "ns_adjoint.hpp"
 #include "ns_model.hpp"
 #include "ref_model.hpp"
 
@@ -147,6 +148,7 @@ void ons_set_threads(void* h, int t) { ((NsOracle*)h)->threads = t; }
 
 void ons_set_bias(void* h, const float* b) {
     NsOracle* o = (NsOracle*)h;
+    o->bias64.clear();
     if (!b) { o->bias.clear(); return; }
     o->bias.assign(b, b + o->phi.size());
 }
@@ -221,6 +223,48 @@ uint64_t ons_expand_given(void* h, const uint64_t* act, uint64_t n, const float*
     o->expand(changed);
     std::memcpy(out, o->active.data(), o->active.size() * 8);
     return o->active.size();
+}
+
+// ---- FP64 adjoint (ns_adjoint.hpp) ----------------------------------------
+// Active sets recorded by the last ons_adj_run of each handle.
+static std::vector<std::vector<uint64_t>>& adj_sets(void* h) {
+    static thread_local std::vector<std::pair<void*, std::vector<std::vector<uint64_t>>>> table;
+    for (auto& e : table)
+        if (e.first == h) return e.second;
+    table.push_back({h, {}});
+    return table.back().second;
+}
+
+// K iterations from the current state (recorded active sets), the soft-Dice
+// loss and its gradients: out[0..3] = loss, dT, deps, dalpha; dbias (nullable,
+// nx*ny*nz doubles).  The oracle's state is unchanged.
+void ons_adj_run(void* h, int K, const uint8_t* target, double tau, double* out, double* dbias) {
+    NsOracle* o = (NsOracle*)h;
+    lssns::AdjointResult r = lssns::adjoint_run(*o, K, target, tau, adj_sets(h));
+    out[0] = r.loss; out[1] = r.dT; out[2] = r.deps; out[3] = r.dalpha;
+    if (dbias) std::memcpy(dbias, r.dbias.data(), r.dbias.size() * 8);
+}
+
+// The loss of K iterations replaying the active sets of the last
+// ons_adj_run (finite differences under the fixed-set convention).
+double ons_adj_loss(void* h, int K, const uint8_t* target, double tau) {
+    NsOracle* o = (NsOracle*)h;
+    return lssns::adjoint_forward(*o, K, target, tau, adj_sets(h), true, nullptr);
+}
+
+// Sets one parameter: 0 T, 1 eps, 2 alpha.
+void ons_set_param(void* h, int which, double v) {
+    NsOracle* o = (NsOracle*)h;
+    if (which == 0) o->p.T = v;
+    if (which == 1) o->p.eps = v;
+    if (which == 2) o->p.alpha = v;
+}
+
+// Bias from doubles (finite differences need perturbations below fp32 ulp).
+void ons_set_bias64(void* h, const double* b) {
+    NsOracle* o = (NsOracle*)h;
+    if (!b) { o->bias64.clear(); return; }
+    o->bias64.assign(b, b + o->phi.size());
 }
 #endif
 

@@ -96,7 +96,8 @@ class NsOracle {
     Params p;
     std::vector<double> phi;
     std::vector<float> I;
-    std::vector<float> bias;  // empty = none
+    std::vector<float> bias;      // empty = none
+    std::vector<double> bias64;   // overrides bias when non-empty (finite differences)
     std::vector<uint64_t> active;  // linear indices, brick-major order
     std::vector<uint8_t> mark;     // scratch membership volume
     std::vector<uint8_t> bmark;    // scratch brick flags
@@ -105,6 +106,11 @@ class NsOracle {
     std::vector<double> last_old, last_new;  // values of the last step, list order
 
     size_t idx(int x, int y, int z) const { return ((size_t)z * ny + y) * nx + x; }
+
+    double bias_at(uint64_t li) const {
+        if (!bias64.empty()) return bias64[li];
+        return bias.empty() ? 0.0 : (double)bias[li];
+    }
 
     void init(int nx_, int ny_, int nz_, const float* img, int bx_, int by_, int bz_) {
         nx = nx_; ny = ny_; nz = nz_;
@@ -221,7 +227,7 @@ class NsOracle {
             for (size_t i = a; i < b; ++i) {
                 uint64_t li = active[i];
                 int x = (int)(li % nx), y = (int)((li / nx) % ny), z = (int)(li / ((size_t)nx * ny));
-                double bb = bias.empty() ? 0.0 : (double)bias[li];
+                double bb = bias_at(li);
                 double nv = ns_update<double>(P, x, y, z, (double)I[li], bb, p);
                 last_old[i] = phi[li];
                 last_new[i] = nv;

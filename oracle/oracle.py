@@ -78,6 +78,11 @@ def lib() -> C.CDLL:
         L.ons_read_phi64.argtypes = [_P, _P]
         L.ons_expand_given.restype = C.c_uint64
         L.ons_expand_given.argtypes = [_P, _P, C.c_uint64, _P, _P, _P]
+        L.ons_adj_run.argtypes = [_P, C.c_int, _P, C.c_double, _P, _P]
+        L.ons_adj_loss.restype = C.c_double
+        L.ons_adj_loss.argtypes = [_P, C.c_int, _P, C.c_double]
+        L.ons_set_param.argtypes = [_P, C.c_int, C.c_double]
+        L.ons_set_bias64.argtypes = [_P, _P]
         _libs["oracle"] = L
     return _libs["oracle"]
 
@@ -298,3 +303,29 @@ class NsOracle:
         out = np.zeros(a.size * 27 + 1, np.uint64)
         m = self._L.ons_expand_given(self._h, _ptr(a), a.size, _ptr(b), _ptr(c), _ptr(out))
         return out[:m]
+
+    # ---- FP64 adjoint (ns_adjoint.hpp) ----
+    def adjoint(self, K: int, target: np.ndarray, tau: float = 0.5) -> dict:
+        """K iterations from the current state with the active sets recorded
+        (and kept for adjoint_loss), the soft-Dice loss and its gradients."""
+        t = np.ascontiguousarray(target, np.uint8)
+        out = np.zeros(4, np.float64)
+        db = np.zeros(self.shape, np.float64)
+        self._L.ons_adj_run(self._h, K, _ptr(t), tau, _ptr(out), _ptr(db))
+        return {"loss": out[0], "d_target": out[1], "d_window": out[2], "d_curvature": out[3],
+                "d_bias": db}
+
+    def adjoint_loss(self, K: int, target: np.ndarray, tau: float = 0.5) -> float:
+        """The loss of K iterations replaying the active sets of adjoint()."""
+        t = np.ascontiguousarray(target, np.uint8)
+        return float(self._L.ons_adj_loss(self._h, K, _ptr(t), tau))
+
+    def set_param(self, which: str, value: float):
+        self._L.ons_set_param(self._h, {"T": 0, "eps": 1, "alpha": 2}[which], value)
+
+    def set_bias64(self, bias: np.ndarray | None):
+        if bias is None:
+            self._L.ons_set_bias64(self._h, None)
+        else:
+            self._bias64 = np.ascontiguousarray(bias, np.float64)
+            self._L.ons_set_bias64(self._h, _ptr(self._bias64))

@@ -1,0 +1,115 @@
+"""The GPU adjoint (lss_adjoint_run) against the FP64 adjoint oracle, its
+checkpointing, the engine state it must leave alone, and a torch.autograd
+wrapper (test harness only) driving an Adam fit of T / eps / alpha."""
+import numpy as np
+import pytest
+
+import aworkefficientgpualgorithmforlevelsetsegmentation_gb300 as lss
+from aworkefficientgpualgorithmforlevelsetsegmentation_gb300 import phantoms as P
+from oracle.oracle import NsOracle
+
+pytestmark = pytest.mark.gpu
+
+
+def make(cfg, brick=(8, 8, 8), threads=256):
+    p = cfg["params"]
+    s = lss.Segmenter(lss.MODE_NS, brick=brick, threads_per_brick=threads)
+    s.load_volume(cfg["image"])
+    s.set_parameters(p.target, p.window, p.curvature, p.time_step, alpha_role=p.alpha_role)
+    s.set_phi(cfg["phi0"])
+    return s
+
+
+def oracle_adjoint(cfg, K, bias=None):
+    p = cfg["params"]
+    o = NsOracle(cfg["image"], threads=8)
+    o.set_params(p.target, p.window, p.curvature, p.time_step, alpha_data=p.alpha_role)
+    if bias is not None:
+        o.set_bias(bias)
+    o.set_phi(cfg["phi0"])
+    return o.adjoint(K, cfg["target"], 0.5)
+
+
+def rel(a, b):
+    return abs(a - b) / max(abs(b), 1e-30)
+
+
+@pytest.mark.parametrize("brick,threads,K,every", [((8, 8, 8), 256, 16, 4), ((8, 8, 4), 32, 24, 5),
+                                                   ((4, 4, 4), 64, 12, 12)])
+def test_gpu_adjoint_matches_fp64_adjoint(brick, threads, K, every):
+    cfg = P.config4(0.25)
+    rng = np.random.default_rng(3)
+    bias = (0.05 * rng.standard_normal(cfg["image"].shape)).astype(np.float32)
+    g = make(cfg, brick, threads).adjoint(K, every, cfg["target"], 0.5, bias=bias)
+    o = oracle_adjoint(cfg, K, bias)
+    assert abs(g["loss"] - o["loss"]) <= 1e-5
+    for key in ("d_target", "d_window", "d_curvature"):
+        assert rel(g[key], o[key]) <= 1e-3, (key, g[key], o[key])
+    db, ob = g["d_bias"].astype(np.float64), o["d_bias"]
+    assert np.linalg.norm(db - ob) <= 1e-3 * np.linalg.norm(ob)
+
+
+def test_gpu_adjoint_checkpoint_spacing_is_invisible():
+    cfg = P.config4(0.25)
+    s = make(cfg)
+    ref = s.adjoint(20, 20, cfg["target"])
+    for every in (1, 4, 7):
+        g = s.adjoint(20, every, cfg["target"])
+        assert g["loss"] == ref["loss"]
+        for key in ("d_target", "d_window", "d_curvature"):
+            assert rel(g[key], ref[key]) <= 1e-5
+        assert np.allclose(g["d_bias"], ref["d_bias"], rtol=1e-4, atol=1e-9)
+
+
+def test_gpu_adjoint_leaves_engine_state():
+    cfg = P.config4(0.25)
+    s = make(cfg)
+    s.step(5)
+    phi, act = s.read_phi(), s.active_linear()
+    s.adjoint(16, 4, cfg["target"])
+    assert np.array_equal(s.read_phi(), phi)
+    assert np.array_equal(s.active_linear(), act)
+    s.step(3)  # the engine keeps running from where it was
+
+
+def test_autograd_wrapper_and_adam_fit():
+    torch = pytest.importorskip("torch")
+    cfg = P.config4(0.25)
+    s = make(cfg)
+    K, every = 24, 6
+
+    class LevelSetLoss(torch.autograd.Function):
+        """loss(T, eps, alpha, bias) through lss_adjoint_run (harness only)."""
+
+        @staticmethod
+        def forward(ctx, T, eps, alpha, bias):
+            p = cfg["params"]
+            s.set_parameters(float(T), float(eps), float(alpha), p.time_step, alpha_role=p.alpha_role)
+            s.set_phi(cfg["phi0"])
+            g = s.adjoint(K, every, cfg["target"], 0.5, bias=bias.detach().cpu().numpy())
+            ctx.save_for_backward(torch.tensor([g["d_target"], g["d_window"], g["d_curvature"]],
+                                               dtype=torch.float64),
+                                  torch.from_numpy(g["d_bias"]))
+            return torch.tensor(g["loss"], dtype=torch.float64)
+
+        @staticmethod
+        def backward(ctx, gl):
+            gs, gb = ctx.saved_tensors
+            return gl * gs[0], gl * gs[1], gl * gs[2], (gl * gb).to(torch.float32)
+
+    T = torch.tensor(0.6, dtype=torch.float64, requires_grad=True)
+    eps = torch.tensor(0.1, dtype=torch.float64, requires_grad=True)
+    alpha = torch.tensor(0.9, dtype=torch.float64, requires_grad=True)
+    bias = torch.zeros(cfg["image"].shape, dtype=torch.float32)
+    opt = torch.optim.Adam([T, eps, alpha], lr=1e-2)
+    losses = []
+    for _ in range(20):
+        opt.zero_grad()
+        loss = LevelSetLoss.apply(T, eps, alpha, bias)
+        loss.backward()
+        opt.step()
+        with torch.no_grad():
+            eps.clamp_(0.02, 1.0)
+            alpha.clamp_(0.0, 1.0)
+        losses.append(float(loss.detach()))
+    assert losses[-1] < losses[0] - 1e-3, losses
