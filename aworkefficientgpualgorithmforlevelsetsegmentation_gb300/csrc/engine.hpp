@@ -54,6 +54,10 @@ class EngineBase {
     virtual void unload_volume() = 0;
     virtual void set_params(const lss_params& p) = 0;
     virtual void initialize_seed(float cx, float cy, float cz, float r) = 0;
+    // Several seeds (x, y, z, r) in a row; the default seeds them one by one.
+    virtual void initialize_seeds(const float* xyzr, int count) {
+        for (int k = 0; k < count; ++k) initialize_seed(xyzr[4 * k], xyzr[4 * k + 1], xyzr[4 * k + 2], xyzr[4 * k + 3]);
+    }
     virtual void set_phi(const float* phi) = 0;
     virtual int step(int n, const lss_conv* conv) = 0;  // conv == nullptr: exactly n
     virtual bool finished() = 0;

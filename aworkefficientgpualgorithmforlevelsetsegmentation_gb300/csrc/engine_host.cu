@@ -196,6 +196,16 @@ class NsEngine : public EngineBase {
         after_init();
     }
 
+    // The active set depends on phi only, so one rebuild after the union of
+    // all spheres gives the same state as one per sphere.
+    void initialize_seeds(const float* xyzr, int count) override {
+        require();
+        for (int k = 0; k < count; ++k)
+            core_->sphere_union(0, xyzr[4 * k], xyzr[4 * k + 1], xyzr[4 * k + 2], xyzr[4 * k + 3]);
+        core_->init_active();
+        after_init();
+    }
+
     void set_phi(const float* phi) override {
         require();
         core_->set_phi(0, phi);

@@ -202,10 +202,7 @@ lss_status lss_initialize_seed(lss_engine* e, float cx, float cy, float cz, floa
 lss_status lss_set_seed_spheres(lss_engine* e, const float* s, int32_t count) {
     CHECK_ENGINE(e);
     if (!s || count <= 0) return LSS_ERR_INVALID_ARGUMENT;
-    return guard(e, [&] {
-        for (int32_t k = 0; k < count; ++k)
-            e->impl->initialize_seed(s[4 * k], s[4 * k + 1], s[4 * k + 2], s[4 * k + 3]);
-    });
+    return guard(e, [&] { e->impl->initialize_seeds(s, count); });
 }
 
 lss_status lss_set_phi(lss_engine* e, const float* phi) {

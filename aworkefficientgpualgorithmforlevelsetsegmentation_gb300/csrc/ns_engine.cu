@@ -392,7 +392,9 @@ void NsCore::init_active() {
     NsArgs a = args(k_total_, 0, nullptr);
     uint32_t p = parity_, sl = s0;
     void* params[] = {&a, &p, &sl};
-    const int grid = (int)std::min<uint64_t>(NB_, (uint64_t)owner_->num_sms * 16);
+    const uint64_t warps = NB_ * (uint64_t)(ks.words * 2);  // 32 voxels per warp
+    const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((warps * 32 + ks.block - 1) / ks.block,
+                                                                    (uint64_t)owner_->num_sms * 16));
     LSS_CUDA(cudaLaunchKernel(ks.init_active, dim3(grid), dim3(ks.block), params, 0, st));
     ++owner_->launches;
     std::vector<unsigned long long> n0(vols_.size());

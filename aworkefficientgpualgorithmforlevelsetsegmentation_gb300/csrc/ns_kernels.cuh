@@ -1060,60 +1060,60 @@ __global__ void __launch_bounds__(W * 32, 1) k_ns_warp(NsArgs a) {
 }
 
 // Initial active set of every brick: voxels whose 6-neighbours differ by more
-// than thr_s (clamped coordinates), one block per brick; bricks with a
-// non-empty mask get their membership bit in bits[s].  Counts land in cnt[0].
+// than thr_s (clamped coordinates).  One thread per voxel slot in brick-major
+// order (grid-stride), so a warp covers 32 consecutive voxels of one brick
+// and its ballot is one 32-bit half of a mask word, stored directly; bricks
+// with a non-empty mask get their membership bit in bits[s].  Counts land in
+// cnt[0] (one atomic per warp and volume run).
 template <int BX, int BY, int BZ, int NT>
 __global__ void __launch_bounds__(NT) k_ns_init_active(NsArgs a, uint32_t p, uint32_t s) {
     using S = Brick<BX, BY, BZ>;
-    __shared__ uint32_t s_w[S::CHG];
-    for (uint32_t b = blockIdx.x; b < a.NB; b += gridDim.x) {
-        const uint32_t v = a.brick_vol[b];
+    const uint64_t total = (uint64_t)a.NB * S::VOX;
+    uint32_t cur_v = 0xFFFFFFFFu;
+    unsigned long long n = 0;
+    auto flush = [&]() {
+        for (int o = 16; o; o >>= 1) n += __shfl_down_sync(0xffffffffu, n, o);
+        if ((threadIdx.x & 31) == 0 && n && cur_v != 0xFFFFFFFFu) atomicAdd(&a.cnt[0][cur_v], n);
+        n = 0;
+    };
+    for (uint64_t t = blockIdx.x * (uint64_t)NT + threadIdx.x; t < total; t += (uint64_t)gridDim.x * NT) {
+        const uint32_t b = (uint32_t)(t / S::VOX);
+        const int j = (int)(t % S::VOX);
+        const uint32_t v = a.brick_vol[b];  // one brick per warp: uniform
+        if (v != cur_v) {
+            flush();
+            cur_v = v;
+        }
         const NsVol& V = a.vols[v];
         const int3 o = brick_origin<S>(V, b);
-        const float* ph = V.phi[p];
-        constexpr int VPT = (S::VOX + NT - 1) / NT;
-        for (int k = 0; k < VPT; ++k) {
-            const int j = threadIdx.x + k * NT;
-            bool act = false;
-            if (j < S::VOX) {
-                const int x = o.x + j % S::X, y = o.y + (j / S::X) % S::Y, z = o.z + j / (S::X * S::Y);
-                if (x < V.nx && y < V.ny && z < V.nz) {
-                    auto at = [&](int xx, int yy, int zz) {
-                        xx = min(max(xx, 0), V.nx - 1);
-                        yy = min(max(yy, 0), V.ny - 1);
-                        zz = min(max(zz, 0), V.nz - 1);
-                        return ph[((size_t)zz * V.py + yy) * V.px + xx];
-                    };
-                    const float c = at(x, y, z);
-                    float m = fabsf(at(x - 1, y, z) - c);
-                    m = fmaxf(m, fabsf(at(x + 1, y, z) - c));
-                    m = fmaxf(m, fabsf(at(x, y - 1, z) - c));
-                    m = fmaxf(m, fabsf(at(x, y + 1, z) - c));
-                    m = fmaxf(m, fabsf(at(x, y, z - 1) - c));
-                    m = fmaxf(m, fabsf(at(x, y, z + 1) - c));
-                    act = m > V.thr_s;
-                }
-            }
-            const uint32_t bal = __ballot_sync(0xffffffffu, act);
-            const int word = (threadIdx.x >> 5) + k * (NT / 32);
-            if ((threadIdx.x & 31) == 0 && word < S::CHG) s_w[word] = bal;
+        const int x = o.x + j % S::X, y = o.y + (j / S::X) % S::Y, z = o.z + j / (S::X * S::Y);
+        bool act = false;
+        if (x < V.nx && y < V.ny && z < V.nz) {
+            const float* ph = V.phi[p];
+            auto at = [&](int xx, int yy, int zz) {
+                xx = min(max(xx, 0), V.nx - 1);
+                yy = min(max(yy, 0), V.ny - 1);
+                zz = min(max(zz, 0), V.nz - 1);
+                return ph[((size_t)zz * V.py + yy) * V.px + xx];
+            };
+            const float c = at(x, y, z);
+            float m = fabsf(at(x - 1, y, z) - c);
+            m = fmaxf(m, fabsf(at(x + 1, y, z) - c));
+            m = fmaxf(m, fabsf(at(x, y - 1, z) - c));
+            m = fmaxf(m, fabsf(at(x, y + 1, z) - c));
+            m = fmaxf(m, fabsf(at(x, y, z - 1) - c));
+            m = fmaxf(m, fabsf(at(x, y, z + 1) - c));
+            act = m > V.thr_s;
         }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            unsigned long long n = 0;
-            for (int q = 0; q < S::WORDS; ++q) {
-                const unsigned long long w =
-                    (unsigned long long)s_w[2 * q] | ((unsigned long long)s_w[2 * q + 1] << 32);
-                a.masks[p][(size_t)b * S::WORDS + q] = w;
-                n += __popcll(w);
-            }
-            if (n) {
-                atomicOr(&a.bits[s][b >> 5], 1u << (b & 31));
-                atomicAdd(&a.cnt[0][v], n);
-            }
+        const uint32_t bal = __ballot_sync(0xffffffffu, act);
+        if ((threadIdx.x & 31) == 0) {
+            // Half (j / 32) % 2 of mask word j / 64 (little-endian halves).
+            reinterpret_cast<uint32_t*>(a.masks[p])[(size_t)b * S::WORDS * 2 + (j >> 5)] = bal;
+            if (bal) atomicOr(&a.bits[s][b >> 5], 1u << (b & 31));
         }
-        __syncthreads();
+        n += act ? 1u : 0u;
     }
+    flush();
 }
 
 // The active voxels of the current set in brick-major order: a single-pass

@@ -290,6 +290,88 @@ def run_ours(args, ws, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def run_batch(args, ws, rank, local):
+    """Batched form: the 48 mixed-size single-ellipsoid volumes in one
+    persistent launch against the same volumes run one after another through
+    the plain engine.  Both arms use the same brick configuration."""
+    import torch
+    import aworkefficientgpualgorithmforlevelsetsegmentation_gb300 as lss
+    from aworkefficientgpualgorithmforlevelsetsegmentation_gb300 import phantoms as P
+
+    torch.cuda.set_device(local)
+    cfg = P.config3(48, scale=args.scale)
+    vols, conv = cfg["volumes"], cfg["conv"]
+    brick = tuple(args.brick) if args.brick else (8, 8, 8)
+    threads = args.threads or 256
+    segs = []
+    for v in vols:
+        p = v["params"]
+        s = lss.Segmenter(lss.MODE_NS, device=local, brick=brick, threads_per_brick=threads)
+        s.load_volume(v["image"])
+        s.set_parameters(p.target, p.window, p.curvature, p.time_step, alpha_role=p.alpha_role)
+        segs.append(s)
+
+    def plain_all():
+        dev_ms, upd, its = 0.0, 0, []
+        for s, v in zip(segs, vols):
+            s.clear_current_segmentation()
+            s.set_seed_spheres(v["spheres"])
+            its.append(s.step_until_converged(conv["rel"], conv["patience"], conv["max_iterations"]))
+            st = s.stats()
+            dev_ms += st["last_step_ms"]
+            upd += st["voxel_updates"]
+        return dev_ms, upd, its
+
+    def batched():
+        b = lss.Batch(device=local, brick=brick, threads_per_brick=threads)
+        for v in vols:
+            b.add_volume(v["image"], v["params"], v["spheres"])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        it = b.run(conv["rel"], conv["patience"], conv["max_iterations"])
+        wall = 1e3 * (time.perf_counter() - t0)
+        st = [b.stats(i) for i in range(len(vols))]
+        return b, wall, st[0]["last_step_ms"], sum(x["voxel_updates"] for x in st), it
+
+    for _ in range(args.warmup):
+        plain_all()
+    seq_wall, seq_dev, seq_upd = [], [], 0
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        d, u, its = plain_all()
+        seq_wall.append(1e3 * (time.perf_counter() - t0))
+        seq_dev.append(d)
+        seq_upd = u
+    for _ in range(args.warmup):
+        batched()
+    bat_wall, bat_dev = [], []
+    for _ in range(args.steps):
+        b, w, d, bupd, bit = batched()
+        bat_wall.append(w)
+        bat_dev.append(d)
+    same = all(np.array_equal(b.read_mask(i), segs[i].get_saveable_segmentation())
+               for i in range(0, len(vols), 7))
+    if rank == 0:
+        sw, bw = statistics.median(seq_wall), statistics.median(bat_wall)
+        line = {
+            "metric": "batched_vs_sequential_plain_speedup", "value": sw / bw, "unit": "x",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": cfg["name"] + "_mixed_size_ellipsoids", "volumes": len(vols),
+                       "voxels": int(sum(v["image"].size for v in vols)), "brick": list(brick),
+                       "threads_per_brick": threads},
+            "sequential_plain": {"ms_wall": sw, "ms_device": statistics.median(seq_dev),
+                                 "voxel_updates": int(seq_upd), "iterations_max": int(max(its))},
+            "batched": {"ms_wall": bw, "ms_device": statistics.median(bat_dev),
+                        "voxel_updates": int(bupd), "iterations": int(bit),
+                        "updates_per_s": bupd / (bw / 1e3)},
+            "device_speedup": statistics.median(seq_dev) / statistics.median(bat_dev),
+            "masks_identical_to_plain": bool(same),
+        }
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -302,6 +384,7 @@ def main():
     ap.add_argument("--ref-iters", type=int, default=150)
     ap.add_argument("--dense-iters", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="plain", choices=["plain", "batch"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     ws, rank, local = dist_env()
@@ -310,6 +393,8 @@ def main():
         dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
     if args.impl == "reference":
         run_reference(args, ws, rank)
+    elif args.workload == "batch":
+        run_batch(args, ws, rank, local)
     else:
         run_ours(args, ws, rank, local)
     if ws > 1:
