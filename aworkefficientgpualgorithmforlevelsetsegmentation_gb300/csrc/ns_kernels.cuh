@@ -127,42 +127,43 @@ struct Brick {
 
 // The spec update of one voxel from the shared-memory halo tile.
 // P(dx,dy,dz) reads the tile around the voxel.  Mirrors ns_update() of the
-// FP64 oracle in fp32.  Every operation is an explicit round-to-nearest
-// intrinsic (no contraction or reassociation left to the compiler), so the
-// result is the same bit for bit in every kernel that inlines it.
+// FP64 oracle in fp32, with the central differences kept unscaled:
+//   X = 2 phi_x, Fxx = phi_xx, Fxy = 4 phi_xy, so
+//   kappa |grad phi| = [Fxx (Y^2+Z^2) + Fyy (X^2+Z^2) + Fzz (X^2+Y^2)
+//                       - (XY Fxy + XZ Fxz + YZ Fyz) / 2] / (X^2+Y^2+Z^2).
+// Every operation is an explicit round-to-nearest intrinsic (no contraction
+// or reassociation left to the compiler), so the result is the same bit for
+// bit in every kernel that inlines it.
 template <class PF>
 __device__ __forceinline__ float ns_update_f32(PF P, float I, float bias, const NsVol& V) {
     const float c = P(0, 0, 0);
     const float xm = P(-1, 0, 0), xp = P(1, 0, 0);
     const float ym = P(0, -1, 0), yp = P(0, 1, 0);
     const float zm = P(0, 0, -1), zp = P(0, 0, 1);
-    const float cx = __fmul_rn(__fsub_rn(xp, xm), 0.5f);
-    const float cy = __fmul_rn(__fsub_rn(yp, ym), 0.5f);
-    const float cz = __fmul_rn(__fsub_rn(zp, zm), 0.5f);
-    const float c2 = __fmul_rn(2.0f, c);
-    const float fxx = __fadd_rn(__fsub_rn(xp, c2), xm);
-    const float fyy = __fadd_rn(__fsub_rn(yp, c2), ym);
-    const float fzz = __fadd_rn(__fsub_rn(zp, c2), zm);
+    const float X = __fsub_rn(xp, xm), Y = __fsub_rn(yp, ym), Z = __fsub_rn(zp, zm);
+    const float Fxx = __fmaf_rn(-2.0f, c, __fadd_rn(xp, xm));
+    const float Fyy = __fmaf_rn(-2.0f, c, __fadd_rn(yp, ym));
+    const float Fzz = __fmaf_rn(-2.0f, c, __fadd_rn(zp, zm));
     auto cross = [&](float pp, float pm, float mp, float mm) {
-        return __fmul_rn(__fadd_rn(__fsub_rn(__fsub_rn(pp, pm), mp), mm), 0.25f);
+        return __fsub_rn(__fadd_rn(pp, mm), __fadd_rn(pm, mp));
     };
-    const float fxy = cross(P(1, 1, 0), P(1, -1, 0), P(-1, 1, 0), P(-1, -1, 0));
-    const float fxz = cross(P(1, 0, 1), P(1, 0, -1), P(-1, 0, 1), P(-1, 0, -1));
-    const float fyz = cross(P(0, 1, 1), P(0, 1, -1), P(0, -1, 1), P(0, -1, -1));
-    const float xx = __fmul_rn(cx, cx), yy = __fmul_rn(cy, cy), zz = __fmul_rn(cz, cz);
-    const float g2 = __fadd_rn(__fadd_rn(xx, yy), zz);
+    const float Fxy = cross(P(1, 1, 0), P(1, -1, 0), P(-1, 1, 0), P(-1, -1, 0));
+    const float Fxz = cross(P(1, 0, 1), P(1, 0, -1), P(-1, 0, 1), P(-1, 0, -1));
+    const float Fyz = cross(P(0, 1, 1), P(0, 1, -1), P(0, -1, 1), P(0, -1, -1));
+    const float xx = __fmul_rn(X, X), yy = __fmul_rn(Y, Y), zz = __fmul_rn(Z, Z);
+    const float g2 = __fadd_rn(__fadd_rn(xx, yy), zz);  // 4 |grad phi|^2
     float curv = 0.0f;
-    if (g2 > 1e-12f) {
-        const float t = __fmaf_rn(fzz, __fadd_rn(xx, yy),
-                                  __fmaf_rn(fyy, __fadd_rn(xx, zz), __fmul_rn(fxx, __fadd_rn(yy, zz))));
-        const float x = __fmaf_rn(__fmul_rn(cy, cz), fyz,
-                                  __fmaf_rn(__fmul_rn(cx, cz), fxz, __fmul_rn(__fmul_rn(cx, cy), fxy)));
-        const float num = __fmaf_rn(-2.0f, x, t);
-        curv = __fdividef(num, g2);  // g2 in (1e-12, 48]: within 2 ulp
+    if (g2 > 4e-12f) {
+        const float t = __fmaf_rn(Fzz, __fadd_rn(xx, yy),
+                                  __fmaf_rn(Fyy, __fadd_rn(xx, zz), __fmul_rn(Fxx, __fadd_rn(yy, zz))));
+        const float x = __fmaf_rn(__fmul_rn(Y, Z), Fyz, __fmaf_rn(__fmul_rn(X, Z), Fxz, __fmul_rn(__fmul_rn(X, Y), Fxy)));
+        curv = __fdividef(__fmaf_rn(-0.5f, x, t), g2);  // g2 in (4e-12, 192]: within 2 ulp
     }
     float D = __fmul_rn(__fsub_rn(V.eps, fabsf(__fsub_rn(I, V.T))), V.inv_eps);
     D = __fadd_rn(fminf(fmaxf(D, -1.0f), 1.0f), bias);
     const float F = __fmul_rn(V.wd, D);
+    // Osher-Sethian upwind |grad phi| for the speed F: one-sided differences
+    // selected by the sign of F.
     const float dxm = __fsub_rn(c, xm), dxp = __fsub_rn(xp, c), dym = __fsub_rn(c, ym),
                 dyp = __fsub_rn(yp, c), dzm = __fsub_rn(c, zm), dzp = __fsub_rn(zp, c);
     float a, b, e, f, h, k;

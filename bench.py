@@ -126,6 +126,17 @@ def sum_over_ranks(ws, value: float) -> float:
     return float(t.item())
 
 
+# DRAM bytes (read + write) of one launch of the persistent kernel on this
+# workload, from the ncu capture summarised in
+# profiles/k_ns_persistent_config2_256.md (dram__bytes_read.sum +
+# dram__bytes_write.sum, one convergence = one launch).
+DRAM_TRAFFIC = {("config2_256", 8, 8, 8, 256): 17020416}
+
+
+def dram_traffic(st, name):
+    return DRAM_TRAFFIC.get((name, st["brick_x"], st["brick_y"], st["brick_z"], st["threads_per_brick"]))
+
+
 def cpu_reference(cfg, iters: int, threads: int):
     """The FP64 CPU restatement on the first `iters` iterations of the run."""
     from oracle.oracle import NsOracle
@@ -176,8 +187,11 @@ def run_ours(args, ws, rank, local):
     cfg = P.config2(args.scale)
     p = cfg["params"]
     conv = cfg["conv"]
-    brick = tuple(args.brick) if args.brick else (0, 0, 0)
-    seg = lss.Segmenter(lss.MODE_NS, device=local, brick=brick, threads_per_brick=args.threads)
+    # The plain workload runs the 8x8x8 / 256-thread configuration unless
+    # --brick (or --brick 0 0 0 for the autotuner) says otherwise.
+    brick = tuple(args.brick) if args.brick else (8, 8, 8)
+    threads = args.threads or (256 if not args.brick else 0)
+    seg = lss.Segmenter(lss.MODE_NS, device=local, brick=brick, threads_per_brick=threads)
     stream = torch.cuda.Stream(device=local)
     import ctypes
     seg._chk(seg._lib.lss_set_stream(seg._h, ctypes.c_void_p(stream.cuda_stream)))
@@ -255,6 +269,7 @@ def run_ours(args, ws, rank, local):
 
     peak, peak_kind = measured_peak()
     achieved = BYTES_PER_UPDATE * updates / (kern_ms / 1e3) / 1e9
+    traffic = dram_traffic(st, cfg["name"])
     if rank == 0:
         cpu_u, cpu_t = (None, None)
         if not args.no_cpu:
@@ -276,8 +291,9 @@ def run_ours(args, ws, rank, local):
             "dense_gpu": {"ms_to_same_iterations": dense_ms, "ms_per_iteration": dense_ms_per_it,
                           "sparse_speedup": dense_ms / sparse_ms},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
-                         "bytes_per_update": BYTES_PER_UPDATE},
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                         "bytes_per_update": BYTES_PER_UPDATE,
+                         "algorithmic_bytes_per_launch": BYTES_PER_UPDATE * updates / args.steps},
             "cpu_baseline": None if cpu_u is None else {
                 "value": cpu_u / cpu_t, "unit": "voxel_updates/s", "cores": os.cpu_count(),
                 "kind": "port", "sample": f"first {args.ref_iters} iterations of {cfg['name']}"},
@@ -372,6 +388,72 @@ def run_batch(args, ws, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def run_stress(args, ws, rank, local):
+    """Large plain volume (512x512x768 three-shell phantom, 16 radius-4
+    seeds) to convergence, and the mixed batch (8 volumes of 384^3 + 64 of
+    64^3) in one persistent launch under a 150 GB HBM budget."""
+    import torch
+    import aworkefficientgpualgorithmforlevelsetsegmentation_gb300 as lss
+    from aworkefficientgpualgorithmforlevelsetsegmentation_gb300 import phantoms as P
+
+    torch.cuda.set_device(local)
+    t0 = time.perf_counter()
+    cfg = P.config5(args.scale)
+    gen_s = time.perf_counter() - t0
+    p, conv = cfg["params"], cfg["conv"]
+    brick = tuple(args.brick) if args.brick else (8, 8, 8)
+    threads = args.threads or 256
+    seg = lss.Segmenter(lss.MODE_NS, device=local, brick=brick, threads_per_brick=threads)
+    seg.load_volume(cfg["image"])
+    seg.set_parameters(p.target, p.window, p.curvature, p.time_step, alpha_role=p.alpha_role)
+    runs = []
+    for s in range(args.warmup + args.steps):
+        seg.clear_current_segmentation()
+        seg.set_seed_spheres(cfg["spheres"])
+        it = seg.step_until_converged(conv["rel"], conv["patience"], conv["max_iterations"])
+        st = seg.stats()
+        if s >= args.warmup:
+            runs.append((st["last_step_ms"], st["voxel_updates"], it))
+    ms = statistics.median(r[0] for r in runs)
+    upd = runs[-1][1]
+    peak, peak_kind = measured_peak()
+    achieved = BYTES_PER_UPDATE * upd / (ms / 1e3) / 1e9
+    plain = {"workload": cfg["name"], "ms_to_converge": ms, "iterations": runs[-1][2],
+             "voxel_updates": int(upd), "updates_per_s": upd / (ms / 1e3),
+             "roofline": {"achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                          "peak_kind": peak_kind, "bytes_per_update": BYTES_PER_UPDATE},
+             "device_bytes": int(st["device_bytes"]), "phantom_s": gen_s}
+    del seg
+    # Mixed batch under a 150 GB budget: 8 three-shell volumes of 384^3 and
+    # 64 single-ellipsoid volumes of 64^3.
+    big = P.config2(1.5 * args.scale)
+    vols = [(big["image"], big["params"], big["spheres"]) for _ in range(8)]
+    rng = np.random.default_rng(9)
+    m = max(16, int(round(64 * args.scale)))
+    for i in range(64):
+        c = (m - 1) / 2 + rng.uniform(-0.1, 0.1, 3) * m
+        axes = rng.uniform(0.2, 0.4, 3) * m
+        fg, bg = rng.uniform(0.6, 0.9), rng.uniform(0.1, 0.3)
+        img = P.ellipsoid((m, m, m), tuple(c), tuple(axes), fg, bg, 0.05, 2000 + i)
+        vols.append((img, P.ns_params(fg, 0.1, 0.9), [(c[0], c[1], c[2], 3.0)]))
+    b = lss.Batch(device=local, brick=brick, threads_per_brick=threads, hbm_budget_bytes=150 << 30)
+    for img, prm, sp in vols:
+        b.add_volume(img, prm, sp)
+    t1 = time.perf_counter()
+    bit = b.run(conv["rel"], conv["patience"], conv["max_iterations"])
+    bwall = 1e3 * (time.perf_counter() - t1)
+    bst = [b.stats(i) for i in range(len(vols))]
+    bupd = sum(x["voxel_updates"] for x in bst)
+    batch = {"volumes": len(vols), "voxels": int(sum(v[0].size for v in vols)), "iterations": int(bit),
+             "ms_device": bst[0]["last_step_ms"], "ms_wall": bwall, "voxel_updates": int(bupd),
+             "updates_per_s": bupd / (bst[0]["last_step_ms"] / 1e3),
+             "device_bytes": int(bst[0]["device_bytes"]), "hbm_budget_bytes": 150 << 30}
+    if rank == 0:
+        print(json.dumps({"metric": "stress", "plain": plain, "batch": batch, "dtype": "f32",
+                          "data": "synthetic", "brick": list(brick), "threads_per_brick": threads}),
+              flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -384,7 +466,7 @@ def main():
     ap.add_argument("--ref-iters", type=int, default=150)
     ap.add_argument("--dense-iters", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="plain", choices=["plain", "batch"])
+    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "stress"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     ws, rank, local = dist_env()
@@ -395,6 +477,8 @@ def main():
         run_reference(args, ws, rank)
     elif args.workload == "batch":
         run_batch(args, ws, rank, local)
+    elif args.workload == "stress":
+        run_stress(args, ws, rank, local)
     else:
         run_ours(args, ws, rank, local)
     if ws > 1:
