@@ -1,0 +1,60 @@
+// Host-side check of the bit-parallel brick dilation (dilate_slot,
+// dilate_word, inside_mask in csrc/ns_kernels.cuh) against a brute-force
+// dilation, for every brick shape, both neighbourhoods and every neighbour
+// slot.  Built and run by tests/test_dilation_host.py (no GPU needed).
+#include "ns_kernels.cuh"
+#include <cstdio>
+#include <random>
+using namespace lss;
+template <class S> int check(std::mt19937_64& rng, int nbh) {
+    int bad = 0;
+    auto bit = [&](const uint64_t* v, int x, int y, int z) {
+        int j = (z * S::Y + y) * S::X + x; return (int)((v[j >> 6] >> (j & 63)) & 1); };
+    for (int trial = 0; trial < 3000; ++trial) {
+        uint64_t c[S::WORDS];
+        const int dens = trial % 4;
+        for (int w = 0; w < S::WORDS; ++w) {
+            c[w] = rng();
+            for (int q = 0; q < dens; ++q) c[w] &= rng();
+        }
+        for (int oz = -1; oz <= 1; ++oz) for (int oy = -1; oy <= 1; ++oy) for (int ox = -1; ox <= 1; ++ox) {
+            uint64_t m[S::WORDS];
+            for (int w = 0; w < S::WORDS; ++w) m[w] = c[w];
+            dilate_slot<S>(m, ox, oy, oz, nbh);
+            uint32_t c32[2 * S::WORDS];
+            for (int w = 0; w < S::WORDS; ++w) { c32[2 * w] = (uint32_t)c[w]; c32[2 * w + 1] = (uint32_t)(c[w] >> 32); }
+            for (int w = 0; w < S::WORDS; ++w) if (dilate_word<S>(c32, ox, oy, oz, w, nbh) != m[w]) ++bad;
+            for (int z = 0; z < S::Z; ++z) for (int y = 0; y < S::Y; ++y) for (int x = 0; x < S::X; ++x) {
+                // voxel of neighbour brick in center coordinates
+                int gx = x + ox * S::X, gy = y + oy * S::Y, gz = z + oz * S::Z;
+                int want = 0;
+                for (int dz = -1; dz <= 1; ++dz) for (int dy = -1; dy <= 1; ++dy) for (int dx = -1; dx <= 1; ++dx) {
+                    if (nbh == 6 && (dx != 0) + (dy != 0) + (dz != 0) > 1) continue;
+                    int sx = gx + dx, sy = gy + dy, sz = gz + dz;
+                    if (sx < 0 || sy < 0 || sz < 0 || sx >= S::X || sy >= S::Y || sz >= S::Z) continue;
+                    want |= bit(c, sx, sy, sz);
+                }
+                if (want != bit(m, x, y, z)) ++bad;
+            }
+        }
+    }
+    // inside_mask
+    for (int lx = 1; lx <= S::X; ++lx) for (int ly = 1; ly <= S::Y; ++ly) for (int lz = 1; lz <= S::Z; ++lz) {
+        uint64_t m[S::WORDS];
+        for (int w = 0; w < S::WORDS; ++w) m[w] = inside_mask<S>(w, lx, ly, lz);
+        for (int z = 0; z < S::Z; ++z) for (int y = 0; y < S::Y; ++y) for (int x = 0; x < S::X; ++x)
+            if (bit(m, x, y, z) != (x < lx && y < ly && z < lz)) ++bad;
+    }
+    return bad;
+}
+int main() {
+    std::mt19937_64 rng(7);
+    int bad = 0;
+    for (int nbh : {26, 6}) {
+        int a = check<Brick<8, 8, 8>>(rng, nbh), b = check<Brick<8, 8, 4>>(rng, nbh), c = check<Brick<4, 4, 4>>(rng, nbh);
+        printf("nbh %d: 888 %d, 884 %d, 444 %d\n", nbh, a, b, c);
+        bad += a + b + c;
+    }
+    printf(bad ? "FAIL\n" : "OK\n");
+    return bad != 0;
+}
