@@ -191,9 +191,7 @@ struct NsSmem {
     alignas(128) float img[2][S::VOX];
     alignas(128) float out[2][S::VOX];
     unsigned long long act[2][S::WORDS];     // the brick's active mask, double buffered
-    uint32_t chg[S::CHG];                    // changed voxels of the brick (bits)
-    uint16_t list[S::VOX];                   // active voxels of the brick, compacted
-    uint8_t chgb[S::VOX];                    // changed voxels of the brick (bytes)
+    uint32_t chg[S::CHG];                    // changed voxels of the brick (ballot words)
     alignas(8) uint64_t bar[2];
 };
 
@@ -389,11 +387,15 @@ __device__ __forceinline__ void ns_fetch_mask(const NsArgs& a, NsSmem<S, NT>& sm
     }
 }
 
+// One brick of A_k by the whole block: wait for its loads, update its active
+// voxels in place of a copy of the tile centre (each thread its own voxels:
+// compacting the active voxels first measured slower, it costs two more block
+// barriers per brick), changed flags -> ballot words, TMA store, dilation.
 // vone: the volume descriptor in shared memory when the launch has one
 // volume (else null: descriptors are read per brick).
 template <class S, int NT>
 __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>& sm, uint32_t b,
-                                                 uint32_t p, uint32_t sn, int buf, uint32_t* mphase,
+                                                 uint32_t p, uint32_t sn, int buf, uint32_t& mphase,
                                                  BlockTally& tally, unsigned long long* cnt,
                                                  const NsVol* vone) {
     const int tid = threadIdx.x;
@@ -402,8 +404,8 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
     const int3 o = brick_origin<S>(V, b);
     const int x0 = o.x, y0 = o.y, z0 = o.z;
     const unsigned long long* act = sm.act[buf];
-    if (!mbar_wait(&sm.bar[buf], mphase[buf])) set_error(&a.ctl->err, ERR_TMA_TIMEOUT);
-    mphase[buf] ^= 1u;
+    if (!mbar_wait(&sm.bar[buf], (mphase >> buf) & 1u)) set_error(&a.ctl->err, ERR_TMA_TIMEOUT);
+    mphase ^= 1u << buf;  // bit b: phase of load barrier b
     // The store issued from out[buf] two bricks ago must have read its source.
     if (tid == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
     __syncthreads();
@@ -427,56 +429,38 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
         const int lx = j % S::X, ly = (j / S::X) % S::Y, lz = j / (S::X * S::Y);
         return ((lz + 1) * S::TY + (ly + 1)) * S::TX + (lx + 4);
     };
-    // Pass 1: copy the brick (inactive voxels keep phi) and compact the active
-    // voxels, ranked in brick order, into list[].
     uint32_t nact = 0;
 #pragma unroll
     for (int w = 0; w < S::WORDS; ++w) nact += __popcll(act[w]);
     constexpr int VPT = (S::VOX + NT - 1) / NT;
-#pragma unroll
-    for (int k = 0; k < VPT; ++k) {
-        const int j = tid + k * NT;
-        if (j < S::VOX) {
-            out[j] = phi[tile_index(j)];
-            sm.chgb[j] = 0;
-            const int w = j >> 6, bit = j & 63;
-            const uint64_t aw = act[w];
-            if ((aw >> bit) & 1ull) {
-                uint32_t r = __popcll(aw & ((1ull << bit) - 1ull));
-                for (int q = 0; q < w; ++q) r += __popcll(act[q]);
-                sm.list[r] = (uint16_t)j;
-            }
-        }
-    }
-    __syncthreads();
-    // Pass 2: update the active voxels, densely packed over the threads.
     const float* bias = V.bias;
-    for (uint32_t i = tid; i < nact; i += NT) {
-        const int j = sm.list[i];
-        const int ti = tile_index(j);
-        auto P = [&](int dx, int dy, int dz) { return phi[ti + (dz * S::TY + dy) * S::TX + dx]; };
-        float bb = 0.0f;
-        if (bias) {
-            const int lx = j % S::X, ly = (j / S::X) % S::Y, lz = j / (S::X * S::Y);
-            bb = bias[((size_t)(z0 + lz) * V.py + (y0 + ly)) * V.px + (x0 + lx)];
-        }
-        const float c = phi[ti];
-        const float nv = ns_update_f32(P, sm.img[buf][j], bb, V);
-        out[j] = nv;
-        sm.chgb[j] = fabsf(nv - c) > V.thr_t;
-    }
-    fence_proxy_async_smem();
-    __syncthreads();
-    // Pass 3: changed bytes -> bit words (warp ballots).
     bool anyl = false;
 #pragma unroll
     for (int k = 0; k < VPT; ++k) {
         const int j = tid + k * NT;
-        const uint32_t bal = __ballot_sync(0xffffffffu, j < S::VOX && sm.chgb[j]);
+        bool chg = false;
+        if (j < S::VOX) {
+            const int ti = tile_index(j);
+            const float c = phi[ti];
+            float nv = c;
+            if ((act[j >> 6] >> (j & 63)) & 1ull) {
+                auto P = [&](int dx, int dy, int dz) { return phi[ti + (dz * S::TY + dy) * S::TX + dx]; };
+                float bb = 0.0f;
+                if (bias) {
+                    const int lx = j % S::X, ly = (j / S::X) % S::Y, lz = j / (S::X * S::Y);
+                    bb = bias[((size_t)(z0 + lz) * V.py + (y0 + ly)) * V.px + (x0 + lx)];
+                }
+                nv = ns_update_f32(P, sm.img[buf][j], bb, V);
+                chg = fabsf(nv - c) > V.thr_t;
+            }
+            out[j] = nv;
+        }
+        const uint32_t bal = __ballot_sync(0xffffffffu, chg);
         anyl |= bal != 0u;
         const int word = (tid >> 5) + k * (NT / 32);
         if ((tid & 31) == 0 && word < S::CHG) sm.chg[word] = bal;
     }
+    fence_proxy_async_smem();
     const int any = __syncthreads_or(anyl ? 1 : 0);
     if (tid == 0) {
         tma_store_3d(&a.tmaps[V.tmap_base + 2 + (p ^ 1u)], x0, y0, z0, out);
@@ -811,10 +795,10 @@ __device__ __forceinline__ void ns_drive(const NsArgs& a, IterShared<NT>& sh, St
 template <class S, int NT>
 struct BlockProc {
     NsSmem<S, NT>& sm;
-    uint32_t mphase[2];
+    uint32_t mphase;   // bit b: phase of load barrier b
     int buf;
     BlockTally tally;  // thread 0
-    __device__ explicit BlockProc(NsSmem<S, NT>& s) : sm(s), mphase{0u, 0u}, buf(0) {}
+    __device__ explicit BlockProc(NsSmem<S, NT>& s) : sm(s), mphase(0u), buf(0) {}
     __device__ void init() {
         if (threadIdx.x == 0) {
             mbar_init(&sm.bar[0], 1);
