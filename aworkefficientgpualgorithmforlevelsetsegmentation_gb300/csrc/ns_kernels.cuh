@@ -191,7 +191,7 @@ struct NsSmem {
     alignas(128) float img[2][S::VOX];
     alignas(128) float out[2][S::VOX];
     unsigned long long act[2][S::WORDS];     // the brick's active mask, double buffered
-    uint32_t chg[S::CHG];                    // changed voxels of the brick (ballot words)
+    uint32_t chg[2][S::CHG];                 // changed voxels of the brick (ballot words)
     alignas(8) uint64_t bar[2];
 };
 
@@ -404,11 +404,11 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
     const int3 o = brick_origin<S>(V, b);
     const int x0 = o.x, y0 = o.y, z0 = o.z;
     const unsigned long long* act = sm.act[buf];
+    // Every thread waits for the loads itself.  out[buf] is free: the store
+    // issued from it two bricks ago was waited for (read) by thread 0 before
+    // the previous brick's block barrier.
     if (!mbar_wait(&sm.bar[buf], (mphase >> buf) & 1u)) set_error(&a.ctl->err, ERR_TMA_TIMEOUT);
     mphase ^= 1u << buf;  // bit b: phase of load barrier b
-    // The store issued from out[buf] two bricks ago must have read its source.
-    if (tid == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
-    __syncthreads();
     float* phi = sm.phi[buf];
     // Clamp-to-edge halo where the tile leaves the volume (TMA filled zeros).
     const bool edge = x0 < 4 || y0 < 1 || z0 < 1 || x0 + S::X + 4 > V.nx || y0 + S::Y + 1 > V.ny ||
@@ -458,9 +458,15 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
         const uint32_t bal = __ballot_sync(0xffffffffu, chg);
         anyl |= bal != 0u;
         const int word = (tid >> 5) + k * (NT / 32);
-        if ((tid & 31) == 0 && word < S::CHG) sm.chg[word] = bal;
+        if ((tid & 31) == 0 && word < S::CHG) sm.chg[buf][word] = bal;
     }
     fence_proxy_async_smem();
+    // The previous brick's store (from out[buf ^ 1], overwritten by the next
+    // brick after this barrier) has read its source.
+    if (tid == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+    // The one block barrier of a brick: out[] and chg[buf] complete; after it
+    // nothing reads phi[buf], img[buf] or act[buf] of this brick, so the next
+    // loads into this buffer may be issued while the dilation below runs.
     const int any = __syncthreads_or(anyl ? 1 : 0);
     if (tid == 0) {
         tma_store_3d(&a.tmaps[V.tmap_base + 2 + (p ^ 1u)], x0, y0, z0, out);
@@ -486,7 +492,7 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
                 // (bricks in the padding beyond the volume hold none).
                 const int lx = V.nx - bx * S::X, ly = V.ny - by * S::Y, lz = V.nz - bz * S::Z;
                 if (bx >= 0 && by >= 0 && bz >= 0 && lx > 0 && ly > 0 && lz > 0) {
-                    x = dilate_word<S>(sm.chg, ox, oy, oz, w, V.nbh);
+                    x = dilate_word<S>(sm.chg[buf], ox, oy, oz, w, V.nbh);
                     if (lx < S::X || ly < S::Y || lz < S::Z)
                         x &= inside_mask<S>(w, min(lx, S::X), min(ly, S::Y), min(lz, S::Z));
                     nb = b + (int32_t)((oz * V.nby + oy) * V.nbx + ox);
@@ -500,7 +506,9 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
             if (lane == g0 && (bal & gmask)) atomicOr(&a.bits[sn][nb >> 5], 1u << (nb & 31));
         }
     }
-    __syncthreads();
+    // No barrier here: the next brick uses the other buffers, and this
+    // brick's buffers are reused two bricks later, behind the next brick's
+    // barrier.
 }
 
 // A brick of A_{k-1} not in A_k: phi[p] -> phi[p^1].
@@ -813,6 +821,7 @@ struct BlockProc {
         if (q < nw) {
             if (tid == 0) ns_issue_loads<S, NT>(a, sm, sh.work[q], p, buf, vone);
             ns_fetch_mask<S, NT>(a, sm, sh.work[q], p, buf);
+            __syncthreads();  // act[buf] of the first brick (later ones are fetched a brick ahead)
         }
         while (q < nw) {
             uint32_t q2 = q + 1;
