@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda.h>
+#include <vector_types.h>
 
 #include <vector>
 
@@ -75,6 +76,10 @@ class NsCore {
         lss_params p{};
         std::vector<uint8_t> frozen;
         unsigned long long iterations = 0;
+        // phi equal in both buffers and uniform outside the voxel box
+        // [dirty_lo, dirty_hi) (after a fill, grown by seeding).
+        bool uniform = false;
+        int3 dirty_lo{0, 0, 0}, dirty_hi{0, 0, 0};
     };
     std::vector<VolHost>& vols() { return vols_; }
 

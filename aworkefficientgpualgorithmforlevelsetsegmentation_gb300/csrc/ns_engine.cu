@@ -70,6 +70,16 @@ __global__ void k_ns_fill(float* p, uint64_t n, float v) {
         p[i] = v;
 }
 
+// dst = src on the voxel box [lo, hi) of a padded volume (pitch px, py).
+__global__ void k_ns_copy_box(float* dst, const float* src, int px, int py, int3 lo, int3 hi) {
+    const uint64_t nx = hi.x - lo.x, ny = hi.y - lo.y, n = nx * ny * (uint64_t)(hi.z - lo.z);
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x) {
+        const int x = lo.x + (int)(t % nx), y = lo.y + (int)((t / nx) % ny), z = lo.z + (int)(t / (nx * ny));
+        const size_t i = ((size_t)z * py + y) * px + x;
+        dst[i] = src[i];
+    }
+}
+
 // phi = min(phi, clamp(|x - c| - r)) over the box [b0, b1) of the logical
 // volume (outside it the clamped distance is hi >= phi, so nothing changes).
 __global__ void k_ns_sphere_union(float* phi, int nx, int ny, int nz, int px, int py, int3 b0, int3 b1,
@@ -216,6 +226,7 @@ int NsCore::add_volume(const float* data, int nx, int ny, int nz, const lss_para
     ++owner_->launches;
     k_ns_fill<<<owner_->num_sms * 4, 256, 0, st>>>(v.phi[1], P, p.phi_max);
     ++owner_->launches;
+    v.uniform = true;  // both buffers phi_max until seeded
     LSS_CUDA(cudaGetLastError());
     owner_->sync();
     arena_.free_last(tmp);
@@ -376,9 +387,29 @@ NsArgs NsCore::args(uint32_t k0, int max_iters, const lss_conv* conv) const {
 void NsCore::init_active() {
     LSS_REQUIRE(configured_, LSS_ERR_STATE, "not configured");
     cudaStream_t st = owner_->stream;
-    for (VolHost& v : vols_) {
-        const uint64_t P = (uint64_t)v.px * v.py * v.pz;
-        LSS_CUDA(cudaMemcpyAsync(v.phi[parity_ ^ 1], v.phi[parity_], P * 4, cudaMemcpyDeviceToDevice, st));
+    // One volume whose phi is uniform outside a box (cleared, then seeded):
+    // only that box can hold active voxels and differ between the buffers.
+    const bool boxed = vols_.size() == 1 && vols_[0].uniform;
+    int3 blo = make_int3(0, 0, 0), bn = make_int3(0, 0, 0);
+    if (boxed) {
+        VolHost& v = vols_[0];
+        if (v.dirty_hi.x > v.dirty_lo.x && v.dirty_hi.y > v.dirty_lo.y && v.dirty_hi.z > v.dirty_lo.z) {
+            // One voxel of margin for the 6-neighbour test, in whole bricks.
+            blo = make_int3(std::max(0, v.dirty_lo.x - 1) / cfg_.bx, std::max(0, v.dirty_lo.y - 1) / cfg_.by,
+                            std::max(0, v.dirty_lo.z - 1) / cfg_.bz);
+            const int3 bhi = make_int3(std::min(v.nbx, (v.dirty_hi.x + 1 + cfg_.bx - 1) / cfg_.bx),
+                                       std::min(v.nby, (v.dirty_hi.y + 1 + cfg_.by - 1) / cfg_.by),
+                                       std::min(v.nbz, (v.dirty_hi.z + 1 + cfg_.bz - 1) / cfg_.bz));
+            bn = make_int3(bhi.x - blo.x, bhi.y - blo.y, bhi.z - blo.z);
+            k_ns_copy_box<<<owner_->num_sms * 4, 256, 0, st>>>(v.phi[parity_ ^ 1], v.phi[parity_], v.px, v.py,
+                                                              v.dirty_lo, v.dirty_hi);
+            ++owner_->launches;
+        }
+    } else {
+        for (VolHost& v : vols_) {
+            const uint64_t P = (uint64_t)v.px * v.py * v.pz;
+            LSS_CUDA(cudaMemcpyAsync(v.phi[parity_ ^ 1], v.phi[parity_], P * 4, cudaMemcpyDeviceToDevice, st));
+        }
     }
     for (int q = 0; q < 2; ++q) LSS_CUDA(cudaMemsetAsync(d_masks_[q], 0, NB_ * words_ * 8, st));
     for (int q = 0; q < 4; ++q) LSS_CUDA(cudaMemsetAsync(d_bits_[q], 0, (size_t)NW_ * 4, st));
@@ -391,12 +422,15 @@ void NsCore::init_active() {
     KernelSet ks = kernels(cfg_);
     NsArgs a = args(k_total_, 0, nullptr);
     uint32_t p = parity_, sl = s0;
-    void* params[] = {&a, &p, &sl};
-    const uint64_t warps = NB_ * (uint64_t)(ks.words * 2);  // 32 voxels per warp
-    const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((warps * 32 + ks.block - 1) / ks.block,
-                                                                    (uint64_t)owner_->num_sms * 16));
-    LSS_CUDA(cudaLaunchKernel(ks.init_active, dim3(grid), dim3(ks.block), params, 0, st));
-    ++owner_->launches;
+    const uint64_t nbr = boxed ? (uint64_t)bn.x * bn.y * bn.z : NB_;
+    if (!boxed || nbr > 0) {
+        void* params[] = {&a, &p, &sl, &blo, &bn};
+        const uint64_t warps = nbr * (uint64_t)(ks.words * 2);  // 32 voxels per warp
+        const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((warps * 32 + ks.block - 1) / ks.block,
+                                                                        (uint64_t)owner_->num_sms * 16));
+        LSS_CUDA(cudaLaunchKernel(ks.init_active, dim3(grid), dim3(ks.block), params, 0, st));
+        ++owner_->launches;
+    }
     std::vector<unsigned long long> n0(vols_.size());
     LSS_CUDA(cudaMemcpyAsync(n0.data(), d_cnt_[0], 8 * vols_.size(), cudaMemcpyDeviceToHost, st));
     LSS_CUDA(cudaMemsetAsync(d_cnt_[0], 0, 8 * vols_.size(), st));
@@ -425,6 +459,17 @@ void NsCore::sphere_union(int v, float cx, float cy, float cz, float r) {
     const int3 b0 = make_int3(lo(cx, V.nx), lo(cy, V.ny), lo(cz, V.nz));
     const int3 b1 = make_int3(hi(cx, V.nx), hi(cy, V.ny), hi(cz, V.nz));
     if (b1.x <= b0.x || b1.y <= b0.y || b1.z <= b0.z) return;
+    if (V.uniform) {  // grow the box of voxels that may differ from the uniform value
+        if (V.dirty_hi.x <= V.dirty_lo.x) {
+            V.dirty_lo = b0;
+            V.dirty_hi = b1;
+        } else {
+            V.dirty_lo = make_int3(std::min(V.dirty_lo.x, b0.x), std::min(V.dirty_lo.y, b0.y),
+                                   std::min(V.dirty_lo.z, b0.z));
+            V.dirty_hi = make_int3(std::max(V.dirty_hi.x, b1.x), std::max(V.dirty_hi.y, b1.y),
+                                   std::max(V.dirty_hi.z, b1.z));
+        }
+    }
     k_ns_sphere_union<<<owner_->num_sms * 4, 256, 0, owner_->stream>>>(
         V.phi[parity_], V.nx, V.ny, V.nz, V.px, V.py, b0, b1, cx, cy, cz, r, V.p.phi_min, V.p.phi_max);
     ++owner_->launches;
@@ -433,6 +478,7 @@ void NsCore::sphere_union(int v, float cx, float cy, float cz, float r) {
 
 void NsCore::set_phi(int v, const float* phi) {
     VolHost& V = vols_.at(v);
+    V.uniform = false;
     float* tmp = (float*)arena_.alloc((uint64_t)V.nx * V.ny * V.nz * 4);
     LSS_CUDA(cudaMemcpyAsync(tmp, phi, (uint64_t)V.nx * V.ny * V.nz * 4, cudaMemcpyHostToDevice,
                              owner_->stream));
@@ -443,17 +489,24 @@ void NsCore::set_phi(int v, const float* phi) {
     arena_.free_last(tmp);
 }
 
+// Both buffers: phi is then uniform, which later seeding and active-set
+// rebuilds exploit (only the seeded box can differ).
 void NsCore::fill_phi(int v, float value) {
     VolHost& V = vols_.at(v);
-    k_ns_fill<<<owner_->num_sms * 4, 256, 0, owner_->stream>>>(V.phi[parity_], (uint64_t)V.px * V.py * V.pz,
-                                                              value);
-    ++owner_->launches;
+    for (int q = 0; q < 2; ++q) {
+        k_ns_fill<<<owner_->num_sms * 4, 256, 0, owner_->stream>>>(V.phi[q], (uint64_t)V.px * V.py * V.pz,
+                                                                  value);
+        ++owner_->launches;
+    }
     LSS_CUDA(cudaGetLastError());
+    V.uniform = true;
+    V.dirty_lo = V.dirty_hi = make_int3(0, 0, 0);
 }
 
 int NsCore::run(int max_iters, const lss_conv* conv, float* ms) {
     LSS_REQUIRE(initialized_, LSS_ERR_STATE, "no seed / phi set");
     if (max_iters <= 0) return 0;
+    for (VolHost& v : vols_) v.uniform = false;
     cudaStream_t st = owner_->stream;
     KernelSet ks = kernels(cfg_);
     NsArgs a = args(k_total_, max_iters, conv);
@@ -573,6 +626,7 @@ void NsCore::estimate(int v, float* t, float* w) {
 
 float NsCore::dense_run(int iters) {
     LSS_REQUIRE(initialized_, LSS_ERR_STATE, "no seed / phi set");
+    for (VolHost& v : vols_) v.uniform = false;
     cudaStream_t st = owner_->stream;
     cudaEvent_t e0, e1;
     LSS_CUDA(cudaEventCreate(&e0));

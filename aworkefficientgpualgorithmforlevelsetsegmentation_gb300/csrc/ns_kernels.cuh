@@ -1059,10 +1059,16 @@ __global__ void __launch_bounds__(W * 32, 1) k_ns_warp(NsArgs a) {
 // and its ballot is one 32-bit half of a mask word, stored directly; bricks
 // with a non-empty mask get their membership bit in bits[s].  Counts land in
 // cnt[0] (one atomic per warp and volume run).
+//
+// box_n.x > 0 restricts the pass to the bricks [box_lo, box_lo + box_n) of a
+// one-volume launch (brick coordinates); the other bricks are known empty.
 template <int BX, int BY, int BZ, int NT>
-__global__ void __launch_bounds__(NT) k_ns_init_active(NsArgs a, uint32_t p, uint32_t s) {
+__global__ void __launch_bounds__(NT) k_ns_init_active(NsArgs a, uint32_t p, uint32_t s, int3 box_lo,
+                                                       int3 box_n) {
     using S = Brick<BX, BY, BZ>;
-    const uint64_t total = (uint64_t)a.NB * S::VOX;
+    const bool boxed = box_n.x > 0;
+    const uint64_t nbricks = boxed ? (uint64_t)box_n.x * box_n.y * box_n.z : (uint64_t)a.NB;
+    const uint64_t total = nbricks * S::VOX;
     uint32_t cur_v = 0xFFFFFFFFu;
     unsigned long long n = 0;
     auto flush = [&]() {
@@ -1071,8 +1077,14 @@ __global__ void __launch_bounds__(NT) k_ns_init_active(NsArgs a, uint32_t p, uin
         n = 0;
     };
     for (uint64_t t = blockIdx.x * (uint64_t)NT + threadIdx.x; t < total; t += (uint64_t)gridDim.x * NT) {
-        const uint32_t b = (uint32_t)(t / S::VOX);
+        uint32_t b = (uint32_t)(t / S::VOX);
         const int j = (int)(t % S::VOX);
+        if (boxed) {
+            const NsVol& V0 = a.vols[0];
+            const int kx = box_lo.x + (int)(b % box_n.x), ky = box_lo.y + (int)((b / box_n.x) % box_n.y),
+                      kz = box_lo.z + (int)(b / ((uint32_t)box_n.x * box_n.y));
+            b = V0.brick_base + (uint32_t)((kz * V0.nby + ky) * V0.nbx + kx);
+        }
         const uint32_t v = a.brick_vol[b];  // one brick per warp: uniform
         if (v != cur_v) {
             flush();
