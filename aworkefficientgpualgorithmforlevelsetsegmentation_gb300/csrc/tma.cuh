@@ -34,16 +34,19 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
 }
 
 // Waits for the phase `parity` of the barrier to complete; false on timeout.
+// Each try_wait may suspend the thread in hardware for up to 20 us (it
+// resumes as soon as the phase completes), so waiting threads issue few
+// instructions; the clock is read once per try.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     uint32_t done = 0;
     uint64_t t0 = 0;
     for (;;) {
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
             "selp.u32 %0, 1, 0, p;\n\t}"
             : "=r"(done)
-            : "r"(smem_addr(bar)), "r"(parity)
+            : "r"(smem_addr(bar)), "r"(parity), "r"(20000u)
             : "memory");
         if (done) return true;
         if (t0 == 0) t0 = globaltimer_ns();
