@@ -130,7 +130,7 @@ def sum_over_ranks(ws, value: float) -> float:
 # workload, from the ncu capture summarised in
 # profiles/k_ns_persistent_config2_256.md (dram__bytes_read.sum +
 # dram__bytes_write.sum, one convergence = one launch).
-DRAM_TRAFFIC = {("config2_256", 8, 8, 8, 256): 17020416}
+DRAM_TRAFFIC = {("config2_256", 8, 8, 8, 256): 15898112}
 
 
 def dram_traffic(st, name):
@@ -461,6 +461,62 @@ def run_stress(args, ws, rank, local):
               flush=True)
 
 
+def run_tour(args, ws, rank, local):
+    """Every kernel of the library once, on small inputs (for a per-kernel
+    ncu launch list with DRAM bytes): the REF engine (u8 volume: seed, steps
+    on the few- and many-active paths, read-backs, parameter estimate), the
+    NS engine (seed, sparse steps, dense steps, read-backs), the batched
+    form, the adjoint and the kernel-level compaction."""
+    import ctypes as C
+    import torch
+    import aworkefficientgpualgorithmforlevelsetsegmentation_gb300 as lss
+    from aworkefficientgpualgorithmforlevelsetsegmentation_gb300 import phantoms as P
+
+    torch.cuda.set_device(local)
+    cfg = P.config1(0.5)
+    u8 = np.clip(cfg["image"] * 200.0, 0, 255).astype(np.uint8)
+    r = lss.Segmenter(lss.MODE_REF)
+    r.load_volume(u8)
+    r.set_parameters(140, 40, 0.2, 0.25)
+    r.initialize_seed((32, 32, 32), 6)
+    r.request_update_segmentation(20)
+    r.get_saveable_segmentation()
+    r.read_active_volume()
+    r.calculate_segmentation_parameters()
+    p = cfg["params"]
+    s = lss.Segmenter(lss.MODE_NS, brick=(8, 8, 8), threads_per_brick=256)
+    s.load_volume(cfg["image"])
+    s.set_parameters(p.target, p.window, p.curvature, p.time_step, alpha_role=p.alpha_role)
+    s.set_seed_spheres(cfg["spheres"])
+    s.step(20)
+    s.active_linear()
+    s.read_phi()
+    s.step_dense(2)
+    c4 = P.config4(0.25)
+    a = lss.Segmenter(lss.MODE_NS, brick=(8, 8, 8), threads_per_brick=256)
+    a.load_volume(c4["image"])
+    q = c4["params"]
+    a.set_parameters(q.target, q.window, q.curvature, q.time_step, alpha_role=q.alpha_role)
+    a.set_phi(c4["phi0"])
+    a.adjoint(8, 4, c4["target"])
+    b = lss.Batch(brick=(8, 8, 4), threads_per_brick=32)
+    for v in P.config3(4, scale=0.25)["volumes"]:
+        b.add_volume(v["image"], v["params"], v["spheres"])
+    b.run(1e-3, 5, 200)
+    n = 1 << 20
+    src = torch.arange(n, dtype=torch.int32, device="cuda")
+    valid = (torch.arange(n, device="cuda") % 3 == 0).to(torch.int32)
+    dst = torch.zeros(n, dtype=torch.int32, device="cuda")
+    cnt = torch.zeros(1, dtype=torch.int64, device="cuda")
+    L = lss.load()
+    for f in (L.lss_compact_u32, L.lss_compact_u32_noalloc):
+        assert f(C.c_void_p(src.data_ptr()), C.c_void_p(valid.data_ptr()), C.c_void_p(dst.data_ptr()), n,
+                 C.c_void_p(cnt.data_ptr()), None) == 0
+    torch.cuda.synchronize()
+    if rank == 0:
+        print(json.dumps({"metric": "tour", "ok": True}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -474,7 +530,7 @@ def main():
     ap.add_argument("--ref-step-iters", type=int, default=80)
     ap.add_argument("--dense-iters", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "stress"])
+    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "stress", "tour"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     ws, rank, local = dist_env()
@@ -487,6 +543,8 @@ def main():
         run_batch(args, ws, rank, local)
     elif args.workload == "stress":
         run_stress(args, ws, rank, local)
+    elif args.workload == "tour":
+        run_tour(args, ws, rank, local)
     else:
         run_ours(args, ws, rank, local)
     if ws > 1:
