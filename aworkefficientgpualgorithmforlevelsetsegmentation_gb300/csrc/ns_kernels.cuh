@@ -692,8 +692,14 @@ __device__ __forceinline__ void ns_drive(const NsArgs& a, IterShared<NT>& sh, St
             const unsigned long long mine = sh.upd;
             sh.upd = 0;
             const uint32_t target = gen + 1;
-            __threadfence();
-            const unsigned long long old = atomicAdd(&a.ctl->bar_arrive, (mine << kArriveShift) | 1ull);
+            // Arrival: one acquire-release add (the block's writes, ordered
+            // before it by the block barrier, are released; the last block
+            // to arrive acquires everyone's).
+            unsigned long long old;
+            asm volatile("atom.acq_rel.gpu.global.add.u64 %0, [%1], %2;"
+                         : "=l"(old)
+                         : "l"(&a.ctl->bar_arrive), "l"((mine << kArriveShift) | 1ull)
+                         : "memory");
             unsigned long long rel;
             if ((old & kArriveMask) == G - 1) {
                 // Last to arrive: evaluate the one-volume stopping rule, release.
