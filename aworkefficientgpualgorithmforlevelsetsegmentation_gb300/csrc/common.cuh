@@ -120,8 +120,10 @@ __device__ __forceinline__ uint64_t tile_exclusive_prefix(uint64_t* status, uint
 // Block-wide exclusive sum of one uint32 per thread (blockDim.x a multiple of
 // 32, at most 1024).  Returns the thread's exclusive prefix; *total gets the
 // block sum.
+// The block total lives in its own slot (s_warp[32]): with 32 warps, slot 31
+// holds warp 31's exclusive prefix.
 __device__ __forceinline__ uint32_t block_exclusive_sum(uint32_t v, uint32_t* total) {
-    __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_warp[33];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     uint32_t x = v;
 #pragma unroll
@@ -140,18 +142,18 @@ __device__ __forceinline__ uint32_t block_exclusive_sum(uint32_t v, uint32_t* to
             if (lane >= o) ws += y;
         }
         if (lane < nw) s_warp[lane] = ws - w;
-        if (lane == nw - 1) s_warp[31] = ws;
+        if (lane == nw - 1) s_warp[32] = ws;
     }
     __syncthreads();
     uint32_t r = s_warp[warp] + x - v;
-    *total = s_warp[31];
+    *total = s_warp[32];
     __syncthreads();
     return r;
 }
 
 // Same for 64-bit values (packed counters).
 __device__ __forceinline__ uint64_t block_exclusive_sum64(uint64_t v, uint64_t* total) {
-    __shared__ uint64_t s_warp64[32];
+    __shared__ uint64_t s_warp64[33];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     uint64_t x = v;
 #pragma unroll
@@ -170,11 +172,11 @@ __device__ __forceinline__ uint64_t block_exclusive_sum64(uint64_t v, uint64_t* 
             if (lane >= o) ws += y;
         }
         if (lane < nw) s_warp64[lane] = ws - w;
-        if (lane == nw - 1) s_warp64[31] = ws;
+        if (lane == nw - 1) s_warp64[32] = ws;
     }
     __syncthreads();
     uint64_t r = s_warp64[warp] + x - v;
-    *total = s_warp64[31];
+    *total = s_warp64[32];
     __syncthreads();
     return r;
 }

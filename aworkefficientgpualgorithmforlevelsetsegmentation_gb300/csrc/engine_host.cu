@@ -83,15 +83,30 @@ static std::mutex g_tune_mu;
 static std::map<std::tuple<int, int, int, int>, BrickConfig> g_tune_cache;
 
 static bool same_config(const BrickConfig& a, const BrickConfig& b) {
-    return a.bx == b.bx && a.by == b.by && a.bz == b.bz && a.threads == b.threads;
+    return a.bx == b.bx && a.by == b.by && a.bz == b.bz && a.threads == b.threads &&
+           a.min_blocks == b.min_blocks;
+}
+
+static std::tuple<int, int, int, int> tune_key(NsCore& core) {
+    auto& vols = core.vols();
+    uint64_t vox = 0;
+    for (auto& v : vols) vox += (uint64_t)v.nx * v.ny * v.nz;
+    return std::make_tuple((int)vols.size(), (int)std::log2((double)vox + 1), vols[0].nx / 64, vols[0].nz / 64);
+}
+
+// The cached choice for this volume-shape bucket, if one was tuned before
+// (lets an engine configure with it directly, before any state exists).
+static bool cached_choice(NsCore& core, BrickConfig* out) {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    auto it = g_tune_cache.find(tune_key(core));
+    if (it == g_tune_cache.end()) return false;
+    *out = it->second;
+    return true;
 }
 
 static BrickConfig autotune(NsCore& core, EngineBase* owner, int iters) {
     auto& vols = core.vols();
-    uint64_t vox = 0;
-    for (auto& v : vols) vox += (uint64_t)v.nx * v.ny * v.nz;
-    auto key = std::make_tuple((int)vols.size(), (int)std::log2((double)vox + 1), vols[0].nx / 64,
-                               vols[0].nz / 64);
+    const auto key = tune_key(core);
     // Save the seeded phi of every volume.
     auto save = [&]() {
         std::vector<std::vector<float>> saved(vols.size());
@@ -166,10 +181,12 @@ class NsEngine : public EngineBase {
         core_.reset(new NsCore(this, cfg.hbm_budget_bytes));
         core_->add_volume(f.data(), nx, ny, nz, params);
         BrickConfig c = brick_configs()[0];
+        tuned_ = cfg.brick_x > 0;
         if (cfg.brick_x > 0) c = BrickConfig{cfg.brick_x, cfg.brick_y, cfg.brick_z,
                                              cfg.threads_per_brick > 0 ? cfg.threads_per_brick : 256};
+        else
+            tuned_ = cached_choice(*core_, &c);
         core_->configure(c);
-        tuned_ = cfg.brick_x > 0;
         nx_ = nx; ny_ = ny; nz_ = nz;
         frozen_.assign((size_t)nx * ny * nz, 0);
         pending_reinit_ = false;
@@ -418,15 +435,18 @@ class BatchEngine : public EngineBase {
         LSS_REQUIRE(core_.nvol() > 0, LSS_ERR_STATE, "empty batch");
         LSS_REQUIRE(!ran_, LSS_ERR_STATE, "a batch runs once");
         BrickConfig c = brick_configs()[0];
+        bool tuned = cfg.brick_x > 0;
         if (cfg.brick_x > 0)
             c = BrickConfig{cfg.brick_x, cfg.brick_y, cfg.brick_z,
                             cfg.threads_per_brick > 0 ? cfg.threads_per_brick : 256};
+        else
+            tuned = cached_choice(core_, &c);
         core_.configure(c);
         for (int v = 0; v < core_.nvol(); ++v)
             for (size_t k = 0; k + 3 < seeds_[v].size(); k += 4)
                 core_.sphere_union(v, seeds_[v][k], seeds_[v][k + 1], seeds_[v][k + 2], seeds_[v][k + 3]);
         core_.init_active();
-        if (cfg.brick_x <= 0) autotune(core_, this, 32);
+        if (!tuned) autotune(core_, this, 32);
         float ms = 0;
         lss_conv cv = conv ? *conv : lss_conv{0.0, 1, 1000, 0};
         int it = core_.run(cv.max_iterations, &cv, &ms);

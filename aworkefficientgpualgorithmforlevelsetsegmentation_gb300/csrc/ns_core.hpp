@@ -18,6 +18,7 @@ struct NsArgs;
 
 struct BrickConfig {
     int bx, by, bz, threads;
+    int min_blocks = 0;  // block per brick: resident blocks per SM the registers allow (0: 1024 threads)
 };
 
 const std::vector<BrickConfig>& brick_configs();

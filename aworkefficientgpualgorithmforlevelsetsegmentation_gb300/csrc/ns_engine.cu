@@ -160,10 +160,10 @@ struct KernelSet {
     size_t smem_fixed;  // dynamic shared memory of the persistent kernel, without the stopping state
 };
 
-template <int BX, int BY, int BZ, int NT>
+template <int BX, int BY, int BZ, int NT, int MINB = 1024 / NT>
 KernelSet kernels_for() {
     using S = Brick<BX, BY, BZ>;
-    return KernelSet{(void*)&k_ns_persistent<BX, BY, BZ, NT>, (void*)&k_ns_init_active<BX, BY, BZ, NT>,
+    return KernelSet{(void*)&k_ns_persistent<BX, BY, BZ, NT, MINB>, (void*)&k_ns_init_active<BX, BY, BZ, NT>,
                      (void*)&k_ns_emit<BX, BY, BZ, NT>, S::WORDS, NT, NT, 0};
 }
 
@@ -182,11 +182,13 @@ KernelSet warp_kernels_for() {
 const std::vector<BrickConfig>& brick_configs() {
     static const std::vector<BrickConfig> v = {
         {8, 8, 8, 256}, {8, 8, 8, 128}, {8, 8, 8, 512}, {8, 8, 4, 128}, {8, 8, 4, 256}, {4, 4, 4, 64},
-        {8, 8, 4, 32},  {8, 8, 8, 32},  {4, 4, 4, 32}};
+        {8, 8, 4, 32},  {8, 8, 8, 32},  {4, 4, 4, 32},  {8, 8, 8, 256, 5}};
     return v;
 }
 
 static KernelSet kernels(const BrickConfig& c) {
+    if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 256 && c.min_blocks == 5)
+        return kernels_for<8, 8, 8, 256, 5>();
     if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 256) return kernels_for<8, 8, 8, 256>();
     if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 128) return kernels_for<8, 8, 8, 128>();
     if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 512) return kernels_for<8, 8, 8, 512>();

@@ -699,7 +699,12 @@ __device__ __forceinline__ void ns_drive(const NsArgs& a, IterShared<NT>& sh, St
                         uint32_t m = m0;
                         for (uint32_t s2 = q - r; s2; --s2) m &= m - 1u;
                         const uint32_t b = w * 32u + (uint32_t)(__ffs(m) - 1);
-                        out[(q - bi) / G - c0] = (!one && ss.done[a.brick_vol[b]]) ? kNoBrick : b;
+                        const uint32_t slot = (q - bi) / G - c0;
+                        if (slot >= (uint32_t)NT || b >= a.NB) {  // a rank outside this chunk: report, skip
+                            set_error(&a.ctl->err, ERR_BOUNDS);
+                            continue;
+                        }
+                        out[slot] = (!one && ss.done[a.brick_vol[b]]) ? kNoBrick : b;
                     }
                 };
                 for (int m = 0; m < kScanCache; ++m) {
@@ -892,10 +897,11 @@ struct BlockProc {
     }
 };
 
-// The persistent kernel, block per brick.  At least 1024 resident threads per
-// SM: 64 registers a thread at most.
-template <int BX, int BY, int BZ, int NT>
-__global__ void __launch_bounds__(NT, 1024 / NT) k_ns_persistent(NsArgs a) {
+// The persistent kernel, block per brick.  MINB resident blocks per SM (the
+// register cap follows: 1024 threads -> 64 registers a thread; 1280 -> 48
+// trades per-thread registers for more bricks in flight at full load).
+template <int BX, int BY, int BZ, int NT, int MINB = 1024 / NT>
+__global__ void __launch_bounds__(NT, MINB) k_ns_persistent(NsArgs a) {
     using S = Brick<BX, BY, BZ>;
     __shared__ NsSmem<S, NT> sm;
     __shared__ IterShared<NT> sh;

@@ -105,7 +105,10 @@ def full():
 def test_full_size_configs_agree_and_split_runs_agree(full):
     p = full["params"]
     ref_phi = ref_act = None
-    for brick, threads in [((8, 8, 8), 256), ((8, 8, 4), 32), ((4, 4, 4), 64), ((8, 8, 8), 512)]:
+    # (4, 4, 4) x 32: one 1024-thread block per SM whose block prefix sum
+    # spans 32 warps, over more than 32 x 1024 membership words' worth of bricks.
+    for brick, threads in [((8, 8, 8), 256), ((8, 8, 4), 32), ((4, 4, 4), 64), ((8, 8, 8), 512),
+                           ((4, 4, 4), 32)]:
         s = seg(full["image"], p, brick, threads)
         s.set_seed_spheres(full["spheres"])
         s.step(60)
