@@ -926,6 +926,7 @@ struct WarpSlot {
     uint32_t chg[S::CHG];
     uint16_t list[S::VOX];
     uint8_t chgb[S::VOX];
+    unsigned long long xy[9 * S::WORDS];  // xy-dilated planes per (ox, oy) pair
     alignas(8) uint64_t bar;
 };
 
@@ -1021,6 +1022,24 @@ __device__ __forceinline__ void ns_warp_brick(const NsArgs& a, WarpSlot<S>& sl, 
         tally.add(a.vstate, cnt, v, nact);
     }
     if (any) {
+        const uint32_t* cw = sl.chg;
+        auto W = [&](int q) -> uint64_t { return (uint64_t)cw[2 * q] | ((uint64_t)cw[2 * q + 1] << 32); };
+        constexpr bool kPlanes = S::XY == 64;  // one z-plane per mask word
+        if constexpr (kPlanes) {
+            // Phase 1: the 9 x WORDS xy-dilated planes, once each.
+            for (int t = lane; t < 9 * S::WORDS; t += 32) {
+                const int pair = t / S::WORDS, w = t % S::WORDS;
+                const int ox = pair % 3 - 1, oy = pair / 3 - 1;
+                const uint64_t c = W(w);
+                uint64_t v;
+                if (V.nbh == 26) v = dil_y<S>(dil_x<S>(c, ox), oy);
+                else if (ox == 0 && oy == 0) v = dil_x<S>(c, 0) | dil_y<S>(c, 0);
+                else if (ox == 0 || oy == 0) v = ox ? dil_x<S>(c, ox) : dil_y<S>(c, oy);
+                else v = 0ull;
+                sl.xy[t] = v;
+            }
+            __syncwarp();
+        }
         constexpr int ROUNDS = (27 * S::WORDS + 31) / 32;
 #pragma unroll
         for (int r = 0; r < ROUNDS; ++r) {
@@ -1035,7 +1054,23 @@ __device__ __forceinline__ void ns_warp_brick(const NsArgs& a, WarpSlot<S>& sl, 
                 // (bricks in the padding beyond the volume hold none).
                 const int lx = V.nx - bx * S::X, ly = V.ny - by * S::Y, lz = V.nz - bz * S::Z;
                 if (bx >= 0 && by >= 0 && bz >= 0 && lx > 0 && ly > 0 && lz > 0) {
-                    x = dilate_word<S>(sl.chg, ox, oy, oz, w, V.nbh);
+                    if constexpr (kPlanes) {
+                        const unsigned long long* xy = sl.xy + ((oy + 1) * 3 + (ox + 1)) * S::WORDS;
+                        const bool center = ox == 0 && oy == 0;
+                        if (V.nbh == 26) {
+                            x = oz == 0 ? (xy[w] | (w > 0 ? xy[w - 1] : 0ull) | (w < S::WORDS - 1 ? xy[w + 1] : 0ull))
+                                        : (oz < 0 ? (w == S::WORDS - 1 ? xy[0] : 0ull)
+                                                  : (w == 0 ? xy[S::WORDS - 1] : 0ull));
+                        } else if (oz == 0) {
+                            x = xy[w] | (center ? ((w > 0 ? W(w - 1) : 0ull) | (w < S::WORDS - 1 ? W(w + 1) : 0ull)) : 0ull);
+                        } else {
+                            x = center ? (oz < 0 ? (w == S::WORDS - 1 ? W(0) : 0ull)
+                                                 : (w == 0 ? W(S::WORDS - 1) : 0ull))
+                                       : 0ull;
+                        }
+                    } else {
+                        x = dilate_word<S>(cw, ox, oy, oz, w, V.nbh);
+                    }
                     if (lx < S::X || ly < S::Y || lz < S::Z)
                         x &= inside_mask<S>(w, min(lx, S::X), min(ly, S::Y), min(lz, S::Z));
                     nb = b + (int32_t)((oz * V.nby + oy) * V.nbx + ox);
