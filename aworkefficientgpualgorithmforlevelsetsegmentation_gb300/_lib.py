@@ -41,7 +41,8 @@ class lss_stats(C.Structure):
                 ("padded_z", C.c_uint32), ("brick_x", C.c_uint32), ("brick_y", C.c_uint32),
                 ("brick_z", C.c_uint32), ("threads_per_brick", C.c_uint32), ("mode", C.c_int32),
                 ("error_flags", C.c_int32), ("update_ms", C.c_double), ("barrier_ms", C.c_double),
-                ("kernel_launches", C.c_uint64)]
+                ("kernel_launches", C.c_uint64), ("grid_blocks", C.c_uint32),
+                ("block_threads", C.c_uint32)]
 
 
 class lss_grads(C.Structure):

@@ -367,6 +367,8 @@ class NsEngine : public EngineBase {
         s->brick_z = core_->config().bz; s->threads_per_brick = core_->config().threads;
         s->device_bytes = core_->held();
         s->last_step_ms = last_ms_;
+        s->grid_blocks = (uint32_t)core_->grid();
+        s->block_threads = (uint32_t)core_->block_threads();
         if (!core_->initialized()) return;
         NsVolState st;
         core_->state(0, &st);
@@ -474,6 +476,8 @@ class BatchEngine : public EngineBase {
         s->threads_per_brick = core_.config().threads;
         s->device_bytes = core_.held();
         s->last_step_ms = last_ms_;
+        s->grid_blocks = (uint32_t)core_.grid();
+        s->block_threads = (uint32_t)core_.block_threads();
         if (!core_.initialized()) return;
         NsVolState st;
         core_.state(v, &st);

@@ -18,7 +18,8 @@ struct NsArgs;
 
 struct BrickConfig {
     int bx, by, bz, threads;
-    int min_blocks = 0;  // block per brick: resident blocks per SM the registers allow (0: 1024 threads)
+    int min_blocks = 0;  // block per brick: resident blocks per SM the registers allow (0: 1024
+                         // threads); warp per brick (threads == 32): warps per block (0: default)
 };
 
 const std::vector<BrickConfig>& brick_configs();
@@ -61,6 +62,7 @@ class NsCore {
     double last_barrier_ms() const { return last_barrier_ns_ * 1e-6; }
     uint64_t bricks() const { return NB_; }
     int grid() const { return grid_; }
+    int block_threads() const { return block_threads_; }
     int words() const { return words_; }
     uint64_t budget_left() const { return arena_.budget_left(); }
     const unsigned long long* masks(uint32_t parity) const { return d_masks_[parity & 1u]; }
@@ -97,7 +99,7 @@ class NsCore {
     int words_ = 8;
     uint64_t NB_ = 0;
     uint32_t NW_ = 0;
-    int grid_ = 0;
+    int grid_ = 0, block_threads_ = 0;
     uint32_t parity_ = 0;   // phi buffer holding the current field (= k_total_ & 1)
     uint32_t k_total_ = 0;  // global iteration index (bits slot k_total_ % 4, count slot % 3)
     unsigned long long last_update_ns_ = 0, last_barrier_ns_ = 0;

@@ -390,7 +390,8 @@ def run_batch(args, ws, rank, local):
                        "voxels": int(sum(v["image"].size for v in vols)),
                        "plain_brick": list(brick), "plain_threads_per_brick": threads,
                        "batched_brick": [b.stats(0)["brick_x"], b.stats(0)["brick_y"], b.stats(0)["brick_z"]],
-                       "batched_threads_per_brick": b.stats(0)["threads_per_brick"]},
+                       "batched_threads_per_brick": b.stats(0)["threads_per_brick"],
+                       "batched_block_threads": b.stats(0)["block_threads"]},
             "sequential_plain": {"ms_wall": sw, "ms_device": statistics.median(seq_dev),
                                  "voxel_updates": int(seq_upd), "iterations_max": int(max(its))},
             "batched": {"ms_wall": bw, "ms_device": statistics.median(bat_dev),

@@ -80,7 +80,7 @@ typedef struct lss_config {
     int32_t  device;            /* CUDA device ordinal                               */
     int32_t  brick_x, brick_y, brick_z;  /* NS brick shape: 8x8x8, 8x8x4 or 4x4x4;
                                             0,0,0 = pick by the autotuner          */
-    int32_t  threads_per_brick; /* NS: 128, 256 or 512; 0 = autotuner's choice       */
+    int32_t  threads_per_brick; /* NS: 64..512, 32 = one warp; 0 = autotuner's choice */
     int32_t  ref_quirk_i3;      /* REF: 1 = the reference's three-of-four element
                                    loop (UpdateActiveElementsVolume.cu:82,329);
                                    0 = every active element emits                   */
@@ -131,6 +131,8 @@ typedef struct lss_stats {
     double   barrier_ms;           /* ... and waiting at the grid barrier            */
     uint64_t kernel_launches;      /* kernels launched by the engine so far (read
                                       before the stats call's own readback)          */
+    uint32_t grid_blocks;          /* NS: blocks of the persistent launch            */
+    uint32_t block_threads;        /* NS: threads per block of the persistent launch */
 } lss_stats;
 
 /* ---- construction / teardown ------------------------------------------ */

@@ -68,3 +68,34 @@ def test_phantoms_are_deterministic():
     assert 0.7 < float(a[32, 32, 32]) < 0.9
     e = P.ellipsoid((8, 8, 8), (3.5, 3.5, 3.5), (2, 2, 2), 1.0, 0.0, 0.0, 0)
     assert e[4, 4, 4] == 1.0 and e[0, 0, 0] == 0.0
+
+
+STRUCTS = ["lss_config", "lss_params", "lss_conv", "lss_stats", "lss_grads"]
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """Every struct the binding mirrors has the header's size and field
+    offsets, as a C compiler lays them out on this machine."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "lss.h"', "int main(void) {"]
+    for sname in STRUCTS:
+        st = getattr(_lib, sname)
+        lines.append(f'printf("{sname} %zu\\n", sizeof({sname}));')
+        for f, _ in st._fields_:
+            lines.append(f'printf("{sname}.{f} %zu\\n", offsetof({sname}, {f}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(l.split() for l in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                text=True).stdout.splitlines())
+    for sname in STRUCTS:
+        st = getattr(_lib, sname)
+        assert int(got[sname]) == C.sizeof(st), sname
+        for f, _ in st._fields_:
+            assert int(got[f"{sname}.{f}"]) == getattr(st, f).offset, (sname, f)
