@@ -18,8 +18,7 @@ struct NsArgs;
 
 struct BrickConfig {
     int bx, by, bz, threads;
-    int min_blocks = 0;  // block per brick: resident blocks per SM the registers allow (0: 1024
-                         // threads); warp per brick (threads == 32): warps per block (0: default)
+    int min_blocks = 0;  // block per brick: resident blocks per SM the registers allow (0: 1024 threads)
 };
 
 const std::vector<BrickConfig>& brick_configs();

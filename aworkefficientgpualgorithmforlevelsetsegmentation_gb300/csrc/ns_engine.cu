@@ -178,12 +178,11 @@ KernelSet warp_kernels_for() {
 }  // namespace
 
 // The instantiated (brick shape, threads per brick) configurations; 32
-// threads per brick = one warp per brick (k_ns_warp; min_blocks then counts
-// warps per block, default 16 or 32).
+// threads per brick = one warp per brick (k_ns_warp).
 const std::vector<BrickConfig>& brick_configs() {
     static const std::vector<BrickConfig> v = {
         {8, 8, 8, 256}, {8, 8, 8, 128}, {8, 8, 8, 512}, {8, 8, 4, 128}, {8, 8, 4, 256}, {4, 4, 4, 64},
-        {8, 8, 4, 32},  {8, 8, 8, 32},  {4, 4, 4, 32},  {8, 8, 8, 256, 5}, {8, 8, 4, 32, 24}};
+        {8, 8, 4, 32},  {8, 8, 8, 32},  {4, 4, 4, 32},  {8, 8, 8, 256, 5}};
     return v;
 }
 
@@ -196,8 +195,6 @@ static KernelSet kernels(const BrickConfig& c) {
     if (c.bx == 8 && c.by == 8 && c.bz == 4 && c.threads == 128) return kernels_for<8, 8, 4, 128>();
     if (c.bx == 8 && c.by == 8 && c.bz == 4 && c.threads == 256) return kernels_for<8, 8, 4, 256>();
     if (c.bx == 4 && c.by == 4 && c.bz == 4 && c.threads == 64) return kernels_for<4, 4, 4, 64>();
-    if (c.bx == 8 && c.by == 8 && c.bz == 4 && c.threads == 32 && c.min_blocks == 24)
-        return warp_kernels_for<8, 8, 4, 24, 256>();
     if (c.bx == 8 && c.by == 8 && c.bz == 4 && c.threads == 32) return warp_kernels_for<8, 8, 4, 16, 256>();
     if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 32) return warp_kernels_for<8, 8, 8, 16, 256>();
     if (c.bx == 4 && c.by == 4 && c.bz == 4 && c.threads == 32) return warp_kernels_for<4, 4, 4, 32, 64>();

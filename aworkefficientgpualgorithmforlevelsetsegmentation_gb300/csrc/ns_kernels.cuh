@@ -193,6 +193,7 @@ struct NsSmem {
     unsigned long long act[2][S::WORDS];     // the brick's active mask, double buffered
     uint32_t chg[2][S::CHG];                 // changed voxels of the brick (ballot words)
     unsigned long long xy[9 * S::WORDS];     // xy-dilated planes per (ox, oy) pair
+    int4 org[2];                             // origin (x, y, z) and volume of the brick in each buffer
     alignas(8) uint64_t bar[2];
 };
 
@@ -338,12 +339,15 @@ __device__ __forceinline__ int3 brick_origin(const NsVol& V, uint32_t b) {
 }
 
 // Issues the TMA loads of brick b (halo tile of phi[p] and the intensities)
-// into buffer `buf` (thread 0 only).
+// into buffer `buf` and records the brick's origin and volume beside them
+// (thread 0 only: the brick's divisions are done once, not by every thread).
 template <class S, int NT>
 __device__ __forceinline__ void ns_issue_loads(const NsArgs& a, NsSmem<S, NT>& sm, uint32_t b,
                                                uint32_t p, int buf, const NsVol* vone) {
-    const NsVol& V = vone ? *vone : a.vols[a.brick_vol[b]];
+    const uint32_t vol = vone ? 0u : a.brick_vol[b];
+    const NsVol& V = vone ? *vone : a.vols[vol];
     const int3 o = brick_origin<S>(V, b);
+    sm.org[buf] = make_int4(o.x, o.y, o.z, (int)vol);
     mbar_expect_tx(&sm.bar[buf], (uint32_t)(S::TILE + S::VOX) * 4u);
     tma_load_3d(sm.phi[buf], &a.tmaps[V.tmap_base + p], o.x - 4, o.y - 1, o.z - 1, &sm.bar[buf]);
     tma_load_3d(sm.img[buf], &a.tmaps[V.tmap_base + 4], o.x, o.y, o.z, &sm.bar[buf]);
@@ -400,10 +404,11 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
                                                  BlockTally& tally, unsigned long long* cnt,
                                                  const NsVol* vone) {
     const int tid = threadIdx.x;
-    const uint32_t v = vone ? 0u : a.brick_vol[b];
+    // Written by thread 0 with the loads, before a block barrier.
+    const int4 og = sm.org[buf];
+    const uint32_t v = (uint32_t)og.w;
     const NsVol& V = vone ? *vone : a.vols[v];
-    const int3 o = brick_origin<S>(V, b);
-    const int x0 = o.x, y0 = o.y, z0 = o.z;
+    const int x0 = og.x, y0 = og.y, z0 = og.z;
     const unsigned long long* act = sm.act[buf];
     // Every thread waits for the loads itself.  out[buf] is free: the store
     // issued from it two bricks ago was waited for (read) by thread 0 before
@@ -430,9 +435,11 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
         const int lx = j % S::X, ly = (j / S::X) % S::Y, lz = j / (S::X * S::Y);
         return ((lz + 1) * S::TY + (ly + 1)) * S::TX + (lx + 4);
     };
-    uint32_t nact = 0;
+    uint32_t nact = 0;  // thread 0: the brick's active voxels, read before the block barrier
+    if (tid == 0) {
 #pragma unroll
-    for (int w = 0; w < S::WORDS; ++w) nact += __popcll(act[w]);
+        for (int w = 0; w < S::WORDS; ++w) nact += __popcll(act[w]);
+    }
     constexpr int VPT = (S::VOX + NT - 1) / NT;
     const float* bias = V.bias;
     bool anyl = false;
