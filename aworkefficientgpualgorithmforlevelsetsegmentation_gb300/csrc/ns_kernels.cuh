@@ -133,7 +133,11 @@ struct Brick {
 //                       - (XY Fxy + XZ Fxz + YZ Fyz) / 2] / (X^2+Y^2+Z^2).
 // Every operation is an explicit round-to-nearest intrinsic (no contraction
 // or reassociation left to the compiler), so the result is the same bit for
-// bit in every kernel that inlines it.
+// bit in every kernel that inlines it.  The paired FP32 intrinsics
+// (__ffma2_rn and kin) are not used: chained, they gave results an ulp off
+// the IEEE operation sequence in about 1.4 % of updates, where the scalar
+// form matched a CPU restatement of the sequence bit for bit.  The
+// evaluation order keeps few values live; it changes no result.
 template <class PF>
 __device__ __forceinline__ float ns_update_f32(PF P, float I, float bias, const NsVol& V) {
     const float c = P(0, 0, 0);
@@ -144,6 +148,24 @@ __device__ __forceinline__ float ns_update_f32(PF P, float I, float bias, const 
     const float Fxx = __fmaf_rn(-2.0f, c, __fadd_rn(xp, xm));
     const float Fyy = __fmaf_rn(-2.0f, c, __fadd_rn(yp, ym));
     const float Fzz = __fmaf_rn(-2.0f, c, __fadd_rn(zp, zm));
+    const float dxm = __fsub_rn(c, xm), dxp = __fsub_rn(xp, c), dym = __fsub_rn(c, ym),
+                dyp = __fsub_rn(yp, c), dzm = __fsub_rn(c, zm), dzp = __fsub_rn(zp, c);
+    float D = __fmul_rn(__fsub_rn(V.eps, fabsf(__fsub_rn(I, V.T))), V.inv_eps);
+    D = __fadd_rn(fminf(fmaxf(D, -1.0f), 1.0f), bias);
+    const float F = __fmul_rn(V.wd, D);
+    // Osher-Sethian upwind |grad phi| for the speed F: one-sided differences
+    // selected by the sign of F.
+    float a, b, e, f, h, k;
+    if (F > 0.0f) {
+        a = fmaxf(dxm, 0.0f); b = fminf(dxp, 0.0f); e = fmaxf(dym, 0.0f);
+        f = fminf(dyp, 0.0f); h = fmaxf(dzm, 0.0f); k = fminf(dzp, 0.0f);
+    } else {
+        a = fminf(dxm, 0.0f); b = fmaxf(dxp, 0.0f); e = fminf(dym, 0.0f);
+        f = fmaxf(dyp, 0.0f); h = fminf(dzm, 0.0f); k = fmaxf(dzp, 0.0f);
+    }
+    const float s2 = __fmaf_rn(k, k, __fmaf_rn(h, h, __fmaf_rn(f, f, __fmaf_rn(e, e,
+                               __fmaf_rn(b, b, __fmul_rn(a, a))))));
+    const float Fg = __fmul_rn(F, __fsqrt_rn(s2));
     auto cross = [&](float pp, float pm, float mp, float mm) {
         return __fsub_rn(__fadd_rn(pp, mm), __fadd_rn(pm, mp));
     };
@@ -159,25 +181,7 @@ __device__ __forceinline__ float ns_update_f32(PF P, float I, float bias, const 
         const float x = __fmaf_rn(__fmul_rn(Y, Z), Fyz, __fmaf_rn(__fmul_rn(X, Z), Fxz, __fmul_rn(__fmul_rn(X, Y), Fxy)));
         curv = __fdividef(__fmaf_rn(-0.5f, x, t), g2);  // g2 in (4e-12, 192]: within 2 ulp
     }
-    float D = __fmul_rn(__fsub_rn(V.eps, fabsf(__fsub_rn(I, V.T))), V.inv_eps);
-    D = __fadd_rn(fminf(fmaxf(D, -1.0f), 1.0f), bias);
-    const float F = __fmul_rn(V.wd, D);
-    // Osher-Sethian upwind |grad phi| for the speed F: one-sided differences
-    // selected by the sign of F.
-    const float dxm = __fsub_rn(c, xm), dxp = __fsub_rn(xp, c), dym = __fsub_rn(c, ym),
-                dyp = __fsub_rn(yp, c), dzm = __fsub_rn(c, zm), dzp = __fsub_rn(zp, c);
-    float a, b, e, f, h, k;
-    if (F > 0.0f) {
-        a = fmaxf(dxm, 0.0f); b = fminf(dxp, 0.0f); e = fmaxf(dym, 0.0f);
-        f = fminf(dyp, 0.0f); h = fmaxf(dzm, 0.0f); k = fminf(dzp, 0.0f);
-    } else {
-        a = fminf(dxm, 0.0f); b = fmaxf(dxp, 0.0f); e = fminf(dym, 0.0f);
-        f = fmaxf(dyp, 0.0f); h = fminf(dzm, 0.0f); k = fmaxf(dzp, 0.0f);
-    }
-    const float s2 = __fmaf_rn(k, k, __fmaf_rn(h, h, __fmaf_rn(f, f, __fmaf_rn(e, e,
-                               __fmaf_rn(b, b, __fmul_rn(a, a))))));
-    const float g = __fsqrt_rn(s2);
-    const float nv = __fmaf_rn(V.dt, __fsub_rn(__fmul_rn(V.wc, curv), __fmul_rn(F, g)), c);
+    const float nv = __fmaf_rn(V.dt, __fsub_rn(__fmul_rn(V.wc, curv), Fg), c);
     return fminf(fmaxf(nv, V.lo), V.hi);
 }
 
@@ -357,9 +361,14 @@ __device__ __forceinline__ void ns_issue_loads(const NsArgs& a, NsSmem<S, NT>& s
 // flushed with one atomic each when the volume changes or the phase ends.
 // `iter` sums the block's updates over all volumes of the iteration.  cnt
 // may be null (one volume: the count travels with the barrier arrival).
+// Plain data (it may live in shared memory): reset() before first use.
 struct BlockTally {
-    uint32_t v = 0xFFFFFFFFu;
-    unsigned long long upd = 0, brk = 0, iter = 0;
+    uint32_t v;
+    unsigned long long upd, brk, iter;
+    __device__ void reset() {
+        v = 0xFFFFFFFFu;
+        upd = brk = iter = 0;
+    }
     __device__ void add(NsVolState* vs, unsigned long long* cnt, uint32_t vol, unsigned long long n) {
         if (vol != v) {
             flush(vs, cnt);
@@ -443,6 +452,10 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
     constexpr int VPT = (S::VOX + NT - 1) / NT;
     const float* bias = V.bias;
     bool anyl = false;
+    auto bias_at = [&](int j) {
+        const int lx = j % S::X, ly = (j / S::X) % S::Y, lz = j / (S::X * S::Y);
+        return bias[((size_t)(z0 + lz) * V.py + (y0 + ly)) * V.px + (x0 + lx)];
+    };
 #pragma unroll
     for (int k = 0; k < VPT; ++k) {
         const int j = tid + k * NT;
@@ -453,12 +466,7 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
             float nv = c;
             if ((act[j >> 6] >> (j & 63)) & 1ull) {
                 auto P = [&](int dx, int dy, int dz) { return phi[ti + (dz * S::TY + dy) * S::TX + dx]; };
-                float bb = 0.0f;
-                if (bias) {
-                    const int lx = j % S::X, ly = (j / S::X) % S::Y, lz = j / (S::X * S::Y);
-                    bb = bias[((size_t)(z0 + lz) * V.py + (y0 + ly)) * V.px + (x0 + lx)];
-                }
-                nv = ns_update_f32(P, sm.img[buf][j], bb, V);
+                nv = ns_update_f32(P, sm.img[buf][j], bias ? bias_at(j) : 0.0f, V);
                 chg = fabsf(nv - c) > V.thr_t;
             }
             out[j] = nv;
@@ -602,7 +610,7 @@ template <int NT>
 struct IterShared {
     NsVol vol;                     // the descriptor of a one-volume launch
     uint32_t gen, abort;
-    unsigned long long rel, n0, upd;
+    unsigned long long rel, n0, upd, t0, t1;  // t0, t1: block 0's phase clock
     int32_t live;
     uint32_t work[NT], flush[NT];  // this block's bricks of the chunk
     uint2 scan[kScanCache][NT];    // (A_k word, A_{k-1} \ A_k word) per thread
@@ -649,11 +657,9 @@ __device__ __forceinline__ void ns_drive(const NsArgs& a, IterShared<NT>& sh, St
     uint32_t gen = sh.gen;
     const bool one = a.nvol == 1;  // one volume: the stopping rule rides on the barrier
     const NsVol* vone = one ? &sh.vol : nullptr;
-    const unsigned long long n0 = sh.n0;
     uint32_t streak = 0;
     const uint32_t patience = (uint32_t)min(max(a.patience, 0), 0xFFFF);
     int ran = 0;
-    uint64_t t0 = 0, t1 = 0;
     for (int it = 0; it < a.max_iters; ++it) {
         const uint32_t k = a.k0 + (uint32_t)it;
         const uint32_t p = k & 1u, c3 = k % 3u, c3n = (k + 1u) % 3u;
@@ -661,7 +667,7 @@ __device__ __forceinline__ void ns_drive(const NsArgs& a, IterShared<NT>& sh, St
         const uint32_t* prev = a.bits[(k + 3u) % 4u];
         const uint32_t sn = (k + 1u) % 4u, sz = (k + 2u) % 4u;
         unsigned long long* cnt = one ? nullptr : a.cnt[c3];
-        if (blockIdx.x == 0 && tid == 0) t0 = globaltimer_ns();
+        if (blockIdx.x == 0 && tid == 0) sh.t0 = globaltimer_ns();
         if (blockIdx.x == 0)
             for (int v = tid; v < a.nvol; v += NT) a.cnt[c3n][v] = 0ull;
         // Ranks: thread t counts the words t, t+NT, ...; ranks follow (thread,
@@ -735,7 +741,7 @@ __device__ __forceinline__ void ns_drive(const NsArgs& a, IterShared<NT>& sh, St
         }
         proc.finish(a, sh, cnt);
         for (uint32_t w = blockIdx.x * NT + tid; w < a.NW; w += G * NT) a.bits[sz][w] = 0u;
-        if (blockIdx.x == 0 && tid == 0) t1 = globaltimer_ns();
+        if (blockIdx.x == 0 && tid == 0) sh.t1 = globaltimer_ns();
         __syncthreads();
         if (tid == 0) {
             const unsigned long long mine = sh.upd;
@@ -759,7 +765,7 @@ __device__ __forceinline__ void ns_drive(const NsArgs& a, IterShared<NT>& sh, St
                     const unsigned long long n = (old >> kArriveShift) + mine;
                     a.ctl->n_last = n;
                     if (a.conv_mode) {
-                        st = ((double)n < a.rel * (double)n0) ? min(st + 1u, 0xFFFFu) : 0u;
+                        st = ((double)n < a.rel * (double)sh.n0) ? min(st + 1u, 0xFFFFu) : 0u;
                         stop = stop || st >= patience || n <= a.abs_thr;
                     }
                 }
@@ -786,8 +792,8 @@ __device__ __forceinline__ void ns_drive(const NsArgs& a, IterShared<NT>& sh, St
             asm volatile("fence.proxy.async.global;" ::: "memory");
             if (blockIdx.x == 0) {
                 const uint64_t t2 = globaltimer_ns();
-                a.ctl->t_phase1_ns += t1 - t0;
-                a.ctl->t_barrier_ns += t2 - t1;
+                a.ctl->t_phase1_ns += sh.t1 - sh.t0;
+                a.ctl->t_barrier_ns += t2 - sh.t1;
             }
         }
         __syncthreads();
@@ -858,14 +864,15 @@ __device__ __forceinline__ void ns_drive(const NsArgs& a, IterShared<NT>& sh, St
 template <class S, int NT>
 struct BlockProc {
     NsSmem<S, NT>& sm;
-    uint32_t mphase;   // bit b: phase of load barrier b
+    BlockTally& tally;  // thread 0; in shared memory, off the threads' registers
+    uint32_t mphase;    // bit b: phase of load barrier b
     int buf;
-    BlockTally tally;  // thread 0
-    __device__ explicit BlockProc(NsSmem<S, NT>& s) : sm(s), mphase(0u), buf(0) {}
+    __device__ BlockProc(NsSmem<S, NT>& s, BlockTally& t) : sm(s), tally(t), mphase(0u), buf(0) {}
     __device__ void init() {
         if (threadIdx.x == 0) {
             mbar_init(&sm.bar[0], 1);
             mbar_init(&sm.bar[1], 1);
+            tally.reset();
         }
     }
     __device__ void chunk(const NsArgs& a, IterShared<NT>& sh, uint32_t nw, uint32_t nf, uint32_t p,
@@ -897,7 +904,7 @@ struct BlockProc {
         if (threadIdx.x == 0) {
             sh.upd = tally.iter;
             tally.flush(a.vstate, cnt);
-            tally = BlockTally();
+            tally.reset();
             tma_store_wait_all();
             asm volatile("fence.proxy.async.global;" ::: "memory");
         }
@@ -912,8 +919,9 @@ __global__ void __launch_bounds__(NT, MINB) k_ns_persistent(NsArgs a) {
     using S = Brick<BX, BY, BZ>;
     __shared__ NsSmem<S, NT> sm;
     __shared__ IterShared<NT> sh;
+    __shared__ BlockTally tally;
     extern __shared__ int32_t s_dyn[];
-    BlockProc<S, NT> proc(sm);
+    BlockProc<S, NT> proc(sm, tally);
     ns_drive<NT>(a, sh, stop_state(s_dyn, a.nvol), proc);
 }
 
@@ -1102,6 +1110,7 @@ struct WarpProc {
     BlockTally tally;  // lane 0 of every warp
     __device__ explicit WarpProc(WarpSlot<S>* s) : slots(s), phase(0u) {}
     __device__ void init() {
+        tally.reset();
         if ((threadIdx.x & 31) == 0) mbar_init(&slots[threadIdx.x >> 5].bar, 1);
     }
     __device__ void chunk(const NsArgs& a, IterShared<NT>& sh, uint32_t nw, uint32_t nf, uint32_t p,
@@ -1118,7 +1127,7 @@ struct WarpProc {
         if ((threadIdx.x & 31) == 0) {
             if (tally.iter) atomicAdd(&sh.upd, tally.iter);
             tally.flush(a.vstate, cnt);
-            tally = BlockTally();
+            tally.reset();
             tma_store_wait_all();
             asm volatile("fence.proxy.async.global;" ::: "memory");
         }
