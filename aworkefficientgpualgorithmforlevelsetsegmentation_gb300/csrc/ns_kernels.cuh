@@ -444,11 +444,12 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
         const int lx = j % S::X, ly = (j / S::X) % S::Y, lz = j / (S::X * S::Y);
         return ((lz + 1) * S::TY + (ly + 1)) * S::TX + (lx + 4);
     };
-    uint32_t nact = 0;  // thread 0: the brick's active voxels, read before the block barrier
-    if (tid == 0) {
-#pragma unroll
-        for (int w = 0; w < S::WORDS; ++w) nact += __popcll(act[w]);
-    }
+    // Warp 1: the brick's active voxels (one mask word a lane), read before
+    // the block barrier; its lane 0 tallies them while thread 0 issues the
+    // store.
+    static_assert(NT >= 64 && S::WORDS <= 32, "tally warp");
+    uint32_t nact = 0;
+    if ((tid >> 5) == 1) nact = __reduce_add_sync(0xffffffffu, (tid & 31) < S::WORDS ? __popcll(act[tid & 31]) : 0u);
     constexpr int VPT = (S::VOX + NT - 1) / NT;
     const float* bias = V.bias;
     bool anyl = false;
@@ -487,6 +488,7 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
     if (tid == 0) {
         tma_store_3d(&a.tmaps[V.tmap_base + 2 + (p ^ 1u)], x0, y0, z0, out);
         tma_store_commit();
+    } else if (tid == 32) {
         tally.add(a.vstate, cnt, v, nact);
     }
     // Dilation of the changed mask into the 27 bricks around (and including)
@@ -603,6 +605,38 @@ __device__ __forceinline__ StopState stop_state(int32_t* base, int nvol) {
 }
 
 constexpr uint32_t kNoBrick = 0xFFFFFFFFu;  // a brick of a finished volume
+
+// x / g for x < 2^31, given gm = 0xFFFFFFFF / g + 1: the high half of x * gm
+// overshoots x / g by less than one and is corrected once (g = 1: gm wraps).
+__host__ __device__ __forceinline__ uint32_t div_magic(uint32_t x, uint32_t g, uint32_t gm) {
+    if (g == 1u) return x;
+#ifdef __CUDA_ARCH__
+    const uint32_t d = __umulhi(x, gm);
+#else
+    const uint32_t d = (uint32_t)(((uint64_t)x * gm) >> 32);
+#endif
+    return d * g > x ? d - 1u : d;
+}
+
+// Position of the s-th set bit (from 0, counted from bit 0) of m; s < popc(m).
+__host__ __device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t s) {
+    uint32_t pos = 0;
+#pragma unroll
+    for (int h = 16; h >= 1; h >>= 1) {
+        const uint32_t low = m & ((1u << h) - 1u);
+#ifdef __CUDA_ARCH__
+        const uint32_t c = __popc(low);
+#else
+        const uint32_t c = (uint32_t)__builtin_popcount(low);
+#endif
+        if (s >= c) {
+            s -= c;
+            pos += (uint32_t)h;
+            m >>= h;
+        }
+    }
+    return pos;
+}
 constexpr int kScanCache = 4;               // membership words per thread kept in shared memory
 
 // Shared state of the iteration driver (static shared memory).
@@ -693,6 +727,8 @@ __device__ __forceinline__ void ns_drive(const NsArgs& a, IterShared<NT>& sh, St
         const uint32_t na = (uint32_t)tot, nfl = (uint32_t)(tot >> 32);
         // Block i takes the ranks i, i+G, i+2G, ... of both kinds.
         const uint32_t bi = blockIdx.x;
+        const uint32_t gm = 0xFFFFFFFFu / G + 1u;
+        auto divg = [&](uint32_t x) { return div_magic(x, G, gm); };
         const uint32_t mya = na > bi ? (na - bi + G - 1) / G : 0u;
         const uint32_t myf = nfl > bi ? (nfl - bi + G - 1) / G : 0u;
         for (uint32_t c0 = 0; c0 < mya || c0 < myf; c0 += NT) {
@@ -707,12 +743,10 @@ __device__ __forceinline__ void ns_drive(const NsArgs& a, IterShared<NT>& sh, St
                 auto visit = [&](uint32_t w, uint32_t m0, uint32_t r, uint32_t hi, uint32_t* out) {
                     const uint32_t n = __popc(m0);
                     uint32_t q = max(r, lo);
-                    q = bi + (q - bi + G - 1) / G * G;
+                    q = bi + divg(q - bi + G - 1) * G;
                     for (; q < r + n && q < hi; q += G) {
-                        uint32_t m = m0;
-                        for (uint32_t s2 = q - r; s2; --s2) m &= m - 1u;
-                        const uint32_t b = w * 32u + (uint32_t)(__ffs(m) - 1);
-                        const uint32_t slot = (q - bi) / G - c0;
+                        const uint32_t b = w * 32u + nth_set_bit(m0, q - r);
+                        const uint32_t slot = divg(q - bi) - c0;
                         if (slot >= (uint32_t)NT || b >= a.NB) {  // a rank outside this chunk: report, skip
                             set_error(&a.ctl->err, ERR_BOUNDS);
                             continue;
@@ -864,7 +898,7 @@ __device__ __forceinline__ void ns_drive(const NsArgs& a, IterShared<NT>& sh, St
 template <class S, int NT>
 struct BlockProc {
     NsSmem<S, NT>& sm;
-    BlockTally& tally;  // thread 0; in shared memory, off the threads' registers
+    BlockTally& tally;  // thread 32; in shared memory, off the threads' registers
     uint32_t mphase;    // bit b: phase of load barrier b
     int buf;
     __device__ BlockProc(NsSmem<S, NT>& s, BlockTally& t) : sm(s), tally(t), mphase(0u), buf(0) {}

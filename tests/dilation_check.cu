@@ -1,7 +1,9 @@
 // Host-side check of the bit-parallel brick dilation (dilate_slot,
 // dilate_word, inside_mask in csrc/ns_kernels.cuh) against a brute-force
 // dilation, for every brick shape, both neighbourhoods and every neighbour
-// slot.  Built and run by tests/test_dilation_host.py (no GPU needed).
+// slot; and the rank-selection helpers nth_set_bit and div_magic against
+// plain loops and division.  Built and run by tests/test_dilation_host.py
+// (no GPU needed).
 #include "ns_kernels.cuh"
 #include <cstdio>
 #include <random>
@@ -47,9 +49,34 @@ template <class S> int check(std::mt19937_64& rng, int nbh) {
     }
     return bad;
 }
+int check_select(std::mt19937_64& rng) {
+    int bad = 0;
+    for (int trial = 0; trial < 20000; ++trial) {
+        uint32_t m = (uint32_t)rng();
+        if (trial % 3 == 1) m &= (uint32_t)rng();
+        if (trial % 3 == 2) m |= (uint32_t)rng();
+        uint32_t mm = m;
+        for (uint32_t s = 0; mm; ++s, mm &= mm - 1u)
+            if (nth_set_bit(m, s) != (uint32_t)__builtin_ctz(mm)) ++bad;
+    }
+    for (uint32_t g = 1; g <= 5000; ++g) {
+        const uint32_t gm = 0xFFFFFFFFu / g + 1u;
+        for (int t = 0; t < 200; ++t) {
+            uint32_t x = (uint32_t)(rng() & 0x7FFFFFFFu);
+            if (t % 4 == 1) x = (x / g) * g;
+            if (t % 4 == 2) x = (x / g) * g + g - 1u;
+            if (t % 4 == 3) x = (x / g) * g - 1u;
+            x &= 0x7FFFFFFFu;
+            if (div_magic(x, g, gm) != x / g) ++bad;
+        }
+        if (div_magic(0x7FFFFFFFu, g, gm) != 0x7FFFFFFFu / g) ++bad;
+    }
+    return bad;
+}
 int main() {
     std::mt19937_64 rng(7);
-    int bad = 0;
+    int bad = check_select(rng);
+    printf("selection helpers: %d\n", bad);
     for (int nbh : {26, 6}) {
         int a = check<Brick<8, 8, 8>>(rng, nbh), b = check<Brick<8, 8, 4>>(rng, nbh), c = check<Brick<4, 4, 4>>(rng, nbh);
         printf("nbh %d: 888 %d, 884 %d, 444 %d\n", nbh, a, b, c);
