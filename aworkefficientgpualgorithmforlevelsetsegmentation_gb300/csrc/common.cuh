@@ -152,6 +152,9 @@ __device__ __forceinline__ uint32_t block_exclusive_sum(uint32_t v, uint32_t* to
 }
 
 // Same for 64-bit values (packed counters).
+// Sync = false leaves out the closing barrier (it only guards the shared
+// slots against a following call): the caller separates calls by a barrier.
+template <bool Sync = true>
 __device__ __forceinline__ uint64_t block_exclusive_sum64(uint64_t v, uint64_t* total) {
     __shared__ uint64_t s_warp64[33];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -177,7 +180,7 @@ __device__ __forceinline__ uint64_t block_exclusive_sum64(uint64_t v, uint64_t* 
     __syncthreads();
     uint64_t r = s_warp64[warp] + x - v;
     *total = s_warp64[32];
-    __syncthreads();
+    if (Sync) __syncthreads();
     return r;
 }
 

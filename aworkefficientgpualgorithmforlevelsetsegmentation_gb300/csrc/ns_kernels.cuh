@@ -723,14 +723,15 @@ __device__ __forceinline__ void ns_drive(const NsArgs& a, IterShared<NT>& sh, St
             cf += __popc(prev[w] & ~c);
         }
         uint64_t tot;
-        const uint64_t ex = block_exclusive_sum64(((uint64_t)cf << 32) | ca, &tot);
+        // (No closing barrier: the next call is many block barriers away.)
+        const uint64_t ex = block_exclusive_sum64<false>(((uint64_t)cf << 32) | ca, &tot);
         const uint32_t na = (uint32_t)tot, nfl = (uint32_t)(tot >> 32);
         // Block i takes the ranks i, i+G, i+2G, ... of both kinds.
         const uint32_t bi = blockIdx.x;
         const uint32_t gm = 0xFFFFFFFFu / G + 1u;
         auto divg = [&](uint32_t x) { return div_magic(x, G, gm); };
-        const uint32_t mya = na > bi ? (na - bi + G - 1) / G : 0u;
-        const uint32_t myf = nfl > bi ? (nfl - bi + G - 1) / G : 0u;
+        const uint32_t mya = na > bi ? divg(na - bi + G - 1) : 0u;
+        const uint32_t myf = nfl > bi ? divg(nfl - bi + G - 1) : 0u;
         for (uint32_t c0 = 0; c0 < mya || c0 < myf; c0 += NT) {
             // Chunk c0: this block's j-th brick for j in [c0, c0 + NT).
             const uint32_t nw = min(mya - min(mya, c0), (uint32_t)NT);
@@ -738,14 +739,33 @@ __device__ __forceinline__ void ns_drive(const NsArgs& a, IterShared<NT>& sh, St
             {
                 const uint32_t lo = bi + c0 * G;
                 const uint32_t hia = bi + (c0 + nw) * G, hif = bi + (c0 + nf) * G;
-                uint32_t ra = (uint32_t)ex, rf = (uint32_t)(ex >> 32);
-                // Ranks q of [r, r + popc(m0)) with q = bi (mod G), q in [lo, hi).
-                auto visit = [&](uint32_t w, uint32_t m0, uint32_t r, uint32_t hi, uint32_t* out) {
-                    const uint32_t n = __popc(m0);
-                    uint32_t q = max(r, lo);
+                // This thread's ranks are [ra, ra + ca) and [rf, rf + cf),
+                // its words in order; the block's ranks q = bi (mod G) among
+                // them (at most one while a thread holds fewer than G bricks)
+                // are located word by word.
+                const uint32_t ra = (uint32_t)ex, rf = (uint32_t)(ex >> 32);
+                auto take = [&](uint32_t r0, uint32_t n, uint32_t hi, bool fl, uint32_t* out) {
+                    uint32_t q = max(r0, lo);
                     q = bi + divg(q - bi + G - 1) * G;
-                    for (; q < r + n && q < hi; q += G) {
-                        const uint32_t b = w * 32u + nth_set_bit(m0, q - r);
+                    for (; q < r0 + n && q < hi; q += G) {
+                        uint32_t s = q - r0, b = 0xFFFFFFFFu;
+                        for (int m = 0; m < kScanCache; ++m) {
+                            const uint2 cf2 = sh.scan[m][tid];
+                            const uint32_t bits = fl ? cf2.y : cf2.x;
+                            const uint32_t c = __popc(bits);
+                            if (s < c) {
+                                b = (tid + (uint32_t)m * NT) * 32u + nth_set_bit(bits, s);
+                                break;
+                            }
+                            s -= c;
+                        }
+                        for (uint32_t w = tid + kScanCache * NT; b == 0xFFFFFFFFu && w < a.NW; w += NT) {
+                            const uint32_t cw = cur[w];
+                            const uint32_t bits = fl ? prev[w] & ~cw : cw;
+                            const uint32_t c = __popc(bits);
+                            if (s < c) b = w * 32u + nth_set_bit(bits, s);
+                            else s -= c;
+                        }
                         const uint32_t slot = divg(q - bi) - c0;
                         if (slot >= (uint32_t)NT || b >= a.NB) {  // a rank outside this chunk: report, skip
                             set_error(&a.ctl->err, ERR_BOUNDS);
@@ -754,21 +774,8 @@ __device__ __forceinline__ void ns_drive(const NsArgs& a, IterShared<NT>& sh, St
                         out[slot] = (!one && ss.done[a.brick_vol[b]]) ? kNoBrick : b;
                     }
                 };
-                for (int m = 0; m < kScanCache; ++m) {
-                    const uint32_t w = tid + (uint32_t)m * NT;
-                    const uint2 cf2 = sh.scan[m][tid];
-                    if (cf2.x) visit(w, cf2.x, ra, hia, sh.work);
-                    if (cf2.y) visit(w, cf2.y, rf, hif, sh.flush);
-                    ra += __popc(cf2.x);
-                    rf += __popc(cf2.y);
-                }
-                for (uint32_t w = tid + kScanCache * NT; w < a.NW; w += NT) {
-                    const uint32_t c = cur[w], f = prev[w] & ~c;
-                    if (c) visit(w, c, ra, hia, sh.work);
-                    if (f) visit(w, f, rf, hif, sh.flush);
-                    ra += __popc(c);
-                    rf += __popc(f);
-                }
+                take(ra, ca, hia, false, sh.work);
+                take(rf, cf, hif, true, sh.flush);
             }
             __syncthreads();
             proc.chunk(a, sh, nw, nf, p, sn, cnt, vone);  // ends with a block barrier
