@@ -99,26 +99,65 @@ __global__ void k_ns_sphere_union(float* phi, int nx, int ny, int nz, int px, in
 }
 
 // Dense all-voxel update with the same arithmetic as the sparse engine: the
-// unconditional update the paper compares against (main.tex:523).  Block =
-// 32 x 8 voxels of one plane, marching 8 planes in z; neighbours are read
-// through the read-only cache.
-__global__ void __launch_bounds__(256) k_ns_dense(const NsVol* vols, int v, uint32_t p) {
-    const NsVol& V = vols[v];
-    const int x = blockIdx.x * 32 + threadIdx.x % 32;
-    const int y = blockIdx.y * 8 + threadIdx.x / 32;
-    if (x >= V.nx || y >= V.ny) return;
-    const float* __restrict__ src = V.phi[p];
-    float* __restrict__ dst = V.phi[p ^ 1u];
-    const int z0 = blockIdx.z * 8;
-    for (int z = z0; z < min(z0 + 8, V.nz); ++z) {
-        auto P = [&](int dx, int dy, int dz) {
-            const int xx = min(max(x + dx, 0), V.nx - 1), yy = min(max(y + dy, 0), V.ny - 1),
-                      zz = min(max(z + dz, 0), V.nz - 1);
-            return __ldg(&src[((size_t)zz * V.py + yy) * V.px + xx]);
-        };
-        const size_t k = ((size_t)z * V.py + y) * V.px + x;
-        const float bb = V.bias ? V.bias[k] : 0.0f;
-        dst[k] = ns_update_f32(P, __ldg(&V.img[k]), bb, V);
+// unconditional update the paper compares against (main.tex:523).  A block
+// covers a 32 x 8 column of the volume over kDenseZ planes and marches in z
+// with three planes of phi (each with a one-voxel halo, clamped to the
+// volume's edge) in a shared-memory ring, so every phi value is read from
+// memory about once and every neighbour from shared memory.  The descriptor
+// is a kernel parameter: its scalars are constant-bank operands.
+constexpr int kDenseX = 32, kDenseY = 8, kDenseZ = 32;
+constexpr int kDensePlane = (kDenseX + 2) * (kDenseY + 2);
+
+__global__ void __launch_bounds__(256) k_ns_dense(const NsVol V, uint32_t p) {
+    __shared__ float ring[3][kDensePlane];
+    const int tx = threadIdx.x % kDenseX, ty = threadIdx.x / kDenseX;
+    const int x0 = blockIdx.x * kDenseX, y0 = blockIdx.y * kDenseY, zb = blockIdx.z * kDenseZ;
+    const float* __restrict__ src = p ? V.phi[1] : V.phi[0];
+    float* __restrict__ dst = p ? V.phi[0] : V.phi[1];
+    const size_t pxy = (size_t)V.px * V.py;
+    // The (at most two) halo-plane elements this thread loads: in-plane
+    // offsets, clamped to the volume, fixed over the march.
+    size_t off[2];
+    bool has[2];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int t = threadIdx.x + r * 256;
+        has[r] = t < kDensePlane;
+        const int lx = t % (kDenseX + 2), ly = t / (kDenseX + 2);
+        const int gx = min(max(x0 - 1 + lx, 0), V.nx - 1), gy = min(max(y0 - 1 + ly, 0), V.ny - 1);
+        off[r] = (size_t)gy * V.px + gx;
+    }
+    auto load_plane = [&](float* d, int z) {
+        const float* s = src + (size_t)min(max(z, 0), V.nz - 1) * pxy;
+#pragma unroll
+        for (int r = 0; r < 2; ++r)
+            if (has[r]) d[threadIdx.x + r * 256] = s[off[r]];
+    };
+    float* pm = ring[0];
+    float* pc = ring[1];
+    float* pp = ring[2];
+    load_plane(pm, zb - 1);
+    load_plane(pc, zb);
+    const int x = x0 + tx, y = y0 + ty;
+    const bool inside = x < V.nx && y < V.ny;
+    const int c0 = (ty + 1) * (kDenseX + 2) + tx + 1;
+    const int zend = min(zb + kDenseZ, V.nz);
+    size_t k = (size_t)zb * pxy + (size_t)y * V.px + x;
+    for (int z = zb; z < zend; ++z, k += pxy) {
+        load_plane(pp, z + 1);  // into the ring slot freed by the barrier below
+        __syncthreads();
+        if (inside) {
+            auto P = [&](int dx, int dy, int dz) {
+                const float* pl = dz < 0 ? pm : (dz > 0 ? pp : pc);
+                return pl[c0 + dy * (kDenseX + 2) + dx];
+            };
+            dst[k] = ns_update_f32(P, V.img[k], V.bias ? V.bias[k] : 0.0f, V);
+        }
+        __syncthreads();
+        float* t = pm;
+        pm = pc;
+        pc = pp;
+        pp = t;
     }
 }
 
@@ -638,8 +677,9 @@ float NsCore::dense_run(int iters) {
     for (int it = 0; it < iters; ++it) {
         for (int v = 0; v < (int)vols_.size(); ++v) {
             const VolHost& V = vols_[v];
-            dim3 grid((V.nx + 31) / 32, (V.ny + 7) / 8, (V.nz + 7) / 8);
-            k_ns_dense<<<grid, 256, 0, st>>>(d_vols_, v, parity_);
+            dim3 grid((V.nx + kDenseX - 1) / kDenseX, (V.ny + kDenseY - 1) / kDenseY,
+                      (V.nz + kDenseZ - 1) / kDenseZ);
+            k_ns_dense<<<grid, 256, 0, st>>>(descriptor(v), parity_);
             ++owner_->launches;
         }
         parity_ ^= 1u;

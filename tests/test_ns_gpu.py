@@ -259,3 +259,19 @@ def test_ns_every_config_uses_both_tma_buffers():
             assert float(np.max(np.abs(phi.astype(np.float64) - o.read_phi64()))) <= 4 * PHI_TOL
         else:
             assert np.array_equal(phi, ref), (bx, by, bz, t)
+
+
+@pytest.mark.parametrize("shape", [(64, 64, 64), (29, 50, 37)])
+def test_dense_pass_equals_all_active_sparse(shape):
+    """The dense all-voxel kernel (the baseline of the sparse-vs-dense
+    comparison) and the sparse engine with every voxel active compute the same
+    field bit for bit, borders (clamp-to-edge) included."""
+    cfg = P.config2(0.25)
+    img = np.ascontiguousarray(cfg["image"][:shape[0], :shape[1], :shape[2]])
+    phi0 = np.ascontiguousarray(cfg["phi0"][:shape[0], :shape[1], :shape[2]])
+    sub = dict(cfg, image=img, phi0=phi0)
+    a = make_gpu(sub, temporal_threshold=-1.0, spatial_threshold=-1.0)
+    b = make_gpu(sub, temporal_threshold=-1.0, spatial_threshold=-1.0)
+    a.step(7)
+    b.step_dense(7)
+    assert np.array_equal(a.read_phi(), b.read_phi())
