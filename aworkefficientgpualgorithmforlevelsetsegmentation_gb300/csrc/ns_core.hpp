@@ -99,6 +99,9 @@ class NsCore {
     uint64_t NB_ = 0;
     uint32_t NW_ = 0;
     int grid_ = 0, block_threads_ = 0;
+    // NsCtl's growing counters as of the last readback (the counter barrier's
+    // starting points for the next launch); zero whenever NsCtl is cleared.
+    unsigned long long ctl_arrivals_ = 0, ctl_upd_sum_[2] = {0, 0};
     uint32_t parity_ = 0;   // phi buffer holding the current field (= k_total_ & 1)
     uint32_t k_total_ = 0;  // global iteration index (bits slot k_total_ % 4, count slot % 3)
     unsigned long long last_update_ns_ = 0, last_barrier_ns_ = 0;

@@ -349,6 +349,7 @@ void NsCore::configure(const BrickConfig& c) {
                              cudaMemcpyHostToDevice, st));
     LSS_CUDA(cudaMemsetAsync(d_vstate_, 0, sizeof(NsVolState) * vols_.size(), st));
     LSS_CUDA(cudaMemsetAsync(d_ctl_, 0, sizeof(NsCtl), st));
+    ctl_arrivals_ = ctl_upd_sum_[0] = ctl_upd_sum_[1] = 0;
     upload_descriptors();
     // Co-residency of the persistent grid.
     const size_t dyn = dyn_smem();
@@ -415,6 +416,9 @@ NsArgs NsCore::args(uint32_t k0, int max_iters, const lss_conv* conv) const {
     a.k0 = k0;
     a.max_iters = max_iters;
     a.conv_mode = conv ? 1 : 0;
+    a.arrivals0 = ctl_arrivals_;
+    a.upd_sum0[0] = ctl_upd_sum_[0];
+    a.upd_sum0[1] = ctl_upd_sum_[1];
     if (conv) {
         a.rel = conv->rel_threshold;
         a.patience = conv->patience;
@@ -457,6 +461,7 @@ void NsCore::init_active() {
     for (int q = 0; q < 4; ++q) LSS_CUDA(cudaMemsetAsync(d_bits_[q], 0, (size_t)NW_ * 4, st));
     for (int q = 0; q < 3; ++q) LSS_CUDA(cudaMemsetAsync(d_cnt_[q], 0, 8 * vols_.size(), st));
     LSS_CUDA(cudaMemsetAsync(d_ctl_, 0, sizeof(NsCtl), st));
+    ctl_arrivals_ = ctl_upd_sum_[0] = ctl_upd_sum_[1] = 0;
     // The global iteration index restarts at the phi parity: bits[k%4] holds
     // A_0 (the other three slots are empty, so A_{-1} is empty too).
     k_total_ = parity_;
@@ -570,6 +575,9 @@ int NsCore::run(int max_iters, const lss_conv* conv, float* ms) {
     cudaEventDestroy(e1);
     NsCtl c;
     d2h(&c, d_ctl_, sizeof(c));
+    ctl_arrivals_ = c.arrivals;
+    ctl_upd_sum_[0] = c.upd_sum[0];
+    ctl_upd_sum_[1] = c.upd_sum[1];
     if (fault_injected("timeout")) c.err |= ERR_BARRIER_TIMEOUT;
     LSS_REQUIRE(c.err == 0, LSS_ERR_TIMEOUT,
                 "device-side wait gave up (error word " + std::to_string(c.err) + ")");

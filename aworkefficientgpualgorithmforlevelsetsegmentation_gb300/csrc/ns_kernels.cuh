@@ -87,7 +87,19 @@ struct NsCtl {
     unsigned long long t_phase1_ns, t_barrier_ns;  // block 0's time split
     alignas(128) unsigned long long bar_release;
     unsigned long long pad2[15];
+    // Counter barrier (grids of at most kCounterBarrierMax blocks): arrivals
+    // counted since the control block was cleared, and the one-volume update
+    // counts summed by iteration parity; all only grow.
+    alignas(128) unsigned long long arrivals;
+    unsigned long long pad3[15];
+    alignas(128) unsigned long long upd_sum[2];
+    unsigned long long pad4[14];
 };
+
+// Up to this many blocks the grid barrier is a counter that every block
+// polls (one hop after the last arrival); above it, polling that one line
+// costs more than the last arriver's release word.
+constexpr uint32_t kCounterBarrierMax = 320;
 
 struct NsArgs {
     const NsVol* vols;
@@ -107,6 +119,8 @@ struct NsArgs {
     double rel;
     int32_t patience;
     unsigned long long abs_thr;
+    unsigned long long arrivals0;   // NsCtl::arrivals and upd_sum at the launch
+    unsigned long long upd_sum0[2];
 };
 
 template <int BX, int BY, int BZ>
@@ -645,6 +659,7 @@ struct IterShared {
     NsVol vol;                     // the descriptor of a one-volume launch
     uint32_t gen, abort;
     unsigned long long rel, n0, upd, t0, t1;  // t0, t1: block 0's phase clock
+    unsigned long long upd_seen[2];           // counter barrier: upd_sum read so far, by parity
     int32_t live;
     uint32_t work[NT], flush[NT];  // this block's bricks of the chunk
     uint2 scan[kScanCache][NT];    // (A_k word, A_{k-1} \ A_k word) per thread
@@ -676,6 +691,8 @@ __device__ __forceinline__ void ns_drive(const NsArgs& a, IterShared<NT>& sh, St
         sh.abort = 0;
         sh.upd = 0;
         sh.n0 = a.vstate[0].n0;
+        sh.upd_seen[0] = a.upd_sum0[0];
+        sh.upd_seen[1] = a.upd_sum0[1];
         if (a.nvol == 1) sh.vol = a.vols[0];
         for (int v = 0; v < a.nvol; ++v)
             for (int m = 0; m < 5; ++m) tmap_acquire(&a.tmaps[a.vols[v].tmap_base + m]);
@@ -784,7 +801,57 @@ __device__ __forceinline__ void ns_drive(const NsArgs& a, IterShared<NT>& sh, St
         for (uint32_t w = blockIdx.x * NT + tid; w < a.NW; w += G * NT) a.bits[sz][w] = 0u;
         if (blockIdx.x == 0 && tid == 0) sh.t1 = globaltimer_ns();
         __syncthreads();
-        if (tid == 0) {
+        if (tid == 0 && G <= kCounterBarrierMax) {
+            // Counter barrier: the block's count, then a release add of one
+            // arrival; every block polls the counter until the iteration's
+            // arrivals are all in and evaluates the one-volume stopping rule
+            // on the same sum (the counts of one parity slot cannot gain the
+            // next iteration's before every block has read them).
+            const unsigned long long mine = sh.upd;
+            sh.upd = 0;
+            const uint32_t target = gen + 1;
+            const uint32_t par = k & 1u;
+            if (one && mine)
+                asm volatile("red.relaxed.gpu.global.add.u64 [%0], %1;" ::"l"(&a.ctl->upd_sum[par]), "l"(mine)
+                             : "memory");
+            asm volatile("red.release.gpu.global.add.u64 [%0], %1;" ::"l"(&a.ctl->arrivals), "l"(1ull) : "memory");
+            const unsigned long long want = a.arrivals0 + (unsigned long long)G * (unsigned long long)(it + 1);
+            const uint64_t w0 = globaltimer_ns();
+            uint32_t ns = 16;
+            unsigned long long rel = target;
+            for (;;) {
+                if (ld_acquire_u64((const uint64_t*)&a.ctl->arrivals) >= want) break;
+                if (globaltimer_ns() - w0 > kWaitLimitNs) {
+                    set_error(&a.ctl->err, ERR_BARRIER_TIMEOUT);
+                    sh.abort = 1;
+                    break;
+                }
+                __nanosleep(ns);
+                if (ns < 64) ns <<= 1;
+            }
+            if (one) {
+                const unsigned long long tot = *(volatile unsigned long long*)&a.ctl->upd_sum[par];
+                const unsigned long long n = tot - sh.upd_seen[par];
+                sh.upd_seen[par] = tot;
+                if (blockIdx.x == 0) a.ctl->n_last = n;
+                uint32_t st = streak;
+                bool stop = it + 1 >= a.max_iters;
+                if (a.conv_mode) {
+                    st = ((double)n < a.rel * (double)sh.n0) ? min(st + 1u, 0xFFFFu) : 0u;
+                    stop = stop || st >= patience || n <= a.abs_thr;
+                }
+                rel = (unsigned long long)target | ((unsigned long long)st << kRelStreakShift) |
+                      (stop ? kRelStop : 0ull);
+            }
+            sh.rel = rel;
+            gen = target;
+            asm volatile("fence.proxy.async.global;" ::: "memory");
+            if (blockIdx.x == 0) {
+                const uint64_t t2 = globaltimer_ns();
+                a.ctl->t_phase1_ns += sh.t1 - sh.t0;
+                a.ctl->t_barrier_ns += t2 - sh.t1;
+            }
+        } else if (tid == 0) {
             const unsigned long long mine = sh.upd;
             sh.upd = 0;
             const uint32_t target = gen + 1;
