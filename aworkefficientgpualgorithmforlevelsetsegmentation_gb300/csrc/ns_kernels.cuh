@@ -356,6 +356,35 @@ __device__ __forceinline__ int3 brick_origin(const NsVol& V, uint32_t b) {
     return make_int3(kx * S::X, ky * S::Y, kz * S::Z);
 }
 
+// A brick tile (origin x0, y0, z0 at tile column 4, row 1, plane 1) whose
+// read region [-1, X] x [-1, Y] x [-1, Z] leaves the volume.
+template <class S>
+__device__ __forceinline__ bool tile_at_edge(const NsVol& V, int x0, int y0, int z0) {
+    return x0 < 1 || y0 < 1 || z0 < 1 || x0 + S::X + 1 > V.nx || y0 + S::Y + 1 > V.ny || z0 + S::Z + 1 > V.nz;
+}
+
+// Clamp-to-edge halo: every element of the read region outside the volume
+// (zero-filled by the TMA load) takes the value of the nearest voxel inside,
+// which no thread writes, so one pass needs no ordering.  Threads t0,
+// t0 + stride, ... each fix whole rows (y, z) of the region.
+template <class S>
+__device__ __forceinline__ void clamp_tile_halo(float* phi, const NsVol& V, int x0, int y0, int z0, int t0,
+                                                int stride) {
+    for (int r = t0; r < (S::Y + 2) * (S::Z + 2); r += stride) {
+        const int ly = r % (S::Y + 2) - 1, lz = r / (S::Y + 2) - 1;
+        const int gy = y0 + ly, gz = z0 + lz;
+        const int cy = min(max(gy, 0), V.ny - 1), cz = min(max(gz, 0), V.nz - 1);
+        float* d = phi + ((lz + 1) * S::TY + (ly + 1)) * S::TX + 4;
+        const float* src = phi + ((cz - z0 + 1) * S::TY + (cy - y0 + 1)) * S::TX + 4;
+        const bool row_out = cy != gy || cz != gz;
+#pragma unroll
+        for (int lx = -1; lx <= S::X; ++lx) {
+            const int gx = x0 + lx, cx = min(max(gx, 0), V.nx - 1);
+            if (row_out || cx != gx) d[lx] = src[cx - x0];
+        }
+    }
+}
+
 // Issues the TMA loads of brick b (halo tile of phi[p] and the intensities)
 // into buffer `buf` and records the brick's origin and volume beside them
 // (thread 0 only: the brick's divisions are done once, not by every thread).
@@ -439,18 +468,8 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
     if (!mbar_wait(&sm.bar[buf], (mphase >> buf) & 1u)) set_error(&a.ctl->err, ERR_TMA_TIMEOUT);
     mphase ^= 1u << buf;  // bit b: phase of load barrier b
     float* phi = sm.phi[buf];
-    // Clamp-to-edge halo where the tile leaves the volume (TMA filled zeros).
-    const bool edge = x0 < 4 || y0 < 1 || z0 < 1 || x0 + S::X + 4 > V.nx || y0 + S::Y + 1 > V.ny ||
-                      z0 + S::Z + 1 > V.nz;
-    if (edge) {
-        for (int t = tid; t < S::TILE; t += NT) {
-            const int tx = t % S::TX, ty = (t / S::TX) % S::TY, tz = t / (S::TX * S::TY);
-            const int gx = x0 - 4 + tx, gy = y0 - 1 + ty, gz = z0 - 1 + tz;
-            const int cx = min(max(gx, 0), V.nx - 1), cy = min(max(gy, 0), V.ny - 1),
-                      cz = min(max(gz, 0), V.nz - 1);
-            if (cx != gx || cy != gy || cz != gz)
-                phi[t] = phi[((cz - z0 + 1) * S::TY + (cy - y0 + 1)) * S::TX + (cx - x0 + 4)];
-        }
+    if (tile_at_edge<S>(V, x0, y0, z0)) {
+        clamp_tile_halo<S>(phi, V, x0, y0, z0, tid, NT);
         __syncthreads();
     }
     float* out = sm.out[buf];
@@ -1082,17 +1101,8 @@ __device__ __forceinline__ void ns_warp_brick(const NsArgs& a, WarpSlot<S>& sl, 
     if (!mbar_wait(&sl.bar, phase)) set_error(&a.ctl->err, ERR_TMA_TIMEOUT);
     phase ^= 1u;
     float* phi = sl.phi;
-    // Clamp-to-edge halo where the tile leaves the volume (TMA filled zeros).
-    if (o.x < 4 || o.y < 1 || o.z < 1 || o.x + S::X + 4 > V.nx || o.y + S::Y + 1 > V.ny ||
-        o.z + S::Z + 1 > V.nz) {
-        for (int t = lane; t < S::TILE; t += 32) {
-            const int tx = t % S::TX, ty = (t / S::TX) % S::TY, tz = t / (S::TX * S::TY);
-            const int gx = o.x - 4 + tx, gy = o.y - 1 + ty, gz = o.z - 1 + tz;
-            const int cx = min(max(gx, 0), V.nx - 1), cy = min(max(gy, 0), V.ny - 1),
-                      cz = min(max(gz, 0), V.nz - 1);
-            if (cx != gx || cy != gy || cz != gz)
-                phi[t] = phi[((cz - o.z + 1) * S::TY + (cy - o.y + 1)) * S::TX + (cx - o.x + 4)];
-        }
+    if (tile_at_edge<S>(V, o.x, o.y, o.z)) {
+        clamp_tile_halo<S>(phi, V, o.x, o.y, o.z, lane, 32);
         __syncwarp();
     }
     auto tile_index = [](int j) {
