@@ -494,6 +494,40 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
         const int lx = j % S::X, ly = (j / S::X) % S::Y, lz = j / (S::X * S::Y);
         return bias[((size_t)(z0 + lz) * V.py + (y0 + ly)) * V.px + (x0 + lx)];
     };
+    if constexpr (VPT == 2 && S::VOX == 2 * NT && S::Z % 2 == 0) {
+        // Two voxels a thread, z-adjacent at the same (x, y): updated in one
+        // straight-line block (their chains interleave) when either is
+        // active, the ten tile reads they share loaded once.
+        const int lo = tid % S::XY;
+        const int j0 = lo + 2 * S::XY * (tid / S::XY), j1 = j0 + S::XY;
+        const int t0 = tile_index(j0), t1 = t0 + S::TY * S::TX;
+        const float c0 = phi[t0], c1 = phi[t1];
+        const bool a0 = (act[j0 >> 6] >> (j0 & 63)) & 1ull, a1 = (act[j1 >> 6] >> (j1 & 63)) & 1ull;
+        float nv0 = c0, nv1 = c1;
+        bool ch0 = false, ch1 = false;
+        if (a0 || a1) {
+            auto P0 = [&](int dx, int dy, int dz) { return phi[t0 + (dz * S::TY + dy) * S::TX + dx]; };
+            auto P1 = [&](int dx, int dy, int dz) { return phi[t1 + (dz * S::TY + dy) * S::TX + dx]; };
+            const float u0 = ns_update_f32(P0, sm.img[buf][j0], bias ? bias_at(j0) : 0.0f, V);
+            const float u1 = ns_update_f32(P1, sm.img[buf][j1], bias ? bias_at(j1) : 0.0f, V);
+            if (a0) {
+                nv0 = u0;
+                ch0 = fabsf(nv0 - c0) > V.thr_t;
+            }
+            if (a1) {
+                nv1 = u1;
+                ch1 = fabsf(nv1 - c1) > V.thr_t;
+            }
+        }
+        out[j0] = nv0;
+        out[j1] = nv1;
+        const uint32_t bal0 = __ballot_sync(0xffffffffu, ch0), bal1 = __ballot_sync(0xffffffffu, ch1);
+        anyl = (bal0 | bal1) != 0u;
+        if ((tid & 31) == 0) {
+            sm.chg[buf][j0 >> 5] = bal0;
+            sm.chg[buf][j1 >> 5] = bal1;
+        }
+    } else {
 #pragma unroll
     for (int k = 0; k < VPT; ++k) {
         const int j = tid + k * NT;
@@ -513,6 +547,7 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
         anyl |= bal != 0u;
         const int word = (tid >> 5) + k * (NT / 32);
         if ((tid & 31) == 0 && word < S::CHG) sm.chg[buf][word] = bal;
+    }
     }
     fence_proxy_async_smem();
     // The previous brick's store (from out[buf ^ 1], overwritten by the next
