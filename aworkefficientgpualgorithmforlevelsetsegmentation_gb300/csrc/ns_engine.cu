@@ -374,6 +374,8 @@ NsVol NsCore::descriptor(int i) const {
     o.nx = v.nx; o.ny = v.ny; o.nz = v.nz;
     o.px = v.px; o.py = v.py; o.pz = v.pz;
     o.nbx = v.nbx; o.nby = v.nby; o.nbz = v.nbz;
+    o.mnbx = 0xFFFFFFFFu / (uint32_t)v.nbx + 1u;
+    o.mnbxy = 0xFFFFFFFFu / ((uint32_t)v.nbx * (uint32_t)v.nby) + 1u;
     o.brick_base = v.brick_base;
     o.phi[0] = v.phi[0]; o.phi[1] = v.phi[1];
     o.img = v.img;

@@ -55,7 +55,7 @@ struct NsVol {
     uint32_t tmap_base;     // 5 maps: phi0 halo-load, phi1 halo-load, phi0 store, phi1 store, img
     float inv_eps;          // 1 / eps
     float wc, wd;           // curvature and data weights (from alpha and alpha_data)
-    int32_t pad[2];
+    uint32_t mnbx, mnbxy;   // 0xFFFFFFFF / nbx + 1 and / (nbx * nby) + 1 (div_magic)
 };
 
 struct NsVolState {
@@ -352,12 +352,26 @@ __host__ __device__ __forceinline__ uint64_t inside_mask(int w, int lx, int ly, 
     return mx & my & mz;
 }
 
+// x / g for x < 2^31, given gm = 0xFFFFFFFF / g + 1: the high half of x * gm
+// overshoots x / g by less than one and is corrected once (g = 1: gm wraps).
+__host__ __device__ __forceinline__ uint32_t div_magic(uint32_t x, uint32_t g, uint32_t gm) {
+    if (g == 1u) return x;
+#ifdef __CUDA_ARCH__
+    const uint32_t d = __umulhi(x, gm);
+#else
+    const uint32_t d = (uint32_t)(((uint64_t)x * gm) >> 32);
+#endif
+    return d * g > x ? d - 1u : d;
+}
+
 // Brick origin of global brick b.
 template <class S>
 __device__ __forceinline__ int3 brick_origin(const NsVol& V, uint32_t b) {
     const uint32_t lb = b - V.brick_base;
-    const int kx = lb % V.nbx, ky = (lb / V.nbx) % V.nby, kz = lb / (V.nbx * V.nby);
-    return make_int3(kx * S::X, ky * S::Y, kz * S::Z);
+    const uint32_t nbx = (uint32_t)V.nbx, nbxy = nbx * (uint32_t)V.nby;
+    const uint32_t kz = div_magic(lb, nbxy, V.mnbxy), r = lb - kz * nbxy;
+    const uint32_t ky = div_magic(r, nbx, V.mnbx), kx = r - ky * nbx;
+    return make_int3((int)kx * S::X, (int)ky * S::Y, (int)kz * S::Z);
 }
 
 // A brick tile (origin x0, y0, z0 at tile column 4, row 1, plane 1) whose
@@ -677,18 +691,6 @@ __device__ __forceinline__ StopState stop_state(int32_t* base, int nvol) {
 }
 
 constexpr uint32_t kNoBrick = 0xFFFFFFFFu;  // a brick of a finished volume
-
-// x / g for x < 2^31, given gm = 0xFFFFFFFF / g + 1: the high half of x * gm
-// overshoots x / g by less than one and is corrected once (g = 1: gm wraps).
-__host__ __device__ __forceinline__ uint32_t div_magic(uint32_t x, uint32_t g, uint32_t gm) {
-    if (g == 1u) return x;
-#ifdef __CUDA_ARCH__
-    const uint32_t d = __umulhi(x, gm);
-#else
-    const uint32_t d = (uint32_t)(((uint64_t)x * gm) >> 32);
-#endif
-    return d * g > x ? d - 1u : d;
-}
 
 // Position of the s-th set bit (from 0, counted from bit 0) of m; s < popc(m).
 __host__ __device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t s) {
