@@ -209,6 +209,10 @@ __device__ __forceinline__ float ns_update_f32(PF P, float I, float bias, const 
 template <class S, int NT>
 struct NsSmem {
     static_assert((S::TILE_PAD * 4) % 128 == 0 && (S::VOX * 4) % 128 == 0, "TMA smem alignment");
+    // The thread that issues, commits and awaits the brick stores and keeps
+    // the tally: lane 0 of the last warp, which has no xy-plane dilation work
+    // (9 x WORDS <= NT - 32), so the store issue delays no barrier.
+    static constexpr int STORE_TID = NT - 32;
     alignas(128) float phi[2][S::TILE_PAD];  // halo tiles, double buffered
     alignas(128) float img[2][S::VOX];
     alignas(128) float out[2][S::VOX];
@@ -495,12 +499,13 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
         const int lx = j % S::X, ly = (j / S::X) % S::Y, lz = j / (S::X * S::Y);
         return ((lz + 1) * S::TY + (ly + 1)) * S::TX + (lx + 4);
     };
-    // Warp 1: the brick's active voxels (one mask word a lane), read before
-    // the block barrier; its lane 0 tallies them while thread 0 issues the
-    // store.
-    static_assert(NT >= 64 && S::WORDS <= 32, "tally warp");
+    // The store thread's warp: the brick's active voxels (one mask word a
+    // lane), read before the block barrier and tallied after it.
+    constexpr int STORE_TID = NsSmem<S, NT>::STORE_TID;
+    static_assert(NT >= 64 && S::WORDS <= 32 && (S::XY != 64 || 9 * S::WORDS <= STORE_TID), "store warp");
     uint32_t nact = 0;
-    if ((tid >> 5) == 1) nact = __reduce_add_sync(0xffffffffu, (tid & 31) < S::WORDS ? __popcll(act[tid & 31]) : 0u);
+    if ((tid >> 5) == (STORE_TID >> 5))
+        nact = __reduce_add_sync(0xffffffffu, (tid & 31) < S::WORDS ? __popcll(act[tid & 31]) : 0u);
     constexpr int VPT = (S::VOX + NT - 1) / NT;
     const float* bias = V.bias;
     bool anyl = false;
@@ -566,15 +571,14 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
     fence_proxy_async_smem();
     // The previous brick's store (from out[buf ^ 1], overwritten by the next
     // brick after this barrier) has read its source.
-    if (tid == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+    if (tid == STORE_TID) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
     // The one block barrier of a brick: out[] and chg[buf] complete; after it
     // nothing reads phi[buf], img[buf] or act[buf] of this brick, so the next
     // loads into this buffer may be issued while the dilation below runs.
     const int any = __syncthreads_or(anyl ? 1 : 0);
-    if (tid == 0) {
+    if (tid == STORE_TID) {
         tma_store_3d(&a.tmaps[V.tmap_base + 2 + (p ^ 1u)], x0, y0, z0, out);
         tma_store_commit();
-    } else if (tid == 32) {
         tally.add(a.vstate, cnt, v, nact);
     }
     // Dilation of the changed mask into the 27 bricks around (and including)
@@ -1032,7 +1036,7 @@ __device__ __forceinline__ void ns_drive(const NsArgs& a, IterShared<NT>& sh, St
 template <class S, int NT>
 struct BlockProc {
     NsSmem<S, NT>& sm;
-    BlockTally& tally;  // thread 32; in shared memory, off the threads' registers
+    BlockTally& tally;  // the store thread's; in shared memory, off the threads' registers
     uint32_t mphase;    // bit b: phase of load barrier b
     int buf;
     __device__ BlockProc(NsSmem<S, NT>& s, BlockTally& t) : sm(s), tally(t), mphase(0u), buf(0) {}
@@ -1069,7 +1073,7 @@ struct BlockProc {
         __syncthreads();
     }
     __device__ void finish(const NsArgs& a, IterShared<NT>& sh, unsigned long long* cnt) {
-        if (threadIdx.x == 0) {
+        if (threadIdx.x == NsSmem<S, NT>::STORE_TID) {
             sh.upd = tally.iter;
             tally.flush(a.vstate, cnt);
             tally.reset();
