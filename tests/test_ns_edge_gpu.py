@@ -125,6 +125,26 @@ def test_full_size_configs_agree_and_split_runs_agree(full):
             assert np.array_equal(act, ref_act), (brick, threads)
 
 
+def test_full_size_six_neighbourhood_configs_agree(full):
+    """The 6-neighbour rule at full size, where blocks take several bricks an
+    iteration: the deferred plane dilation (8^3 and 8x8x4 bricks) and the
+    direct per-word dilation of 4^3 bricks give the same field and list."""
+    p = full["params"]
+    ref_phi = ref_act = None
+    for brick, threads in [((4, 4, 4), 64), ((8, 8, 8), 256), ((8, 8, 4), 128), ((8, 8, 8), 32)]:
+        s = lss.Segmenter(lss.MODE_NS, brick=brick, threads_per_brick=threads)
+        s.load_volume(full["image"])
+        s.set_parameters(p.target, p.window, p.curvature, p.time_step, alpha_role=p.alpha_role, neighbourhood=6)
+        s.set_seed_spheres(full["spheres"])
+        s.step(150)
+        phi, act = s.read_phi(), np.sort(s.active_linear())
+        if ref_phi is None:
+            ref_phi, ref_act = phi, act
+        else:
+            assert np.array_equal(phi, ref_phi), (brick, threads)
+            assert np.array_equal(act, ref_act), (brick, threads)
+
+
 def test_full_size_run_invariants(full):
     p = full["params"]
     s = seg(full["image"], p)
