@@ -130,7 +130,7 @@ def sum_over_ranks(ws, value: float) -> float:
 # workload, from the ncu capture summarised in
 # profiles/k_ns_persistent_config2_256.md (dram__bytes_read.sum +
 # dram__bytes_write.sum, one convergence = one launch).
-DRAM_TRAFFIC = {("config2_256", 8, 8, 8, 256): 15817472}
+DRAM_TRAFFIC = {("config2_256", 8, 8, 8, 256): 15938048}
 
 
 def dram_traffic(st, name):
