@@ -409,7 +409,8 @@ __device__ __forceinline__ void clamp_tile_halo(float* phi, const NsVol& V, int 
 
 // Issues the TMA loads of brick b (halo tile of phi[p] and the intensities)
 // into buffer `buf` and records the brick's origin and volume beside them
-// (thread 0 only: the brick's divisions are done once, not by every thread).
+// (thread 0 only: the brick's index arithmetic is done once, not by every
+// thread).
 template <class S, int NT>
 __device__ __forceinline__ void ns_issue_loads(const NsArgs& a, NsSmem<S, NT>& sm, uint32_t b,
                                                uint32_t p, int buf, const NsVol* vone) {
@@ -485,8 +486,8 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
     const int x0 = og.x, y0 = og.y, z0 = og.z;
     const unsigned long long* act = sm.act[buf];
     // Every thread waits for the loads itself.  out[buf] is free: the store
-    // issued from it two bricks ago was waited for (read) by thread 0 before
-    // the previous brick's block barrier.
+    // issued from it two bricks ago was waited for (read) by the store thread
+    // before the previous brick's block barrier.
     if (!mbar_wait(&sm.bar[buf], (mphase >> buf) & 1u)) set_error(&a.ctl->err, ERR_TMA_TIMEOUT);
     mphase ^= 1u << buf;  // bit b: phase of load barrier b
     float* phi = sm.phi[buf];
