@@ -176,10 +176,21 @@ class NsEngine : public EngineBase {
     void load_volume(const void* data, int nx, int ny, int nz, int dtype, float aniso) override {
         LSS_REQUIRE(data && nx > 0 && ny > 0 && nz > 0, LSS_ERR_INVALID_ARGUMENT, "bad volume");
         (void)aniso;
+        const uint64_t n = (uint64_t)nx * ny * nz;
+        std::vector<float> f;
+        if (dtype != LSS_F32) f = to_float(data, n, dtype);
+        const float* fp = dtype == LSS_F32 ? (const float*)data : f.data();
+        if (core_ && core_->configured() && nx == nx_ && ny == ny_ && nz == nz_) {
+            // Same shape: the device buffers, tensor maps and brick
+            // configuration stay; only the intensities and the state change.
+            core_->reload_volume(0, fp, params);
+            pending_reinit_ = false;
+            Tp_ = params.target; Wp_ = params.window; Ap_ = params.curvature;
+            return;
+        }
         unload_volume();
-        std::vector<float> f = to_float(data, (uint64_t)nx * ny * nz, dtype);
         core_.reset(new NsCore(this, cfg.hbm_budget_bytes));
-        core_->add_volume(f.data(), nx, ny, nz, params);
+        core_->add_volume(fp, nx, ny, nz, params);
         BrickConfig c = brick_configs()[0];
         tuned_ = cfg.brick_x > 0;
         if (cfg.brick_x > 0) c = BrickConfig{cfg.brick_x, cfg.brick_y, cfg.brick_z,
@@ -188,7 +199,6 @@ class NsEngine : public EngineBase {
             tuned_ = cached_choice(*core_, &c);
         core_->configure(c);
         nx_ = nx; ny_ = ny; nz_ = nz;
-        frozen_.assign((size_t)nx * ny * nz, 0);
         pending_reinit_ = false;
         Tp_ = params.target; Wp_ = params.window; Ap_ = params.curvature;
     }
@@ -303,9 +313,7 @@ class NsEngine : public EngineBase {
 
     void read_mask(uint8_t* out) override {
         require();
-        std::vector<float> phi((size_t)nx_ * ny_ * nz_);
-        core_->read_phi(0, phi.data());
-        for (size_t i = 0; i < phi.size(); ++i) out[i] = (phi[i] <= 0.0f || frozen_[i]) ? 1 : 0;
+        core_->read_mask(0, out);
     }
 
     void read_export(int8_t* out) override {
@@ -330,9 +338,7 @@ class NsEngine : public EngineBase {
 
     void freeze() override {
         require();
-        std::vector<uint8_t> m((size_t)nx_ * ny_ * nz_);
-        read_mask(m.data());
-        frozen_ = m;
+        core_->freeze(0);
     }
 
     void clear_current() override {
@@ -344,7 +350,7 @@ class NsEngine : public EngineBase {
 
     void clear_all() override {
         clear_current();
-        std::fill(frozen_.begin(), frozen_.end(), 0);
+        core_->clear_frozen(0);
     }
 
     void estimate_params(float* t, float* w) override {
@@ -388,7 +394,7 @@ class NsEngine : public EngineBase {
 
     std::unique_ptr<NsCore> core_;
     int nx_ = 0, ny_ = 0, nz_ = 0;
-    std::vector<uint8_t> frozen_;
+
     bool pending_reinit_ = false, tuned_ = false;
     float Tp_ = 0, Wp_ = 0, Ap_ = 0;
     double last_ms_ = 0;
@@ -459,12 +465,7 @@ class BatchEngine : public EngineBase {
 
     void read_phi_v(int v, float* out) { core_.read_phi(v, out); }
 
-    void read_mask_v(int v, uint8_t* out) {
-        const auto& V = core_.vols().at(v);
-        std::vector<float> phi((size_t)V.nx * V.ny * V.nz);
-        core_.read_phi(v, phi.data());
-        for (size_t i = 0; i < phi.size(); ++i) out[i] = phi[i] <= 0.0f ? 1 : 0;
-    }
+    void read_mask_v(int v, uint8_t* out) { core_.read_mask(v, out); }
 
     void stats_v(int v, lss_stats* s) {
         std::memset(s, 0, sizeof(*s));

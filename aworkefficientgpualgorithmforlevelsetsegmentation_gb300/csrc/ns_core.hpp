@@ -34,6 +34,9 @@ class NsCore {
     ~NsCore();
 
     int add_volume(const float* data, int nx, int ny, int nz, const lss_params& p);
+    // New intensities for volume v (same dimensions): the state after
+    // add_volume + configure, the buffers and the configuration kept.
+    void reload_volume(int v, const float* data, const lss_params& p);
     void set_params(int v, const lss_params& p) { vols_.at(v).p = p; upload_descriptors(); }
     void set_bias(int v, const float* bias);
     void configure(const BrickConfig& c);
@@ -44,6 +47,10 @@ class NsCore {
     int run(int max_iters, const lss_conv* conv, float* ms);
     float dense_run(int iters);
     void read_phi(int v, float* out);
+    // mask = phi <= 0, or'ed with the frozen mask; made on the device.
+    void read_mask(int v, uint8_t* out);
+    void freeze(int v);        // frozen |= (phi <= 0)
+    void clear_frozen(int v);
     uint64_t read_active(int v, uint64_t* out, uint64_t cap);
     void estimate(int v, float* t, float* w);
     void state(int v, NsVolState* out);
@@ -76,7 +83,7 @@ class NsCore {
         float* bias = nullptr;
         float* bias_buf = nullptr;
         lss_params p{};
-        std::vector<uint8_t> frozen;
+        uint8_t* frozen = nullptr;  // unpadded u8 mask of frozen segmentations (device), once frozen
         unsigned long long iterations = 0;
         // phi equal in both buffers and uniform outside the voxel box
         // [dirty_lo, dirty_hi) (after a fill, grown by seeding).

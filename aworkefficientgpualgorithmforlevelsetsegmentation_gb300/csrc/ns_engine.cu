@@ -64,6 +64,19 @@ __global__ void k_ns_gather(float* dst, const float* src, int nx, int ny, int nz
     }
 }
 
+// dst[i] = phi <= 0 at unpadded voxel i, or'ed with frozen[i] (may be null;
+// dst may be frozen itself).
+__global__ void k_ns_mask(uint8_t* dst, const float* src, const uint8_t* frozen, int nx, int ny, int nz, int px,
+                          int py) {
+    const uint64_t n = (uint64_t)nx * ny * nz;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t x = i % nx, y = (i / nx) % ny, z = i / ((uint64_t)nx * ny);
+        const bool in = src[(z * py + y) * px + x] <= 0.0f || (frozen && frozen[i]);
+        dst[i] = in ? 1 : 0;
+    }
+}
+
 __global__ void k_ns_fill(float* p, uint64_t n, float v) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x)
@@ -271,7 +284,6 @@ int NsCore::add_volume(const float* data, int nx, int ny, int nz, const lss_para
     LSS_CUDA(cudaGetLastError());
     owner_->sync();
     arena_.free_last(tmp);
-    v.frozen.assign((size_t)nx * ny * nz, 0);
     vols_.push_back(v);
     configured_ = false;
     return (int)vols_.size() - 1;
@@ -608,6 +620,71 @@ uint32_t NsCore::vol_parity(int v) {
     NsVolState s;
     state(v, &s);
     return (uint32_t)s.parity;
+}
+
+void NsCore::reload_volume(int v, const float* data, const lss_params& p) {
+    LSS_REQUIRE(configured_, LSS_ERR_STATE, "not configured");
+    VolHost& V = vols_.at(v);
+    cudaStream_t st = owner_->stream;
+    const uint64_t n = (uint64_t)V.nx * V.ny * V.nz, P = (uint64_t)V.px * V.py * V.pz;
+    float* tmp = (float*)arena_.alloc(n * 4);
+    LSS_CUDA(cudaMemcpyAsync(tmp, data, n * 4, cudaMemcpyHostToDevice, st));
+    k_ns_scatter<<<owner_->num_sms * 4, 256, 0, st>>>(V.img, tmp, V.nx, V.ny, V.nz, V.px, V.py);
+    ++owner_->launches;
+    for (int q = 0; q < 2; ++q) {
+        k_ns_fill<<<owner_->num_sms * 4, 256, 0, st>>>(V.phi[q], P, p.phi_max);
+        ++owner_->launches;
+    }
+    V.p = p;
+    V.bias = nullptr;  // a bias belongs to the previous volume
+    V.uniform = true;
+    V.dirty_lo = V.dirty_hi = make_int3(0, 0, 0);
+    V.iterations = 0;
+    if (V.frozen) LSS_CUDA(cudaMemsetAsync(V.frozen, 0, n, st));
+    LSS_CUDA(cudaMemsetAsync(d_vstate_, 0, sizeof(NsVolState) * vols_.size(), st));
+    LSS_CUDA(cudaMemsetAsync(d_ctl_, 0, sizeof(NsCtl), st));
+    ctl_arrivals_ = ctl_upd_sum_[0] = ctl_upd_sum_[1] = 0;
+    parity_ = 0;
+    k_total_ = 0;
+    initialized_ = false;
+    upload_descriptors();
+    LSS_CUDA(cudaGetLastError());
+    owner_->sync();
+    arena_.free_last(tmp);
+}
+
+void NsCore::read_mask(int v, uint8_t* out) {
+    VolHost& V = vols_.at(v);
+    const uint32_t p = vols_.size() == 1 ? parity_ : vol_parity(v);
+    const uint64_t n = (uint64_t)V.nx * V.ny * V.nz;
+    uint8_t* tmp = (uint8_t*)arena_.alloc(n);
+    k_ns_mask<<<owner_->num_sms * 4, 256, 0, owner_->stream>>>(tmp, V.phi[p], V.frozen, V.nx, V.ny, V.nz, V.px,
+                                                              V.py);
+    ++owner_->launches;
+    LSS_CUDA(cudaMemcpyAsync(out, tmp, n, cudaMemcpyDeviceToHost, owner_->stream));
+    owner_->sync();
+    arena_.free_last(tmp);
+}
+
+void NsCore::freeze(int v) {
+    VolHost& V = vols_.at(v);
+    const uint32_t p = vols_.size() == 1 ? parity_ : vol_parity(v);
+    const uint64_t n = (uint64_t)V.nx * V.ny * V.nz;
+    if (!V.frozen) {
+        V.frozen = (uint8_t*)arena_.alloc(n);
+        LSS_CUDA(cudaMemsetAsync(V.frozen, 0, n, owner_->stream));
+    }
+    k_ns_mask<<<owner_->num_sms * 4, 256, 0, owner_->stream>>>(V.frozen, V.phi[p], V.frozen, V.nx, V.ny, V.nz,
+                                                              V.px, V.py);
+    ++owner_->launches;
+    LSS_CUDA(cudaGetLastError());
+    owner_->sync();
+}
+
+void NsCore::clear_frozen(int v) {
+    VolHost& V = vols_.at(v);
+    if (V.frozen) LSS_CUDA(cudaMemsetAsync(V.frozen, 0, (uint64_t)V.nx * V.ny * V.nz, owner_->stream));
+    owner_->sync();
 }
 
 void NsCore::read_phi(int v, float* out) {

@@ -275,3 +275,52 @@ def test_dense_pass_equals_all_active_sparse(shape):
     a.step(7)
     b.step_dense(7)
     assert np.array_equal(a.read_phi(), b.read_phi())
+
+
+def test_ns_reload_same_shape_equals_fresh_engine():
+    """Loading a new volume of the same shape reuses the engine's buffers;
+    the state afterwards is that of a fresh engine: same field, list, mask and
+    statistics after seeding and running."""
+    a_cfg, b_cfg = P.config1(0.25), P.config2(0.125)
+    assert a_cfg["image"].shape == b_cfg["image"].shape
+    p = b_cfg["params"]
+    s = make_gpu(a_cfg)
+    s.step(7)
+    s.freeze_current_segmentation()
+    s.load_volume(b_cfg["image"])  # same shape: the reload path
+    s.set_parameters(p.target, p.window, p.curvature, p.time_step, alpha_role=p.alpha_role)
+    fresh = lss.Segmenter(lss.MODE_NS, brick=(8, 8, 8), threads_per_brick=256)
+    fresh.load_volume(b_cfg["image"])
+    fresh.set_parameters(p.target, p.window, p.curvature, p.time_step, alpha_role=p.alpha_role)
+    for e in (s, fresh):
+        assert e.get_active_element_count() == 0
+        assert np.all(e.get_saveable_segmentation() == 0)
+        e.set_seed_spheres(b_cfg["spheres"])
+        e.step_until_converged(1e-3, 5, 500)
+    assert np.array_equal(s.read_phi(), fresh.read_phi())
+    assert np.array_equal(s.active_linear(), fresh.active_linear())
+    assert np.array_equal(s.get_saveable_segmentation(), fresh.get_saveable_segmentation())
+    assert s.stats()["iterations"] == fresh.stats()["iterations"]
+    assert s.stats()["voxel_updates"] == fresh.stats()["voxel_updates"]
+
+
+def test_ns_freeze_and_clear_on_device():
+    """Frozen segmentations stay in the mask after the current one is cleared
+    and reseeded elsewhere; clearing all removes them."""
+    cfg = P.config1(0.25)
+    s = make_gpu(cfg)
+    s.step(20)
+    m1 = s.get_saveable_segmentation().astype(bool)
+    assert m1.any()
+    assert np.array_equal(m1, s.read_phi() <= 0)
+    s.freeze_current_segmentation()
+    s.clear_current_segmentation()
+    assert np.array_equal(s.get_saveable_segmentation().astype(bool), m1)
+    nz, ny, nx = cfg["image"].shape
+    s.set_seed_spheres([(2, 2, 2, 1.5)])
+    s.step(3)
+    m2 = s.get_saveable_segmentation().astype(bool)
+    assert np.array_equal(m2, m1 | (s.read_phi() <= 0))
+    s.freeze_current_segmentation()
+    s.clear_all_segmentations()
+    assert not s.get_saveable_segmentation().any()
