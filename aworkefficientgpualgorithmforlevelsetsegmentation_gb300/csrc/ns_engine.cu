@@ -113,18 +113,18 @@ __global__ void k_ns_sphere_union(float* phi, int nx, int ny, int nz, int px, in
 
 // Dense all-voxel update with the same arithmetic as the sparse engine: the
 // unconditional update the paper compares against (main.tex:523).  A block
-// covers a 32 x 8 column of the volume over kDenseZ planes and marches in z
+// covers a 32 x 8 column of the volume over zc planes and marches in z
 // with three planes of phi (each with a one-voxel halo, clamped to the
 // volume's edge) in a shared-memory ring, so every phi value is read from
 // memory about once and every neighbour from shared memory.  The descriptor
 // is a kernel parameter: its scalars are constant-bank operands.
-constexpr int kDenseX = 32, kDenseY = 8, kDenseZ = 32;
+constexpr int kDenseX = 32, kDenseY = 8, kDenseZMax = 32;
 constexpr int kDensePlane = (kDenseX + 2) * (kDenseY + 2);
 
-__global__ void __launch_bounds__(256) k_ns_dense(const NsVol V, uint32_t p) {
+__global__ void __launch_bounds__(256) k_ns_dense(const NsVol V, uint32_t p, int zc) {
     __shared__ float ring[3][kDensePlane];
     const int tx = threadIdx.x % kDenseX, ty = threadIdx.x / kDenseX;
-    const int x0 = blockIdx.x * kDenseX, y0 = blockIdx.y * kDenseY, zb = blockIdx.z * kDenseZ;
+    const int x0 = blockIdx.x * kDenseX, y0 = blockIdx.y * kDenseY, zb = blockIdx.z * zc;
     const float* __restrict__ src = p ? V.phi[1] : V.phi[0];
     float* __restrict__ dst = p ? V.phi[0] : V.phi[1];
     const size_t pxy = (size_t)V.px * V.py;
@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(256) k_ns_dense(const NsVol V, uint32_t p) {
     const int x = x0 + tx, y = y0 + ty;
     const bool inside = x < V.nx && y < V.ny;
     const int c0 = (ty + 1) * (kDenseX + 2) + tx + 1;
-    const int zend = min(zb + kDenseZ, V.nz);
+    const int zend = min(zb + zc, V.nz);
     size_t k = (size_t)zb * pxy + (size_t)y * V.px + x;
     for (int z = zb; z < zend; ++z, k += pxy) {
         load_plane(pp, z + 1);  // into the ring slot freed by the barrier below
@@ -764,9 +764,13 @@ float NsCore::dense_run(int iters) {
     for (int it = 0; it < iters; ++it) {
         for (int v = 0; v < (int)vols_.size(); ++v) {
             const VolHost& V = vols_[v];
-            dim3 grid((V.nx + kDenseX - 1) / kDenseX, (V.ny + kDenseY - 1) / kDenseY,
-                      (V.nz + kDenseZ - 1) / kDenseZ);
-            k_ns_dense<<<grid, 256, 0, st>>>(descriptor(v), parity_);
+            // Planes per block: up to kDenseZMax, fewer when the volume is
+            // small, so that the grid still has about four blocks per SM.
+            const int gx = (V.nx + kDenseX - 1) / kDenseX, gy = (V.ny + kDenseY - 1) / kDenseY;
+            const int chunks = std::max(1, (4 * owner_->num_sms + gx * gy - 1) / (gx * gy));
+            const int zc = std::max(2, std::min(kDenseZMax, (V.nz + chunks - 1) / chunks));
+            dim3 grid(gx, gy, (V.nz + zc - 1) / zc);
+            k_ns_dense<<<grid, 256, 0, st>>>(descriptor(v), parity_, zc);
             ++owner_->launches;
         }
         parity_ ^= 1u;

@@ -499,6 +499,8 @@ def run_tour(args, ws, rank, local):
     s.step(20)
     s.active_linear()
     s.read_phi()
+    s.freeze_current_segmentation()
+    s.get_saveable_segmentation()
     s.step_dense(2)
     c4 = P.config4(0.25)
     a = lss.Segmenter(lss.MODE_NS, brick=(8, 8, 8), threads_per_brick=256)
