@@ -708,7 +708,8 @@ uint64_t NsCore::read_active(int v, uint64_t* out, uint64_t cap) {
     const uint32_t s = k_total_ % 4u;
     unsigned long long* total = (unsigned long long*)d_misc_;
     auto emit = [&](uint64_t* dout) {
-        LSS_CUDA(cudaMemsetAsync(d_status_, 0, ((uint64_t)NW_ / ks.block + 2) * 8, st));
+        // one status word per tile of block / 32 membership words
+        LSS_CUDA(cudaMemsetAsync(d_status_, 0, ((uint64_t)NW_ / (ks.block / 32) + 2) * 8, st));
         LSS_CUDA(cudaMemsetAsync(d_misc_, 0, 16, st));
         LSS_CUDA(cudaMemsetAsync(&d_ctl_->emit_tile, 0, 4, st));
         NsArgs a = args(k_total_, 0, nullptr);

@@ -1386,52 +1386,83 @@ __global__ void __launch_bounds__(NT) k_ns_init_active(NsArgs a, uint32_t p, uin
     flush();
 }
 
-// The active voxels of the current set in brick-major order: a single-pass
-// decoupled-lookback compaction over the membership bits of slot s (tiles of
-// NT bit words = 32*NT bricks); per brick the voxel count is popc of its
-// mask.  Writes volume-local linear indices (x + nx*(y + ny*z)) and, from the
-// last tile, the total count.
+// The active voxels of A_k (membership slot s, masks of parity p) as one
+// brick-major list: tiles of NT/32 membership words (a warp each) are placed
+// by a single-pass decoupled lookback over their voxel counts; inside a word
+// the warp emits brick after brick, its lanes splitting each brick's voxels
+// (VOX/32 a lane) and placing them by a warp prefix sum.  Writes
+// volume-local linear indices (x + nx*(y + ny*z)) when `out` is set and,
+// from the last tile, the total count.
 template <int BX, int BY, int BZ, int NT>
 __global__ void __launch_bounds__(NT) k_ns_emit(NsArgs a, uint32_t p, uint32_t s, uint64_t* out,
                                                unsigned long long* total_out) {
     using S = Brick<BX, BY, BZ>;
+    constexpr int NWARP = NT / 32;
+    constexpr int VPL = S::VOX / 32;  // voxels of a brick a lane
+    static_assert(VPL >= 1 && VPL <= 32 && 64 % VPL == 0, "voxels a lane");
     __shared__ uint32_t s_tile;
-    const uint32_t ntiles = (a.NW + NT - 1) / NT;
+    __shared__ unsigned long long s_warp[NWARP];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t ntiles = (a.NW + NWARP - 1) / NWARP;
     for (;;) {
         if (threadIdx.x == 0) s_tile = atomicAdd(&a.ctl->emit_tile, 1u);
         __syncthreads();
         const uint32_t tile = s_tile;
         __syncthreads();
         if (tile >= ntiles) break;
-        const uint32_t w = tile * NT + threadIdx.x;
+        const uint32_t w = tile * NWARP + warp;
         const uint32_t bw = w < a.NW ? a.bits[s][w] : 0u;
-        unsigned long long cnt = 0;
-        for (uint32_t m = bw; m; m &= m - 1) {
-            const uint32_t b = w * 32 + (__ffs(m) - 1);
-            for (int q = 0; q < S::WORDS; ++q) cnt += __popcll(a.masks[p][(size_t)b * S::WORDS + q]);
+        // Lane l: the voxel count of brick 32 w + l (if in A_k).
+        uint32_t bc = 0;
+        if ((bw >> lane) & 1u) {
+            const uint32_t b = w * 32u + (uint32_t)lane;
+#pragma unroll
+            for (int q = 0; q < S::WORDS; ++q) bc += (uint32_t)__popcll(a.masks[p][(size_t)b * S::WORDS + q]);
         }
-        uint64_t total;
-        const uint64_t excl = block_exclusive_sum64(cnt, &total);
-        const uint64_t prefix = tile_exclusive_prefix(a.status, tile, total, &a.ctl->err);
-        uint64_t o = prefix + excl;
-        for (uint32_t m = bw; m; m &= m - 1) {
-            const uint32_t b = w * 32 + (__ffs(m) - 1);
-            const NsVol& V = a.vols[a.brick_vol[b]];
-            const int3 og = brick_origin<S>(V, b);
-            for (int q = 0; q < S::WORDS; ++q) {
-                unsigned long long mm = a.masks[p][(size_t)b * S::WORDS + q];
-                while (mm) {
-                    const int bit = __ffsll(mm) - 1;
-                    mm &= mm - 1;
-                    const int j = q * 64 + bit;
-                    const uint64_t x = og.x + j % S::X, y = og.y + (j / S::X) % S::Y,
-                                   z = og.z + j / (S::X * S::Y);
-                    if (out) out[o] = (z * V.ny + y) * V.nx + x;
-                    ++o;
+        uint32_t inc = bc;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        if (lane == 31) s_warp[warp] = inc;
+        __syncthreads();
+        unsigned long long woff = 0, ttot = 0;
+#pragma unroll
+        for (int i = 0; i < NWARP; ++i) {
+            const unsigned long long x = s_warp[i];
+            if (i < warp) woff += x;
+            ttot += x;
+        }
+        const uint64_t prefix = tile_exclusive_prefix(a.status, tile, ttot, &a.ctl->err);
+        if (out) {
+            const uint64_t base = prefix + woff;
+            for (uint32_t m = bw; m; m &= m - 1u) {
+                const int bl = __ffs(m) - 1;
+                const uint32_t b = w * 32u + (uint32_t)bl;
+                const uint64_t bstart = base + __shfl_sync(0xffffffffu, inc - bc, bl);
+                const int j0 = lane * VPL;
+                const unsigned long long word = a.masks[p][(size_t)b * S::WORDS + j0 / 64];
+                const uint32_t chunk =
+                    (uint32_t)((word >> (j0 % 64)) & (VPL == 32 ? 0xFFFFFFFFull : ((1ull << VPL) - 1ull)));
+                const uint32_t cc = (uint32_t)__popc(chunk);
+                uint32_t ci = cc;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xffffffffu, ci, o);
+                    if (lane >= o) ci += y;
+                }
+                const NsVol& V = a.vols[a.brick_vol[b]];
+                const int3 og = brick_origin<S>(V, b);
+                uint64_t o = bstart + (ci - cc);
+                for (uint32_t cm = chunk; cm; cm &= cm - 1u) {
+                    const int j = j0 + __ffs(cm) - 1;
+                    const uint64_t x = og.x + j % S::X, y = og.y + (j / S::X) % S::Y, z = og.z + j / (S::X * S::Y);
+                    out[o++] = (z * V.ny + y) * V.nx + x;
                 }
             }
         }
-        if (tile == ntiles - 1 && threadIdx.x == 0) *total_out = prefix + total;
+        if (tile == ntiles - 1 && threadIdx.x == 0) *total_out = prefix + ttot;
     }
 }
 
