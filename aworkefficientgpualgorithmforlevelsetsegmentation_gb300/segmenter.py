@@ -39,6 +39,17 @@ def _ptr(a: np.ndarray) -> C.c_void_p:
     return C.c_void_p(a.ctypes.data)
 
 
+def _out(out, shape, dtype) -> np.ndarray:
+    """A new zeroed array, or the caller's `out` (e.g. a view of pinned host
+    memory reused across calls) after checking its shape, dtype and layout."""
+    if out is None:
+        return np.zeros(shape, dtype)
+    if out.shape != tuple(shape) or out.dtype != np.dtype(dtype) or not out.flags.c_contiguous \
+            or not out.flags.writeable:
+        raise ValueError(f"out must be a writeable C-contiguous {np.dtype(dtype)} array of shape {tuple(shape)}")
+    return out
+
+
 def config(mode: int = MODE_NS, device: int = 0, brick=(0, 0, 0), threads_per_brick: int = 0,
            quirk_i3: bool = True, use_graph: bool = True, hbm_budget_bytes: int = 0) -> L.lss_config:
     c = L.lss_config()
@@ -187,13 +198,13 @@ class Segmenter:
         nz, ny, nx = self.shape
         return xyz[:, 0] + nx * (xyz[:, 1] + ny * xyz[:, 2])
 
-    def read_phi(self) -> np.ndarray:
-        out = np.zeros(self.shape, np.float32)
+    def read_phi(self, out=None) -> np.ndarray:
+        out = _out(out, self.shape, np.float32)
         self._chk(self._lib.lss_read_phi(self._h, _ptr(out)))
         return out
 
-    def get_saveable_segmentation(self) -> np.ndarray:
-        out = np.zeros(self.shape, np.uint8)
+    def get_saveable_segmentation(self, out=None) -> np.ndarray:
+        out = _out(out, self.shape, np.uint8)
         self._chk(self._lib.lss_read_mask(self._h, _ptr(out)))
         return out
 
@@ -285,13 +296,13 @@ class Batch:
         self._chk(self._lib.lss_batch_run(self._h, C.byref(c), C.byref(it)))
         return it.value
 
-    def read_phi(self, i: int) -> np.ndarray:
-        out = np.zeros(self.shapes[i], np.float32)
+    def read_phi(self, i: int, out=None) -> np.ndarray:
+        out = _out(out, self.shapes[i], np.float32)
         self._chk(self._lib.lss_batch_read_phi(self._h, i, _ptr(out)))
         return out
 
-    def read_mask(self, i: int) -> np.ndarray:
-        out = np.zeros(self.shapes[i], np.uint8)
+    def read_mask(self, i: int, out=None) -> np.ndarray:
+        out = _out(out, self.shapes[i], np.uint8)
         self._chk(self._lib.lss_batch_read_mask(self._h, i, _ptr(out)))
         return out
 

@@ -10,7 +10,9 @@ set) + the full run to convergence, in LSS_MODE_NS.
 metric: active-voxel updates per second (sum over iterations of the active
 count, from the device counter) over the device time of the steps.
 e2e: the same metric through the public API with host buffers each step
-(volume upload, seeding, run, mask readback).
+(volume upload, seeding, run, mask readback), the volume and the mask in
+pinned host memory; e2e.pageable_value: the same with a pageable numpy volume
+and a newly allocated mask array each step.
 roofline: 20 algorithmic bytes per active-voxel update (phi in, I, phi out,
 coordinate in/out) over the persistent kernel's CUDA-event time, against the
 measured HBM copy bandwidth.
@@ -242,24 +244,34 @@ def run_ours(args, ws, rank, local):
     st = seg.stats()
     mask = seg.get_saveable_segmentation()
 
-    # e2e through the public API with host buffers.
-    e2e_ms = 0.0
-    e2e_updates = 0
+    # e2e through the public API with host buffers: every step uploads the
+    # volume, seeds, runs to convergence and reads the mask back.  The main
+    # figure stages the volume and the mask in pinned host memory (allocated
+    # once, outside the timed steps); the second passes a pageable numpy
+    # volume and lets the call allocate a new mask array each step.
+    def e2e(img, out):
+        ms, upd, m = 0.0, 0, None
+        for s in range(args.warmup + args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            seg.load_volume(img)
+            seg.set_parameters(p.target, p.window, p.curvature, p.time_step, alpha_role=p.alpha_role)
+            seg.set_seed_spheres(cfg["spheres"])
+            seg.step_until_converged(conv["rel"], conv["patience"], conv["max_iterations"])
+            m = seg.get_saveable_segmentation(out=out)
+            t1 = time.perf_counter()
+            if s >= args.warmup:
+                ms += 1e3 * (t1 - t0)
+                upd += seg.stats()["voxel_updates"]
+        assert np.array_equal(m, mask)
+        return sum_over_ranks(ws, float(upd)) / (max_over_ranks(ws, ms) / 1e3)
+
     img = np.ascontiguousarray(cfg["image"])
-    for s in range(args.warmup + args.steps):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        seg.load_volume(img)
-        seg.set_parameters(p.target, p.window, p.curvature, p.time_step, alpha_role=p.alpha_role)
-        seg.set_seed_spheres(cfg["spheres"])
-        seg.step_until_converged(conv["rel"], conv["patience"], conv["max_iterations"])
-        m = seg.get_saveable_segmentation()
-        t1 = time.perf_counter()
-        if s >= args.warmup:
-            e2e_ms += 1e3 * (t1 - t0)
-            e2e_updates += seg.stats()["voxel_updates"]
-    assert np.array_equal(m, mask)
-    e2e_value = sum_over_ranks(ws, float(e2e_updates)) / (max_over_ranks(ws, e2e_ms) / 1e3)
+    img_pinned = torch.empty(img.shape, dtype=torch.float32, pin_memory=True).numpy()
+    img_pinned[...] = img
+    mask_pinned = torch.empty(mask.shape, dtype=torch.uint8, pin_memory=True).numpy()
+    e2e_value = e2e(img_pinned, mask_pinned)
+    e2e_pageable = e2e(img, None)
 
     # Dense all-voxel GPU update (same arithmetic, every voxel, no active set)
     # timed over the same number of iterations the sparse run needed.
@@ -306,7 +318,9 @@ def run_ours(args, ws, rank, local):
                                           "expansion on one)"},
             "e2e": {"value": e2e_value, "unit": "voxel_updates/s",
                     "h2d_bytes_per_step": int(img.nbytes),
-                    "d2h_bytes_per_step": int(mask.nbytes)},
+                    "d2h_bytes_per_step": int(mask.nbytes),
+                    "host_buffers": "pinned (volume staged once; mask read into a reused pinned array)",
+                    "pageable_value": e2e_pageable},
             "gpu_launches": int(launches_steps),
             "clocks": clk.summary(),
         }

@@ -99,3 +99,19 @@ def test_struct_layouts_match_header(tmp_path):
         assert int(got[sname]) == C.sizeof(st), sname
         for f, _ in st._fields_:
             assert int(got[f"{sname}.{f}"]) == getattr(st, f).offset, (sname, f)
+
+
+def test_readback_out_arrays_are_checked():
+    """Read-backs accept a caller-owned output array only with the volume's
+    shape and dtype, C-contiguous and writeable."""
+    from aworkefficientgpualgorithmforlevelsetsegmentation_gb300.segmenter import _out
+    a = np.empty((3, 4, 5), np.uint8)
+    assert _out(a, (3, 4, 5), np.uint8) is a
+    fresh = _out(None, (3, 4, 5), np.float32)
+    assert fresh.shape == (3, 4, 5) and fresh.dtype == np.float32 and not fresh.any()
+    ro = np.empty((3, 4, 5), np.uint8)
+    ro.flags.writeable = False
+    for bad in (np.empty((3, 4, 6), np.uint8), np.empty((3, 4, 5), np.int8),
+                np.empty((5, 4, 3), np.uint8).transpose(2, 1, 0), ro):
+        with pytest.raises(ValueError):
+            _out(bad, (3, 4, 5), np.uint8)

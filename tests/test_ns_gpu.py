@@ -172,6 +172,10 @@ def test_ns_seeds_and_readbacks():
     s.step(20)
     m = s.get_saveable_segmentation()
     assert np.array_equal(m.astype(bool), s.read_phi() <= 0)
+    # Read-backs into caller-owned arrays (reused across calls).
+    mb, pb = np.full(m.shape, 7, np.uint8), np.full(m.shape, 9.0, np.float32)
+    assert s.get_saveable_segmentation(out=mb) is mb and np.array_equal(mb, m)
+    assert s.read_phi(out=pb) is pb and np.array_equal(pb, s.read_phi())
     s.freeze_current_segmentation()
     s.clear_current_segmentation()
     assert s.get_active_element_count() == 0
