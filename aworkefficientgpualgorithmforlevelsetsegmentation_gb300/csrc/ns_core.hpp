@@ -95,6 +95,7 @@ class NsCore {
    private:
     size_t dyn_smem() const;
     void upload_descriptors();
+    void upload_padded(float* dst, const float* host, const VolHost& V, float* stage);
     NsArgs args(uint32_t k0, int max_iters, const lss_conv* conv) const;
 
     EngineBase* owner_;

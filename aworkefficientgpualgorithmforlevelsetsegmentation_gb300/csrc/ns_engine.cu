@@ -46,34 +46,58 @@ void encode_tmap_f32_3d(CUtensorMap* out, const float* base, uint64_t nx, uint64
 
 namespace {
 
+// Unpadded fields (x fastest, rows of nx) <-> padded device fields (pitch px,
+// py).  Block i takes the rows (y, z) i, i + gridDim.x, ... and its threads
+// cover x, so there is one division a row, none an element.  The host side
+// of an unpadded field may be pinned host memory read or written in place.
 __global__ void k_ns_scatter(float* dst, const float* src, int nx, int ny, int nz, int px, int py) {
-    const uint64_t n = (uint64_t)nx * ny * nz;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
-         i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t x = i % nx, y = (i / nx) % ny, z = i / ((uint64_t)nx * ny);
-        dst[(z * py + y) * px + x] = src[i];
+    const uint32_t rows = (uint32_t)ny * (uint32_t)nz;
+    for (uint32_t r = blockIdx.x; r < rows; r += gridDim.x) {
+        const uint32_t z = r / (uint32_t)ny, y = r - z * (uint32_t)ny;
+        const float* s = src + (size_t)r * nx;
+        float* d = dst + ((size_t)z * py + y) * px;
+        for (int x = threadIdx.x; x < nx; x += blockDim.x) d[x] = s[x];
     }
 }
 
 __global__ void k_ns_gather(float* dst, const float* src, int nx, int ny, int nz, int px, int py) {
-    const uint64_t n = (uint64_t)nx * ny * nz;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
-         i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t x = i % nx, y = (i / nx) % ny, z = i / ((uint64_t)nx * ny);
-        dst[i] = src[(z * py + y) * px + x];
+    const uint32_t rows = (uint32_t)ny * (uint32_t)nz;
+    for (uint32_t r = blockIdx.x; r < rows; r += gridDim.x) {
+        const uint32_t z = r / (uint32_t)ny, y = r - z * (uint32_t)ny;
+        const float* s = src + ((size_t)z * py + y) * px;
+        float* d = dst + (size_t)r * nx;
+        for (int x = threadIdx.x; x < nx; x += blockDim.x) d[x] = s[x];
     }
 }
 
 // dst[i] = phi <= 0 at unpadded voxel i, or'ed with frozen[i] (may be null;
-// dst may be frozen itself).
+// dst may be frozen itself: each element is read and written by one thread).
+// Four voxels a thread, one 4-byte store, when the rows and both byte
+// arrays allow it.
 __global__ void k_ns_mask(uint8_t* dst, const float* src, const uint8_t* frozen, int nx, int ny, int nz, int px,
                           int py) {
-    const uint64_t n = (uint64_t)nx * ny * nz;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
-         i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t x = i % nx, y = (i / nx) % ny, z = i / ((uint64_t)nx * ny);
-        const bool in = src[(z * py + y) * px + x] <= 0.0f || (frozen && frozen[i]);
-        dst[i] = in ? 1 : 0;
+    const uint32_t rows = (uint32_t)ny * (uint32_t)nz;
+    const bool vec = nx % 4 == 0 && (uintptr_t)dst % 4 == 0 && (uintptr_t)frozen % 4 == 0;
+    for (uint32_t r = blockIdx.x; r < rows; r += gridDim.x) {
+        const uint32_t z = r / (uint32_t)ny, y = r - z * (uint32_t)ny;
+        const float* s = src + ((size_t)z * py + y) * px;
+        uint8_t* d = dst + (size_t)r * nx;
+        const uint8_t* f = frozen ? frozen + (size_t)r * nx : nullptr;
+        if (vec) {
+            for (int x = 4 * threadIdx.x; x < nx; x += 4 * blockDim.x) {
+                uint32_t m = (uint32_t)(s[x] <= 0.0f) | (uint32_t)(s[x + 1] <= 0.0f) << 8 |
+                             (uint32_t)(s[x + 2] <= 0.0f) << 16 | (uint32_t)(s[x + 3] <= 0.0f) << 24;
+                if (f) {
+                    const uint32_t fw = *reinterpret_cast<const uint32_t*>(f + x);
+                    // Nonzero frozen bytes -> 1.
+                    m |= ((fw | (fw >> 1) | (fw >> 2) | (fw >> 3) | (fw >> 4) | (fw >> 5) | (fw >> 6) | (fw >> 7)) &
+                          0x01010101u);
+                }
+                *reinterpret_cast<uint32_t*>(d + x) = m;
+            }
+        } else {
+            for (int x = threadIdx.x; x < nx; x += blockDim.x) d[x] = (s[x] <= 0.0f || (f && f[x])) ? 1 : 0;
+        }
     }
 }
 
@@ -259,6 +283,42 @@ static KernelSet kernels(const BrickConfig& c) {
 NsCore::NsCore(EngineBase* owner, uint64_t budget) : owner_(owner), arena_(budget), brick_arena_(0) {}
 NsCore::~NsCore() = default;
 
+// Device address of a host buffer in pinned host memory (cudaHostAlloc or
+// cudaHostRegister, mapped into the device's address space under unified
+// addressing), or null for pageable memory.  Kernels read or write pinned
+// buffers in place over the host link: as fast as a copy-engine transfer
+// (about 200 GB/s each way on GB300), with no device staging buffer and no
+// second pass.
+static void* pinned_device_ptr(const void* host) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// Unpadded host field -> padded device field dst of volume V.  Pageable host
+// memory is copied into `stage` first (a device buffer of at least nx*ny*nz
+// floats that is free during the call), or into a temporary without one.
+// Returns after the host buffer was read.
+void NsCore::upload_padded(float* dst, const float* host, const VolHost& V, float* stage) {
+    cudaStream_t st = owner_->stream;
+    const uint64_t n = (uint64_t)V.nx * V.ny * V.nz;
+    const float* src = (const float*)pinned_device_ptr(host);
+    float* tmp = nullptr;
+    if (!src) {
+        float* buf = stage ? stage : (tmp = (float*)arena_.alloc(n * 4));
+        LSS_CUDA(cudaMemcpyAsync(buf, host, n * 4, cudaMemcpyHostToDevice, st));
+        src = buf;
+    }
+    k_ns_scatter<<<owner_->num_sms * 4, 256, 0, st>>>(dst, src, V.nx, V.ny, V.nz, V.px, V.py);
+    ++owner_->launches;
+    LSS_CUDA(cudaGetLastError());
+    owner_->sync();
+    if (tmp) arena_.free_last(tmp);
+}
+
 int NsCore::add_volume(const float* data, int nx, int ny, int nz, const lss_params& p) {
     LSS_REQUIRE(data && nx > 0 && ny > 0 && nz > 0, LSS_ERR_INVALID_ARGUMENT, "bad volume");
     LSS_REQUIRE(vols_.size() < 4096, LSS_ERR_CAPACITY, "at most 4096 volumes per batch");
@@ -272,10 +332,7 @@ int NsCore::add_volume(const float* data, int nx, int ny, int nz, const lss_para
     v.phi[1] = (float*)arena_.alloc(P * 4);
     cudaStream_t st = owner_->stream;
     LSS_CUDA(cudaMemsetAsync(v.img, 0, P * 4, st));
-    float* tmp = (float*)arena_.alloc((uint64_t)nx * ny * nz * 4);
-    LSS_CUDA(cudaMemcpyAsync(tmp, data, (uint64_t)nx * ny * nz * 4, cudaMemcpyHostToDevice, st));
-    k_ns_scatter<<<owner_->num_sms * 4, 256, 0, st>>>(v.img, tmp, nx, ny, nz, v.px, v.py);
-    ++owner_->launches;
+    upload_padded(v.img, data, v, v.phi[1]);  // phi[1] stages; it is filled below
     k_ns_fill<<<owner_->num_sms * 4, 256, 0, st>>>(v.phi[0], P, p.phi_max);
     ++owner_->launches;
     k_ns_fill<<<owner_->num_sms * 4, 256, 0, st>>>(v.phi[1], P, p.phi_max);
@@ -283,7 +340,6 @@ int NsCore::add_volume(const float* data, int nx, int ny, int nz, const lss_para
     v.uniform = true;  // both buffers phi_max until seeded
     LSS_CUDA(cudaGetLastError());
     owner_->sync();
-    arena_.free_last(tmp);
     vols_.push_back(v);
     configured_ = false;
     return (int)vols_.size() - 1;
@@ -297,14 +353,7 @@ void NsCore::set_bias(int v, const float* bias) {
     } else {
         if (!V.bias_buf) V.bias_buf = (float*)arena_.alloc(P * 4);
         LSS_CUDA(cudaMemsetAsync(V.bias_buf, 0, P * 4, owner_->stream));
-        float* tmp = (float*)arena_.alloc((uint64_t)V.nx * V.ny * V.nz * 4);
-        LSS_CUDA(cudaMemcpyAsync(tmp, bias, (uint64_t)V.nx * V.ny * V.nz * 4, cudaMemcpyHostToDevice,
-                                 owner_->stream));
-        k_ns_scatter<<<owner_->num_sms * 4, 256, 0, owner_->stream>>>(V.bias_buf, tmp, V.nx, V.ny, V.nz,
-                                                                     V.px, V.py);
-        ++owner_->launches;
-        owner_->sync();
-        arena_.free_last(tmp);
+        upload_padded(V.bias_buf, bias, V, nullptr);
         V.bias = V.bias_buf;
     }
     upload_descriptors();
@@ -540,14 +589,7 @@ void NsCore::sphere_union(int v, float cx, float cy, float cz, float r) {
 void NsCore::set_phi(int v, const float* phi) {
     VolHost& V = vols_.at(v);
     V.uniform = false;
-    float* tmp = (float*)arena_.alloc((uint64_t)V.nx * V.ny * V.nz * 4);
-    LSS_CUDA(cudaMemcpyAsync(tmp, phi, (uint64_t)V.nx * V.ny * V.nz * 4, cudaMemcpyHostToDevice,
-                             owner_->stream));
-    k_ns_scatter<<<owner_->num_sms * 4, 256, 0, owner_->stream>>>(V.phi[parity_], tmp, V.nx, V.ny, V.nz,
-                                                                 V.px, V.py);
-    ++owner_->launches;
-    owner_->sync();
-    arena_.free_last(tmp);
+    upload_padded(V.phi[parity_], phi, V, nullptr);
 }
 
 // Both buffers: phi is then uniform, which later seeding and active-set
@@ -627,10 +669,7 @@ void NsCore::reload_volume(int v, const float* data, const lss_params& p) {
     VolHost& V = vols_.at(v);
     cudaStream_t st = owner_->stream;
     const uint64_t n = (uint64_t)V.nx * V.ny * V.nz, P = (uint64_t)V.px * V.py * V.pz;
-    float* tmp = (float*)arena_.alloc(n * 4);
-    LSS_CUDA(cudaMemcpyAsync(tmp, data, n * 4, cudaMemcpyHostToDevice, st));
-    k_ns_scatter<<<owner_->num_sms * 4, 256, 0, st>>>(V.img, tmp, V.nx, V.ny, V.nz, V.px, V.py);
-    ++owner_->launches;
+    upload_padded(V.img, data, V, V.phi[1]);  // phi[1] stages; both are filled below
     for (int q = 0; q < 2; ++q) {
         k_ns_fill<<<owner_->num_sms * 4, 256, 0, st>>>(V.phi[q], P, p.phi_max);
         ++owner_->launches;
@@ -650,20 +689,22 @@ void NsCore::reload_volume(int v, const float* data, const lss_params& p) {
     upload_descriptors();
     LSS_CUDA(cudaGetLastError());
     owner_->sync();
-    arena_.free_last(tmp);
 }
 
 void NsCore::read_mask(int v, uint8_t* out) {
     VolHost& V = vols_.at(v);
     const uint32_t p = vols_.size() == 1 ? parity_ : vol_parity(v);
     const uint64_t n = (uint64_t)V.nx * V.ny * V.nz;
-    uint8_t* tmp = (uint8_t*)arena_.alloc(n);
-    k_ns_mask<<<owner_->num_sms * 4, 256, 0, owner_->stream>>>(tmp, V.phi[p], V.frozen, V.nx, V.ny, V.nz, V.px,
-                                                              V.py);
+    // Pinned host memory is written in place; else through a temporary.
+    uint8_t* dev = (uint8_t*)pinned_device_ptr(out);
+    uint8_t* tmp = dev ? nullptr : (uint8_t*)arena_.alloc(n);
+    k_ns_mask<<<owner_->num_sms * 4, 256, 0, owner_->stream>>>(dev ? dev : tmp, V.phi[p], V.frozen, V.nx, V.ny,
+                                                              V.nz, V.px, V.py);
     ++owner_->launches;
-    LSS_CUDA(cudaMemcpyAsync(out, tmp, n, cudaMemcpyDeviceToHost, owner_->stream));
+    if (tmp) LSS_CUDA(cudaMemcpyAsync(out, tmp, n, cudaMemcpyDeviceToHost, owner_->stream));
+    LSS_CUDA(cudaGetLastError());
     owner_->sync();
-    arena_.free_last(tmp);
+    if (tmp) arena_.free_last(tmp);
 }
 
 void NsCore::freeze(int v) {
@@ -690,14 +731,18 @@ void NsCore::clear_frozen(int v) {
 void NsCore::read_phi(int v, float* out) {
     VolHost& V = vols_.at(v);
     const uint32_t p = vols_.size() == 1 ? parity_ : vol_parity(v);
-    float* tmp = (float*)arena_.alloc((uint64_t)V.nx * V.ny * V.nz * 4);
-    k_ns_gather<<<owner_->num_sms * 4, 256, 0, owner_->stream>>>(tmp, V.phi[p], V.nx, V.ny, V.nz, V.px,
-                                                                V.py);
+    // Pinned host memory is written in place; else through a temporary.
+    float* dev = (float*)pinned_device_ptr(out);
+    float* tmp = dev ? nullptr : (float*)arena_.alloc((uint64_t)V.nx * V.ny * V.nz * 4);
+    k_ns_gather<<<owner_->num_sms * 4, 256, 0, owner_->stream>>>(dev ? dev : tmp, V.phi[p], V.nx, V.ny, V.nz,
+                                                                V.px, V.py);
     ++owner_->launches;
-    LSS_CUDA(cudaMemcpyAsync(out, tmp, (uint64_t)V.nx * V.ny * V.nz * 4, cudaMemcpyDeviceToHost,
-                             owner_->stream));
+    if (tmp)
+        LSS_CUDA(cudaMemcpyAsync(out, tmp, (uint64_t)V.nx * V.ny * V.nz * 4, cudaMemcpyDeviceToHost,
+                                 owner_->stream));
+    LSS_CUDA(cudaGetLastError());
     owner_->sync();
-    arena_.free_last(tmp);
+    if (tmp) arena_.free_last(tmp);
 }
 
 uint64_t NsCore::read_active(int v, uint64_t* out, uint64_t cap) {

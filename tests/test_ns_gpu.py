@@ -328,3 +328,46 @@ def test_ns_freeze_and_clear_on_device():
     s.freeze_current_segmentation()
     s.clear_all_segmentations()
     assert not s.get_saveable_segmentation().any()
+
+
+def test_ns_pinned_host_buffers_match_pageable():
+    """Pinned host buffers are read and written in place by the kernels
+    (volume, phi and reload uploads; phi and mask read-backs, with and without
+    a frozen segmentation); every result equals the pageable-numpy path, for
+    rows of a multiple of four voxels and for odd rows."""
+    torch = pytest.importorskip("torch")
+
+    def pinned(a):
+        t = torch.empty(a.shape, dtype={np.float32: torch.float32, np.uint8: torch.uint8}[a.dtype.type],
+                        pin_memory=True).numpy()
+        t[...] = a
+        return t
+
+    p = P.ns_params(0.6, 0.2, 0.7)
+    for shape in [(40, 48, 64), (29, 50, 37)]:
+        rng = np.random.default_rng(shape[2])
+        nz, ny, nx = shape
+        imgs = [(0.5 + 0.2 * rng.standard_normal(shape)).astype(np.float32) for _ in range(2)]
+        phi0 = P.sdf_spheres(shape, [((nx - 1) / 2, (ny - 1) / 2, (nz - 1) / 2, 6.0)])
+        a = lss.Segmenter(lss.MODE_NS, brick=(8, 8, 8), threads_per_brick=256)
+        b = lss.Segmenter(lss.MODE_NS, brick=(8, 8, 8), threads_per_brick=256)
+        for img in imgs:  # the second load is a same-shape reload
+            a.load_volume(img)
+            b.load_volume(pinned(img))
+            for s in (a, b):
+                s.set_parameters(p.target, p.window, p.curvature, p.time_step, alpha_role=p.alpha_role)
+            a.set_phi(phi0)
+            b.set_phi(pinned(phi0))
+            a.step(12)
+            b.step(12)
+            phi_b = b.read_phi(out=pinned(np.zeros(shape, np.float32)))
+            assert np.array_equal(a.read_phi(), phi_b)
+            mask_b = b.get_saveable_segmentation(out=pinned(np.full(shape, 9, np.uint8)))
+            assert np.array_equal(a.get_saveable_segmentation(), mask_b)
+            assert np.array_equal(b.get_saveable_segmentation(), mask_b)
+        a.freeze_current_segmentation()
+        b.freeze_current_segmentation()
+        for s in (a, b):
+            s.set_phi(np.full(shape, 1.0, np.float32))
+        frozen_b = b.get_saveable_segmentation(out=pinned(np.zeros(shape, np.uint8)))
+        assert np.array_equal(a.get_saveable_segmentation(), frozen_b) and frozen_b.any()
