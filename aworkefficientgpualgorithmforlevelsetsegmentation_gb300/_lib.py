@@ -47,7 +47,7 @@ class lss_stats(C.Structure):
 
 class lss_grads(C.Structure):
     _fields_ = [("loss", C.c_double), ("d_target", C.c_double), ("d_window", C.c_double),
-                ("d_curvature", C.c_double)]
+                ("d_curvature", C.c_double), ("active_voxel_iterations", C.c_uint64)]
 
 
 P = C.c_void_p

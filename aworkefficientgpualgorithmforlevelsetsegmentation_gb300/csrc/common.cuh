@@ -188,4 +188,19 @@ __device__ __forceinline__ uint64_t block_exclusive_sum64(uint64_t v, uint64_t* 
 // the named host step fail with LSS_ERR_INJECTED (no GPU fault is made).
 bool fault_injected(const char* what);
 
+// Device address of a host buffer in pinned host memory (cudaHostAlloc or
+// cudaHostRegister, mapped into the device's address space under unified
+// addressing), or null for pageable memory.  Kernels read or write pinned
+// buffers in place over the host link: as fast as a copy-engine transfer
+// (about 200 GB/s each way on GB300), with no device staging buffer and no
+// second pass.
+inline void* pinned_device_ptr(const void* host) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 }  // namespace lss

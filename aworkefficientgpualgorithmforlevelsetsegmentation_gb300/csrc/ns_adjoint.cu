@@ -4,16 +4,23 @@
 // fixed, the soft-Dice loss of sigmoid(-phi/tau) against a target mask, and
 // its gradients with respect to T, eps, alpha and a per-voxel speed bias.
 //
-// Forward: iteration k updates the voxels of A_k (brick masks, the layout of
-// the sparse engine) and writes every other voxel through; the changed
-// voxels' ballot words are dilated into A_{k+1} exactly as in the persistent
-// kernel, so the recorded sets are the sparse engine's sets.  phi is
-// checkpointed every `every` iterations; the reverse pass recomputes each
-// segment from its checkpoint (bit-identical: the update arithmetic is
-// deterministic) and runs the segment's iterations backwards:
-//   lambda_k = lambda_{k+1} on inactive voxels (pass-through), and for every
-//   active voxel v the transposed stencil Jacobian of the update scatters
-//   lambda_{k+1}[v] onto its 19 stencil voxels (fp32 atomics);
+// Work-efficient like the forward engine: every iteration touches the bricks
+// of its active set only.  The forward keeps the brick list of each A_k
+// (built while dilating: the first thread to put a word into a brick appends
+// it) beside the recorded brick masks.  It runs over a ping-pong pair in
+// which both buffers stay current: iteration k writes the bricks of A_k
+// whole (active voxels updated, the rest copied) and copies across the
+// bricks of A_{k-1} that left the set; the changed voxels' ballot words are
+// dilated into A_{k+1} exactly as in the persistent kernel, so the recorded
+// sets are the sparse engine's sets.  phi is checkpointed every `every`
+// iterations (a device copy); the reverse pass recomputes each segment from
+// its checkpoint (a copy of the previous state plus the sparse update:
+// bit-identical, the arithmetic is deterministic) and runs the segment's
+// iterations backwards on one lambda field, in place:
+//   take:  U = lambda_{k+1} at the voxels of A_k, lambda = 0 there (lambda
+//          keeps lambda_{k+1} everywhere else: the pass-through);
+//   vjp:   every active voxel v scatters U[v] through the transposed stencil
+//          Jacobian of the update onto its 19 stencil voxels (fp32 atomics);
 // parameter gradients are reduced per block in FP64 (the gradient-check
 // reduction) and the bias gradient accumulates per voxel.
 #include <cuda_runtime.h>
@@ -21,6 +28,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -29,6 +37,11 @@
 
 namespace lss {
 namespace {
+
+void count_launch(EngineBase* owner) {
+    ++owner->launches;
+    LSS_CUDA(cudaGetLastError());
+}
 
 __device__ __forceinline__ int clampi(int v, int n) { return v < 0 ? 0 : (v >= n ? n - 1 : v); }
 
@@ -39,52 +52,88 @@ __device__ __forceinline__ int3 voxel_of(const NsVol& V, uint32_t b, int j) {
     return make_int3(o.x + j % S::X, o.y + (j / S::X) % S::Y, o.z + j / (S::X * S::Y));
 }
 
-// Forward iteration: phi_out = update of phi_in on A_k (act), pass-through
-// elsewhere; changed voxels -> ballot words chg[brick * CHG + j / 32] (when
-// chg is not null).  One thread per voxel slot in brick-major order.
+// Per-iteration brick lists: list[k][0 .. count[k]) = the bricks of A_k in
+// no particular order (each brick once), flag[k][b] = b is in it.
+
+// list_0 and flag_0 from the recorded masks of A_0.
 template <class S>
-__global__ void __launch_bounds__(256) k_adj_update(NsVol V, const float* __restrict__ in, float* __restrict__ out,
-                                                    const unsigned long long* __restrict__ act,
-                                                    uint32_t* __restrict__ chg, uint32_t nb) {
-    const uint64_t total = (uint64_t)nb * S::VOX;
-    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
-         t += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t b = (uint32_t)(t / S::VOX);
-        const int j = (int)(t % S::VOX);
-        const int3 p = voxel_of<S>(V, b, j);
-        bool changed = false;
-        if (p.x < V.nx && p.y < V.ny && p.z < V.nz) {
-            const size_t idx = ((size_t)p.z * V.py + p.y) * V.px + p.x;
-            const float c = in[idx];
-            if ((act[(size_t)b * S::WORDS + (j >> 6)] >> (j & 63)) & 1ull) {
-                auto P = [&](int dx, int dy, int dz) {
-                    return in[((size_t)clampi(p.z + dz, V.nz) * V.py + clampi(p.y + dy, V.ny)) * V.px +
-                              clampi(p.x + dx, V.nx)];
-                };
-                const float nv = ns_update_f32(P, V.img[idx], V.bias ? V.bias[idx] : 0.0f, V);
-                changed = fabsf(nv - c) > V.thr_t;
-                out[idx] = nv;
-            } else {
-                out[idx] = c;
-            }
-        }
-        if (chg) {
-            const uint32_t bal = __ballot_sync(0xffffffffu, changed);
-            if ((threadIdx.x & 31) == 0) chg[t >> 5] = bal;
+__global__ void __launch_bounds__(256) k_adj_list0(const unsigned long long* __restrict__ act, uint32_t* flag,
+                                                   uint32_t* list, uint32_t* count, uint32_t nb) {
+    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+        unsigned long long any = 0ull;
+#pragma unroll
+        for (int w = 0; w < S::WORDS; ++w) any |= act[(size_t)b * S::WORDS + w];
+        if (any) {
+            flag[b] = 1u;
+            list[atomicAdd(count, 1u)] = b;
         }
     }
 }
 
-// A_{k+1}: the changed words of every brick dilated into its 27 neighbours
-// (one thread per neighbour mask word).
+// Iteration k: block per brick.  The bricks of list_k are written whole into
+// out (active voxels updated from in, the others copied); with `prev` (the
+// recorded forward's ping-pong pair), the bricks of list_{k-1} not in
+// list_k (flag_k clear) are copied from in to out, so that out equals in
+// outside the bricks of A_k.  With chg: the changed voxels' ballot words of
+// list_k's bricks and the count of updated voxels added to *nact.
+template <class S>
+__global__ void __launch_bounds__(256) k_adj_update(NsVol V, const float* __restrict__ in, float* __restrict__ out,
+                                                    const unsigned long long* __restrict__ act,
+                                                    const uint32_t* __restrict__ list, const uint32_t* count,
+                                                    const uint32_t* __restrict__ prev, const uint32_t* prev_count,
+                                                    const uint32_t* __restrict__ flag_k, uint32_t* __restrict__ chg,
+                                                    unsigned long long* nact) {
+    const uint32_t n = *count, np = prev ? *prev_count : 0u;
+    uint32_t mine = 0;
+    for (uint32_t i = blockIdx.x; i < n + np; i += gridDim.x) {
+        const bool upd = i < n;
+        const uint32_t b = upd ? list[i] : prev[i - n];
+        if (!upd && flag_k[b]) continue;  // also in list_k: written above
+        for (int j = threadIdx.x; j < S::VOX; j += blockDim.x) {
+            const int3 p = voxel_of<S>(V, b, j);
+            bool changed = false;
+            if (p.x < V.nx && p.y < V.ny && p.z < V.nz) {
+                const size_t idx = ((size_t)p.z * V.py + p.y) * V.px + p.x;
+                const float c = in[idx];
+                if (upd && ((act[(size_t)b * S::WORDS + (j >> 6)] >> (j & 63)) & 1ull)) {
+                    auto P = [&](int dx, int dy, int dz) {
+                        return in[((size_t)clampi(p.z + dz, V.nz) * V.py + clampi(p.y + dy, V.ny)) * V.px +
+                                  clampi(p.x + dx, V.nx)];
+                    };
+                    const float nv = ns_update_f32(P, V.img[idx], V.bias ? V.bias[idx] : 0.0f, V);
+                    changed = fabsf(nv - c) > V.thr_t;
+                    out[idx] = nv;
+                    ++mine;
+                } else {
+                    out[idx] = c;
+                }
+            }
+            // VOX is a multiple of 32: a warp's slots are all in or all out.
+            if (chg && upd) {
+                const uint32_t bal = __ballot_sync(0xffffffffu, changed);
+                if ((threadIdx.x & 31) == 0) chg[(size_t)b * S::CHG + (j >> 5)] = bal;
+            }
+        }
+    }
+    if (nact) {
+        mine = __reduce_add_sync(0xffffffffu, mine);
+        if ((threadIdx.x & 31) == 0 && mine) atomicAdd(nact, (unsigned long long)mine);
+    }
+}
+
+// A_{k+1}: the changed words of list_k's bricks dilated into their 27
+// neighbours (one thread per brick, neighbour and mask word); the first
+// thread to put a word into a brick appends the brick to list_{k+1}.
 template <class S>
 __global__ void __launch_bounds__(256) k_adj_dilate(NsVol V, const uint32_t* __restrict__ chg,
-                                                    unsigned long long* __restrict__ nxt, uint32_t nb) {
+                                                    const uint32_t* __restrict__ list, const uint32_t* count,
+                                                    unsigned long long* __restrict__ nxt, uint32_t* flag_next,
+                                                    uint32_t* list_next, uint32_t* count_next) {
     constexpr int PER = 27 * S::WORDS;
-    const uint64_t total = (uint64_t)nb * PER;
+    const uint64_t total = (uint64_t)(*count) * PER;
     for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
          t += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t b = (uint32_t)(t / PER);
+        const uint32_t b = list[t / PER];
         const int r = (int)(t % PER), slot = r / S::WORDS, w = r % S::WORDS;
         const uint32_t* cb = chg + (size_t)b * S::CHG;
         uint32_t any = 0;
@@ -99,27 +148,32 @@ __global__ void __launch_bounds__(256) k_adj_dilate(NsVol V, const uint32_t* __r
         uint64_t x = dilate_word<S>(cb, ox, oy, oz, w, V.nbh);
         if (lx < S::X || ly < S::Y || lz < S::Z)
             x &= inside_mask<S>(w, min(lx, S::X), min(ly, S::Y), min(lz, S::Z));
+        if (!x) continue;
         const uint32_t nbi = b + (int32_t)((oz * V.nby + oy) * V.nbx + ox);
-        if (x) atomicOr(&nxt[(size_t)nbi * S::WORDS + w], (unsigned long long)x);
+        atomicOr(&nxt[(size_t)nbi * S::WORDS + w], (unsigned long long)x);
+        if (*(volatile uint32_t*)&flag_next[nbi] == 0u && atomicExch(&flag_next[nbi], 1u) == 0u)
+            list_next[atomicAdd(count_next, 1u)] = nbi;
     }
 }
 
-// lambda_k = lambda_{k+1} on the voxels outside A_k, 0 on A_k (their
-// contributions are scattered by k_adj_vjp).
+// Reverse iteration k, first half (block per brick of list_k): U =
+// lambda_{k+1} at the voxels of A_k and lambda = 0 there; lambda keeps
+// lambda_{k+1} at every other voxel.
 template <class S>
-__global__ void __launch_bounds__(256) k_adj_lambda_init(NsVol V, const unsigned long long* __restrict__ act,
-                                                         const float* __restrict__ nxt, float* __restrict__ lam,
-                                                         uint32_t nb) {
-    const uint64_t total = (uint64_t)nb * S::VOX;
-    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
-         t += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t b = (uint32_t)(t / S::VOX);
-        const int j = (int)(t % S::VOX);
-        const int3 p = voxel_of<S>(V, b, j);
-        if (p.x >= V.nx || p.y >= V.ny || p.z >= V.nz) continue;
-        const size_t idx = ((size_t)p.z * V.py + p.y) * V.px + p.x;
-        const bool a = (act[(size_t)b * S::WORDS + (j >> 6)] >> (j & 63)) & 1ull;
-        lam[idx] = a ? 0.0f : nxt[idx];
+__global__ void __launch_bounds__(256) k_adj_take(NsVol V, const unsigned long long* __restrict__ act,
+                                                  const uint32_t* __restrict__ list, const uint32_t* count,
+                                                  float* __restrict__ lam, float* __restrict__ U) {
+    const uint32_t n = *count;
+    for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
+        const uint32_t b = list[i];
+        for (int j = threadIdx.x; j < S::VOX; j += blockDim.x) {
+            if (!((act[(size_t)b * S::WORDS + (j >> 6)] >> (j & 63)) & 1ull)) continue;
+            const int3 p = voxel_of<S>(V, b, j);
+            if (p.x >= V.nx || p.y >= V.ny || p.z >= V.nz) continue;
+            const size_t idx = ((size_t)p.z * V.py + p.y) * V.px + p.x;
+            U[idx] = lam[idx];
+            lam[idx] = 0.0f;
+        }
     }
 }
 
@@ -245,80 +299,85 @@ __device__ __forceinline__ void block_sum3(double a0, double a1, double a2, doub
     __syncthreads();
 }
 
-// Reverse iteration k: scatters lambda_{k+1} of the voxels of A_k through the
-// update's transposed Jacobian into lam, adds the bias gradient and the
-// parameter gradients (gsum[0..2] = T, eps, alpha; FP64).
+// Reverse iteration k, second half (block per brick of list_k): scatters U
+// (lambda_{k+1}) of the voxels of A_k through the update's transposed
+// Jacobian into lam, adds the bias gradient and the parameter gradients
+// (gsum[0..2] = T, eps, alpha; FP64).
 template <class S>
 __global__ void __launch_bounds__(256) k_adj_vjp(NsVol V, const float* __restrict__ phi,
                                                  const unsigned long long* __restrict__ act,
-                                                 const float* __restrict__ nxt, float* lam, float* dbias,
-                                                 double* gsum, uint32_t nb) {
-    const uint64_t total = (uint64_t)nb * S::VOX;
+                                                 const uint32_t* __restrict__ list, const uint32_t* count,
+                                                 const float* __restrict__ U, float* lam, float* dbias,
+                                                 double* gsum) {
+    const uint32_t n = *count;
     double sT = 0.0, sE = 0.0, sA = 0.0;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    // Every thread runs the same number of loop trips (block_sum3 below).
-    for (uint64_t t0 = (uint64_t)blockIdx.x * blockDim.x; t0 < total; t0 += stride) {
-        const uint64_t t = t0 + threadIdx.x;
-        if (t >= total) continue;
-        const uint32_t b = (uint32_t)(t / S::VOX);
-        const int j = (int)(t % S::VOX);
-        if (!((act[(size_t)b * S::WORDS + (j >> 6)] >> (j & 63)) & 1ull)) continue;
-        const int3 p = voxel_of<S>(V, b, j);
-        if (p.x >= V.nx || p.y >= V.ny || p.z >= V.nz) continue;
-        const size_t idx = ((size_t)p.z * V.py + p.y) * V.px + p.x;
-        const float u = nxt[idx];
-        if (u == 0.0f) continue;
-        auto at = [&](int dx, int dy, int dz) {
-            return ((size_t)clampi(p.z + dz, V.nz) * V.py + clampi(p.y + dy, V.ny)) * V.px + clampi(p.x + dx, V.nx);
-        };
-        auto P = [&](int dx, int dy, int dz) { return phi[at(dx, dy, dz)]; };
-        auto add = [&](int dx, int dy, int dz, float g) {
-            if (g != 0.0f) atomicAdd(&lam[at(dx, dy, dz)], g);
-        };
-        float g4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        ns_update_vjp_f32(P, add, V.img[idx], V.bias ? V.bias[idx] : 0.0f, V, u, g4);
-        sT += g4[0];
-        sE += g4[1];
-        sA += g4[2];
-        if (dbias) dbias[idx] += g4[3];
+    for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
+        const uint32_t b = list[i];
+        for (int j = threadIdx.x; j < S::VOX; j += blockDim.x) {
+            if (!((act[(size_t)b * S::WORDS + (j >> 6)] >> (j & 63)) & 1ull)) continue;
+            const int3 p = voxel_of<S>(V, b, j);
+            if (p.x >= V.nx || p.y >= V.ny || p.z >= V.nz) continue;
+            const size_t idx = ((size_t)p.z * V.py + p.y) * V.px + p.x;
+            const float u = U[idx];
+            if (u == 0.0f) continue;
+            auto at = [&](int dx, int dy, int dz) {
+                return ((size_t)clampi(p.z + dz, V.nz) * V.py + clampi(p.y + dy, V.ny)) * V.px +
+                       clampi(p.x + dx, V.nx);
+            };
+            auto P = [&](int dx, int dy, int dz) { return phi[at(dx, dy, dz)]; };
+            auto add = [&](int dx, int dy, int dz, float g) {
+                if (g != 0.0f) atomicAdd(&lam[at(dx, dy, dz)], g);
+            };
+            float g4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            ns_update_vjp_f32(P, add, V.img[idx], V.bias ? V.bias[idx] : 0.0f, V, u, g4);
+            sT += g4[0];
+            sE += g4[1];
+            sA += g4[2];
+            if (dbias) dbias[idx] += g4[3];
+        }
     }
-    block_sum3(sT, sE, sA, gsum);
+    block_sum3(sT, sE, sA, gsum);  // every thread of the block reaches it
 }
 
-// Soft-Dice sums over the volume: gsum[0..2] = (sum s, sum t, sum s t), FP64.
+// Soft-Dice sums over the volume: gsum[0..2] = (sum s, sum t, sum s t).
+// Per voxel in fp32 (a thread sums a few tens of voxels); the block and grid
+// reduction in FP64.
 __global__ void __launch_bounds__(256) k_adj_dice_sums(NsVol V, const float* __restrict__ phi,
                                                        const uint8_t* __restrict__ target, float tau,
                                                        double* gsum) {
-    const uint64_t total = (uint64_t)V.nx * V.ny * V.nz;
-    double ss = 0.0, tt = 0.0, st = 0.0;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t t0 = (uint64_t)blockIdx.x * blockDim.x; t0 < total; t0 += stride) {
-        const uint64_t t = t0 + threadIdx.x;
-        if (t >= total) continue;
-        const int x = (int)(t % V.nx), y = (int)((t / V.nx) % V.ny), z = (int)(t / ((uint64_t)V.nx * V.ny));
-        const size_t idx = ((size_t)z * V.py + y) * V.px + x;
-        const double s = 1.0 / (1.0 + (double)expf(phi[idx] / tau));
-        const double tv = target[idx] ? 1.0 : 0.0;
-        ss += s;
-        tt += tv;
-        st += s * tv;
+    const uint32_t rows = (uint32_t)V.ny * (uint32_t)V.nz;
+    float ss = 0.0f, tt = 0.0f, st = 0.0f;
+    // Block per row (y, z), threads over x (every thread reaches block_sum3).
+    for (uint32_t r = blockIdx.x; r < rows; r += gridDim.x) {
+        const uint32_t z = r / (uint32_t)V.ny, y = r - z * (uint32_t)V.ny;
+        const size_t row = ((size_t)z * V.py + y) * V.px;
+        for (int x = threadIdx.x; x < V.nx; x += blockDim.x) {
+            const float s = 1.0f / (1.0f + expf(phi[row + x] / tau));
+            const float tv = target[row + x] ? 1.0f : 0.0f;
+            ss += s;
+            tt += tv;
+            st += s * tv;
+        }
     }
     block_sum3(ss, tt, st, gsum);
 }
 
-// lambda_K = dloss/dphi_K of the soft-Dice loss.
+// lambda_K = dloss/dphi_K of the soft-Dice loss, per voxel in fp32 from the
+// FP64 sums: dloss/ds = (2 st - 2 t den) / den^2.
 __global__ void __launch_bounds__(256) k_adj_dice_grad(NsVol V, const float* __restrict__ phi,
                                                        const uint8_t* __restrict__ target, float tau,
                                                        const double* __restrict__ sums, float* lam) {
-    const uint64_t total = (uint64_t)V.nx * V.ny * V.nz;
     const double den = sums[0] + sums[1], st = sums[2];
-    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
-         t += (uint64_t)gridDim.x * blockDim.x) {
-        const int x = (int)(t % V.nx), y = (int)((t / V.nx) % V.ny), z = (int)(t / ((uint64_t)V.nx * V.ny));
-        const size_t idx = ((size_t)z * V.py + y) * V.px + x;
-        const float s = 1.0f / (1.0f + expf(phi[idx] / tau));
-        const double dl_ds = -2.0 * ((target[idx] ? 1.0 : 0.0) * den - st) / (den * den);
-        lam[idx] = (float)(dl_ds * (double)(-s * (1.0f - s) / tau));
+    const float c_out = (float)(2.0 * st / (den * den)), c_in = (float)(2.0 * st / (den * den) - 2.0 / den);
+    const uint32_t rows = (uint32_t)V.ny * (uint32_t)V.nz;
+    for (uint32_t r = blockIdx.x; r < rows; r += gridDim.x) {
+        const uint32_t z = r / (uint32_t)V.ny, y = r - z * (uint32_t)V.ny;
+        const size_t row = ((size_t)z * V.py + y) * V.px;
+        for (int x = threadIdx.x; x < V.nx; x += blockDim.x) {
+            const float s = 1.0f / (1.0f + expf(phi[row + x] / tau));
+            const float dl_ds = target[row + x] ? c_in : c_out;
+            lam[row + x] = dl_ds * (-s * (1.0f - s) / tau);
+        }
     }
 }
 
@@ -333,96 +392,131 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     const uint64_t P = (uint64_t)V.px * V.py * V.pz;
     const size_t mwords = (size_t)nb * S::WORDS;
     const int nck = (K + every - 1) / every;
-    DeviceArena mem(core.budget_left());
-    auto F = [&]() { return (float*)mem.alloc(P * 4); };
+    const int grid = owner->num_sms * 8;        // element-wise kernels
+    const int bgrid = owner->num_sms * 4;       // block-per-brick kernels
+    // One device workspace (kept by the engine between calls), carved into
+    // 256-byte aligned parts.
+    auto al = [](uint64_t b) { return (b + 255) / 256 * 256; };
+    const uint64_t nfields = (uint64_t)nck + (every - 1) + 4 + (dbias ? 1 : 0) + (bias ? 1 : 0);
+    const uint64_t total = nfields * al(P * 4) + (uint64_t)(K + 1) * al(mwords * 8) + al((uint64_t)nb * S::CHG * 4) +
+                           2 * (uint64_t)(K + 1) * al((uint64_t)nb * 4) + al((uint64_t)(K + 1) * 4) + al(P) + 256;
+    char* base = (char*)core.workspace(total);
+    auto carve = [&](uint64_t bytes) {
+        char* p = base;
+        base += al(bytes);
+        return p;
+    };
+    auto F = [&]() { return (float*)carve(P * 4); };
     std::vector<float*> ck(nck), seg(every);
     for (auto& p : ck) p = F();
     for (int i = 1; i < every; ++i) seg[i] = F();
-    float* fw[2] = {F(), F()};
-    float* lam[2] = {F(), F()};
+    float* fw[2] = {F(), F()};  // the forward's ping-pong pair
+    float* lam = F();
+    float* U = F();
     std::vector<unsigned long long*> act(K + 1);
-    for (auto& a : act) a = (unsigned long long*)mem.alloc(mwords * 8);
-    uint32_t* chg = (uint32_t*)mem.alloc((size_t)nb * S::CHG * 4);
-    uint8_t* tgt = (uint8_t*)mem.alloc(P);
-    double* gsum = (double*)mem.alloc(8 * sizeof(double));
+    for (auto& a : act) a = (unsigned long long*)carve(mwords * 8);
+    uint32_t* chg = (uint32_t*)carve((size_t)nb * S::CHG * 4);
+    std::vector<uint32_t*> list(K + 1), flag(K + 1);
+    for (auto& l : list) l = (uint32_t*)carve((uint64_t)nb * 4);
+    for (auto& f : flag) f = (uint32_t*)carve((uint64_t)nb * 4);
+    uint32_t* counts = (uint32_t*)carve((uint64_t)(K + 1) * 4);
+    uint8_t* tgt = (uint8_t*)carve(P);
+    double* gsum = (double*)carve(8 * sizeof(double) + 8);
+    unsigned long long* nact = (unsigned long long*)(gsum + 8);
     float* dbias_d = dbias ? F() : nullptr;
-    // Target and bias, padded on the host.
-    {
-        std::vector<uint8_t> t(P, 0);
-        std::vector<float> bb(bias ? P : 0, 0.0f);
-        for (int z = 0; z < V.nz; ++z)
-            for (int y = 0; y < V.ny; ++y)
-                for (int x = 0; x < V.nx; ++x) {
-                    const size_t i = ((size_t)z * V.ny + y) * V.nx + x, o = ((size_t)z * V.py + y) * V.px + x;
-                    t[o] = target[i] ? 1 : 0;
-                    if (bias) bb[o] = bias[i];
-                }
-        LSS_CUDA(cudaMemcpyAsync(tgt, t.data(), P, cudaMemcpyHostToDevice, st));
-        if (bias) {
-            float* bd = F();
-            LSS_CUDA(cudaMemcpyAsync(bd, bb.data(), P * 4, cudaMemcpyHostToDevice, st));
-            V.bias = bd;
+    auto count_k = [&](int k) { return counts + k; };
+    // Target and bias into the padded layout on the device (pinned host
+    // buffers are read in place, pageable ones through the copy engine into
+    // fw[0], which is free until the forward starts).
+    const uint64_t n = (uint64_t)V.nx * V.ny * V.nz;
+    auto upload = [&](auto* dst, const auto* host) {
+        using T = std::remove_cv_t<std::remove_pointer_t<decltype(host)>>;
+        const T* src = (const T*)pinned_device_ptr(host);
+        if (!src) {
+            T* stage = (T*)(void*)fw[0];
+            LSS_CUDA(cudaMemcpyAsync(stage, host, n * sizeof(T), cudaMemcpyHostToDevice, st));
+            src = stage;
         }
-        owner->sync();  // host staging buffers go out of scope
+        k_ns_scatter<<<grid, 256, 0, st>>>(dst, src, V.nx, V.ny, V.nz, V.px, V.py);
+        count_launch(owner);
+    };
+    LSS_CUDA(cudaMemsetAsync(tgt, 0, P, st));
+    upload(tgt, target);
+    if (bias) {
+        float* bd = F();
+        LSS_CUDA(cudaMemsetAsync(bd, 0, P * 4, st));
+        upload(bd, bias);
+        V.bias = bd;
     }
-    for (float* p : {fw[0], fw[1], lam[0], lam[1]}) LSS_CUDA(cudaMemsetAsync(p, 0, P * 4, st));
     if (dbias_d) LSS_CUDA(cudaMemsetAsync(dbias_d, 0, P * 4, st));
-    LSS_CUDA(cudaMemsetAsync(gsum, 0, 8 * sizeof(double), st));
-    const int grid = owner->num_sms * 8;
-    auto count = [&]() { ++owner->launches; LSS_CUDA(cudaGetLastError()); };
-    // Forward from the engine's current phi and active set.
-    LSS_CUDA(cudaMemcpyAsync(ck[0], V.phi[core.parity()], P * 4, cudaMemcpyDeviceToDevice, st));
+    LSS_CUDA(cudaMemsetAsync(gsum, 0, 8 * sizeof(double) + 8, st));
+    LSS_CUDA(cudaMemsetAsync(act[1], 0, (uint64_t)K * al(mwords * 8), st));  // act[1..K] are contiguous
+    LSS_CUDA(cudaMemsetAsync(flag[0], 0, (uint64_t)(K + 1) * al((uint64_t)nb * 4), st));
+    LSS_CUDA(cudaMemsetAsync(counts, 0, (uint64_t)(K + 1) * 4, st));
+    auto count = [&]() { count_launch(owner); };
+    // Forward from the engine's current phi and active set: both buffers of
+    // the pair and the first checkpoint hold phi_0.
+    const float* phi0 = V.phi[core.parity()];
+    for (float* d : {ck[0], fw[0], fw[1]})
+        LSS_CUDA(cudaMemcpyAsync(d, phi0, P * 4, cudaMemcpyDeviceToDevice, st));
     LSS_CUDA(cudaMemcpyAsync(act[0], core.masks(core.parity()), mwords * 8, cudaMemcpyDeviceToDevice, st));
-    const float* cur = ck[0];
-    for (int k = 0; k < K; ++k) {
-        float* dst = ((k + 1) % every == 0 && k + 1 < K) ? ck[(k + 1) / every] : fw[k & 1];
-        LSS_CUDA(cudaMemsetAsync(act[k + 1], 0, mwords * 8, st));
-        k_adj_update<S><<<grid, 256, 0, st>>>(V, cur, dst, act[k], chg, nb);
-        count();
-        k_adj_dilate<S><<<grid, 256, 0, st>>>(V, chg, act[k + 1], nb);
-        count();
-        cur = dst;
-    }
-    // Loss and lambda_K.
-    k_adj_dice_sums<<<grid, 256, 0, st>>>(V, cur, tgt, tau, gsum + 4);
+    k_adj_list0<S><<<(nb + 255) / 256, 256, 0, st>>>(act[0], flag[0], list[0], count_k(0), nb);
     count();
-    k_adj_dice_grad<<<grid, 256, 0, st>>>(V, cur, tgt, tau, gsum + 4, lam[K & 1]);
+    for (int k = 0; k < K; ++k) {
+        const float* src = fw[k & 1];
+        float* dst = fw[(k + 1) & 1];
+        k_adj_update<S><<<bgrid, 256, 0, st>>>(V, src, dst, act[k], list[k], count_k(k),
+                                               k ? list[k - 1] : nullptr, k ? count_k(k - 1) : nullptr, flag[k],
+                                               chg, nact);
+        count();
+        k_adj_dilate<S><<<grid, 256, 0, st>>>(V, chg, list[k], count_k(k), act[k + 1], flag[k + 1], list[k + 1],
+                                              count_k(k + 1));
+        count();
+        if ((k + 1) % every == 0 && k + 1 < K)
+            LSS_CUDA(cudaMemcpyAsync(ck[(k + 1) / every], dst, P * 4, cudaMemcpyDeviceToDevice, st));
+    }
+    const float* phiK = fw[K & 1];
+    // Loss and lambda_K.
+    k_adj_dice_sums<<<grid, 256, 0, st>>>(V, phiK, tgt, tau, gsum + 4);
+    count();
+    k_adj_dice_grad<<<grid, 256, 0, st>>>(V, phiK, tgt, tau, gsum + 4, lam);
     count();
     // Reverse, segment by segment from the last checkpoint.
     for (int sgi = nck - 1; sgi >= 0; --sgi) {
         const int s0 = sgi * every, s1 = std::min(K, s0 + every);
         seg[0] = ck[sgi];
         for (int k = s0; k + 1 < s1; ++k) {
-            k_adj_update<S><<<grid, 256, 0, st>>>(V, seg[k - s0], seg[k - s0 + 1], act[k], nullptr, nb);
+            float* d = seg[k - s0 + 1];
+            LSS_CUDA(cudaMemcpyAsync(d, seg[k - s0], P * 4, cudaMemcpyDeviceToDevice, st));
+            k_adj_update<S><<<bgrid, 256, 0, st>>>(V, seg[k - s0], d, act[k], list[k], count_k(k), nullptr,
+                                                   nullptr, nullptr, nullptr, nullptr);
             count();
         }
         for (int k = s1 - 1; k >= s0; --k) {
-            float* nxt = lam[(k + 1) & 1];
-            float* l = lam[k & 1];
-            k_adj_lambda_init<S><<<grid, 256, 0, st>>>(V, act[k], nxt, l, nb);
+            k_adj_take<S><<<bgrid, 256, 0, st>>>(V, act[k], list[k], count_k(k), lam, U);
             count();
-            k_adj_vjp<S><<<grid, 256, 0, st>>>(V, seg[k - s0], act[k], nxt, l, dbias_d, gsum, nb);
+            k_adj_vjp<S><<<bgrid, 256, 0, st>>>(V, seg[k - s0], act[k], list[k], count_k(k), U, lam, dbias_d, gsum);
             count();
         }
     }
-    double h[8];
-    LSS_CUDA(cudaMemcpyAsync(h, gsum, sizeof(h), cudaMemcpyDeviceToHost, st));
-    std::vector<float> db;
+    // d_bias back to the caller's unpadded layout (in place when pinned).
     if (dbias) {
-        db.resize(P);
-        LSS_CUDA(cudaMemcpyAsync(db.data(), dbias_d, P * 4, cudaMemcpyDeviceToHost, st));
+        float* dev = (float*)pinned_device_ptr(dbias);
+        k_ns_gather<<<grid, 256, 0, st>>>(dev ? dev : fw[0], dbias_d, V.nx, V.ny, V.nz, V.px, V.py);
+        count();
+        if (!dev) LSS_CUDA(cudaMemcpyAsync(dbias, fw[0], n * 4, cudaMemcpyDeviceToHost, st));
     }
+    double h[8];
+    unsigned long long na = 0;
+    LSS_CUDA(cudaMemcpyAsync(h, gsum, sizeof(h), cudaMemcpyDeviceToHost, st));
+    LSS_CUDA(cudaMemcpyAsync(&na, nact, 8, cudaMemcpyDeviceToHost, st));
     owner->sync();
     const double den = h[4] + h[5];
     out->loss = 1.0 - 2.0 * h[6] / den;
     out->d_target = h[0];
     out->d_window = h[1];
     out->d_curvature = h[2];
-    if (dbias)
-        for (int z = 0; z < V.nz; ++z)
-            for (int y = 0; y < V.ny; ++y)
-                for (int x = 0; x < V.nx; ++x)
-                    dbias[((size_t)z * V.ny + y) * V.nx + x] = db[((size_t)z * V.py + y) * V.px + x];
+    out->active_voxel_iterations = na;
 }
 
 }  // namespace

@@ -71,6 +71,11 @@ class NsCore {
     int block_threads() const { return block_threads_; }
     int words() const { return words_; }
     uint64_t budget_left() const { return arena_.budget_left(); }
+    // A device workspace of at least `bytes`, kept between calls (the
+    // adjoint's checkpoints, adjoint fields and recorded sets) and freed with
+    // the volume; grown when a call needs more.  Counted against the HBM
+    // budget.
+    void* workspace(uint64_t bytes);
     const unsigned long long* masks(uint32_t parity) const { return d_masks_[parity & 1u]; }
     NsVol descriptor(int v) const;  // host copy of the device descriptor of volume v
     EngineBase* owner() const { return owner_; }
@@ -124,6 +129,8 @@ class NsCore {
     uint64_t* d_status_ = nullptr;
     NsCtl* d_ctl_ = nullptr;
     uint32_t* d_misc_ = nullptr;
+    void* ws_ = nullptr;
+    uint64_t ws_bytes_ = 0;
 };
 
 }  // namespace lss

@@ -46,30 +46,6 @@ void encode_tmap_f32_3d(CUtensorMap* out, const float* base, uint64_t nx, uint64
 
 namespace {
 
-// Unpadded fields (x fastest, rows of nx) <-> padded device fields (pitch px,
-// py).  Block i takes the rows (y, z) i, i + gridDim.x, ... and its threads
-// cover x, so there is one division a row, none an element.  The host side
-// of an unpadded field may be pinned host memory read or written in place.
-__global__ void k_ns_scatter(float* dst, const float* src, int nx, int ny, int nz, int px, int py) {
-    const uint32_t rows = (uint32_t)ny * (uint32_t)nz;
-    for (uint32_t r = blockIdx.x; r < rows; r += gridDim.x) {
-        const uint32_t z = r / (uint32_t)ny, y = r - z * (uint32_t)ny;
-        const float* s = src + (size_t)r * nx;
-        float* d = dst + ((size_t)z * py + y) * px;
-        for (int x = threadIdx.x; x < nx; x += blockDim.x) d[x] = s[x];
-    }
-}
-
-__global__ void k_ns_gather(float* dst, const float* src, int nx, int ny, int nz, int px, int py) {
-    const uint32_t rows = (uint32_t)ny * (uint32_t)nz;
-    for (uint32_t r = blockIdx.x; r < rows; r += gridDim.x) {
-        const uint32_t z = r / (uint32_t)ny, y = r - z * (uint32_t)ny;
-        const float* s = src + ((size_t)z * py + y) * px;
-        float* d = dst + (size_t)r * nx;
-        for (int x = threadIdx.x; x < nx; x += blockDim.x) d[x] = s[x];
-    }
-}
-
 // dst[i] = phi <= 0 at unpadded voxel i, or'ed with frozen[i] (may be null;
 // dst may be frozen itself: each element is read and written by one thread).
 // Four voxels a thread, one 4-byte store, when the rows and both byte
@@ -283,19 +259,15 @@ static KernelSet kernels(const BrickConfig& c) {
 NsCore::NsCore(EngineBase* owner, uint64_t budget) : owner_(owner), arena_(budget), brick_arena_(0) {}
 NsCore::~NsCore() = default;
 
-// Device address of a host buffer in pinned host memory (cudaHostAlloc or
-// cudaHostRegister, mapped into the device's address space under unified
-// addressing), or null for pageable memory.  Kernels read or write pinned
-// buffers in place over the host link: as fast as a copy-engine transfer
-// (about 200 GB/s each way on GB300), with no device staging buffer and no
-// second pass.
-static void* pinned_device_ptr(const void* host) {
-    cudaPointerAttributes a{};
-    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
-        cudaGetLastError();
-        return nullptr;
+void* NsCore::workspace(uint64_t bytes) {
+    if (bytes > ws_bytes_) {
+        if (ws_) arena_.free_last(ws_);
+        ws_ = nullptr;
+        ws_bytes_ = 0;
+        ws_ = arena_.alloc(bytes);
+        ws_bytes_ = bytes;
     }
-    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+    return ws_;
 }
 
 // Unpadded host field -> padded device field dst of volume V.  Pageable host

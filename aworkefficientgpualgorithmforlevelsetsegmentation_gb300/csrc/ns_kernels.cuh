@@ -695,6 +695,32 @@ __device__ __forceinline__ StopState stop_state(int32_t* base, int nvol) {
     return s;
 }
 
+// Unpadded fields (x fastest, rows of nx) <-> padded device fields (pitch px,
+// py).  Block i takes the rows (y, z) i, i + gridDim.x, ... and its threads
+// cover x, so there is one division a row, none an element.  The unpadded
+// side may be pinned host memory read or written in place.
+template <class T>
+__global__ void k_ns_scatter(T* dst, const T* src, int nx, int ny, int nz, int px, int py) {
+    const uint32_t rows = (uint32_t)ny * (uint32_t)nz;
+    for (uint32_t r = blockIdx.x; r < rows; r += gridDim.x) {
+        const uint32_t z = r / (uint32_t)ny, y = r - z * (uint32_t)ny;
+        const T* s = src + (size_t)r * nx;
+        T* d = dst + ((size_t)z * py + y) * px;
+        for (int x = threadIdx.x; x < nx; x += blockDim.x) d[x] = s[x];
+    }
+}
+
+template <class T>
+__global__ void k_ns_gather(T* dst, const T* src, int nx, int ny, int nz, int px, int py) {
+    const uint32_t rows = (uint32_t)ny * (uint32_t)nz;
+    for (uint32_t r = blockIdx.x; r < rows; r += gridDim.x) {
+        const uint32_t z = r / (uint32_t)ny, y = r - z * (uint32_t)ny;
+        const T* s = src + ((size_t)z * py + y) * px;
+        T* d = dst + (size_t)r * nx;
+        for (int x = threadIdx.x; x < nx; x += blockDim.x) d[x] = s[x];
+    }
+}
+
 constexpr uint32_t kNoBrick = 0xFFFFFFFFu;  // a brick of a finished volume
 
 // Position of the s-th set bit (from 0, counted from bit 0) of m; s < popc(m).

@@ -244,16 +244,17 @@ class Segmenter:
         return {k: getattr(s, k) for k, _ in L.lss_stats._fields_}
 
     def adjoint(self, K: int, checkpoint_every: int, target_mask: np.ndarray, sigmoid_scale: float = 0.5,
-                bias: np.ndarray | None = None, want_dbias: bool = True):
+                bias: np.ndarray | None = None, want_dbias: bool = True, d_bias_out=None):
         t = np.ascontiguousarray(target_mask, np.uint8)
         b = None if bias is None else np.ascontiguousarray(bias, np.float32)
-        db = np.zeros(self.shape, np.float32) if want_dbias else None
+        db = _out(d_bias_out, self.shape, np.float32) if want_dbias else None
         g = L.lss_grads()
         self._chk(self._lib.lss_adjoint_run(self._h, K, checkpoint_every, _ptr(t), sigmoid_scale,
                                             None if b is None else _ptr(b),
                                             None if db is None else _ptr(db), C.byref(g)))
         return {"loss": g.loss, "d_target": g.d_target, "d_window": g.d_window,
-                "d_curvature": g.d_curvature, "d_bias": db}
+                "d_curvature": g.d_curvature, "d_bias": db,
+                "active_voxel_iterations": g.active_voxel_iterations}
 
 
 class Batch:

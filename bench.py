@@ -37,6 +37,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 BYTES_PER_UPDATE = 20
+# Adjoint: phi 4, I 4, bias 4, lambda in 4 and out 4, bias gradient 8.
+ADJOINT_BYTES = 28
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -483,6 +485,86 @@ def run_stress(args, ws, rank, local):
               flush=True)
 
 
+def run_adjoint(args, ws, rank, local):
+    """Differentiation form: the 192^3 two-shell phantom, K = 64 unrolled
+    iterations from the seed, phi checkpointed every 8, soft-Dice loss of
+    sigmoid(-phi/0.5) against the inner ellipsoid.  One step = one
+    lss_adjoint_run: the forward records the K active sets, the loss, the
+    reverse pass recomputes each segment from its checkpoint and scatters the
+    transposed stencil Jacobian, giving dloss/dT, deps, dalpha and the bias
+    volume's gradient.  Target, bias and the bias gradient live in pinned host
+    buffers.  The metric is active-voxel iterations (the sum over the forward
+    iterations of the active voxels updated) per second of the whole call;
+    the roofline counts 28 bytes each (phi, I, bias, lambda in and out, the
+    bias gradient read and written)."""
+    import ctypes
+    import torch
+    import aworkefficientgpualgorithmforlevelsetsegmentation_gb300 as lss
+    from aworkefficientgpualgorithmforlevelsetsegmentation_gb300 import phantoms as P
+
+    torch.cuda.set_device(local)
+    cfg = P.config4(args.scale)
+    p = cfg["params"]
+    K, every = cfg["K"], cfg["checkpoint_every"]
+    seg = lss.Segmenter(lss.MODE_NS, device=local, brick=(8, 8, 8), threads_per_brick=256)
+    stream = torch.cuda.Stream(device=local)
+    seg._chk(seg._lib.lss_set_stream(seg._h, ctypes.c_void_p(stream.cuda_stream)))
+    seg.load_volume(cfg["image"])
+    seg.set_parameters(p.target, p.window, p.curvature, p.time_step, alpha_role=p.alpha_role)
+    seg.set_phi(cfg["phi0"])
+    shape = cfg["image"].shape
+
+    def pinned(dt):
+        return torch.empty(shape, dtype=dt, pin_memory=True).numpy()
+
+    tgt, bias, dbias = pinned(torch.uint8), pinned(torch.float32), pinned(torch.float32)
+    tgt[...] = cfg["target"]
+    bias[...] = 0.0
+    for _ in range(args.warmup):
+        g = seg.adjoint(K, every, tgt, 0.5, bias=bias, d_bias_out=dbias)
+    torch.cuda.synchronize()
+    barrier(ws)
+    ev_ms, nact = 0.0, 0
+    launches0 = seg.stats()["kernel_launches"]
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            g = seg.adjoint(K, every, tgt, 0.5, bias=bias, d_bias_out=dbias)
+            e1.record(stream)
+            e1.synchronize()
+            ev_ms += e0.elapsed_time(e1)
+            nact += g["active_voxel_iterations"]
+    launches = (seg.stats()["kernel_launches"] - launches0) // args.steps
+    torch.cuda.synchronize()
+    barrier(ws)
+    t_max = max_over_ranks(ws, ev_ms)
+    value = sum_over_ranks(ws, float(nact)) / (t_max / 1e3)
+    peak, peak_kind = measured_peak()
+    achieved = ADJOINT_BYTES * nact / (ev_ms / 1e3) / 1e9
+    if rank == 0:
+        line = {
+            "metric": "adjoint_active_voxel_iterations_per_s", "value": value,
+            "unit": "active_voxel_iterations/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": cfg["name"] + "_two_shell_adjoint", "K": K, "checkpoint_every": every,
+                       "loss": g["loss"], "d_target": g["d_target"], "d_window": g["d_window"],
+                       "d_curvature": g["d_curvature"],
+                       "active_voxel_iterations_per_call": int(g["active_voxel_iterations"]),
+                       "brick": [8, 8, 8], "threads_per_brick": 256,
+                       "host_buffers": "pinned (target, bias, bias gradient)",
+                       "parallelism": "replicas" if ws > 1 else "single"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                         "bytes_per_update": ADJOINT_BYTES},
+            "gpu_launches": int(launches),
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+
+
 def run_tour(args, ws, rank, local):
     """Every kernel of the library once, on small inputs (for a per-kernel
     ncu launch list with DRAM bytes): the REF engine (u8 volume: seed, steps
@@ -554,7 +636,7 @@ def main():
     ap.add_argument("--ref-step-iters", type=int, default=80)
     ap.add_argument("--dense-iters", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "stress", "tour"])
+    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "stress", "tour", "adjoint"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     ws, rank, local = dist_env()
@@ -569,6 +651,8 @@ def main():
         run_stress(args, ws, rank, local)
     elif args.workload == "tour":
         run_tour(args, ws, rank, local)
+    elif args.workload == "adjoint":
+        run_adjoint(args, ws, rank, local)
     else:
         run_ours(args, ws, rank, local)
     if ws > 1:

@@ -281,6 +281,8 @@ typedef struct lss_grads {
     double d_target;     /* dloss/dT                                  */
     double d_window;     /* dloss/deps                                */
     double d_curvature;  /* dloss/dalpha                              */
+    uint64_t active_voxel_iterations; /* sum over the K forward iterations of
+                                         the active voxels updated          */
 } lss_grads;
 
 /* Runs K iterations from the current state with the active set of each

@@ -42,6 +42,18 @@ def test_gpu_adjoint_matches_fp64_adjoint(brick, threads, K, every):
     bias = (0.05 * rng.standard_normal(cfg["image"].shape)).astype(np.float32)
     g = make(cfg, brick, threads).adjoint(K, every, cfg["target"], 0.5, bias=bias)
     o = oracle_adjoint(cfg, K, bias)
+    # Pinned host buffers for the bias, the target and the bias gradient are
+    # read and written in place: same results.
+    torch = pytest.importorskip("torch")
+    pb = torch.empty(bias.shape, dtype=torch.float32, pin_memory=True).numpy()
+    pt = torch.empty(bias.shape, dtype=torch.uint8, pin_memory=True).numpy()
+    pb[...], pt[...] = bias, cfg["target"]
+    db_pinned = torch.empty(bias.shape, dtype=torch.float32, pin_memory=True).numpy()
+    gp = make(cfg, brick, threads).adjoint(K, every, pt, 0.5, bias=pb, d_bias_out=db_pinned)
+    # (The float atomics of the reverse pass sum in no fixed order.)
+    assert gp["d_bias"] is db_pinned and np.allclose(db_pinned, g["d_bias"], rtol=1e-4, atol=1e-9)
+    assert rel(gp["loss"], g["loss"]) <= 1e-9 and rel(gp["d_target"], g["d_target"]) <= 1e-5
+    assert gp["active_voxel_iterations"] == g["active_voxel_iterations"] > 0
     assert abs(g["loss"] - o["loss"]) <= 1e-5
     for key in ("d_target", "d_window", "d_curvature"):
         assert rel(g[key], o[key]) <= 1e-3, (key, g[key], o[key])
@@ -53,12 +65,18 @@ def test_gpu_adjoint_checkpoint_spacing_is_invisible():
     cfg = P.config4(0.25)
     s = make(cfg)
     ref = s.adjoint(20, 20, cfg["target"])
+    # The forward's recorded sets are the sparse engine's: the same number of
+    # active-voxel updates over the same 20 iterations.
+    fresh = make(cfg)
+    fresh.step(20)
+    assert ref["active_voxel_iterations"] == fresh.stats()["voxel_updates"] > 0
     for every in (1, 4, 7):
         g = s.adjoint(20, every, cfg["target"])
         assert g["loss"] == ref["loss"]
         for key in ("d_target", "d_window", "d_curvature"):
             assert rel(g[key], ref[key]) <= 1e-5
         assert np.allclose(g["d_bias"], ref["d_bias"], rtol=1e-4, atol=1e-9)
+        assert g["active_voxel_iterations"] == ref["active_voxel_iterations"]
 
 
 def test_gpu_adjoint_leaves_engine_state():
