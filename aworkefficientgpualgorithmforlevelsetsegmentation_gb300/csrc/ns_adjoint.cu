@@ -7,7 +7,8 @@
 // Work-efficient like the forward engine: every iteration touches the bricks
 // of its active set only.  The forward keeps the brick list of each A_k
 // (built while dilating: the first thread to put a word into a brick appends
-// it) beside the recorded brick masks.  It runs over a ping-pong pair in
+// it; the block that updates a brick dilates it) beside the recorded brick
+// masks.  It runs over a ping-pong pair in
 // which both buffers stay current: iteration k writes the bricks of A_k
 // whole (active voxels updated, the rest copied) and copies across the
 // bricks of A_{k-1} that left the set; the changed voxels' ballot words are
@@ -70,25 +71,62 @@ __global__ void __launch_bounds__(256) k_adj_list0(const unsigned long long* __r
     }
 }
 
+// The changed-voxel ballot words of one brick (chg, CHG words) dilated into
+// its 27 neighbours' masks of A_{k+1}; the first thread to put a word into a
+// brick appends the brick to list_{k+1}.  Threads t0, t0 + stride, ... take
+// the (neighbour, mask word) pairs.
+template <class S>
+__device__ __forceinline__ void adj_dilate_brick(const NsVol& V, uint32_t b, const uint32_t* chg, int t0, int stride,
+                                                 unsigned long long* nxt, uint32_t* flag_next, uint32_t* list_next,
+                                                 uint32_t* count_next) {
+    const int3 o = brick_origin<S>(V, b + V.brick_base);
+    for (int r = t0; r < 27 * S::WORDS; r += stride) {
+        const int slot = r / S::WORDS, w = r % S::WORDS;
+        const int ox = slot % 3 - 1, oy = (slot / 3) % 3 - 1, oz = slot / 9 - 1;
+        const int bx = o.x / S::X + ox, by = o.y / S::Y + oy, bz = o.z / S::Z + oz;
+        const int lx = V.nx - bx * S::X, ly = V.ny - by * S::Y, lz = V.nz - bz * S::Z;
+        if (bx < 0 || by < 0 || bz < 0 || lx <= 0 || ly <= 0 || lz <= 0) continue;
+        uint64_t x = dilate_word<S>(chg, ox, oy, oz, w, V.nbh);
+        if (lx < S::X || ly < S::Y || lz < S::Z)
+            x &= inside_mask<S>(w, min(lx, S::X), min(ly, S::Y), min(lz, S::Z));
+        if (!x) continue;
+        const uint32_t nbi = b + (int32_t)((oz * V.nby + oy) * V.nbx + ox);
+        atomicOr(&nxt[(size_t)nbi * S::WORDS + w], (unsigned long long)x);
+        if (*(volatile uint32_t*)&flag_next[nbi] == 0u && atomicExch(&flag_next[nbi], 1u) == 0u)
+            list_next[atomicAdd(count_next, 1u)] = nbi;
+    }
+}
+
 // Iteration k: block per brick.  The bricks of list_k are written whole into
 // out (active voxels updated from in, the others copied); with `prev` (the
 // recorded forward's ping-pong pair), the bricks of list_{k-1} not in
 // list_k (flag_k clear) are copied from in to out, so that out equals in
-// outside the bricks of A_k.  With chg: the changed voxels' ballot words of
-// list_k's bricks and the count of updated voxels added to *nact.
+// outside the bricks of A_k.  With nxt (the recorded forward, not a
+// recomputation): each updated brick's changed voxels are dilated into A_{k+1}
+// by the same block (adj_dilate_brick) and the updated voxels are counted
+// into *nact.
 template <class S>
 __global__ void __launch_bounds__(256) k_adj_update(NsVol V, const float* __restrict__ in, float* __restrict__ out,
                                                     const unsigned long long* __restrict__ act,
                                                     const uint32_t* __restrict__ list, const uint32_t* count,
                                                     const uint32_t* __restrict__ prev, const uint32_t* prev_count,
-                                                    const uint32_t* __restrict__ flag_k, uint32_t* __restrict__ chg,
+                                                    const uint32_t* __restrict__ flag_k, unsigned long long* nxt,
+                                                    uint32_t* flag_next, uint32_t* list_next, uint32_t* count_next,
                                                     unsigned long long* nact) {
+    __shared__ uint32_t chg[S::CHG];
+    __shared__ uint32_t any;
     const uint32_t n = *count, np = prev ? *prev_count : 0u;
     uint32_t mine = 0;
     for (uint32_t i = blockIdx.x; i < n + np; i += gridDim.x) {
         const bool upd = i < n;
         const uint32_t b = upd ? list[i] : prev[i - n];
-        if (!upd && flag_k[b]) continue;  // also in list_k: written above
+        if (!upd && flag_k[b]) continue;  // also in list_k: written above (uniform over the block)
+        const bool dil = nxt && upd;      // uniform over the block
+        if (dil) {
+            __syncthreads();  // chg and any free: the previous brick's dilation is done
+            if (threadIdx.x == 0) any = 0u;
+            __syncthreads();
+        }
         for (int j = threadIdx.x; j < S::VOX; j += blockDim.x) {
             const int3 p = voxel_of<S>(V, b, j);
             bool changed = false;
@@ -109,50 +147,22 @@ __global__ void __launch_bounds__(256) k_adj_update(NsVol V, const float* __rest
                 }
             }
             // VOX is a multiple of 32: a warp's slots are all in or all out.
-            if (chg && upd) {
+            if (dil) {
                 const uint32_t bal = __ballot_sync(0xffffffffu, changed);
-                if ((threadIdx.x & 31) == 0) chg[(size_t)b * S::CHG + (j >> 5)] = bal;
+                if ((threadIdx.x & 31) == 0) {
+                    chg[j >> 5] = bal;
+                    if (bal) any = 1u;
+                }
             }
+        }
+        if (dil) {
+            __syncthreads();  // chg and any complete
+            if (any) adj_dilate_brick<S>(V, b, chg, threadIdx.x, blockDim.x, nxt, flag_next, list_next, count_next);
         }
     }
     if (nact) {
         mine = __reduce_add_sync(0xffffffffu, mine);
         if ((threadIdx.x & 31) == 0 && mine) atomicAdd(nact, (unsigned long long)mine);
-    }
-}
-
-// A_{k+1}: the changed words of list_k's bricks dilated into their 27
-// neighbours (one thread per brick, neighbour and mask word); the first
-// thread to put a word into a brick appends the brick to list_{k+1}.
-template <class S>
-__global__ void __launch_bounds__(256) k_adj_dilate(NsVol V, const uint32_t* __restrict__ chg,
-                                                    const uint32_t* __restrict__ list, const uint32_t* count,
-                                                    unsigned long long* __restrict__ nxt, uint32_t* flag_next,
-                                                    uint32_t* list_next, uint32_t* count_next) {
-    constexpr int PER = 27 * S::WORDS;
-    const uint64_t total = (uint64_t)(*count) * PER;
-    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
-         t += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t b = list[t / PER];
-        const int r = (int)(t % PER), slot = r / S::WORDS, w = r % S::WORDS;
-        const uint32_t* cb = chg + (size_t)b * S::CHG;
-        uint32_t any = 0;
-#pragma unroll
-        for (int q = 0; q < S::CHG; ++q) any |= cb[q];
-        if (!any) continue;
-        const int3 o = brick_origin<S>(V, b + V.brick_base);
-        const int ox = slot % 3 - 1, oy = (slot / 3) % 3 - 1, oz = slot / 9 - 1;
-        const int bx = o.x / S::X + ox, by = o.y / S::Y + oy, bz = o.z / S::Z + oz;
-        const int lx = V.nx - bx * S::X, ly = V.ny - by * S::Y, lz = V.nz - bz * S::Z;
-        if (bx < 0 || by < 0 || bz < 0 || lx <= 0 || ly <= 0 || lz <= 0) continue;
-        uint64_t x = dilate_word<S>(cb, ox, oy, oz, w, V.nbh);
-        if (lx < S::X || ly < S::Y || lz < S::Z)
-            x &= inside_mask<S>(w, min(lx, S::X), min(ly, S::Y), min(lz, S::Z));
-        if (!x) continue;
-        const uint32_t nbi = b + (int32_t)((oz * V.nby + oy) * V.nbx + ox);
-        atomicOr(&nxt[(size_t)nbi * S::WORDS + w], (unsigned long long)x);
-        if (*(volatile uint32_t*)&flag_next[nbi] == 0u && atomicExch(&flag_next[nbi], 1u) == 0u)
-            list_next[atomicAdd(count_next, 1u)] = nbi;
     }
 }
 
@@ -268,7 +278,10 @@ __device__ __forceinline__ void ns_update_vjp_f32(PF P, AF add, float I, float b
     g4[2] += lam * (V.alpha_data ? du_dalpha : -du_dalpha);
 }
 
-// Block sum of three doubles into gsum[0..2] (one atomic each per block).
+// Block sum of three doubles into gsum[0..2] (one atomic each per block;
+// none for a zero sum, which changes nothing: most blocks of a sparse
+// reverse iteration hold no active brick, and the atomics of one address
+// serialise).
 __device__ __forceinline__ void block_sum3(double a0, double a1, double a2, double* gsum) {
     __shared__ double s[3][32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -291,9 +304,9 @@ __device__ __forceinline__ void block_sum3(double a0, double a1, double a2, doub
             a2 += __shfl_down_sync(0xffffffffu, a2, o);
         }
         if (lane == 0) {
-            atomicAdd(&gsum[0], a0);
-            atomicAdd(&gsum[1], a1);
-            atomicAdd(&gsum[2], a2);
+            if (a0 != 0.0) atomicAdd(&gsum[0], a0);
+            if (a1 != 0.0) atomicAdd(&gsum[1], a1);
+            if (a2 != 0.0) atomicAdd(&gsum[2], a2);
         }
     }
     __syncthreads();
@@ -398,7 +411,7 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     // 256-byte aligned parts.
     auto al = [](uint64_t b) { return (b + 255) / 256 * 256; };
     const uint64_t nfields = (uint64_t)nck + (every - 1) + 4 + (dbias ? 1 : 0) + (bias ? 1 : 0);
-    const uint64_t total = nfields * al(P * 4) + (uint64_t)(K + 1) * al(mwords * 8) + al((uint64_t)nb * S::CHG * 4) +
+    const uint64_t total = nfields * al(P * 4) + (uint64_t)(K + 1) * al(mwords * 8) +
                            2 * (uint64_t)(K + 1) * al((uint64_t)nb * 4) + al((uint64_t)(K + 1) * 4) + al(P) + 256;
     char* base = (char*)core.workspace(total);
     auto carve = [&](uint64_t bytes) {
@@ -415,7 +428,6 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     float* U = F();
     std::vector<unsigned long long*> act(K + 1);
     for (auto& a : act) a = (unsigned long long*)carve(mwords * 8);
-    uint32_t* chg = (uint32_t*)carve((size_t)nb * S::CHG * 4);
     std::vector<uint32_t*> list(K + 1), flag(K + 1);
     for (auto& l : list) l = (uint32_t*)carve((uint64_t)nb * 4);
     for (auto& f : flag) f = (uint32_t*)carve((uint64_t)nb * 4);
@@ -467,10 +479,7 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
         float* dst = fw[(k + 1) & 1];
         k_adj_update<S><<<bgrid, 256, 0, st>>>(V, src, dst, act[k], list[k], count_k(k),
                                                k ? list[k - 1] : nullptr, k ? count_k(k - 1) : nullptr, flag[k],
-                                               chg, nact);
-        count();
-        k_adj_dilate<S><<<grid, 256, 0, st>>>(V, chg, list[k], count_k(k), act[k + 1], flag[k + 1], list[k + 1],
-                                              count_k(k + 1));
+                                               act[k + 1], flag[k + 1], list[k + 1], count_k(k + 1), nact);
         count();
         if ((k + 1) % every == 0 && k + 1 < K)
             LSS_CUDA(cudaMemcpyAsync(ck[(k + 1) / every], dst, P * 4, cudaMemcpyDeviceToDevice, st));
@@ -489,7 +498,7 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
             float* d = seg[k - s0 + 1];
             LSS_CUDA(cudaMemcpyAsync(d, seg[k - s0], P * 4, cudaMemcpyDeviceToDevice, st));
             k_adj_update<S><<<bgrid, 256, 0, st>>>(V, seg[k - s0], d, act[k], list[k], count_k(k), nullptr,
-                                                   nullptr, nullptr, nullptr, nullptr);
+                                                   nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
             count();
         }
         for (int k = s1 - 1; k >= s0; --k) {
