@@ -536,6 +536,7 @@ void ns_adjoint(NsCore& core, int K, int every, const uint8_t* target, float tau
     LSS_REQUIRE(core.initialized(), LSS_ERR_STATE, "no seed or phi set");
     LSS_REQUIRE(K > 0 && every > 0 && target && out && tau > 0.0f, LSS_ERR_INVALID_ARGUMENT,
                 "bad adjoint arguments");
+    every = std::min(every, K);  // one segment holds all K iterations at most
     const BrickConfig& c = core.config();
     if (c.bx == 8 && c.by == 8 && c.bz == 8) return run_adjoint<Brick<8, 8, 8>>(core, K, every, target, tau, bias, dbias, out);
     if (c.bx == 8 && c.by == 8 && c.bz == 4) return run_adjoint<Brick<8, 8, 4>>(core, K, every, target, tau, bias, dbias, out);
