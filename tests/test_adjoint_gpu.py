@@ -61,6 +61,25 @@ def test_gpu_adjoint_matches_fp64_adjoint(brick, threads, K, every):
     assert np.linalg.norm(db - ob) <= 1e-3 * np.linalg.norm(ob)
 
 
+def test_gpu_adjoint_ragged_volume_matches_fp64_adjoint():
+    """A volume whose sides are not multiples of the brick: partial bricks at
+    the far faces in the active lists, the dilation and the layout kernels."""
+    c = P.config4(0.25)
+    sl = (slice(3, 44), slice(1, 46), slice(5, 42))  # 41 x 45 x 37
+    cfg = dict(c, image=np.ascontiguousarray(c["image"][sl]), target=np.ascontiguousarray(c["target"][sl]),
+               phi0=np.ascontiguousarray(c["phi0"][sl]))
+    rng = np.random.default_rng(5)
+    bias = (0.05 * rng.standard_normal(cfg["image"].shape)).astype(np.float32)
+    for brick, threads in [((8, 8, 8), 256), ((4, 4, 4), 64)]:
+        g = make(cfg, brick, threads).adjoint(12, 5, cfg["target"], 0.5, bias=bias)
+        o = oracle_adjoint(cfg, 12, bias)
+        assert abs(g["loss"] - o["loss"]) <= 1e-5
+        for key in ("d_target", "d_window", "d_curvature"):
+            assert rel(g[key], o[key]) <= 1e-3, (brick, key, g[key], o[key])
+        db, ob = g["d_bias"].astype(np.float64), o["d_bias"]
+        assert np.linalg.norm(db - ob) <= 1e-3 * np.linalg.norm(ob)
+
+
 def test_gpu_adjoint_checkpoint_spacing_is_invisible():
     cfg = P.config4(0.25)
     s = make(cfg)
