@@ -109,12 +109,14 @@ extern "C" lss_status lss_compact_u32(const uint32_t* d_src, const uint32_t* d_v
 // Allocation-free variant.
 //
 // Some callers cannot allocate device memory at the moment they need a
-// compaction: code running inside a CUDA-graph capture that must not add
-// allocation nodes, real-time pipelines whose memory is reserved once at
-// start-up, or hosts whose allocator is owned by another framework.  For
+// compaction: real-time pipelines whose device memory is reserved once at
+// start-up, or hosts whose allocator is owned by another framework (a
+// cudaMalloc of their own would bypass its pool or its accounting).  For
 // them lss_compact_u32_noalloc keeps its scratch in this file-scope device
 // array instead of asking the stream-ordered allocator.  Every GPU that loads
 // the library holds the array (a little over 128 KiB) until the process exits.
+// The call reads the error word back and synchronises its stream before it
+// returns.
 namespace lss {
 
 // Largest n the allocation-free call accepts.

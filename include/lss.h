@@ -25,7 +25,8 @@
  *   LSS_MODE_NS   fp32 phi and intensity:
  *                   phi += dt * (wc * div(grad phi/|grad phi|) |grad phi|
  *                                - wd * D * |grad phi|_upwind),
- *                   D = clamp((eps - |I - T|) / eps, -1, 1) + bias,
+ *                   D = clamp((eps - |I - T|) / eps, -1, 1) + bias   (default), or
+ *                   D = eps - |I - T| + bias          (lss_params.data_term),
  *                 phi clamped to [phi_min, phi_max], inside = phi <= 0,
  *                 (wc, wd) = (1 - alpha, alpha) or (alpha, 1 - alpha) by
  *                 lss_params.alpha_role; bricked active set with 26-neighbour
@@ -41,7 +42,7 @@
 extern "C" {
 #endif
 
-#define LSS_ABI_VERSION 1
+#define LSS_ABI_VERSION 2
 
 typedef enum lss_status {
     LSS_OK                   = 0,
@@ -71,6 +72,13 @@ typedef enum lss_mode { LSS_MODE_REF = 0, LSS_MODE_NS = 1 } lss_mode;
  * (UpdateLevelSetVolume.cu:303; main.tex:178); LSS_ALPHA_DATA is
  * F = alpha*D + (1-alpha)*C (Lefohn et al. 2004), the default. */
 typedef enum lss_alpha_role { LSS_ALPHA_CURVATURE = 0, LSS_ALPHA_DATA = 1 } lss_alpha_role;
+
+/* The data speed D of LSS_MODE_NS.  LSS_DATA_NORMALISED (the default) is
+ * the paper's eps - |I - T| (main.tex:176) divided by eps as the reference's
+ * ComputeDensityTerm does (UpdateLevelSetVolume.cu:335-342) and clamped to
+ * [-1, 1], which keeps dt*|F| inside the upwind scheme's stability bound;
+ * LSS_DATA_LITERAL is eps - |I - T| as written, unscaled and unclamped. */
+typedef enum lss_data_term { LSS_DATA_NORMALISED = 0, LSS_DATA_LITERAL = 1 } lss_data_term;
 
 typedef struct lss_engine lss_engine;
 
@@ -104,6 +112,7 @@ typedef struct lss_params {
                                      (Segmenter.cpp:1053-1056)                          */
     int32_t neighbourhood;        /* expansion neighbourhood: 6 (REF) or 26 (NS)         */
     int32_t alpha_role;           /* NS: lss_alpha_role (default LSS_ALPHA_DATA)         */
+    int32_t data_term;            /* NS: lss_data_term (default LSS_DATA_NORMALISED)     */
 } lss_params;
 
 /* Stopping rule of lss_step_until_converged. */
@@ -311,17 +320,20 @@ lss_status lss_compact_u32(const uint32_t* d_src, const uint32_t* d_valid, uint3
 #define LSS_COMPACT_NOALLOC_MAX_ELEMENTS (1ull << 26)
 
 /* lss_compact_u32 for callers that cannot allocate device memory when they
- * compact: code inside a CUDA-graph capture that must not add allocations,
- * pipelines whose device memory is reserved once at start-up, hosts whose
- * allocator belongs to another framework.  No counterpart in the reference
+ * compact: pipelines whose device memory is reserved once at start-up, and
+ * hosts whose allocator belongs to another framework (an allocation of the
+ * library's own would bypass that allocator's pool and accounting).  No
+ * counterpart in the reference
  * (which allocates through CUDPP's plan).  Same arguments and result as
  * lss_compact_u32; allocates nothing: its scratch is a fixed device array of
  * the library (about 128 KiB, held by every GPU that loads the library until
  * the process exits).  n above LSS_COMPACT_NOALLOC_MAX_ELEMENTS returns
  * LSS_ERR_CAPACITY without touching the buffers.  The first call on a device
- * looks the array up on that device (make it before any stream capture).
- * All calls share the array: calls that overlap on the GPU (other streams,
- * other threads) race and must be serialised by the caller.  The call
+ * looks the array up on that device (with that device current); make that
+ * first call before any stream capture.  All calls share the array, which
+ * keeps the last call's contents (each call clears what it reads first):
+ * calls that overlap on the GPU (other streams, other threads) race and must
+ * be serialised by the caller.  The call reads a status word back and
  * synchronises `stream` before returning. */
 lss_status lss_compact_u32_noalloc(const uint32_t* d_src, const uint32_t* d_valid, uint32_t* d_dst,
                                    uint64_t n, uint64_t* d_count, void* stream);

@@ -1,9 +1,8 @@
 """The allocation-free compaction entry point (lss_compact_u32_noalloc).
 
 It serves callers that cannot allocate device memory when they compact
-(inside a graph capture, with memory reserved at start-up, under another
-framework's allocator), so its scratch is a fixed device array of the
-library.  This checks it through the C ABI against the allocating entry
+(device memory reserved once at start-up, or an allocator owned by another
+framework), so its scratch is a fixed device array of the library.  This checks it through the C ABI against the allocating entry
 point lss_compact_u32 on the same inputs, on two calls in a row (the second
 call must not see the first call's scratch), and that sizes above its stated
 maximum are refused.  Integer outputs: equality is exact.  The file runs last
