@@ -2,7 +2,7 @@
 
 Recipe that compiles the reference's own kernel sources for the CPU, for
 pinning the restated oracle (oracle/ref_model.hpp) against them.  It reads the
-sources where they lie under /root/reference (read-only), rewrites only the
+sources where they lie under the reference checkout (read-only), rewrites only the
 CUDA launch syntax `K<<<grid, block>>>(args)` into a call of the serial
 launcher of shim_cuda.h, and writes the rewritten translation units and the
 library into oracle/_ref/ (git-ignored, never committed).  Nothing else of the
@@ -14,13 +14,14 @@ Returns None when the reference sources are not mounted (the GPU machines).
 """
 from __future__ import annotations
 
+import json
 import os
 import re
 import subprocess
 
-REF_ROOT = "/root/reference/code/gpuseg/code"
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
+REPO = os.path.dirname(ORACLE)
 OUT = os.path.join(ORACLE, "_ref")
 GEN = os.path.join(OUT, "gen")
 LIB = os.path.join(OUT, "libref_oracle.so")
@@ -41,8 +42,31 @@ def rewrite(text: str) -> str:
     return _LAUNCH.sub(lambda m: f"::lss_shim::launcher({m.group(2)}, &{m.group(1)})(", text)
 
 
+def reference_root() -> str | None:
+    """The reference checkout: $LSS_REFERENCE_ROOT, else the `reference_path`
+    recorded in the repository's benchmark spec; None when neither names an
+    existing directory."""
+    root = os.environ.get("LSS_REFERENCE_ROOT")
+    if not root:
+        try:
+            with open(os.path.join(REPO, "BASELINE.json")) as f:
+                root = json.load(f).get("reference_path")
+        except (OSError, ValueError):
+            root = None
+    return root if root and os.path.isdir(root) else None
+
+
+def code_root() -> str | None:
+    """code/gpuseg/code of the reference checkout, or None."""
+    root = reference_root()
+    return os.path.join(root, "code", "gpuseg", "code") if root else None
+
+
 def build() -> str | None:
-    src_dir = os.path.join(REF_ROOT, "src", "cuda")
+    ref = code_root()
+    if ref is None:
+        return None
+    src_dir = os.path.join(ref, "src", "cuda")
     if not os.path.isdir(src_dir):
         return None
     os.makedirs(GEN, exist_ok=True)
@@ -53,7 +77,7 @@ def build() -> str | None:
             fh.write(rewrite(text))
     cmd = ["g++", "-O2", "-std=c++20", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
            "-w", "-DLSS_ORACLE_REFERENCE_KERNELS", "-DCUDA_ARCH_SM_13",
-           "-I", ORACLE, "-I", HERE, "-I", OUT, "-I", REF_ROOT,
+           "-I", ORACLE, "-I", HERE, "-I", OUT, "-I", ref,
            os.path.join(ORACLE, "lss_oracle.cpp"), "-o", LIB + ".tmp"]
     subprocess.run(cmd, check=True)
     os.replace(LIB + ".tmp", LIB)
