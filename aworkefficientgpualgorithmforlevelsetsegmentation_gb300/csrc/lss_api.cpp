@@ -1,6 +1,7 @@
 // The C ABI of include/lss.h over the engine objects.  Every entry point
 // converts exceptions into an lss_status and keeps the message for
 // lss_last_error_string; nothing aborts the process.
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <exception>
@@ -93,6 +94,7 @@ lss_status lss_params_default(int32_t mode, lss_params* p) {
     p->convergence_threshold = 0;
     p->neighbourhood = 26;
     p->alpha_role = LSS_ALPHA_DATA;
+    p->data_term = LSS_DATA_NORMALISED;
     return LSS_OK;
 }
 
@@ -155,20 +157,25 @@ lss_status lss_load_volume_raw(lss_engine* e, const char* path, int32_t nx, int3
     CHECK_ENGINE(e);
     if (!path || nx <= 0 || ny <= 0 || nz <= 0 || dtype < LSS_U8 || dtype > LSS_F32)
         return LSS_ERR_INVALID_ARGUMENT;
-    const size_t bpv = dtype <= LSS_S8 ? 1 : dtype <= LSS_S16 ? 2 : 4;
-    const size_t bytes = (size_t)nx * ny * nz * bpv;
-    std::vector<uint8_t> buf(bytes);
-    FILE* f = std::fopen(path, "rb");
-    if (!f) {
-        e->err = std::string("cannot open ") + path;
-        return LSS_ERR_INVALID_ARGUMENT;
-    }
-    size_t got = std::fread(buf.data(), 1, bytes, f);
-    std::fclose(f);
-    if (got != bytes) {
-        e->err = "raw file holds " + std::to_string(got) + " bytes, expected " + std::to_string(bytes);
-        return LSS_ERR_INVALID_ARGUMENT;
-    }
+    // The reference reads numVoxels * numBytesPerVoxel bytes and asserts that
+    // the file held them (VolumeLoader.cpp:275-303); here a missing or short
+    // file, or a size whose byte count overflows, is an error status.
+    std::vector<uint8_t> buf;
+    const lss_status s = guard(e, [&] {
+        const uint64_t bpv = dtype <= LSS_S8 ? 1 : dtype <= LSS_S16 ? 2 : 4;
+        uint64_t xy = 0, vox = 0, bytes = 0;
+        const bool wrap = __builtin_mul_overflow((uint64_t)nx, (uint64_t)ny, &xy) ||
+                          __builtin_mul_overflow(xy, (uint64_t)nz, &vox) ||
+                          __builtin_mul_overflow(vox, bpv, &bytes);
+        LSS_REQUIRE(!wrap && bytes <= (uint64_t)PTRDIFF_MAX, LSS_ERR_CAPACITY, "raw volume size overflows");
+        std::unique_ptr<FILE, int (*)(FILE*)> f(std::fopen(path, "rb"), &std::fclose);
+        LSS_REQUIRE(f != nullptr, LSS_ERR_INVALID_ARGUMENT, std::string("cannot open ") + path);
+        buf.resize((size_t)bytes);
+        const size_t got = std::fread(buf.data(), 1, (size_t)bytes, f.get());
+        LSS_REQUIRE(got == bytes, LSS_ERR_INVALID_ARGUMENT,
+                    "raw file holds " + std::to_string(got) + " bytes, expected " + std::to_string(bytes));
+    });
+    if (s != LSS_OK) return s;
     return lss_load_volume(e, buf.data(), nx, ny, nz, dtype, aniso);
 }
 
@@ -183,7 +190,8 @@ lss_status lss_set_params(lss_engine* e, const lss_params* p) {
     // A negative threshold marks every updated voxel as changed (and every
     // voxel as initially active): the dense all-voxel update.
     if (!(p->phi_min < p->phi_max) || !(p->window > 0) ||
-        (p->neighbourhood != 6 && p->neighbourhood != 26))
+        (p->neighbourhood != 6 && p->neighbourhood != 26) ||
+        (p->data_term != LSS_DATA_NORMALISED && p->data_term != LSS_DATA_LITERAL))
         return LSS_ERR_INVALID_ARGUMENT;
     return guard(e, [&] { e->impl->set_params(*p); });
 }
@@ -281,17 +289,18 @@ lss_status lss_read_mask(lss_engine* e, uint8_t* out) {
 lss_status lss_save_mask_raw(lss_engine* e, const char* path) {
     CHECK_ENGINE(e);
     if (!path || e->nx <= 0) return LSS_ERR_INVALID_ARGUMENT;
-    std::vector<uint8_t> m((size_t)e->nx * e->ny * e->nz);
-    lss_status s = lss_read_mask(e, m.data());
+    std::vector<uint8_t> m;
+    lss_status s = guard(e, [&] { m.resize((size_t)e->nx * e->ny * e->nz); });
     if (s != LSS_OK) return s;
-    FILE* f = std::fopen(path, "wb");
-    if (!f) {
-        e->err = std::string("cannot write ") + path;
-        return LSS_ERR_INVALID_ARGUMENT;
-    }
-    size_t put = std::fwrite(m.data(), 1, m.size(), f);
-    std::fclose(f);
-    return put == m.size() ? LSS_OK : LSS_ERR_INVALID_ARGUMENT;
+    s = lss_read_mask(e, m.data());
+    if (s != LSS_OK) return s;
+    return guard(e, [&] {
+        std::unique_ptr<FILE, int (*)(FILE*)> f(std::fopen(path, "wb"), &std::fclose);
+        LSS_REQUIRE(f != nullptr, LSS_ERR_INVALID_ARGUMENT, std::string("cannot write ") + path);
+        const size_t put = std::fwrite(m.data(), 1, m.size(), f.get());
+        LSS_REQUIRE(put == m.size() && std::fflush(f.get()) == 0, LSS_ERR_INVALID_ARGUMENT,
+                    std::string("short write to ") + path);
+    });
 }
 
 lss_status lss_read_export(lss_engine* e, int8_t* out) {
