@@ -144,6 +144,8 @@ void ons_set_params(void* h, double T, double eps, double alpha, double dt, doub
 
 void ons_set_alpha_role(void* h, int alpha_data) { ((NsOracle*)h)->p.alpha_data = alpha_data; }
 
+void ons_set_data_term(void* h, int literal) { ((NsOracle*)h)->p.data_literal = literal; }
+
 void ons_set_threads(void* h, int t) { ((NsOracle*)h)->threads = t; }
 
 void ons_set_bias(void* h, const float* b) {
@@ -250,6 +252,13 @@ void ons_adj_run(void* h, int K, const uint8_t* target, double tau, double* out,
 double ons_adj_loss(void* h, int K, const uint8_t* target, double tau) {
     NsOracle* o = (NsOracle*)h;
     return lssns::adjoint_forward(*o, K, target, tau, adj_sets(h), true, nullptr);
+}
+
+// The soft-Dice coefficient (1 - loss) of the same replay, at full
+// resolution (finite differences of single bias voxels).
+double ons_adj_dice(void* h, int K, const uint8_t* target, double tau) {
+    NsOracle* o = (NsOracle*)h;
+    return lssns::adjoint_forward(*o, K, target, tau, adj_sets(h), true, nullptr, true);
 }
 
 // Sets one parameter: 0 T, 1 eps, 2 alpha.

@@ -45,9 +45,9 @@ inline void ns_update_vjp(PF P, AF addphi, int x, int y, int z, double I, double
               2 * (cx * cy * fxy + cx * cz * fxz + cy * cz * fyz);
         curv = num / g2;
     }
-    const double Draw = (p.eps - std::fabs(I - p.T)) / p.eps;
-    const bool dclamp = Draw < -1 || Draw > 1;
-    const double Dt = std::min(std::max(Draw, -1.0), 1.0) + bias;
+    const double Draw = p.data_literal ? p.eps - std::fabs(I - p.T) : (p.eps - std::fabs(I - p.T)) / p.eps;
+    const bool dclamp = !p.data_literal && (Draw < -1 || Draw > 1);
+    const double Dt = (p.data_literal ? Draw : std::min(std::max(Draw, -1.0), 1.0)) + bias;
     const double wc = p.alpha_data ? 1 - p.alpha : p.alpha;
     const double wd = 1 - wc;
     const double F = wd * Dt;
@@ -105,13 +105,19 @@ inline void ns_update_vjp(PF P, AF addphi, int x, int y, int z, double I, double
         addphi(x, y, z - 1, -s * h);
         addphi(x, y, z + 1, s * k);
     }
-    // F = wd (Dc + bias); Dc = (eps - |I - T|) / eps unless clamped.
+    // F = wd (Dc + bias); Dc = (eps - |I - T|) / eps unless clamped, or
+    // eps - |I - T| (literal).
     const double gDt = gF * wd;
     g[3] += gDt;
     if (!dclamp) {
         const double sg = I > p.T ? 1.0 : (I < p.T ? -1.0 : 0.0);
-        g[0] += gDt * sg / p.eps;
-        g[1] += gDt * std::fabs(I - p.T) / (p.eps * p.eps);
+        if (p.data_literal) {  // D = eps - |I - T|
+            g[0] += gDt * sg;
+            g[1] += gDt;
+        } else {  // D = (eps - |I - T|) / eps
+            g[0] += gDt * sg / p.eps;
+            g[1] += gDt * std::fabs(I - p.T) / (p.eps * p.eps);
+        }
     }
     // alpha: u = c + dt (wc curv - wd Dt gn), (wc, wd) = (1 - alpha, alpha) or (alpha, 1 - alpha).
     const double du_dalpha = p.dt * (-curv - Dt * gn);
@@ -123,20 +129,37 @@ struct AdjointResult {
     std::vector<double> dbias;  // per voxel (nx*ny*nz)
 };
 
+// Compensated (Neumaier) running sum: the rounding error of a sum over
+// millions of voxels stays at one ulp of the result, so that two losses whose
+// fields differ in a few voxels (central finite differences of a single bias
+// voxel) differ by what those voxels contribute, not by rounding noise.
+struct CompensatedSum {
+    double sum = 0, c = 0;
+    void add(double x) {
+        const double t = sum + x;
+        c += std::fabs(sum) >= std::fabs(x) ? (sum - t) + x : (x - t) + sum;
+        sum = t;
+    }
+    double value() const { return sum + c; }
+};
+
 // Soft-Dice loss of sigmoid(-phi/tau) against target, and dloss/dphi.
 inline double soft_dice(const std::vector<double>& phi, const uint8_t* target, double tau,
-                        std::vector<double>* grad) {
-    double ss = 0, st = 0, tt = 0;
+                        std::vector<double>* grad, double* coefficient = nullptr) {
+    CompensatedSum css, cst;
+    double tt = 0;
     const size_t N = phi.size();
     std::vector<double> s(N);
     for (size_t i = 0; i < N; ++i) {
         s[i] = 1.0 / (1.0 + std::exp(phi[i] / tau));
-        ss += s[i];
+        css.add(s[i]);
         tt += target[i] ? 1.0 : 0.0;
-        st += target[i] ? s[i] : 0.0;
+        if (target[i]) cst.add(s[i]);
     }
+    const double ss = css.value(), st = cst.value();
     const double den = ss + tt;
     const double loss = 1.0 - 2.0 * st / den;
+    if (coefficient) *coefficient = 2.0 * st / den;
     if (grad) {
         grad->assign(N, 0.0);
         for (size_t i = 0; i < N; ++i) {
@@ -151,9 +174,13 @@ inline double soft_dice(const std::vector<double>& phi, const uint8_t* target, d
 // K iterations of o (from its current phi and active list), recording the
 // active lists in `sets` (or replaying them when `replay`), then the loss.
 // o's phi / active / counters are restored on return.
+// With `coefficient`, returns the soft-Dice coefficient 2 sum(s t) / (sum s +
+// sum t) instead of the loss 1 - coefficient: near a loss of 1 the
+// coefficient keeps ~1000x finer resolution (the subtraction from 1 rounds to
+// the ulp of 1), which central differences of one bias voxel need.
 inline double adjoint_forward(NsOracle& o, int K, const uint8_t* target, double tau,
                               std::vector<std::vector<uint64_t>>& sets, bool replay,
-                              std::vector<std::vector<double>>* history) {
+                              std::vector<std::vector<double>>* history, bool coefficient = false) {
     const std::vector<double> phi0 = o.phi;
     const std::vector<uint64_t> act0 = o.active;
     const uint64_t it0 = o.iterations, up0 = o.updates;
@@ -165,12 +192,13 @@ inline double adjoint_forward(NsOracle& o, int K, const uint8_t* target, double 
         if (!replay) sets.push_back(o.active);
         if (history) history->push_back(o.phi);
     }
-    const double loss = soft_dice(o.phi, target, tau, nullptr);
+    double coef = 0;
+    const double loss = soft_dice(o.phi, target, tau, nullptr, &coef);
     o.phi = phi0;
     o.active = act0;
     o.iterations = it0;
     o.updates = up0;
-    return loss;
+    return coefficient ? coef : loss;
 }
 
 inline AdjointResult adjoint_run(NsOracle& o, int K, const uint8_t* target, double tau,

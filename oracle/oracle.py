@@ -64,6 +64,7 @@ def lib() -> C.CDLL:
         L.ons_set_params.argtypes = [_P] + [C.c_double] * 8 + [C.c_int]
         L.ons_set_threads.argtypes = [_P, C.c_int]
         L.ons_set_alpha_role.argtypes = [_P, C.c_int]
+        L.ons_set_data_term.argtypes = [_P, C.c_int]
         L.ons_set_bias.argtypes = [_P, _P]
         L.ons_set_phi.argtypes = [_P, _P]
         L.ons_set_state.argtypes = [_P, _P, _P, C.c_uint64]
@@ -81,6 +82,8 @@ def lib() -> C.CDLL:
         L.ons_adj_run.argtypes = [_P, C.c_int, _P, C.c_double, _P, _P]
         L.ons_adj_loss.restype = C.c_double
         L.ons_adj_loss.argtypes = [_P, C.c_int, _P, C.c_double]
+        L.ons_adj_dice.restype = C.c_double
+        L.ons_adj_dice.argtypes = [_P, C.c_int, _P, C.c_double]
         L.ons_set_param.argtypes = [_P, C.c_int, C.c_double]
         L.ons_set_bias64.argtypes = [_P, _P]
         _libs["oracle"] = L
@@ -240,9 +243,10 @@ class NsOracle:
     __del__ = close
 
     def set_params(self, T, eps, alpha, dt, lo=-4.0, hi=4.0, thr_t=0.01, thr_s=0.0, nbh=26,
-                   alpha_data=1):
+                   alpha_data=1, data_literal=0):
         self._L.ons_set_params(self._h, T, eps, alpha, dt, lo, hi, thr_t, thr_s, nbh)
         self._L.ons_set_alpha_role(self._h, int(alpha_data))
+        self._L.ons_set_data_term(self._h, int(data_literal))
 
     def set_threads(self, t: int):
         self._L.ons_set_threads(self._h, t)
@@ -319,6 +323,13 @@ class NsOracle:
         """The loss of K iterations replaying the active sets of adjoint()."""
         t = np.ascontiguousarray(target, np.uint8)
         return float(self._L.ons_adj_loss(self._h, K, _ptr(t), tau))
+
+    def adjoint_dice(self, K: int, target: np.ndarray, tau: float = 0.5) -> float:
+        """The soft-Dice coefficient (1 - loss) of the same replay, computed
+        without the subtraction from 1: finite differences of the loss are
+        minus those of this value, at ~1000x finer resolution near loss 1."""
+        t = np.ascontiguousarray(target, np.uint8)
+        return float(self._L.ons_adj_dice(self._h, K, _ptr(t), tau))
 
     def set_param(self, which: str, value: float):
         self._L.ons_set_param(self._h, {"T": 0, "eps": 1, "alpha": 2}[which], value)
