@@ -7,8 +7,9 @@ object; `Batch` runs many volumes in one persistent launch; `phantoms` makes
 the seeded synthetic workloads.
 """
 from ._lib import LssError, library_path, load  # noqa: F401
-from .segmenter import (ALPHA_CURVATURE, ALPHA_DATA, MODE_NS, MODE_REF, Batch,  # noqa: F401
-                        Segmenter, config, default_params)
+from .segmenter import (ALPHA_CURVATURE, ALPHA_DATA, DATA_LITERAL, DATA_NORMALISED,  # noqa: F401
+                        MODE_NS, MODE_REF, Batch, Segmenter, config, default_params)
 
 __all__ = ["Segmenter", "Batch", "LssError", "MODE_REF", "MODE_NS", "ALPHA_CURVATURE",
-           "ALPHA_DATA", "config", "default_params", "load", "library_path"]
+           "ALPHA_DATA", "DATA_NORMALISED", "DATA_LITERAL", "config", "default_params", "load",
+           "library_path"]

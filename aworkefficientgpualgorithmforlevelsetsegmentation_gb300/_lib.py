@@ -25,7 +25,7 @@ class lss_params(C.Structure):
                 ("time_step", C.c_float), ("phi_min", C.c_float), ("phi_max", C.c_float),
                 ("temporal_threshold", C.c_float), ("spatial_threshold", C.c_float),
                 ("convergence_threshold", C.c_float), ("neighbourhood", C.c_int32),
-                ("alpha_role", C.c_int32)]
+                ("alpha_role", C.c_int32), ("data_term", C.c_int32)]
 
 
 class lss_conv(C.Structure):

@@ -211,9 +211,9 @@ __device__ __forceinline__ void ns_update_vjp_f32(PF P, AF add, float I, float b
                           2.0f * (cx * cy * fxy + cx * cz * fxz + cy * cz * fyz);
         curv = num / g2;
     }
-    const float Draw = (V.eps - fabsf(I - V.T)) / V.eps;
-    const bool dclamp = Draw < -1.0f || Draw > 1.0f;
-    const float Dt = fminf(fmaxf(Draw, -1.0f), 1.0f) + bias;
+    const float Draw = V.data_literal ? V.eps - fabsf(I - V.T) : (V.eps - fabsf(I - V.T)) / V.eps;
+    const bool dclamp = Draw < V.dlo || Draw > V.dhi;
+    const float Dt = fminf(fmaxf(Draw, V.dlo), V.dhi) + bias;
     const float F = V.wd * Dt;
     const float dxm = c - xm, dxp = xp - c, dym = c - ym, dyp = yp - c, dzm = c - zm, dzp = zp - c;
     float a, b, e, f, h, k;
@@ -271,8 +271,13 @@ __device__ __forceinline__ void ns_update_vjp_f32(PF P, AF add, float I, float b
     g4[3] += gDt;
     if (!dclamp) {
         const float sg = I > V.T ? 1.0f : (I < V.T ? -1.0f : 0.0f);
-        g4[0] += gDt * sg / V.eps;
-        g4[1] += gDt * fabsf(I - V.T) / (V.eps * V.eps);
+        if (V.data_literal) {  // D = eps - |I - T|
+            g4[0] += gDt * sg;
+            g4[1] += gDt;
+        } else {  // D = (eps - |I - T|) / eps
+            g4[0] += gDt * sg / V.eps;
+            g4[1] += gDt * fabsf(I - V.T) / (V.eps * V.eps);
+        }
     }
     const float du_dalpha = V.dt * (-curv - Dt * gn);
     g4[2] += lam * (V.alpha_data ? du_dalpha : -du_dalpha);

@@ -417,7 +417,10 @@ NsVol NsCore::descriptor(int i) const {
     o.lo = v.p.phi_min; o.hi = v.p.phi_max;
     o.thr_t = v.p.temporal_threshold; o.thr_s = v.p.spatial_threshold;
     o.alpha_data = v.p.alpha_role == LSS_ALPHA_CURVATURE ? 0 : 1;
-    o.inv_eps = 1.0f / v.p.window;
+    o.data_literal = v.p.data_term == LSS_DATA_LITERAL ? 1 : 0;
+    o.inv_eps = o.data_literal ? 1.0f : 1.0f / v.p.window;
+    o.dlo = o.data_literal ? -INFINITY : -1.0f;
+    o.dhi = o.data_literal ? INFINITY : 1.0f;
     o.wc = o.alpha_data ? 1.0f - v.p.curvature : v.p.curvature;
     o.wd = 1.0f - o.wc;
     o.nbh = v.p.neighbourhood == 6 ? 6 : 26;

@@ -53,7 +53,9 @@ struct NsVol {
     int32_t alpha_data;     // 1: alpha weights the data term, 0: the curvature term
     int32_t nbh;            // 26 or 6
     uint32_t tmap_base;     // 5 maps: phi0 halo-load, phi1 halo-load, phi0 store, phi1 store, img
-    float inv_eps;          // 1 / eps
+    float inv_eps;          // 1 / eps (LSS_DATA_NORMALISED), 1 (LSS_DATA_LITERAL)
+    float dlo, dhi;         // clamp of the data term: -1, 1 or -inf, +inf (literal)
+    int32_t data_literal;   // 1: D = eps - |I - T| as written
     float wc, wd;           // curvature and data weights (from alpha and alpha_data)
     uint32_t mnbx, mnbxy;   // 0xFFFFFFFF / nbx + 1 and / (nbx * nby) + 1 (div_magic)
 };
@@ -168,8 +170,10 @@ __device__ __forceinline__ float ns_update_f32(PF P, float I, float bias, const 
     const float Fzz = __fmaf_rn(-2.0f, c, __fadd_rn(zp, zm));
     const float dxm = __fsub_rn(c, xm), dxp = __fsub_rn(xp, c), dym = __fsub_rn(c, ym),
                 dyp = __fsub_rn(yp, c), dzm = __fsub_rn(c, zm), dzp = __fsub_rn(zp, c);
+    // Literal data term: inv_eps = 1 (an exact product) and an infinite
+    // clamp, so both readings share one instruction sequence.
     float D = __fmul_rn(__fsub_rn(V.eps, fabsf(__fsub_rn(I, V.T))), V.inv_eps);
-    D = __fadd_rn(fminf(fmaxf(D, -1.0f), 1.0f), bias);
+    D = __fadd_rn(fminf(fmaxf(D, V.dlo), V.dhi), bias);
     const float F = __fmul_rn(V.wd, D);
     // Osher-Sethian upwind |grad phi| for the speed F: one-sided differences
     // selected by the sign of F.

@@ -30,6 +30,7 @@ from . import _lib as L
 
 MODE_REF, MODE_NS = 0, 1
 ALPHA_CURVATURE, ALPHA_DATA = 0, 1
+DATA_NORMALISED, DATA_LITERAL = 0, 1
 DTYPES = {np.dtype(np.uint8): 0, np.dtype(np.int8): 1, np.dtype(np.uint16): 2,
           np.dtype(np.int16): 3, np.dtype(np.uint32): 4, np.dtype(np.int32): 5,
           np.dtype(np.float32): 6}

@@ -1,0 +1,94 @@
+"""LSS_MODE_NS with the data speed as the spec formula writes it
+(lss_params.data_term = LSS_DATA_LITERAL: D = eps - |I - T| + bias, no
+division by eps, no clamp) against the FP64 oracle under the same reading.
+
+The default reading (LSS_DATA_NORMALISED: clamp((eps - |I - T|)/eps, -1, 1)
++ bias) is what the benchmark workloads run; these tests pin the literal one
+with the same criteria: one iteration from an identical state within 1e-4,
+active lists bit-exact given identical phi, masks after 300 iterations (the
+plain 128^3 workload's iteration count) disagreeing on at most 0.01 % of
+voxels, and the adjoint within 1e-3 of the FP64 adjoint."""
+import numpy as np
+import pytest
+
+import aworkefficientgpualgorithmforlevelsetsegmentation_gb300 as lss
+from aworkefficientgpualgorithmforlevelsetsegmentation_gb300 import phantoms as P
+from oracle.oracle import NsOracle
+from tests.gpu_util import dice
+
+pytestmark = pytest.mark.gpu
+
+PHI_TOL = 1e-4
+
+
+def gpu(cfg, literal=True, brick=(8, 8, 8), threads=256):
+    p = cfg["params"]
+    s = lss.Segmenter(lss.MODE_NS, brick=brick, threads_per_brick=threads)
+    s.load_volume(cfg["image"])
+    s.set_parameters(p.target, p.window, p.curvature, p.time_step, alpha_role=p.alpha_role,
+                     data_term=lss.DATA_LITERAL if literal else lss.DATA_NORMALISED)
+    s.set_phi(cfg["phi0"])
+    return s
+
+
+def oracle(cfg, brick=(8, 8, 8)):
+    p = cfg["params"]
+    o = NsOracle(cfg["image"], brick=brick, threads=8)
+    o.set_params(p.target, p.window, p.curvature, p.time_step, p.phi_min, p.phi_max,
+                 p.temporal_threshold, p.spatial_threshold, 26, p.alpha_role, data_literal=1)
+    return o
+
+
+@pytest.mark.parametrize("brick,threads", [((8, 8, 8), 256), ((8, 8, 4), 32), ((4, 4, 4), 64)])
+def test_literal_each_iteration_vs_fp64(brick, threads):
+    cfg = P.config1(0.5)
+    s = gpu(cfg, brick=brick, threads=threads)
+    o = oracle(cfg, brick)
+    worst = 0.0
+    for it in range(40):
+        before = s.read_phi()
+        act = s.active_linear()
+        o.set_state(before, act)
+        o.step(1)
+        s.step(1)
+        after = s.read_phi()
+        err = float(np.max(np.abs(after.astype(np.float64) - o.read_phi64())))
+        worst = max(worst, err)
+        assert err <= PHI_TOL, (it, err)
+        idx = act.astype(np.int64)
+        assert np.array_equal(s.active_linear(), o.expand_given(act, before.ravel()[idx], after.ravel()[idx])), it
+    assert worst <= PHI_TOL
+    # The switch changes the run: the normalised reading moves the front faster.
+    n = gpu(cfg, literal=False, brick=brick, threads=threads)
+    n.step(40)
+    assert not np.array_equal(n.read_phi(), s.read_phi())
+
+
+def test_literal_mask_after_300_iterations_vs_fp64():
+    cfg = P.config1(0.5)
+    s = gpu(cfg)
+    s.step(300)
+    o = oracle(cfg)
+    o.set_phi(cfg["phi0"])
+    o.step(300)
+    mg = s.get_saveable_segmentation().astype(bool)
+    mo = o.read_phi() <= 0
+    assert mo.sum() > 1000
+    assert float(np.mean(mg != mo)) <= 1e-4
+    assert dice(mg, mo) >= 0.999
+
+
+def test_literal_adjoint_vs_fp64_adjoint():
+    cfg = P.config4(0.25)
+    rng = np.random.default_rng(4)
+    bias = (0.02 * rng.standard_normal(cfg["image"].shape)).astype(np.float32)
+    g = gpu(cfg).adjoint(16, 4, cfg["target"], 0.5, bias=bias)
+    o = oracle(cfg)
+    o.set_bias(bias)
+    o.set_phi(cfg["phi0"])
+    r = o.adjoint(16, cfg["target"], 0.5)
+    assert abs(g["loss"] - r["loss"]) <= 1e-5
+    for key in ("d_target", "d_window", "d_curvature"):
+        assert abs(g[key] - r[key]) <= 1e-3 * abs(r[key]), (key, g[key], r[key])
+    db, ob = g["d_bias"].astype(np.float64), r["d_bias"]
+    assert np.linalg.norm(db - ob) <= 1e-3 * np.linalg.norm(ob)
