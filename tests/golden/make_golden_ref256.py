@@ -1,0 +1,112 @@
+"""Generates tests/golden/ref_config2_256.npz: LSS_MODE_REF at the headline
+size, run on the CPU through the reference's own kernel sources (oracle/_ref;
+needs the reference sources mounted), for the GPU parity test of the REF
+benchmark workload.
+
+Workload (the one `bench.py --workload ref` times): the 256^3 three-shell
+phantom quantised to u8 (round(255 I)), the four radius-3 seeds of the plain
+workload applied as consecutive InitializeSeed calls, grow level 204, window
+26, curvature 0.1, dt 0.25, one iteration a RequestUpdateSegmentation call,
+stopped once the active count stays under 0.1 % of its value after seeding
+for 5 consecutive iterations (at most 2000).
+
+The workload is run twice on one solver: from a fresh load, and again after
+ClearCurrentSegmentation and the same seeds (what a benchmark step does after
+its first): the reference keeps stale buffer contents across the clear, so
+the second run is its own case.  Stored per run: the active count after every
+iteration, SHA-256 digests (first 128 bits) of the compacted active list at
+the snapshot iterations and at the end, and digests of the final mask, phi
+and export volumes.  The restated oracle (oracle/ref_model.hpp) is run beside
+the reference kernels and must agree everywhere.
+Run: python tests/golden/make_golden_ref256.py
+"""
+import hashlib
+import os
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from aworkefficientgpualgorithmforlevelsetsegmentation_gb300 import phantoms as P  # noqa: E402
+from oracle import build as OB  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+PARAMS = (204, 26, 0.1, 0.25)
+SNAPSHOTS = (1, 2, 5, 10, 20, 50, 100, 150, 200, 250, 300)
+REL, PATIENCE, MAX_IT = 1e-3, 5, 2000
+OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "ref_config2_256.npz")
+
+
+def digest(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()[:32]
+
+
+def workload():
+    cfg = P.config2(1.0)
+    u8 = np.clip(np.rint(cfg["image"] * 255.0), 0, 255).astype(np.uint8)
+    return u8, cfg["spheres"]
+
+
+def run_once(o, spheres, log=None):
+    """Seeds o, iterates under the stopping rule; returns (counts, snapshot
+    digests {iteration: sha}, final digests)."""
+    for (x, y, z, r) in spheres:
+        o.initialize_seed(x, y, z, r)
+    n0 = o.n
+    counts, snaps, streak, it = [n0], {0: digest(o.active())}, 0, 0
+    while it < MAX_IT:
+        o.step(1)
+        it += 1
+        n = o.n
+        counts.append(n)
+        if it in SNAPSHOTS:
+            snaps[it] = digest(o.active())
+            if log:
+                log(f"  iteration {it}: n = {n}")
+        streak = streak + 1 if n < REL * n0 else 0
+        if streak >= PATIENCE:
+            break
+    snaps[it] = digest(o.active())
+    mask = o.read_mask()
+    final = {"mask": digest(mask), "phi": digest(o.read_phi()), "export": digest(o.read_export()),
+             "mask_voxels": int(mask.sum())}
+    return np.array(counts, np.int64), snaps, final
+
+
+def run(o, spheres, log=None):
+    """The two runs (fresh, then after clear_current) on one solver."""
+    o.set_params(*PARAMS)
+    first = run_once(o, spheres, log)
+    o.clear_current()
+    second = run_once(o, spheres, log)
+    return first, second
+
+
+def main():
+    if OB.build_reference() is None:
+        raise SystemExit("reference sources not mounted")
+    u8, spheres = workload()
+    t = time.time()
+    runs = run(O.RefOracle(u8, 0, use_reference_kernels=True), spheres, log=lambda m: print(m, flush=True))
+    print(f"reference kernels: {time.time() - t:.0f} s")
+    again = run(O.RefOracle(u8, 0), spheres)
+    out = {"params": np.array(PARAMS, np.float64)}
+    for tag, (counts, snaps, final), (c2, s2, f2) in zip(("fresh", "rerun"), runs, again):
+        assert np.array_equal(counts, c2) and snaps == s2 and final == f2, f"restated oracle differs ({tag})"
+        its = np.array(sorted(snaps), np.int64)
+        out[tag + "/counts"] = counts
+        out[tag + "/snap_iterations"] = its
+        out[tag + "/snap_sha"] = np.array([snaps[i] for i in its])
+        out[tag + "/final_sha"] = np.array([final["mask"], final["phi"], final["export"]])
+        out[tag + "/mask_voxels"] = np.int64(final["mask_voxels"])
+        print(f"{tag}: {len(counts) - 1} iterations, {int(counts[:-1].sum())} updates, "
+              f"{final['mask_voxels']} voxels segmented")
+    np.savez_compressed(OUT, **out)
+    print(OUT, os.path.getsize(OUT), "bytes")
+
+
+if __name__ == "__main__":
+    main()

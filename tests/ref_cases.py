@@ -1,16 +1,23 @@
 """Deterministic LSS_MODE_REF cases shared by the oracle pin, the golden
 fixtures and the GPU parity tests.
 
-Each case is a small integer volume drawn from numpy's PCG64 (identical on
-every platform), the reference's parameters, seeds and a step schedule.  A
-schedule entry is an int (substeps of one RequestUpdateSegmentation call) or
-an action tuple: ("params", T, eps, alpha, dt), ("seed", x, y, z, r),
+Each case is an integer volume, the reference's parameters, seeds and a step
+schedule.  Volumes are either small blobs drawn from numpy's PCG64 (identical
+on every platform) or one of the reference's own test volumes
+(code/gpuseg/bin/data/test/Bucky.raw, 32^3 u8, and Hydrogen.raw, 128^3 u8),
+copied into tests/golden/reference_volumes.npz by tests/golden/make_golden.py.
+A schedule entry is an int (substeps of one RequestUpdateSegmentation call)
+or an action tuple: ("params", T, eps, alpha, dt), ("seed", x, y, z, r),
 ("mask",) (a readback, which clears the tag volume as the reference does),
 ("freeze",), ("clear",).
 """
 from __future__ import annotations
 
+import os
+
 import numpy as np
+
+VOLUMES = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_volumes.npz")
 
 DT = {"u8": (0, np.uint8), "s8": (1, np.int8), "u16": (2, np.uint16), "s16": (3, np.int16),
       "u32": (4, np.uint32), "s32": (5, np.int32)}
@@ -48,11 +55,39 @@ CASES = {
                    [(8, 8, 8, 3)], [4, 4, ("freeze",), ("clear",), ("seed", 5, 5, 5, 2), 3, 3]),
     "no_curvature_u8": ((24, 24, 24), "u8", (0, 40, 100, 8, 8), (100, 50, 0.0, 0.5),
                         [(12, 12, 12, 3)], [1] * 10),
+    # The reference's test volumes.  Bucky.raw with the parameters of
+    # code/gpuseg/bin/parameters/Bucky.par (growLevel 140, growWindow 80,
+    # curvatureInfluence 0.16, timeStep 0.253333, numSubSteps 15), seeded in a
+    # bright lobe of the shell.
+    "bucky_par": ((32, 32, 32), "u8", "bucky", (140, 80, 0.16, 0.253333),
+                  [(16, 4, 16, 3)], [15] * 20 + [("mask",)] + [15] * 4),
+    # Hydrogen.raw seeded with the REPRODUCIBLE_SEED constants of
+    # Segmenter.cpp:507-513 (64, 88, 98, radius 15), growing through the dim
+    # region around the orbital (T 0, window 12): large active sets, the
+    # many-active path.
+    "hydrogen_seed_u8": ((128, 128, 128), "u8", "hydrogen", (0, 12, 0.16, 0.25),
+                         [(64, 88, 98, 15)], [15] * 10),
+    # Hydrogen.raw seeded in the orbital's bright core, growing outwards.
+    "hydrogen_core_u8": ((128, 128, 128), "u8", "hydrogen", (40, 40, 0.16, 0.25),
+                         [(64, 64, 62, 4)], [15] * 8),
 }
+
+# Cases on the reference's 128^3 test volume: the slowest for the reference
+# kernels compiled for the CPU.
+LARGE = ("hydrogen_seed_u8", "hydrogen_core_u8")
+
+
+def reference_volume(which: str) -> np.ndarray:
+    with np.load(VOLUMES) as z:
+        return np.ascontiguousarray(z[which])
 
 
 def make_volume(name):
     shape, dt, va, *_ = CASES[name]
+    if isinstance(va, str):
+        v = reference_volume(va)
+        assert v.shape == shape and v.dtype == DT[dt][1]
+        return v
     return blob_volume(shape, dt, *va)
 
 
