@@ -11,6 +11,7 @@ import os
 from . import build as _build
 
 _lib: C.CDLL | None = None
+_phantom: C.CDLL | None = None
 
 
 class lss_config(C.Structure):
@@ -138,3 +139,27 @@ def load(build_if_missing: bool = True) -> C.CDLL:
             f.argtypes = args
         _lib = L
     return _lib
+
+
+PHANTOM_FUNCTIONS = ("lss_phantom_ellipsoid", "lss_phantom_shells", "lss_phantom_sdf_spheres",
+                     "lss_phantom_uniform")
+
+
+def load_phantom(build_if_missing: bool = True) -> C.CDLL:
+    """Loads libphantom.so, the host-only build of the include/lss_phantom.h
+    generators (building it first if it is absent)."""
+    global _phantom
+    if _phantom is None:
+        path = _build.PHANTOM_LIB
+        if not os.path.exists(path):
+            if not build_if_missing:
+                raise RuntimeError(f"{path} is missing: run the package build first")
+            _build.build_phantom()
+        L = C.CDLL(path)
+        for name in PHANTOM_FUNCTIONS:
+            res, args = SIGNATURES[name]
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _phantom = L
+    return _phantom

@@ -4,6 +4,11 @@ nvcc compiles every translation unit for sm_103a in parallel, then links one
 shared library with the CUDA runtime linked statically, so the library loads
 on machines without a GPU driver (nothing in it touches the GPU until an
 engine is created).  Output: <package>/_build/liblss.so (git-ignored).
+
+The synthetic-volume generators of include/lss_phantom.h are also built on
+their own, host code only, into _build/libphantom.so: a process that only
+needs the workloads' inputs (the CPU baseline) loads that one and not the
+solver library.
 """
 from __future__ import annotations
 
@@ -18,6 +23,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "liblss.so")
+PHANTOM_LIB = os.path.join(BUILD, "libphantom.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -66,11 +72,30 @@ def _compile(src: str, extra: list[str]) -> str:
     return out
 
 
+def build_phantom() -> str:
+    """libphantom.so: the generators of include/lss_phantom.h alone, built by
+    the host compiler with the same IEEE settings as liblss.so (identical
+    bits; tests/test_abi.py compares the two)."""
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(CSRC, "phantom.cpp")
+    deps = [src, os.path.join(INCLUDE, "lss.h"), os.path.join(INCLUDE, "lss_phantom.h"), __file__]
+    if _newer(PHANTOM_LIB, deps):
+        cxx = shutil.which("g++") or "g++"
+        cmd = [cxx, "-O3", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
+               "-I", INCLUDE, src, "-o", PHANTOM_LIB + ".tmp"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"phantom library build failed:\n{r.stderr}")
+        os.replace(PHANTOM_LIB + ".tmp", PHANTOM_LIB)
+    return PHANTOM_LIB
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     if force:
         for f in os.listdir(BUILD):
             os.remove(os.path.join(BUILD, f))
+    build_phantom()
     with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         objs = list(ex.map(lambda u: _compile(*u), UNITS))
     if _newer(LIB, objs):

@@ -22,6 +22,9 @@ include/lss_phantom.h (identical bits on x86-64 and aarch64).
   config5  512x512x768 three-shell phantom scaled to the box with 16 random
            radius-4 seeds in the inner shell; batch of 8 x 384^3 + 64 x 64^3.
 The scale argument shrinks a workload uniformly for tests.
+
+The generators run from _build/libphantom.so (host code only), so making a
+workload does not load the solver library.
 """
 from __future__ import annotations
 
@@ -30,7 +33,13 @@ import ctypes as C
 import numpy as np
 
 from . import _lib as L
-from .segmenter import ALPHA_DATA, MODE_NS, default_params
+
+# The defaults lss_params_default(LSS_MODE_NS) fills (tests/test_abi.py checks
+# that the two agree); kept here so that making a workload needs no solver
+# library.
+NS_DEFAULTS = {"target": 0.5, "window": 0.1, "curvature": 0.5, "time_step": 0.5, "phi_min": -4.0,
+               "phi_max": 4.0, "temporal_threshold": 0.01, "spatial_threshold": 0.0,
+               "convergence_threshold": 0.0, "neighbourhood": 26, "alpha_role": 1, "data_term": 0}
 
 
 def _p(a):
@@ -42,7 +51,7 @@ def ellipsoid(shape_zyx, centre_xyz, axes_xyz, fg, bg, noise, seed) -> np.ndarra
     out = np.zeros(shape_zyx, np.float32)
     c = np.asarray(centre_xyz, np.float32)
     a = np.asarray(axes_xyz, np.float32)
-    rc = L.load().lss_phantom_ellipsoid(nx, ny, nz, _p(c), _p(a), fg, bg, noise, seed, _p(out))
+    rc = L.load_phantom().lss_phantom_ellipsoid(nx, ny, nz, _p(c), _p(a), fg, bg, noise, seed, _p(out))
     if rc:
         raise L.LssError(rc, "lss_phantom_ellipsoid")
     return out
@@ -54,7 +63,7 @@ def shells(shape_zyx, axes_xyz_list, values, bg, disp_amp, lattice, disp_seed, b
     out = np.zeros(shape_zyx, np.float32)
     ax = np.ascontiguousarray(np.asarray(axes_xyz_list, np.float32).ravel())
     vals = np.asarray(values, np.float32)
-    rc = L.load().lss_phantom_shells(nx, ny, nz, len(values), _p(ax), _p(vals), bg, disp_amp,
+    rc = L.load_phantom().lss_phantom_shells(nx, ny, nz, len(values), _p(ax), _p(vals), bg, disp_amp,
                                      max(1, int(lattice)), disp_seed, blur, noise, noise_seed, _p(out))
     if rc:
         raise L.LssError(rc, "lss_phantom_shells")
@@ -65,20 +74,20 @@ def sdf_spheres(shape_zyx, spheres_xyzr, lo=-4.0, hi=4.0) -> np.ndarray:
     nz, ny, nx = shape_zyx
     out = np.zeros(shape_zyx, np.float32)
     s = np.ascontiguousarray(np.asarray(spheres_xyzr, np.float32).ravel())
-    rc = L.load().lss_phantom_sdf_spheres(nx, ny, nz, _p(s), len(s) // 4, lo, hi, _p(out))
+    rc = L.load_phantom().lss_phantom_sdf_spheres(nx, ny, nz, _p(s), len(s) // 4, lo, hi, _p(out))
     if rc:
         raise L.LssError(rc, "lss_phantom_sdf_spheres")
     return out
 
 
 def uniform(seed: int, index: int) -> float:
-    return float(L.load().lss_phantom_uniform(seed, index))
+    return float(L.load_phantom().lss_phantom_uniform(seed, index))
 
 
 def ns_params(T, eps, alpha, dt=0.5, **kw):
-    p = default_params(MODE_NS)
+    """LSS_MODE_NS parameters with alpha weighting the data term."""
+    p = L.lss_params(**NS_DEFAULTS)
     p.target, p.window, p.curvature, p.time_step = T, eps, alpha, dt
-    p.alpha_role = ALPHA_DATA
     for k, v in kw.items():
         setattr(p, k, v)
     return p

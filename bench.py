@@ -2,13 +2,13 @@
 
 Workload (default): the 256^3 three-shell phantom (seeded synthetic stand-in
 for the reference's BrainWeb MRI) with four radius-3 seeds, T=0.8, eps=0.1,
-alpha=0.85, dt=0.5, run until the active count stays under 0.1% of the
-initial count for 5 iterations (at most 2000).  One step = reseed from the
-device-resident volume (fill phi, union the seed spheres, rebuild the active
-set) + the full run to convergence, in LSS_MODE_NS.
+alpha=0.85 (data weight), dt=0.5, run until the active count stays under 0.1%
+of the initial count for 5 iterations (at most 2000).  The unit of work is
+one seeding plus the whole run to convergence, in LSS_MODE_NS.
 
 metric: active-voxel updates per second (sum over iterations of the active
-count, from the device counter) over the device time of the steps.
+count, from the device counter) over the device time of the steps; one step
+= reseed from the device-resident volume + the run to convergence.
 e2e: the same metric through the public API with host buffers each step
 (volume upload, seeding, run, mask readback), the volume and the mask in
 pinned host memory; e2e.pageable_value: the same with a pageable numpy volume
@@ -16,8 +16,15 @@ and a newly allocated mask array each step.
 roofline: 20 algorithmic bytes per active-voxel update (phi in, I, phi out,
 coordinate in/out) over the persistent kernel's CUDA-event time, against the
 measured HBM copy bandwidth.
+The default line also carries the other workloads, each measured briefly:
+config1 (128^3, 300 iterations, GPU and CPU), batch (48 mixed-size volumes,
+batched vs sequential plain), adjoint (192^3, K = 64), stress (512x512x768
+and the 150 GB mixed batch) and ref_mode (the reference's algorithm at
+256^3); --workload X runs one of them alone with the full step count.
 --impl reference: the CPU restatement of the path (the FP64 oracle, all host
-threads) on a bounded sample of the same workload.
+threads) on the same workload: one whole seeding + run to convergence, timed
+as --steps consecutive segments (W warm-up segments first), in a process
+that loads the oracle and the input generator only.
 Multi-GPU: replicas only (each rank runs the whole workload on its GPU).
 """
 from __future__ import annotations
@@ -131,27 +138,91 @@ def sum_over_ranks(ws, value: float) -> float:
 
 
 # DRAM bytes (read + write) of one launch of the persistent kernel on this
-# workload, from the ncu capture summarised in
-# profiles/k_ns_persistent_config2_256.md (dram__bytes_read.sum +
-# dram__bytes_write.sum, one convergence = one launch).
-DRAM_TRAFFIC = {("config2_256", 8, 8, 8, 256): 15938048}
+# workload, from an ncu capture of the build whose kernel sources hash to
+# the key's first field (profiles/k_ns_persistent_config2_256.md gives the
+# capture); a build from other sources reports null rather than a stale
+# figure.
+DRAM_TRAFFIC = {("90d5b0c6e1f1", "config2_256", 8, 8, 8, 256): 15938048}
+KERNEL_SOURCES = ("ns_kernels.cuh", "ns_engine.cu", "tma.cuh", "common.cuh")
+
+
+def kernel_source_hash() -> str:
+    import hashlib
+    h = hashlib.sha256()
+    csrc = os.path.join(ROOT, "aworkefficientgpualgorithmforlevelsetsegmentation_gb300", "csrc")
+    for f in KERNEL_SOURCES:
+        with open(os.path.join(csrc, f), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:12]
 
 
 def dram_traffic(st, name):
-    return DRAM_TRAFFIC.get((name, st["brick_x"], st["brick_y"], st["brick_z"], st["threads_per_brick"]))
+    return DRAM_TRAFFIC.get((kernel_source_hash(), name, st["brick_x"], st["brick_y"], st["brick_z"],
+                             st["threads_per_brick"]))
 
 
-def cpu_reference(cfg, iters: int, threads: int):
-    """The FP64 CPU restatement on the first `iters` iterations of the run."""
+def workload_config(cfg):
+    """The workload as both arms name it (identical dicts)."""
+    p = cfg["params"]
+    nz, ny, nx = cfg["image"].shape
+    return {"workload": cfg["name"] + "_three_shell_phantom", "mode": "LSS_MODE_NS",
+            "volume_xyz": [nx, ny, nz], "seeds": len(cfg["spheres"]),
+            "params": {"T": round(p.target, 6), "eps": round(p.window, 6), "alpha": round(p.curvature, 6),
+                       "dt": round(p.time_step, 6), "alpha_weights": "data", "data_term": "normalised"},
+            "stopping": "n < 0.1% n0 for 5 iterations, max 2000",
+            "unit_of_work": "seeding + the whole run to convergence"}
+
+
+def oracle_run(cfg, threads, parts=1, warmup_parts=0, max_iters=None):
+    """The FP64 oracle on the host cores: seeding (phi and the initial active
+    set) + the run to the workload's stopping rule (or max_iters iterations),
+    timed as `parts` consecutive segments of about equal iteration counts
+    (the last one runs to the stop); `warmup_parts` untimed segments from the
+    seeds come first.  Returns (updates, seconds, iterations, per-part ms)."""
     from oracle.oracle import NsOracle
     p = cfg["params"]
-    o = NsOracle(cfg["image"], threads=threads)
-    o.set_params(p.target, p.window, p.curvature, p.time_step, alpha_data=p.alpha_role)
-    o.set_phi(cfg["phi0"])
-    t0 = time.perf_counter()
-    o.step(iters)
-    dt = time.perf_counter() - t0
-    return o.updates, dt
+    conv = cfg.get("conv")
+    o = NsOracle(cfg["image"], brick=(8, 8, 8), threads=threads)
+    o.set_params(p.target, p.window, p.curvature, p.time_step, p.phi_min, p.phi_max,
+                 p.temporal_threshold, p.spatial_threshold, 26, p.alpha_role)
+    expect = max_iters or 450  # iterations of the 256^3 run (434), for the split
+    seg = max(1, -(-expect // max(1, parts)))
+
+    def segment(state, m):
+        for _ in range(m):
+            n = o.n
+            o.step(1)
+            state["it"] += 1
+            if max_iters is not None:
+                if state["it"] >= max_iters:
+                    return True
+                continue
+            state["streak"] = state["streak"] + 1 if n < conv["rel"] * o.n0 else 0
+            if state["streak"] >= conv["patience"] or n == 0 or state["it"] >= conv["max_iterations"]:
+                return True
+        return False
+
+    if warmup_parts:
+        o.set_phi(cfg["phi0"])
+        st = {"it": 0, "streak": 0}
+        for _ in range(warmup_parts):
+            if segment(st, seg):
+                break
+    u0 = o.updates
+    st = {"it": 0, "streak": 0}
+    part_ms, stopped = [], False
+    t_all = time.perf_counter()
+    for k in range(parts):
+        t0 = time.perf_counter()
+        if k == 0:
+            o.set_phi(cfg["phi0"])
+            u0 = o.updates
+        stopped = segment(st, seg if k < parts - 1 else 1 << 30)
+        part_ms.append(1e3 * (time.perf_counter() - t0))
+        if stopped:
+            break
+    dt = time.perf_counter() - t_all
+    return o.updates - u0, dt, st["it"], part_ms
 
 
 def run_reference(args, ws, rank):
@@ -160,27 +231,23 @@ def run_reference(args, ws, rank):
     from aworkefficientgpualgorithmforlevelsetsegmentation_gb300 import phantoms as P
     cfg = P.config2(args.scale)
     threads = os.cpu_count() or 1
-    # A bounded sample per step (the first ref_step_iters iterations from the
-    # seeds), so --steps 20 --warmup 3 ends within a few minutes.
-    iters = args.ref_step_iters
-    times, ups = [], []
-    for s in range(args.warmup + args.steps):
-        u, dt = cpu_reference(cfg, iters, threads)
-        if s >= args.warmup:
-            times.append(dt)
-            ups.append(u)
-    value = sum(ups) / sum(times)
+    steps = max(1, args.steps)
+    upd, sec, its, part_ms = oracle_run(cfg, threads, steps, args.warmup)
+    value = upd / sec
+    c1 = P.config1(args.scale)
+    u1, s1, i1, _ = oracle_run(c1, threads, 1, 0, max_iters=c1["iterations"])
     line = {
         "impl": "reference", "metric": "active_voxel_updates_per_s", "value": value,
         "unit": "voxel_updates/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
+        "ms_per_step": 1e3 * sec / max(1, len(part_ms)), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": cfg["name"] + "_three_shell_phantom",
-                   "sample": f"first {iters} iterations from the seeds"},
+        "config": workload_config(cfg),
         "cpu_baseline": {"value": value, "unit": "voxel_updates/s", "cores": threads, "kind": "port",
-                         "sample": f"first {iters} iterations of {cfg['name']} per step (FP64 oracle; "
-                                   "the update phase runs on all threads, the active-set expansion "
-                                   "on one)"},
+                         "sample": f"one whole run of {cfg['name']} (seeding + {its} iterations to "
+                                   f"convergence, {upd} updates) timed as {len(part_ms)} consecutive "
+                                   f"segments; FP64 oracle on all host threads",
+                         "config1": {"value": u1 / s1, "ms": 1e3 * s1, "iterations": i1,
+                                     "voxel_updates": int(u1), "workload": c1["name"]}},
         "e2e": {"value": value, "unit": "voxel_updates/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -188,6 +255,7 @@ def run_reference(args, ws, rank):
 
 
 def run_ours(args, ws, rank, local):
+    import ctypes
     import torch
     import aworkefficientgpualgorithmforlevelsetsegmentation_gb300 as lss
     from aworkefficientgpualgorithmforlevelsetsegmentation_gb300 import phantoms as P
@@ -202,7 +270,6 @@ def run_ours(args, ws, rank, local):
     threads = args.threads or (256 if not args.brick else 0)
     seg = lss.Segmenter(lss.MODE_NS, device=local, brick=brick, threads_per_brick=threads)
     stream = torch.cuda.Stream(device=local)
-    import ctypes
     seg._chk(seg._lib.lss_set_stream(seg._h, ctypes.c_void_p(stream.cuda_stream)))
     seg.load_volume(cfg["image"])
     seg.set_parameters(p.target, p.window, p.curvature, p.time_step, alpha_role=p.alpha_role)
@@ -285,39 +352,50 @@ def run_ours(args, ws, rank, local):
     dense_ms_per_it = seg.step_dense(args.dense_iters) / args.dense_iters
     sparse_ms = ev_ms / args.steps
     dense_ms = dense_ms_per_it * statistics.mean(iters)
+    del seg
+    torch.cuda.synchronize()
 
     peak, peak_kind = measured_peak()
     achieved = BYTES_PER_UPDATE * updates / (kern_ms / 1e3) / 1e9
     traffic = dram_traffic(st, cfg["name"])
+    extra = {}
+    if not args.no_extra:
+        extra["config1"] = measure_config1(local, args.scale, 10, 3, cpu=rank == 0 and not args.no_cpu)
+        extra["batch"] = measure_batch(local, args.scale, 3, 1)
+        extra["adjoint"] = measure_adjoint(local, args.scale, 10, 3)
+        extra["stress"] = measure_stress(local, args.scale, 2, 1)
+        extra["ref_mode"] = measure_ref_mode(local, args.scale, 5, 2)
     if rank == 0:
-        cpu_u, cpu_t = (None, None)
+        cpu = None
         if not args.no_cpu:
-            cpu_u, cpu_t = cpu_reference(cfg, args.ref_iters, os.cpu_count() or 1)
+            cu, ct, cit, _ = oracle_run(cfg, os.cpu_count() or 1)
+            cpu = {"value": cu / ct, "unit": "voxel_updates/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"one whole run of {cfg['name']} (seeding + {cit} iterations to convergence, "
+                             f"{cu} updates); FP64 oracle on all host threads"}
+            if "config1" in extra:
+                cpu["config1"] = extra["config1"].pop("cpu")
         line = {
             "metric": "active_voxel_updates_per_s", "value": value, "unit": "voxel_updates/s",
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": cfg["name"] + "_three_shell_phantom", "mode": "LSS_MODE_NS",
-                       "stopping": "n < 0.1% n0 for 5 iterations, max 2000",
-                       "iterations_to_converge": iters[-1],
-                       "converge_ms": sparse_ms,
-                       "brick": [st["brick_x"], st["brick_y"], st["brick_z"]],
-                       "block0_update_ms": st["update_ms"], "block0_barrier_ms": st["barrier_ms"],
-                       "threads_per_brick": st["threads_per_brick"],
-                       "l2": "flushed between steps (256 MiB write); volume 192 MiB > L2",
-                       "parallelism": "replicas" if ws > 1 else "single"},
+            "config": workload_config(cfg),
+            "run": {"iterations_to_converge": iters[-1], "converge_ms": sparse_ms,
+                    "brick": [st["brick_x"], st["brick_y"], st["brick_z"]],
+                    "threads_per_brick": st["threads_per_brick"], "grid_blocks": st["grid_blocks"],
+                    "block0_update_ms": st["update_ms"], "block0_barrier_ms": st["barrier_ms"],
+                    "l2": "flushed between steps (256 MiB write); volume 192 MiB > L2",
+                    "parallelism": "replicas" if ws > 1 else "single"},
             "dense_gpu": {"ms_to_same_iterations": dense_ms, "ms_per_iteration": dense_ms_per_it,
                           "sparse_speedup": dense_ms / sparse_ms},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                         "traffic_source": None if traffic is None else
+                         "ncu capture of this kernel build (profiles/k_ns_persistent_config2_256.md)",
+                         "kernel_source_hash": kernel_source_hash(),
                          "bytes_per_update": BYTES_PER_UPDATE,
                          "algorithmic_bytes_per_launch": BYTES_PER_UPDATE * updates / args.steps},
-            "cpu_baseline": None if cpu_u is None else {
-                "value": cpu_u / cpu_t, "unit": "voxel_updates/s", "cores": os.cpu_count(),
-                "kind": "port", "sample": f"first {args.ref_iters} iterations of {cfg['name']} (FP64 "
-                                          "oracle; the update phase on all threads, the active-set "
-                                          "expansion on one)"},
+            "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "voxel_updates/s",
                     "h2d_bytes_per_step": int(img.nbytes),
                     "d2h_bytes_per_step": int(mask.nbytes),
@@ -326,26 +404,59 @@ def run_ours(args, ws, rank, local):
             "gpu_launches": int(launches_steps),
             "clocks": clk.summary(),
         }
+        line.update(extra)
         print(json.dumps(line), flush=True)
 
 
-def run_batch(args, ws, rank, local):
+def measure_config1(local, scale, steps, warmup, cpu=True):
+    """Config 1: the 128^3 ellipsoid, phi0 = signed distance to a radius-5
+    sphere, 300 iterations; GPU device time (set_phi + 300 iterations) and the
+    FP64 oracle on all host threads."""
+    import torch
+    import aworkefficientgpualgorithmforlevelsetsegmentation_gb300 as lss
+    from aworkefficientgpualgorithmforlevelsetsegmentation_gb300 import phantoms as P
+    c = P.config1(scale)
+    p = c["params"]
+    s = lss.Segmenter(lss.MODE_NS, device=local, brick=(8, 8, 8), threads_per_brick=256)
+    s.load_volume(c["image"])
+    s.set_parameters(p.target, p.window, p.curvature, p.time_step, alpha_role=p.alpha_role)
+    ms, upd = [], 0
+    for k in range(warmup + steps):
+        s.set_phi(c["phi0"])
+        s.step(c["iterations"])
+        st = s.stats()
+        if k >= warmup:
+            ms.append(st["last_step_ms"])
+            upd = st["voxel_updates"]
+    out = {"workload": c["name"] + "_ellipsoid", "iterations": c["iterations"],
+           "gpu": {"ms": statistics.median(ms), "voxel_updates": int(upd),
+                   "value": upd / (statistics.median(ms) / 1e3), "unit": "voxel_updates/s"}}
+    del s
+    torch.cuda.synchronize()
+    if cpu:
+        u1, s1, i1, _ = oracle_run(c, os.cpu_count() or 1, max_iters=c["iterations"])
+        out["cpu"] = {"value": u1 / s1, "ms": 1e3 * s1, "iterations": i1, "voxel_updates": int(u1),
+                      "cores": os.cpu_count(), "kind": "port", "workload": c["name"]}
+    return out
+
+
+def measure_batch(local, scale, steps, warmup, brick=None, threads=0):
     """Batched form: the 48 mixed-size single-ellipsoid volumes in one
-    persistent launch against the same volumes run one after another through
-    the plain engine.  Both arms use the same brick configuration."""
+    persistent launch (autotuned brick configuration unless `brick` fixes
+    it) against the same volumes run one after another through the plain
+    engine (8^3 x 256 unless `brick` fixes it)."""
     import torch
     import aworkefficientgpualgorithmforlevelsetsegmentation_gb300 as lss
     from aworkefficientgpualgorithmforlevelsetsegmentation_gb300 import phantoms as P
 
-    torch.cuda.set_device(local)
-    cfg = P.config3(48, scale=args.scale)
+    cfg = P.config3(48, scale=scale)
     vols, conv = cfg["volumes"], cfg["conv"]
-    brick = tuple(args.brick) if args.brick else (8, 8, 8)
-    threads = args.threads or 256
+    pbrick = tuple(brick) if brick else (8, 8, 8)
+    pthreads = threads or 256
     segs = []
     for v in vols:
         p = v["params"]
-        s = lss.Segmenter(lss.MODE_NS, device=local, brick=brick, threads_per_brick=threads)
+        s = lss.Segmenter(lss.MODE_NS, device=local, brick=pbrick, threads_per_brick=pthreads)
         s.load_volume(v["image"])
         s.set_parameters(p.target, p.window, p.curvature, p.time_step, alpha_role=p.alpha_role)
         segs.append(s)
@@ -361,10 +472,7 @@ def run_batch(args, ws, rank, local):
             upd += st["voxel_updates"]
         return dev_ms, upd, its
 
-    # The batched form picks its brick configuration with the autotuner (the
-    # first, untimed run tunes; later runs reuse the cached choice) unless
-    # --brick fixes it; the plain arm uses the plain engine's configuration.
-    bbrick, bthreads = (brick, threads) if args.brick else ((0, 0, 0), 0)
+    bbrick, bthreads = (pbrick, pthreads) if brick else ((0, 0, 0), 0)
 
     def batched():
         b = lss.Batch(device=local, brick=bbrick, threads_per_brick=bthreads)
@@ -377,49 +485,56 @@ def run_batch(args, ws, rank, local):
         st = [b.stats(i) for i in range(len(vols))]
         return b, wall, st[0]["last_step_ms"], sum(x["voxel_updates"] for x in st), it
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         plain_all()
-    seq_wall, seq_dev, seq_upd = [], [], 0
-    for _ in range(args.steps):
+    seq_wall, seq_dev, seq_upd, its = [], [], 0, []
+    for _ in range(steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         d, u, its = plain_all()
         seq_wall.append(1e3 * (time.perf_counter() - t0))
         seq_dev.append(d)
         seq_upd = u
-    for _ in range(args.warmup):
+    for _ in range(max(1, warmup)):  # the first run tunes the brick configuration
         batched()
     bat_wall, bat_dev = [], []
-    for _ in range(args.steps):
+    for _ in range(steps):
         b, w, d, bupd, bit = batched()
         bat_wall.append(w)
         bat_dev.append(d)
     same = all(np.array_equal(b.read_mask(i), segs[i].get_saveable_segmentation())
                for i in range(0, len(vols), 7))
+    sw, bw = statistics.median(seq_wall), statistics.median(bat_wall)
+    out = {"workload": cfg["name"] + "_mixed_size_ellipsoids", "volumes": len(vols),
+           "voxels": int(sum(v["image"].size for v in vols)),
+           "speedup_wall": sw / bw,
+           "speedup_device": statistics.median(seq_dev) / statistics.median(bat_dev),
+           "sequential_plain": {"ms_wall": sw, "ms_device": statistics.median(seq_dev),
+                                "voxel_updates": int(seq_upd), "iterations_max": int(max(its)),
+                                "brick": list(pbrick), "threads_per_brick": pthreads},
+           "batched": {"ms_wall": bw, "ms_device": statistics.median(bat_dev), "voxel_updates": int(bupd),
+                       "iterations": int(bit), "updates_per_s": bupd / (bw / 1e3),
+                       "brick": [b.stats(0)["brick_x"], b.stats(0)["brick_y"], b.stats(0)["brick_z"]],
+                       "threads_per_brick": b.stats(0)["threads_per_brick"],
+                       "block_threads": b.stats(0)["block_threads"]},
+           "masks_identical_to_plain": bool(same), "steps": steps}
+    del b, segs
+    torch.cuda.synchronize()
+    return out
+
+
+def run_batch(args, ws, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    r = measure_batch(local, args.scale, args.steps, args.warmup, args.brick, args.threads)
     if rank == 0:
-        sw, bw = statistics.median(seq_wall), statistics.median(bat_wall)
-        line = {
-            "metric": "batched_vs_sequential_plain_speedup", "value": sw / bw, "unit": "x",
-            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
-            "dtype": "f32", "data": "synthetic",
-            "config": {"workload": cfg["name"] + "_mixed_size_ellipsoids", "volumes": len(vols),
-                       "voxels": int(sum(v["image"].size for v in vols)),
-                       "plain_brick": list(brick), "plain_threads_per_brick": threads,
-                       "batched_brick": [b.stats(0)["brick_x"], b.stats(0)["brick_y"], b.stats(0)["brick_z"]],
-                       "batched_threads_per_brick": b.stats(0)["threads_per_brick"],
-                       "batched_block_threads": b.stats(0)["block_threads"]},
-            "sequential_plain": {"ms_wall": sw, "ms_device": statistics.median(seq_dev),
-                                 "voxel_updates": int(seq_upd), "iterations_max": int(max(its))},
-            "batched": {"ms_wall": bw, "ms_device": statistics.median(bat_dev),
-                        "voxel_updates": int(bupd), "iterations": int(bit),
-                        "updates_per_s": bupd / (bw / 1e3)},
-            "device_speedup": statistics.median(seq_dev) / statistics.median(bat_dev),
-            "masks_identical_to_plain": bool(same),
-        }
+        line = {"metric": "batched_vs_sequential_plain_speedup", "value": r["speedup_wall"], "unit": "x",
+                "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                "dtype": "f32", "data": "synthetic", "config": {"workload": r["workload"]}, "batch": r}
         print(json.dumps(line), flush=True)
 
 
-def run_stress(args, ws, rank, local):
+def measure_stress(local, scale, steps, warmup, brick=None, threads=0):
     """Large plain volume (512x512x768 three-shell phantom, 16 radius-4
     seeds) to convergence, and the mixed batch (8 volumes of 384^3 + 64 of
     64^3) in one persistent launch under a 150 GB HBM budget."""
@@ -427,23 +542,22 @@ def run_stress(args, ws, rank, local):
     import aworkefficientgpualgorithmforlevelsetsegmentation_gb300 as lss
     from aworkefficientgpualgorithmforlevelsetsegmentation_gb300 import phantoms as P
 
-    torch.cuda.set_device(local)
     t0 = time.perf_counter()
-    cfg = P.config5(args.scale)
+    cfg = P.config5(scale)
     gen_s = time.perf_counter() - t0
     p, conv = cfg["params"], cfg["conv"]
-    brick = tuple(args.brick) if args.brick else (8, 8, 8)
-    threads = args.threads or 256
+    brick = tuple(brick) if brick else (8, 8, 8)
+    threads = threads or 256
     seg = lss.Segmenter(lss.MODE_NS, device=local, brick=brick, threads_per_brick=threads)
     seg.load_volume(cfg["image"])
     seg.set_parameters(p.target, p.window, p.curvature, p.time_step, alpha_role=p.alpha_role)
     runs = []
-    for s in range(args.warmup + args.steps):
+    for s in range(warmup + steps):
         seg.clear_current_segmentation()
         seg.set_seed_spheres(cfg["spheres"])
         it = seg.step_until_converged(conv["rel"], conv["patience"], conv["max_iterations"])
         st = seg.stats()
-        if s >= args.warmup:
+        if s >= warmup:
             runs.append((st["last_step_ms"], st["voxel_updates"], it))
     ms = statistics.median(r[0] for r in runs)
     upd = runs[-1][1]
@@ -454,13 +568,14 @@ def run_stress(args, ws, rank, local):
              "roofline": {"achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                           "peak_kind": peak_kind, "bytes_per_update": BYTES_PER_UPDATE},
              "device_bytes": int(st["device_bytes"]), "phantom_s": gen_s}
-    del seg
+    del seg, cfg
+    torch.cuda.synchronize()
     # Mixed batch under a 150 GB budget: 8 three-shell volumes of 384^3 and
     # 64 single-ellipsoid volumes of 64^3.
-    big = P.config2(1.5 * args.scale)
+    big = P.config2(1.5 * scale)
     vols = [(big["image"], big["params"], big["spheres"]) for _ in range(8)]
     rng = np.random.default_rng(9)
-    m = max(16, int(round(64 * args.scale)))
+    m = max(16, int(round(64 * scale)))
     for i in range(64):
         c = (m - 1) / 2 + rng.uniform(-0.1, 0.1, 3) * m
         axes = rng.uniform(0.2, 0.4, 3) * m
@@ -479,13 +594,20 @@ def run_stress(args, ws, rank, local):
              "ms_device": bst[0]["last_step_ms"], "ms_wall": bwall, "voxel_updates": int(bupd),
              "updates_per_s": bupd / (bst[0]["last_step_ms"] / 1e3),
              "device_bytes": int(bst[0]["device_bytes"]), "hbm_budget_bytes": 150 << 30}
+    del b
+    torch.cuda.synchronize()
+    return {"plain": plain, "batch": batch, "brick": list(brick), "threads_per_brick": threads}
+
+
+def run_stress(args, ws, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    r = measure_stress(local, args.scale, args.steps, args.warmup, args.brick, args.threads)
     if rank == 0:
-        print(json.dumps({"metric": "stress", "plain": plain, "batch": batch, "dtype": "f32",
-                          "data": "synthetic", "brick": list(brick), "threads_per_brick": threads}),
-              flush=True)
+        print(json.dumps({"metric": "stress", "dtype": "f32", "data": "synthetic", **r}), flush=True)
 
 
-def run_adjoint(args, ws, rank, local):
+def measure_adjoint(local, scale, steps, warmup):
     """Differentiation form: the 192^3 two-shell phantom, K = 64 unrolled
     iterations from the seed, phi checkpointed every 8, soft-Dice loss of
     sigmoid(-phi/0.5) against the inner ellipsoid.  One step = one
@@ -502,8 +624,7 @@ def run_adjoint(args, ws, rank, local):
     import aworkefficientgpualgorithmforlevelsetsegmentation_gb300 as lss
     from aworkefficientgpualgorithmforlevelsetsegmentation_gb300 import phantoms as P
 
-    torch.cuda.set_device(local)
-    cfg = P.config4(args.scale)
+    cfg = P.config4(scale)
     p = cfg["params"]
     K, every = cfg["K"], cfg["checkpoint_every"]
     seg = lss.Segmenter(lss.MODE_NS, device=local, brick=(8, 8, 8), threads_per_brick=256)
@@ -520,52 +641,53 @@ def run_adjoint(args, ws, rank, local):
     tgt, bias, dbias = pinned(torch.uint8), pinned(torch.float32), pinned(torch.float32)
     tgt[...] = cfg["target"]
     bias[...] = 0.0
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         g = seg.adjoint(K, every, tgt, 0.5, bias=bias, d_bias_out=dbias)
     torch.cuda.synchronize()
-    barrier(ws)
-    ev_ms, nact = 0.0, 0
+    ev_ms, nact = [], 0
     launches0 = seg.stats()["kernel_launches"]
-    with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            g = seg.adjoint(K, every, tgt, 0.5, bias=bias, d_bias_out=dbias)
-            e1.record(stream)
-            e1.synchronize()
-            ev_ms += e0.elapsed_time(e1)
-            nact += g["active_voxel_iterations"]
-    launches = (seg.stats()["kernel_launches"] - launches0) // args.steps
-    torch.cuda.synchronize()
-    barrier(ws)
-    t_max = max_over_ranks(ws, ev_ms)
-    value = sum_over_ranks(ws, float(nact)) / (t_max / 1e3)
+    for _ in range(steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        g = seg.adjoint(K, every, tgt, 0.5, bias=bias, d_bias_out=dbias)
+        e1.record(stream)
+        e1.synchronize()
+        ev_ms.append(e0.elapsed_time(e1))
+        nact += g["active_voxel_iterations"]
+    launches = (seg.stats()["kernel_launches"] - launches0) // steps
+    tot = sum(ev_ms)
     peak, peak_kind = measured_peak()
-    achieved = ADJOINT_BYTES * nact / (ev_ms / 1e3) / 1e9
-    if rank == 0:
-        line = {
-            "metric": "adjoint_active_voxel_iterations_per_s", "value": value,
-            "unit": "active_voxel_iterations/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": cfg["name"] + "_two_shell_adjoint", "K": K, "checkpoint_every": every,
-                       "loss": g["loss"], "d_target": g["d_target"], "d_window": g["d_window"],
-                       "d_curvature": g["d_curvature"],
-                       "active_voxel_iterations_per_call": int(g["active_voxel_iterations"]),
-                       "brick": [8, 8, 8], "threads_per_brick": 256,
-                       "host_buffers": "pinned (target, bias, bias gradient)",
-                       "parallelism": "replicas" if ws > 1 else "single"},
+    achieved = ADJOINT_BYTES * nact / (tot / 1e3) / 1e9
+    del seg
+    torch.cuda.synchronize()
+    return {"workload": cfg["name"] + "_two_shell_adjoint", "K": K, "checkpoint_every": every,
+            "ms_per_call": tot / steps, "ms_per_call_median": statistics.median(ev_ms),
+            "active_voxel_iterations_per_call": int(g["active_voxel_iterations"]),
+            "value": nact / (tot / 1e3), "unit": "active_voxel_iterations/s",
+            "loss": g["loss"], "d_target": g["d_target"], "d_window": g["d_window"],
+            "d_curvature": g["d_curvature"], "gpu_launches_per_call": int(launches),
+            "host_buffers": "pinned (target, bias, bias gradient)",
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
-                         "bytes_per_update": ADJOINT_BYTES},
-            "gpu_launches": int(launches),
-            "clocks": clk.summary(),
-        }
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "bytes_per_update": ADJOINT_BYTES}, "steps": steps}
+
+
+def run_adjoint(args, ws, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    with ClockSampler(local) as clk:
+        r = measure_adjoint(local, args.scale, args.steps, args.warmup)
+    if rank == 0:
+        line = {"metric": "adjoint_active_voxel_iterations_per_s", "value": r["value"], "unit": r["unit"],
+                "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_call"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "config": {"workload": r["workload"]}, "adjoint": r,
+                "clocks": clk.summary()}
         print(json.dumps(line), flush=True)
 
 
-def run_ref_mode(args, ws, rank, local):
+def measure_ref_mode(local, scale, steps, warmup):
     """LSS_MODE_REF at the headline size: the reference's own solver
     reproduced bit for bit (int8 phi in 16^3 tiles, integer intensities, the
     6-connected output, duplicate-filter and compaction pipeline, one CUDA
@@ -573,16 +695,17 @@ def run_ref_mode(args, ws, rank, local):
     (round(255 I)), seeded with the same four spheres; grow level 204 (the
     inner shell's 0.8), window 26 (0.1 in u8 units), curvature weight 0.1,
     dt 0.25; run until the active count stays under 0.1 % of its initial value
-    for 5 iterations.  One step = clear + seed + run.  Metric: active-voxel
-    updates per second (device count over the iterations' CUDA-event time),
-    the figure the GTX 280 reached at 41.4 M/s with the same algorithm on
-    BrainWeb MRI (a different input: a throughput comparison only)."""
+    for 5 iterations.  One step = clear + seed + run (the state the fixtures
+    of tests/golden/make_golden_ref256.py pin as "rerun").  Metric:
+    active-voxel updates per second (device count over the iterations'
+    CUDA-event time), the figure the GTX 280 reached at 41.4 M/s with the
+    same algorithm on BrainWeb MRI (a different input: a throughput
+    comparison only)."""
     import torch
     import aworkefficientgpualgorithmforlevelsetsegmentation_gb300 as lss
     from aworkefficientgpualgorithmforlevelsetsegmentation_gb300 import phantoms as P
 
-    torch.cuda.set_device(local)
-    cfg = P.config2(args.scale)
+    cfg = P.config2(scale)
     u8 = np.clip(np.rint(cfg["image"] * 255.0), 0, 255).astype(np.uint8)
     r = lss.Segmenter(lss.MODE_REF, device=local)
     r.load_volume(u8)
@@ -597,38 +720,40 @@ def run_ref_mode(args, ws, rank, local):
         st = r.stats()
         return it, st["voxel_updates"] - u0, st["last_step_ms"]
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         one_step()
     torch.cuda.synchronize()
-    barrier(ws)
     ms, upd, its = 0.0, 0, []
     launches0 = r.stats()["kernel_launches"]
-    with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            it, u, t = one_step()
-            ms += t
-            upd += u
-            its.append(it)
-    launches = (r.stats()["kernel_launches"] - launches0) // args.steps
-    t_max = max_over_ranks(ws, ms)
-    value = sum_over_ranks(ws, float(upd)) / (t_max / 1e3)
+    for _ in range(steps):
+        it, u, t = one_step()
+        ms += t
+        upd += u
+        its.append(it)
+    launches = (r.stats()["kernel_launches"] - launches0) // steps
     mask = r.get_saveable_segmentation()
+    del r
+    torch.cuda.synchronize()
+    return {"workload": cfg["name"] + "_three_shell_phantom_u8", "mode": "LSS_MODE_REF",
+            "params": {"grow_level": 204, "grow_window": 26, "curvature": 0.1, "dt": 0.25},
+            "stopping": "n < 0.1% n0 for 5 iterations, max 2000",
+            "value": upd / (ms / 1e3), "unit": "voxel_updates/s", "ms_per_run": ms / steps,
+            "iterations_to_converge": its[-1], "updates_per_run": upd // steps,
+            "segmented_voxels": int(mask.sum()), "gpu_launches_per_run": int(launches),
+            "gtx280_published_updates_per_s": 41.4e6, "steps": steps}
+
+
+def run_ref_mode(args, ws, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    with ClockSampler(local) as clk:
+        r = measure_ref_mode(local, args.scale, args.steps, args.warmup)
     if rank == 0:
-        line = {
-            "metric": "ref_mode_active_voxel_updates_per_s", "value": value, "unit": "voxel_updates/s",
-            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int8 phi, u8 I",
-            "data": "synthetic",
-            "config": {"workload": cfg["name"] + "_three_shell_phantom_u8", "mode": "LSS_MODE_REF",
-                       "params": {"grow_level": 204, "grow_window": 26, "curvature": 0.1, "dt": 0.25},
-                       "stopping": "n < 0.1% n0 for 5 iterations, max 2000",
-                       "iterations_to_converge": its[-1], "updates_per_step": upd // args.steps,
-                       "segmented_voxels": int(mask.sum()),
-                       "gtx280_published_updates_per_s": 41.4e6,
-                       "parallelism": "replicas" if ws > 1 else "single"},
-            "gpu_launches": int(launches),
-            "clocks": clk.summary(),
-        }
+        line = {"metric": "ref_mode_active_voxel_updates_per_s", "value": r["value"], "unit": r["unit"],
+                "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_run"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "int8 phi, u8 I", "data": "synthetic", "config": {"workload": r["workload"]},
+                "ref_mode": r, "clocks": clk.summary()}
         print(json.dumps(line), flush=True)
 
 
@@ -699,10 +824,10 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--brick", type=int, nargs=3, default=None)
     ap.add_argument("--threads", type=int, default=0)
-    ap.add_argument("--ref-iters", type=int, default=150)
-    ap.add_argument("--ref-step-iters", type=int, default=80)
     ap.add_argument("--dense-iters", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="plain workload only (no config1/batch/adjoint/stress/ref_mode keys)")
     ap.add_argument("--workload", default="plain",
                     choices=["plain", "batch", "stress", "tour", "adjoint", "ref"])
     args = ap.parse_args()

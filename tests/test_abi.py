@@ -115,3 +115,31 @@ def test_readback_out_arrays_are_checked():
                 np.empty((5, 4, 3), np.uint8).transpose(2, 1, 0), ro):
         with pytest.raises(ValueError):
             _out(bad, (3, 4, 5), np.uint8)
+
+
+def test_phantom_library_matches_solver_library_and_defaults():
+    """libphantom.so (host-only generators) gives the same bits as the
+    generators inside liblss.so, and the workloads' parameter defaults equal
+    lss_params_default(LSS_MODE_NS)."""
+    from aworkefficientgpualgorithmforlevelsetsegmentation_gb300 import phantoms as P
+    L, G = lss.load(), _lib.load_phantom()
+    shape = (21, 18, 27)
+    outs = []
+    for lib in (L, G):
+        a = np.zeros(shape, np.float32)
+        ax = np.array([9, 8, 7, 5, 4, 3], np.float32)
+        vals = np.array([0.3, 0.7], np.float32)
+        assert lib.lss_phantom_shells(27, 18, 21, 2, C.c_void_p(ax.ctypes.data), C.c_void_p(vals.ctypes.data),
+                                      0.1, 2.0, 8, 5, 1.0, 0.04, 6, C.c_void_p(a.ctypes.data)) == 0
+        s = np.zeros(shape, np.float32)
+        sp = np.array([13.2, 8.5, 10.1, 3.0], np.float32)
+        assert lib.lss_phantom_sdf_spheres(27, 18, 21, C.c_void_p(sp.ctypes.data), 1, -4.0, 4.0,
+                                           C.c_void_p(s.ctypes.data)) == 0
+        outs.append((a, s, lib.lss_phantom_uniform(4, 17)))
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+    assert outs[0][2] == outs[1][2]
+    p = _lib.lss_params()
+    assert L.lss_params_default(1, C.byref(p)) == 0
+    q = _lib.lss_params(**P.NS_DEFAULTS)  # the same float32 / int32 fields
+    for k, _ in _lib.lss_params._fields_:
+        assert getattr(p, k) == getattr(q, k), k

@@ -1,7 +1,10 @@
 """bench.py's reference arm (the CPU restatement timed on the host cores)
 prints the benchmark line the driver reads: checked on the CPU at a small
-scale.  The GPU arms print the same keys plus roofline, clocks and e2e
-figures; they run in the GPU environment only."""
+scale.  The arm names the same workload as the GPU arm (the same `config`
+dict, built by one function for both), times one whole seeding + run to
+convergence, and its process loads the oracle and the input generator but
+not the solver library.  The GPU arm prints the same keys plus roofline,
+clocks and e2e figures; it runs in the GPU environment only."""
 import json
 import os
 import subprocess
@@ -9,12 +12,26 @@ import sys
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
+# Runs the reference arm in a fresh interpreter, then reports which in-tree
+# shared libraries that process mapped.
+_PROBE = r"""
+import io, json, sys, contextlib
+sys.argv = ["bench.py", "--impl", "reference", "--steps", "3", "--warmup", "1", "--scale", "0.125"]
+import bench
+buf = io.StringIO()
+with contextlib.redirect_stdout(buf):
+    bench.main()
+maps = open("/proc/self/maps").read()
+libs = sorted({l.split()[-1].rsplit("/", 1)[-1] for l in maps.splitlines() if l.endswith(".so")})
+print(json.dumps({"line": buf.getvalue(), "libs": libs}))
+"""
+
 
 def test_reference_arm_prints_one_contract_line():
-    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "0",
-                        "--scale", "0.125"], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    r = subprocess.run([sys.executable, "-c", _PROBE], cwd=ROOT, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
-    lines = [ln for ln in r.stdout.splitlines() if ln.strip()]
+    probe = json.loads(r.stdout.strip().splitlines()[-1])
+    lines = [ln for ln in probe["line"].splitlines() if ln.strip()]
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert d["impl"] == "reference"
@@ -22,9 +39,38 @@ def test_reference_arm_prints_one_contract_line():
               "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
         assert k in d, k
     assert d["metric"] == "active_voxel_updates_per_s" and d["value"] > 0 and d["higher_is_better"] is True
-    assert d["steps"] == 1 and d["n_gpus"] == 1 and "workload" in d["config"]
+    assert d["steps"] == 3 and d["n_gpus"] == 1
     cb = d["cpu_baseline"]
-    assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]
+    assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1
+    assert "to convergence" in cb["sample"] and cb["config1"]["iterations"] == 300
     e = d["e2e"]
     assert e["value"] == d["value"] and e["unit"] == d["unit"]
     assert e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
+    # The same workload dict as the GPU arm builds.
+    sys.path.insert(0, ROOT)
+    import bench
+    from aworkefficientgpualgorithmforlevelsetsegmentation_gb300 import phantoms as P
+    assert d["config"] == json.loads(json.dumps(bench.workload_config(P.config2(0.125))))
+    # Loads the oracle and the generator, not the solver library.
+    assert "liboracle.so" in probe["libs"] and "libphantom.so" in probe["libs"], probe["libs"]
+    assert "liblss.so" not in probe["libs"], probe["libs"]
+
+
+def test_oracle_run_covers_the_whole_run_in_segments():
+    """Segmenting the timed run does not change the work: any split gives
+    the same iterations and updates as one piece, and the same as the
+    oracle's own stopping-rule loop."""
+    sys.path.insert(0, ROOT)
+    import bench
+    from aworkefficientgpualgorithmforlevelsetsegmentation_gb300 import phantoms as P
+    from oracle.oracle import NsOracle
+    cfg = P.config2(0.125)
+    runs = [bench.oracle_run(cfg, 2, parts, warm) for parts, warm in ((1, 0), (4, 2), (20, 3))]
+    assert len({(r[0], r[2]) for r in runs}) == 1
+    p = cfg["params"]
+    o = NsOracle(cfg["image"], threads=2)
+    o.set_params(p.target, p.window, p.curvature, p.time_step, p.phi_min, p.phi_max,
+                 p.temporal_threshold, p.spatial_threshold, 26, p.alpha_role)
+    o.set_phi(cfg["phi0"])
+    it = o.run(cfg["conv"]["rel"], cfg["conv"]["patience"], cfg["conv"]["max_iterations"])
+    assert (o.updates, it) == (runs[0][0], runs[0][2])
