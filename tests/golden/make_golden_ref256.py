@@ -8,7 +8,9 @@ phantom quantised to u8 (round(255 I)), the four radius-3 seeds of the plain
 workload applied as consecutive InitializeSeed calls, grow level 204, window
 26, curvature 0.1, dt 0.25, one iteration a RequestUpdateSegmentation call,
 stopped once the active count stays under 0.1 % of its value after seeding
-for 5 consecutive iterations (at most 2000).
+for 5 consecutive iterations or the list is empty (at most 2000): the rule
+lss_step_until_converged applies with relative threshold 1e-3, patience 5
+and absolute threshold 0.
 
 The workload is run twice on one solver: from a fresh load, and again after
 ClearCurrentSegmentation and the same seeds (what a benchmark step does after
@@ -66,6 +68,8 @@ def run_once(o, spheres, log=None):
             snaps[it] = digest(o.active())
             if log:
                 log(f"  iteration {it}: n = {n}")
+        if n == 0:  # nothing left to update (the rule's absolute threshold, 0)
+            break
         streak = streak + 1 if n < REL * n0 else 0
         if streak >= PATIENCE:
             break
