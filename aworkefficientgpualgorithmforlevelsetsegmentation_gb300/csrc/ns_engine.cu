@@ -261,6 +261,7 @@ NsCore::~NsCore() = default;
 
 void* NsCore::workspace(uint64_t bytes) {
     if (bytes > ws_bytes_) {
+        owner_->sync();  // no kernel of an earlier call still uses the old workspace
         if (ws_) arena_.free_last(ws_);
         ws_ = nullptr;
         ws_bytes_ = 0;
