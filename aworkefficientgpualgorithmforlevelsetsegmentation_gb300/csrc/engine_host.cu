@@ -104,7 +104,10 @@ static bool cached_choice(NsCore& core, BrickConfig* out) {
     return true;
 }
 
-static BrickConfig autotune(NsCore& core, EngineBase* owner, int iters) {
+// `iters` iterations from the seeded state, or (conv non-null) the run to
+// the stopping rule: a batch spends most of its time at the widest fronts,
+// which the first iterations from the seeds do not reach.
+static BrickConfig autotune(NsCore& core, EngineBase* owner, int iters, const lss_conv* conv = nullptr) {
     auto& vols = core.vols();
     const auto key = tune_key(core);
     // Save the seeded phi of every volume.
@@ -138,7 +141,7 @@ static BrickConfig autotune(NsCore& core, EngineBase* owner, int iters) {
         for (size_t i = 0; i < vols.size(); ++i) core.set_phi((int)i, saved[i].data());
         core.init_active();
         float ms = 0;
-        core.run(iters, nullptr, &ms);
+        core.run(conv ? conv->max_iterations : iters, conv, &ms);
         if (ms < best_ms) { best_ms = ms; best = c; }
     }
     core.configure(best);
@@ -454,9 +457,9 @@ class BatchEngine : public EngineBase {
             for (size_t k = 0; k + 3 < seeds_[v].size(); k += 4)
                 core_.sphere_union(v, seeds_[v][k], seeds_[v][k + 1], seeds_[v][k + 2], seeds_[v][k + 3]);
         core_.init_active();
-        if (!tuned) autotune(core_, this, 32);
-        float ms = 0;
         lss_conv cv = conv ? *conv : lss_conv{0.0, 1, 1000, 0};
+        if (!tuned) autotune(core_, this, 0, &cv);  // each configuration runs the whole batch once
+        float ms = 0;
         int it = core_.run(cv.max_iterations, &cv, &ms);
         last_ms_ = ms;
         ran_ = true;
