@@ -160,9 +160,37 @@ __global__ void __launch_bounds__(256) k_adj_update(NsVol V, const float* __rest
             if (any) adj_dilate_brick<S>(V, b, chg, threadIdx.x, blockDim.x, nxt, flag_next, list_next, count_next);
         }
     }
-    if (nact) {
+    if (nact) {  // uniform: one atomic per block on the shared counter, not one per warp
+        __shared__ uint32_t s_cnt;
+        if (threadIdx.x == 0) s_cnt = 0u;
+        __syncthreads();
         mine = __reduce_add_sync(0xffffffffu, mine);
-        if ((threadIdx.x & 31) == 0 && mine) atomicAdd(nact, (unsigned long long)mine);
+        if ((threadIdx.x & 31) == 0 && mine) atomicAdd(&s_cnt, mine);
+        __syncthreads();
+        if (threadIdx.x == 0 && s_cnt) atomicAdd(nact, (unsigned long long)s_cnt);
+    }
+}
+
+// The bricks of lists k_lo .. k_hi (list k at lists + k * stride, count k at
+// counts[k]; bricks may repeat) copied from src to dst, a brick a block.
+template <class S>
+__global__ void __launch_bounds__(256) k_adj_copy_bricks(NsVol V, const float* __restrict__ src,
+                                                         float* __restrict__ dst, const uint32_t* __restrict__ lists,
+                                                         uint64_t stride, const uint32_t* __restrict__ counts,
+                                                         int k_lo, int k_hi) {
+    for (int k = k_lo; k <= k_hi; ++k) {
+        const uint32_t n = counts[k];
+        const uint32_t* list = lists + (uint64_t)k * stride;
+        for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
+            const uint32_t b = list[i];
+            for (int j = threadIdx.x; j < S::VOX; j += blockDim.x) {
+                const int3 p = voxel_of<S>(V, b, j);
+                if (p.x < V.nx && p.y < V.ny && p.z < V.nz) {
+                    const size_t idx = ((size_t)p.z * V.py + p.y) * V.px + p.x;
+                    dst[idx] = src[idx];
+                }
+            }
+        }
     }
 }
 
@@ -283,10 +311,11 @@ __device__ __forceinline__ void ns_update_vjp_f32(PF P, AF add, float I, float b
     g4[2] += lam * (V.alpha_data ? du_dalpha : -du_dalpha);
 }
 
-// Block sum of three doubles into gsum[0..2] (one atomic each per block;
-// none for a zero sum, which changes nothing: most blocks of a sparse
-// reverse iteration hold no active brick, and the atomics of one address
-// serialise).
+// Block sum of three doubles into gsum[0..2]: one atomic each per block (none
+// for a zero sum, which changes nothing), or, with Slot, added into the
+// block's own three words (gsum = its slot; no other block writes them, so
+// no atomics, and launches of the same grid accumulate in a fixed order).
+template <bool Slot = false>
 __device__ __forceinline__ void block_sum3(double a0, double a1, double a2, double* gsum) {
     __shared__ double s[3][32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -308,7 +337,11 @@ __device__ __forceinline__ void block_sum3(double a0, double a1, double a2, doub
             a1 += __shfl_down_sync(0xffffffffu, a1, o);
             a2 += __shfl_down_sync(0xffffffffu, a2, o);
         }
-        if (lane == 0) {
+        if (lane == 0 && Slot) {
+            gsum[0] += a0;
+            gsum[1] += a1;
+            gsum[2] += a2;
+        } else if (lane == 0) {
             if (a0 != 0.0) atomicAdd(&gsum[0], a0);
             if (a1 != 0.0) atomicAdd(&gsum[1], a1);
             if (a2 != 0.0) atomicAdd(&gsum[2], a2);
@@ -320,13 +353,13 @@ __device__ __forceinline__ void block_sum3(double a0, double a1, double a2, doub
 // Reverse iteration k, second half (block per brick of list_k): scatters U
 // (lambda_{k+1}) of the voxels of A_k through the update's transposed
 // Jacobian into lam, adds the bias gradient and the parameter gradients
-// (gsum[0..2] = T, eps, alpha; FP64).
+// (T, eps, alpha; FP64) into the block's slot gpart[3 * blockIdx.x ..].
 template <class S>
 __global__ void __launch_bounds__(256) k_adj_vjp(NsVol V, const float* __restrict__ phi,
                                                  const unsigned long long* __restrict__ act,
                                                  const uint32_t* __restrict__ list, const uint32_t* count,
                                                  const float* __restrict__ U, float* lam, float* dbias,
-                                                 double* gsum) {
+                                                 double* gpart) {
     const uint32_t n = *count;
     double sT = 0.0, sE = 0.0, sA = 0.0;
     for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
@@ -354,7 +387,7 @@ __global__ void __launch_bounds__(256) k_adj_vjp(NsVol V, const float* __restric
             if (dbias) dbias[idx] += g4[3];
         }
     }
-    block_sum3(sT, sE, sA, gsum);  // every thread of the block reaches it
+    block_sum3<true>(sT, sE, sA, gpart + 3 * (size_t)blockIdx.x);  // every thread of the block reaches it
 }
 
 // Soft-Dice sums over the volume: gsum[0..2] = (sum s, sum t, sum s t).
@@ -417,7 +450,8 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     auto al = [](uint64_t b) { return (b + 255) / 256 * 256; };
     const uint64_t nfields = (uint64_t)nck + (every - 1) + 4 + (dbias ? 1 : 0) + (bias ? 1 : 0);
     const uint64_t total = nfields * al(P * 4) + (uint64_t)(K + 1) * al(mwords * 8) +
-                           2 * (uint64_t)(K + 1) * al((uint64_t)nb * 4) + al((uint64_t)(K + 1) * 4) + al(P) + 256;
+                           2 * (uint64_t)(K + 1) * al((uint64_t)nb * 4) + al((uint64_t)(K + 1) * 4) + al(P) + 256 +
+                           al((uint64_t)bgrid * 3 * sizeof(double));
     char* base = (char*)core.workspace(total);
     auto carve = [&](uint64_t bytes) {
         char* p = base;
@@ -440,6 +474,7 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     uint8_t* tgt = (uint8_t*)carve(P);
     double* gsum = (double*)carve(8 * sizeof(double) + 8);
     unsigned long long* nact = (unsigned long long*)(gsum + 8);
+    double* gpart = (double*)carve((uint64_t)bgrid * 3 * sizeof(double));  // per-block dT, deps, dalpha
     float* dbias_d = dbias ? F() : nullptr;
     auto count_k = [&](int k) { return counts + k; };
     // Target and bias into the padded layout on the device (pinned host
@@ -467,6 +502,7 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     }
     if (dbias_d) LSS_CUDA(cudaMemsetAsync(dbias_d, 0, P * 4, st));
     LSS_CUDA(cudaMemsetAsync(gsum, 0, 8 * sizeof(double) + 8, st));
+    LSS_CUDA(cudaMemsetAsync(gpart, 0, (uint64_t)bgrid * 3 * sizeof(double), st));
     LSS_CUDA(cudaMemsetAsync(act[1], 0, (uint64_t)K * al(mwords * 8), st));  // act[1..K] are contiguous
     LSS_CUDA(cudaMemsetAsync(flag[0], 0, (uint64_t)(K + 1) * al((uint64_t)nb * 4), st));
     LSS_CUDA(cudaMemsetAsync(counts, 0, (uint64_t)(K + 1) * 4, st));
@@ -495,21 +531,35 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     count();
     k_adj_dice_grad<<<grid, 256, 0, st>>>(V, phiK, tgt, tau, gsum + 4, lam);
     count();
-    // Reverse, segment by segment from the last checkpoint.
+    // Reverse, segment by segment from the last checkpoint.  seg[i] holds
+    // phi_{held[i]} (-1: nothing of this call): to turn it into phi_{k+1}
+    // only the bricks of lists k+1 .. held[i]-1 can differ from phi_k (the
+    // bricks of list_k are rewritten whole by the update), so only those are
+    // copied from seg[i-1] = phi_k; the first use copies the whole field.
+    const uint64_t lstride = al((uint64_t)nb * 4) / 4;
+    std::vector<int> held(every, -1);
     for (int sgi = nck - 1; sgi >= 0; --sgi) {
         const int s0 = sgi * every, s1 = std::min(K, s0 + every);
         seg[0] = ck[sgi];
         for (int k = s0; k + 1 < s1; ++k) {
-            float* d = seg[k - s0 + 1];
-            LSS_CUDA(cudaMemcpyAsync(d, seg[k - s0], P * 4, cudaMemcpyDeviceToDevice, st));
-            k_adj_update<S><<<bgrid, 256, 0, st>>>(V, seg[k - s0], d, act[k], list[k], count_k(k), nullptr,
+            const int i = k - s0 + 1;
+            float* d = seg[i];
+            if (held[i] < 0) {
+                LSS_CUDA(cudaMemcpyAsync(d, seg[i - 1], P * 4, cudaMemcpyDeviceToDevice, st));
+            } else if (held[i] - 1 >= k + 1) {
+                k_adj_copy_bricks<S><<<bgrid, 256, 0, st>>>(V, seg[i - 1], d, list[0], lstride, counts, k + 1,
+                                                            held[i] - 1);
+                count();
+            }
+            k_adj_update<S><<<bgrid, 256, 0, st>>>(V, seg[i - 1], d, act[k], list[k], count_k(k), nullptr,
                                                    nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
             count();
+            held[i] = k + 1;
         }
         for (int k = s1 - 1; k >= s0; --k) {
             k_adj_take<S><<<bgrid, 256, 0, st>>>(V, act[k], list[k], count_k(k), lam, U);
             count();
-            k_adj_vjp<S><<<bgrid, 256, 0, st>>>(V, seg[k - s0], act[k], list[k], count_k(k), U, lam, dbias_d, gsum);
+            k_adj_vjp<S><<<bgrid, 256, 0, st>>>(V, seg[k - s0], act[k], list[k], count_k(k), U, lam, dbias_d, gpart);
             count();
         }
     }
@@ -522,14 +572,20 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     }
     double h[8];
     unsigned long long na = 0;
+    std::vector<double> parts((size_t)bgrid * 3);
     LSS_CUDA(cudaMemcpyAsync(h, gsum, sizeof(h), cudaMemcpyDeviceToHost, st));
     LSS_CUDA(cudaMemcpyAsync(&na, nact, 8, cudaMemcpyDeviceToHost, st));
+    LSS_CUDA(cudaMemcpyAsync(parts.data(), gpart, parts.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
     owner->sync();
+    // The blocks' parameter sums, added in block order (the same every call).
+    double g3[3] = {0.0, 0.0, 0.0};
+    for (int b = 0; b < bgrid; ++b)
+        for (int q = 0; q < 3; ++q) g3[q] += parts[(size_t)3 * b + q];
     const double den = h[4] + h[5];
     out->loss = 1.0 - 2.0 * h[6] / den;
-    out->d_target = h[0];
-    out->d_window = h[1];
-    out->d_curvature = h[2];
+    out->d_target = g3[0];
+    out->d_window = g3[1];
+    out->d_curvature = g3[2];
     out->active_voxel_iterations = na;
 }
 
