@@ -18,7 +18,7 @@ class lss_config(C.Structure):
     _fields_ = [("mode", C.c_int32), ("device", C.c_int32), ("brick_x", C.c_int32),
                 ("brick_y", C.c_int32), ("brick_z", C.c_int32), ("threads_per_brick", C.c_int32),
                 ("ref_quirk_i3", C.c_int32), ("use_graph", C.c_int32),
-                ("hbm_budget_bytes", C.c_uint64)]
+                ("hbm_budget_bytes", C.c_uint64), ("brick_workers", C.c_int32), ("pad_", C.c_int32)]
 
 
 class lss_params(C.Structure):

@@ -84,7 +84,7 @@ static std::map<std::tuple<int, int, int, int>, BrickConfig> g_tune_cache;
 
 static bool same_config(const BrickConfig& a, const BrickConfig& b) {
     return a.bx == b.bx && a.by == b.by && a.bz == b.bz && a.threads == b.threads &&
-           a.min_blocks == b.min_blocks;
+           a.min_blocks == b.min_blocks && a.groups == b.groups;
 }
 
 static std::tuple<int, int, int, int> tune_key(NsCore& core) {
@@ -197,7 +197,8 @@ class NsEngine : public EngineBase {
         BrickConfig c = brick_configs()[0];
         tuned_ = cfg.brick_x > 0;
         if (cfg.brick_x > 0) c = BrickConfig{cfg.brick_x, cfg.brick_y, cfg.brick_z,
-                                             cfg.threads_per_brick > 0 ? cfg.threads_per_brick : 256};
+                                             cfg.threads_per_brick > 0 ? cfg.threads_per_brick : 256, 0,
+                                             cfg.brick_workers > 1 ? cfg.brick_workers : 1};
         else
             tuned_ = cached_choice(*core_, &c);
         core_->configure(c);
@@ -449,7 +450,8 @@ class BatchEngine : public EngineBase {
         bool tuned = cfg.brick_x > 0;
         if (cfg.brick_x > 0)
             c = BrickConfig{cfg.brick_x, cfg.brick_y, cfg.brick_z,
-                            cfg.threads_per_brick > 0 ? cfg.threads_per_brick : 256};
+                            cfg.threads_per_brick > 0 ? cfg.threads_per_brick : 256, 0,
+                            cfg.brick_workers > 1 ? cfg.brick_workers : 1};
         else
             tuned = cached_choice(core_, &c);
         core_.configure(c);

@@ -105,6 +105,7 @@ lss_status lss_create(lss_engine** out, const lss_config* cfg) {
     if (cfg) c = *cfg;
     else lss_config_default(&c);
     if (c.mode != LSS_MODE_REF && c.mode != LSS_MODE_NS) return LSS_ERR_INVALID_ARGUMENT;
+    if (c.brick_workers < 0) return LSS_ERR_INVALID_ARGUMENT;
     std::unique_ptr<lss_engine> e(new lss_engine());
     lss_status s = guard(e.get(), [&] {
         if (c.mode == LSS_MODE_REF) e->impl = lss::make_ref_engine(c);

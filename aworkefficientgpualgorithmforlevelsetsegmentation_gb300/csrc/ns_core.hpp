@@ -19,6 +19,7 @@ struct NsArgs;
 struct BrickConfig {
     int bx, by, bz, threads;
     int min_blocks = 0;  // block per brick: resident blocks per SM the registers allow (0: 1024 threads)
+    int groups = 1;      // > 1: one block per SM with this many brick workers of `threads` threads
 };
 
 const std::vector<BrickConfig>& brick_configs();

@@ -219,6 +219,15 @@ KernelSet kernels_for() {
                      (void*)&k_ns_emit<BX, BY, BZ, NT>, S::WORDS, NT, NT, 0};
 }
 
+// Brick workers: GROUPS groups of NT threads in the one block per SM.
+template <int BX, int BY, int BZ, int NT, int GROUPS>
+KernelSet group_kernels_for() {
+    using S = Brick<BX, BY, BZ>;
+    return KernelSet{(void*)&k_ns_group<BX, BY, BZ, NT, GROUPS>, (void*)&k_ns_init_active<BX, BY, BZ, NT>,
+                     (void*)&k_ns_emit<BX, BY, BZ, NT>, S::WORDS, NT, NT * GROUPS,
+                     group_smem_fixed<S, NT, GROUPS>()};
+}
+
 // Warp per brick, W warps in the one block per SM.
 template <int BX, int BY, int BZ, int W, int NT>
 KernelSet warp_kernels_for() {
@@ -234,11 +243,16 @@ KernelSet warp_kernels_for() {
 const std::vector<BrickConfig>& brick_configs() {
     static const std::vector<BrickConfig> v = {
         {8, 8, 8, 256}, {8, 8, 8, 128}, {8, 8, 8, 512}, {8, 8, 4, 128}, {8, 8, 4, 256}, {4, 4, 4, 64},
-        {8, 8, 4, 32},  {8, 8, 8, 32},  {4, 4, 4, 32},  {8, 8, 8, 256, 5}};
+        {8, 8, 4, 32},  {8, 8, 8, 32},  {4, 4, 4, 32},  {8, 8, 8, 256, 5}, {8, 8, 8, 256, 0, 4}};
     return v;
 }
 
 static KernelSet kernels(const BrickConfig& c) {
+    if (c.groups > 1) {
+        if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 256 && c.groups == 4)
+            return group_kernels_for<8, 8, 8, 256, 4>();
+        throw Error(LSS_ERR_UNSUPPORTED, "unsupported brick-worker configuration");
+    }
     if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 256 && c.min_blocks == 5)
         return kernels_for<8, 8, 8, 256, 5>();
     if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 256) return kernels_for<8, 8, 8, 256>();

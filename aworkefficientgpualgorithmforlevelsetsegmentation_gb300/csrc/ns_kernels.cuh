@@ -458,16 +458,47 @@ struct BlockTally {
     }
 };
 
+// The threads that work on one brick together, and how they synchronise:
+// the whole block (BlockTeam: __syncthreads), or one of several groups of NT
+// threads in a block (GroupTeam: named barrier 1 + g, NT threads), so that
+// one block per SM can run several bricks at once with one rank selection
+// and one grid-barrier participant.  Named barriers order shared and global
+// memory among their threads as __syncthreads does.
+struct BlockTeam {
+    __device__ int tid() const { return threadIdx.x; }
+    __device__ void sync() const { __syncthreads(); }
+    __device__ int sync_or(int pred) const { return __syncthreads_or(pred); }
+};
+
+template <int NT>
+struct GroupTeam {
+    int g;  // group index; barrier id 1 + g
+    __device__ int tid() const { return (int)threadIdx.x - g * NT; }
+    __device__ void sync() const { asm volatile("bar.sync %0, %1;" ::"r"(1 + g), "r"(NT) : "memory"); }
+    __device__ int sync_or(int pred) const {
+        int r;
+        asm volatile(
+            "{\n\t.reg .pred p, q;\n\t"
+            "setp.ne.s32 q, %1, 0;\n\t"
+            "bar.red.or.pred p, %2, %3, q;\n\t"
+            "selp.s32 %0, 1, 0, p;\n\t}"
+            : "=r"(r)
+            : "r"(pred), "r"(1 + g), "r"(NT)
+            : "memory");
+        return r;
+    }
+};
+
 // Work on one brick of A_k whose loads were issued into `buf`.
 // The brick's mask words -> act[buf] (threads < WORDS), cleared in global
 // memory: the mask array of parity p becomes the accumulator of iteration k+1.
 template <class S, int NT>
 __device__ __forceinline__ void ns_fetch_mask(const NsArgs& a, NsSmem<S, NT>& sm, uint32_t b, uint32_t p,
-                                              int buf) {
-    if (threadIdx.x < S::WORDS) {
+                                              int buf, int tid) {
+    if (tid < S::WORDS) {
         unsigned long long* cur = a.masks[p] + (size_t)b * S::WORDS;
-        sm.act[buf][threadIdx.x] = cur[threadIdx.x];
-        cur[threadIdx.x] = 0ull;
+        sm.act[buf][tid] = cur[tid];
+        cur[tid] = 0ull;
     }
 }
 
@@ -477,12 +508,12 @@ __device__ __forceinline__ void ns_fetch_mask(const NsArgs& a, NsSmem<S, NT>& sm
 // barriers per brick), changed flags -> ballot words, TMA store, dilation.
 // vone: the volume descriptor in shared memory when the launch has one
 // volume (else null: descriptors are read per brick).
-template <class S, int NT>
+template <class S, int NT, class Team = BlockTeam>
 __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>& sm, uint32_t b,
                                                  uint32_t p, uint32_t sn, int buf, uint32_t& mphase,
                                                  BlockTally& tally, unsigned long long* cnt,
-                                                 const NsVol* vone) {
-    const int tid = threadIdx.x;
+                                                 const NsVol* vone, const Team team = Team{}) {
+    const int tid = team.tid();
     // Written by thread 0 with the loads, before a block barrier.
     const int4 og = sm.org[buf];
     const uint32_t v = (uint32_t)og.w;
@@ -497,7 +528,7 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
     float* phi = sm.phi[buf];
     if (tile_at_edge<S>(V, x0, y0, z0)) {
         clamp_tile_halo<S>(phi, V, x0, y0, z0, tid, NT);
-        __syncthreads();
+        team.sync();
     }
     float* out = sm.out[buf];
     auto tile_index = [](int j) {
@@ -580,7 +611,7 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
     // The one block barrier of a brick: out[] and chg[buf] complete; after it
     // nothing reads phi[buf], img[buf] or act[buf] of this brick, so the next
     // loads into this buffer may be issued while the dilation below runs.
-    const int any = __syncthreads_or(anyl ? 1 : 0);
+    const int any = team.sync_or(anyl ? 1 : 0);
     if (tid == STORE_TID) {
         tma_store_3d(&a.tmaps[V.tmap_base + 2 + (p ^ 1u)], x0, y0, z0, out);
         tma_store_commit();
@@ -609,7 +640,7 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
                 else v = 0ull;
                 sm.xy[t] = v;
             }
-            __syncthreads();  // uniform: `any` is
+            team.sync();  // uniform: `any` is
         }
         constexpr int ROUNDS = (27 * S::WORDS + NT - 1) / NT;
 #pragma unroll
@@ -1085,7 +1116,7 @@ struct BlockProc {
         while (q < nw && sh.work[q] == kNoBrick) ++q;
         if (q < nw) {
             if (tid == 0) ns_issue_loads<S, NT>(a, sm, sh.work[q], p, buf, vone);
-            ns_fetch_mask<S, NT>(a, sm, sh.work[q], p, buf);
+            ns_fetch_mask<S, NT>(a, sm, sh.work[q], p, buf, tid);
             __syncthreads();  // act[buf] of the first brick (later ones are fetched a brick ahead)
         }
         while (q < nw) {
@@ -1093,7 +1124,7 @@ struct BlockProc {
             while (q2 < nw && sh.work[q2] == kNoBrick) ++q2;
             if (q2 < nw) {
                 if (tid == 0) ns_issue_loads<S, NT>(a, sm, sh.work[q2], p, buf ^ 1, vone);
-                ns_fetch_mask<S, NT>(a, sm, sh.work[q2], p, buf ^ 1);
+                ns_fetch_mask<S, NT>(a, sm, sh.work[q2], p, buf ^ 1, tid);
             }
             ns_process_brick<S, NT>(a, sm, sh.work[q], p, sn, buf, mphase, tally, cnt, vone);
             buf ^= 1;
@@ -1126,6 +1157,90 @@ __global__ void __launch_bounds__(NT, MINB) k_ns_persistent(NsArgs a) {
     extern __shared__ int32_t s_dyn[];
     BlockProc<S, NT> proc(sm, tally);
     ns_drive<NT>(a, sh, stop_state(s_dyn, a.nvol), proc);
+}
+
+// ---------------------------------------------------------------------------
+// Brick workers: one block per SM of GROUPS groups of NT threads; group g
+// takes the block's bricks g, g + GROUPS, ... of each chunk and works on each
+// exactly as a block-per-brick block does (its own double-buffered TMA loads,
+// store thread and tally), synchronising on its named barrier only.  The
+// iteration's rank selection and the grid-barrier arrival are done once per
+// SM, and the SM's bricks are spread over its groups.
+template <class S, int NT, int GROUPS>
+struct GroupProc {
+    NsSmem<S, NT>* sm;   // GROUPS of them (dynamic shared memory)
+    BlockTally* tally;   // GROUPS of them (shared memory), one per store thread
+    GroupTeam<NT> team;
+    uint32_t mphase;     // bit b: phase of this group's load barrier b
+    int buf;
+    __device__ GroupProc(NsSmem<S, NT>* s, BlockTally* t) : sm(s), tally(t), mphase(0u), buf(0) {
+        team.g = (int)threadIdx.x / NT;
+    }
+    __device__ void init() {
+        if (team.tid() == 0) {
+            mbar_init(&sm[team.g].bar[0], 1);
+            mbar_init(&sm[team.g].bar[1], 1);
+            tally[team.g].reset();
+        }
+    }
+    template <int BT>
+    __device__ void chunk(const NsArgs& a, IterShared<BT>& sh, uint32_t nw, uint32_t nf, uint32_t p, uint32_t sn,
+                          unsigned long long* cnt, const NsVol* vone) {
+        const int g = team.g, tid = team.tid();
+        NsSmem<S, NT>& s = sm[g];
+        uint32_t q = (uint32_t)g;
+        while (q < nw && sh.work[q] == kNoBrick) q += GROUPS;
+        if (q < nw) {
+            if (tid == 0) ns_issue_loads<S, NT>(a, s, sh.work[q], p, buf, vone);
+            ns_fetch_mask<S, NT>(a, s, sh.work[q], p, buf, tid);
+            team.sync();  // act[buf] of the group's first brick
+        }
+        while (q < nw) {
+            uint32_t q2 = q + GROUPS;
+            while (q2 < nw && sh.work[q2] == kNoBrick) q2 += GROUPS;
+            if (q2 < nw) {
+                if (tid == 0) ns_issue_loads<S, NT>(a, s, sh.work[q2], p, buf ^ 1, vone);
+                ns_fetch_mask<S, NT>(a, s, sh.work[q2], p, buf ^ 1, tid);
+            }
+            ns_process_brick<S, NT, GroupTeam<NT>>(a, s, sh.work[q], p, sn, buf, mphase, tally[g], cnt, vone, team);
+            buf ^= 1;
+            q = q2;
+        }
+        for (uint32_t r = (uint32_t)g; r < nf; r += GROUPS)
+            if (sh.flush[r] != kNoBrick) ns_flush_brick<S>(a, sh.flush[r], p, vone, tid, NT);
+        __syncthreads();
+    }
+    template <int BT>
+    __device__ void finish(const NsArgs& a, IterShared<BT>& sh, unsigned long long* cnt) {
+        if (team.tid() == NsSmem<S, NT>::STORE_TID) {
+            BlockTally& t = tally[team.g];
+            if (t.iter) atomicAdd(&sh.upd, t.iter);
+            t.flush(a.vstate, cnt);
+            t.reset();
+            tma_store_wait_all();
+            asm volatile("fence.proxy.async.global;" ::: "memory");
+        }
+    }
+};
+
+// Dynamic shared memory of the brick-worker kernel: 128 bytes of alignment
+// slack, the GROUPS work areas, then the stopping state.
+template <class S, int NT, int GROUPS>
+__host__ __device__ constexpr size_t group_smem_fixed() {
+    return 128 + (size_t)GROUPS * sizeof(NsSmem<S, NT>);
+}
+
+template <int BX, int BY, int BZ, int NT, int GROUPS>
+__global__ void __launch_bounds__(NT * GROUPS, 1) k_ns_group(NsArgs a) {
+    using S = Brick<BX, BY, BZ>;
+    __shared__ IterShared<NT * GROUPS> sh;
+    __shared__ BlockTally tally[GROUPS];
+    extern __shared__ unsigned char s_dyn_raw[];
+    unsigned char* dyn = s_dyn_raw + ((128u - (smem_addr(s_dyn_raw) & 127u)) & 127u);
+    NsSmem<S, NT>* sm = reinterpret_cast<NsSmem<S, NT>*>(dyn);
+    int32_t* state = reinterpret_cast<int32_t*>(s_dyn_raw + group_smem_fixed<S, NT, GROUPS>());
+    GroupProc<S, NT, GROUPS> proc(sm, tally);
+    ns_drive<NT * GROUPS>(a, sh, stop_state(state, a.nvol), proc);
 }
 
 // ---------------------------------------------------------------------------

@@ -52,7 +52,8 @@ def _out(out, shape, dtype) -> np.ndarray:
 
 
 def config(mode: int = MODE_NS, device: int = 0, brick=(0, 0, 0), threads_per_brick: int = 0,
-           quirk_i3: bool = True, use_graph: bool = True, hbm_budget_bytes: int = 0) -> L.lss_config:
+           quirk_i3: bool = True, use_graph: bool = True, hbm_budget_bytes: int = 0,
+           brick_workers: int = 0) -> L.lss_config:
     c = L.lss_config()
     lib = L.load()
     lib.lss_config_default(C.byref(c))
@@ -62,6 +63,7 @@ def config(mode: int = MODE_NS, device: int = 0, brick=(0, 0, 0), threads_per_br
     c.ref_quirk_i3 = int(quirk_i3)
     c.use_graph = int(use_graph)
     c.hbm_budget_bytes = hbm_budget_bytes
+    c.brick_workers = brick_workers
     return c
 
 

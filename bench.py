@@ -268,7 +268,8 @@ def run_ours(args, ws, rank, local):
     # --brick (or --brick 0 0 0 for the autotuner) says otherwise.
     brick = tuple(args.brick) if args.brick else (8, 8, 8)
     threads = args.threads or (256 if not args.brick else 0)
-    seg = lss.Segmenter(lss.MODE_NS, device=local, brick=brick, threads_per_brick=threads)
+    seg = lss.Segmenter(lss.MODE_NS, device=local, brick=brick, threads_per_brick=threads,
+                        brick_workers=args.workers)
     stream = torch.cuda.Stream(device=local)
     seg._chk(seg._lib.lss_set_stream(seg._h, ctypes.c_void_p(stream.cuda_stream)))
     seg.load_volume(cfg["image"])
@@ -383,6 +384,7 @@ def run_ours(args, ws, rank, local):
             "run": {"iterations_to_converge": iters[-1], "converge_ms": sparse_ms,
                     "brick": [st["brick_x"], st["brick_y"], st["brick_z"]],
                     "threads_per_brick": st["threads_per_brick"], "grid_blocks": st["grid_blocks"],
+                    "block_threads": st["block_threads"],
                     "block0_update_ms": st["update_ms"], "block0_barrier_ms": st["barrier_ms"],
                     "l2": "flushed between steps (256 MiB write); volume 192 MiB > L2",
                     "parallelism": "replicas" if ws > 1 else "single"},
@@ -824,6 +826,8 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--brick", type=int, nargs=3, default=None)
     ap.add_argument("--threads", type=int, default=0)
+    ap.add_argument("--workers", type=int, default=0,
+                    help="brick workers per block (4: one block per SM with four groups of 256 threads)")
     ap.add_argument("--dense-iters", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extra", action="store_true",

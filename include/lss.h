@@ -94,6 +94,11 @@ typedef struct lss_config {
                                    0 = every active element emits                   */
     int32_t  use_graph;         /* REF: capture each step's iterations in a graph   */
     uint64_t hbm_budget_bytes;  /* refuse allocations above this total (0 = none)   */
+    int32_t  brick_workers;     /* NS, 8x8x8 x 256: 1 = a block per brick (several
+                                   blocks per SM); 4 = one block per SM whose four
+                                   groups of 256 threads each work on a brick;
+                                   0 = 1 (the autotuner may pick either)          */
+    int32_t  pad_;              /* reserved, 0                                     */
 } lss_config;
 
 /* Solver parameters; ≈ the content::Parameter set of

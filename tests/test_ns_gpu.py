@@ -96,6 +96,37 @@ def test_ns_converged_mask_vs_fp64(which, scale):
     assert st["voxel_updates"] > 0 and st["iterations"] == it_g
 
 
+def test_ns_brick_workers_are_voxel_exact():
+    """One block per SM with four brick workers of 256 threads (named
+    barriers) gives the same field and list as a block per brick, bit for
+    bit, in the one-volume and the batched form."""
+    cfg = P.config2(0.25)
+    a = make_gpu(cfg, brick=(8, 8, 8), threads=256)
+    s = lss.Segmenter(lss.MODE_NS, brick=(8, 8, 8), threads_per_brick=256, brick_workers=4)
+    s.load_volume(cfg["image"])
+    p = cfg["params"]
+    s.set_parameters(p.target, p.window, p.curvature, p.time_step, alpha_role=p.alpha_role)
+    s.set_phi(cfg["phi0"])
+    assert s.stats()["block_threads"] == 1024
+    for k in (1, 7, 30):
+        a.step(k)
+        s.step(k)
+        assert np.array_equal(a.read_phi(), s.read_phi()), k
+        assert np.array_equal(a.active_linear(), s.active_linear()), k
+    assert a.step_until_converged(1e-3, 5, 2000) == s.step_until_converged(1e-3, 5, 2000)
+    assert np.array_equal(a.get_saveable_segmentation(), s.get_saveable_segmentation())
+    vols = P.config3(6, scale=0.25)["volumes"]
+    out = []
+    for workers in (1, 4):
+        b = lss.Batch(brick=(8, 8, 8), threads_per_brick=256, brick_workers=workers)
+        for v in vols:
+            b.add_volume(v["image"], v["params"], v["spheres"])
+        it = b.run(1e-3, 5, 2000)
+        out.append((it, [b.read_phi(i) for i in range(len(vols))]))
+    assert out[0][0] == out[1][0]
+    assert all(np.array_equal(x, y) for x, y in zip(out[0][1], out[1][1]))
+
+
 def test_ns_brick_configs_are_voxel_exact():
     cfg = P.config2(0.25)
     ref_phi = ref_act = None
