@@ -4,26 +4,38 @@
 // fixed, the soft-Dice loss of sigmoid(-phi/tau) against a target mask, and
 // its gradients with respect to T, eps, alpha and a per-voxel speed bias.
 //
-// Work-efficient like the forward engine: every iteration touches the bricks
-// of its active set only.  The forward keeps the brick list of each A_k
-// (built while dilating: the first thread to put a word into a brick appends
-// it; the block that updates a brick dilates it) beside the recorded brick
-// masks.  It runs over a ping-pong pair in
-// which both buffers stay current: iteration k writes the bricks of A_k
-// whole (active voxels updated, the rest copied) and copies across the
-// bricks of A_{k-1} that left the set; the changed voxels' ballot words are
-// dilated into A_{k+1} exactly as in the persistent kernel, so the recorded
-// sets are the sparse engine's sets.  phi is checkpointed every `every`
-// iterations (a device copy); the reverse pass recomputes each segment from
-// its checkpoint (a copy of the previous state plus the sparse update:
-// bit-identical, the arithmetic is deterministic) and runs the segment's
-// iterations backwards on one lambda field, in place:
+// Two cooperative launches, one per direction; the phases inside each are
+// separated by the cooperative-groups grid barrier, so a call costs two
+// launches instead of a few hundred dependent ones.  Work-efficient like the
+// forward engine: every iteration touches the bricks of its active set only.
+//
+// Forward (k_adj_forward).  The brick list of each A_k is built while
+// dilating (the first thread to put a word into a brick appends it; the
+// block that updates a brick dilates it) beside the recorded brick masks.
+// It runs over a ping-pong pair in which both buffers stay current:
+// iteration k writes the bricks of A_k whole (active voxels updated, the rest
+// copied) and copies across the bricks of A_{k-1} that left the set; the
+// changed voxels' ballot words are dilated into A_{k+1} exactly as in the
+// persistent kernel, so the recorded sets are the sparse engine's sets.  phi
+// is checkpointed every `every` iterations.
+//
+// Reverse (k_adj_reverse).  The soft-Dice sums and lambda_K, then segment by
+// segment from the last checkpoint: the segment's states are recomputed from
+// its checkpoint (bit-identical, the arithmetic is deterministic) into
+// `every` - 1 buffers, copying into each only the bricks that can differ
+// from what it held for the later segment, and the segment's iterations run
+// backwards on one lambda field, in place:
 //   take:  U = lambda_{k+1} at the voxels of A_k, lambda = 0 there (lambda
 //          keeps lambda_{k+1} everywhere else: the pass-through);
 //   vjp:   every active voxel v scatters U[v] through the transposed stencil
 //          Jacobian of the update onto its 19 stencil voxels (fp32 atomics);
-// parameter gradients are reduced per block in FP64 (the gradient-check
-// reduction) and the bias gradient accumulates per voxel.
+// the parameter gradients are summed per block in FP64 (the gradient-check
+// reduction) into the block's own slot and the bias gradient per voxel.
+//
+// Data other blocks wrote earlier in the same launch is read with plain
+// loads after a grid barrier (its fence orders them), never through the
+// read-only path: no pointer into a buffer the launch writes is __restrict__.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -39,6 +51,14 @@
 namespace lss {
 namespace {
 
+namespace cg = cooperative_groups;
+
+// Threads of the two cooperative launches (a voxel of an 8^3 brick each) and
+// their blocks per SM: an iteration holds a few hundred bricks, so one block
+// an SM keeps every SM busy, and fewer blocks make the grid barrier cheaper.
+constexpr int kAdjThreads = 512;
+constexpr int kAdjBlocksPerSm = 1;
+
 void count_launch(EngineBase* owner) {
     ++owner->launches;
     LSS_CUDA(cudaGetLastError());
@@ -53,13 +73,47 @@ __device__ __forceinline__ int3 voxel_of(const NsVol& V, uint32_t b, int j) {
     return make_int3(o.x + j % S::X, o.y + (j / S::X) % S::Y, o.z + j / (S::X * S::Y));
 }
 
+// Everything one call works on.  Per-iteration arrays are evenly spaced in
+// the workspace: act[k] = act0 + k * astride words, list[k] = list0 +
+// k * lstride, flag[k] = flag0 + k * lstride; fields (checkpoints, the
+// recompute buffers, the forward's pair) are fstride floats apart.
+struct AdjPlan {
+    NsVol V;                    // the one volume (brick_base 0)
+    float* ck0;                 // checkpoint s = ck0 + s * fstride (phi_{s * every})
+    float* seg1;                // recompute buffer i >= 1 = seg1 + (i - 1) * fstride
+    float* fw[2];               // the forward's ping-pong pair
+    float* lam;
+    float* U;
+    float* dbias;               // nullable
+    const uint8_t* tgt;
+    unsigned long long* act0;   // [K+1][NB * WORDS]: the recorded brick masks of A_k
+    uint32_t* list0;            // [K+1][NB]
+    uint32_t* flag0;            // [K+1][NB]
+    uint32_t* counts;           // [K+1]
+    double* gsum;               // [8]: soft-Dice sums in 4..6
+    double* gpart;              // [grid][3]: each block's dT, deps, dalpha
+    unsigned long long* nact;   // active-voxel updates of the forward
+    uint64_t fstride, astride, lstride, P;
+    uint32_t nb;
+    int32_t K, every, nck;
+    float tau;
+};
+
+__device__ __forceinline__ unsigned long long* plan_act(const AdjPlan& a, int k) { return a.act0 + (uint64_t)k * a.astride; }
+__device__ __forceinline__ uint32_t* plan_list(const AdjPlan& a, int k) { return a.list0 + (uint64_t)k * a.lstride; }
+__device__ __forceinline__ uint32_t* plan_flag(const AdjPlan& a, int k) { return a.flag0 + (uint64_t)k * a.lstride; }
+// Recompute buffer i of a segment whose checkpoint is s (i = 0: the checkpoint).
+__device__ __forceinline__ float* plan_seg(const AdjPlan& a, int s, int i) {
+    return i == 0 ? a.ck0 + (uint64_t)s * a.fstride : a.seg1 + (uint64_t)(i - 1) * a.fstride;
+}
+
 // Per-iteration brick lists: list[k][0 .. count[k]) = the bricks of A_k in
 // no particular order (each brick once), flag[k][b] = b is in it.
 
 // list_0 and flag_0 from the recorded masks of A_0.
 template <class S>
-__global__ void __launch_bounds__(256) k_adj_list0(const unsigned long long* __restrict__ act, uint32_t* flag,
-                                                   uint32_t* list, uint32_t* count, uint32_t nb) {
+__device__ __forceinline__ void adj_list0(const unsigned long long* act, uint32_t* flag, uint32_t* list,
+                                          uint32_t* count, uint32_t nb) {
     for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
         unsigned long long any = 0ull;
 #pragma unroll
@@ -97,22 +151,18 @@ __device__ __forceinline__ void adj_dilate_brick(const NsVol& V, uint32_t b, con
     }
 }
 
-// Iteration k: block per brick.  The bricks of list_k are written whole into
+// Iteration k, block per brick.  The bricks of list_k are written whole into
 // out (active voxels updated from in, the others copied); with `prev` (the
 // recorded forward's ping-pong pair), the bricks of list_{k-1} not in
 // list_k (flag_k clear) are copied from in to out, so that out equals in
 // outside the bricks of A_k.  With nxt (the recorded forward, not a
 // recomputation): each updated brick's changed voxels are dilated into A_{k+1}
-// by the same block (adj_dilate_brick) and the updated voxels are counted
-// into *nact.
+// by the same block.  Returns the active voxels this thread updated.
 template <class S>
-__global__ void __launch_bounds__(256) k_adj_update(NsVol V, const float* __restrict__ in, float* __restrict__ out,
-                                                    const unsigned long long* __restrict__ act,
-                                                    const uint32_t* __restrict__ list, const uint32_t* count,
-                                                    const uint32_t* __restrict__ prev, const uint32_t* prev_count,
-                                                    const uint32_t* __restrict__ flag_k, unsigned long long* nxt,
-                                                    uint32_t* flag_next, uint32_t* list_next, uint32_t* count_next,
-                                                    unsigned long long* nact) {
+__device__ uint32_t adj_update(const NsVol& V, const float* in, float* out, const unsigned long long* act,
+                               const uint32_t* list, const uint32_t* count, const uint32_t* prev,
+                               const uint32_t* prev_count, const uint32_t* flag_k, unsigned long long* nxt,
+                               uint32_t* flag_next, uint32_t* list_next, uint32_t* count_next) {
     __shared__ uint32_t chg[S::CHG];
     __shared__ uint32_t any;
     const uint32_t n = *count, np = prev ? *prev_count : 0u;
@@ -160,47 +210,54 @@ __global__ void __launch_bounds__(256) k_adj_update(NsVol V, const float* __rest
             if (any) adj_dilate_brick<S>(V, b, chg, threadIdx.x, blockDim.x, nxt, flag_next, list_next, count_next);
         }
     }
-    if (nact) {  // uniform: one atomic per block on the shared counter, not one per warp
-        __shared__ uint32_t s_cnt;
-        if (threadIdx.x == 0) s_cnt = 0u;
-        __syncthreads();
-        mine = __reduce_add_sync(0xffffffffu, mine);
-        if ((threadIdx.x & 31) == 0 && mine) atomicAdd(&s_cnt, mine);
-        __syncthreads();
-        if (threadIdx.x == 0 && s_cnt) atomicAdd(nact, (unsigned long long)s_cnt);
+    __syncthreads();  // chg and any are reused by the next call
+    return mine;
+}
+
+// Copies src to dst brick by brick: every brick (lists == null) or the bricks
+// of lists k_lo .. k_hi (bricks may repeat); bricks flagged in `skip` (the
+// next update rewrites them whole) are left out, so the copy and that update
+// write disjoint bricks.
+template <class S>
+__device__ void adj_copy_bricks(const AdjPlan& a, const float* src, float* dst, int k_lo, int k_hi,
+                                const uint32_t* skip, bool all) {
+    const NsVol& V = a.V;
+    auto copy = [&](uint32_t b) {
+        if (skip[b]) return;
+        for (int j = threadIdx.x; j < S::VOX; j += blockDim.x) {
+            const int3 p = voxel_of<S>(V, b, j);
+            if (p.x < V.nx && p.y < V.ny && p.z < V.nz) {
+                const size_t idx = ((size_t)p.z * V.py + p.y) * V.px + p.x;
+                dst[idx] = src[idx];
+            }
+        }
+    };
+    if (all) {
+        for (uint32_t b = blockIdx.x; b < a.nb; b += gridDim.x) copy(b);
+        return;
+    }
+    for (int k = k_lo; k <= k_hi; ++k) {
+        const uint32_t n = a.counts[k];
+        const uint32_t* list = plan_list(a, k);
+        for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) copy(list[i]);
     }
 }
 
-// The bricks of lists k_lo .. k_hi (list k at lists + k * stride, count k at
-// counts[k]; bricks may repeat) copied from src to dst, a brick a block.
-template <class S>
-__global__ void __launch_bounds__(256) k_adj_copy_bricks(NsVol V, const float* __restrict__ src,
-                                                         float* __restrict__ dst, const uint32_t* __restrict__ lists,
-                                                         uint64_t stride, const uint32_t* __restrict__ counts,
-                                                         int k_lo, int k_hi) {
-    for (int k = k_lo; k <= k_hi; ++k) {
-        const uint32_t n = counts[k];
-        const uint32_t* list = lists + (uint64_t)k * stride;
-        for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
-            const uint32_t b = list[i];
-            for (int j = threadIdx.x; j < S::VOX; j += blockDim.x) {
-                const int3 p = voxel_of<S>(V, b, j);
-                if (p.x < V.nx && p.y < V.ny && p.z < V.nz) {
-                    const size_t idx = ((size_t)p.z * V.py + p.y) * V.px + p.x;
-                    dst[idx] = src[idx];
-                }
-            }
-        }
-    }
+// The whole padded field src -> dst (grid-stride, float4).
+__device__ void adj_copy_field(const float* src, float* dst, uint64_t P) {
+    const uint64_t n4 = P / 4;  // P is a multiple of 8 (padded dims)
+    const float4* s4 = reinterpret_cast<const float4*>(src);
+    float4* d4 = reinterpret_cast<float4*>(dst);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n4; i += (uint64_t)gridDim.x * blockDim.x)
+        d4[i] = s4[i];
 }
 
 // Reverse iteration k, first half (block per brick of list_k): U =
 // lambda_{k+1} at the voxels of A_k and lambda = 0 there; lambda keeps
 // lambda_{k+1} at every other voxel.
 template <class S>
-__global__ void __launch_bounds__(256) k_adj_take(NsVol V, const unsigned long long* __restrict__ act,
-                                                  const uint32_t* __restrict__ list, const uint32_t* count,
-                                                  float* __restrict__ lam, float* __restrict__ U) {
+__device__ void adj_take(const NsVol& V, const unsigned long long* act, const uint32_t* list, const uint32_t* count,
+                         float* lam, float* U) {
     const uint32_t n = *count;
     for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
         const uint32_t b = list[i];
@@ -352,16 +409,12 @@ __device__ __forceinline__ void block_sum3(double a0, double a1, double a2, doub
 
 // Reverse iteration k, second half (block per brick of list_k): scatters U
 // (lambda_{k+1}) of the voxels of A_k through the update's transposed
-// Jacobian into lam, adds the bias gradient and the parameter gradients
-// (T, eps, alpha; FP64) into the block's slot gpart[3 * blockIdx.x ..].
+// Jacobian into lam, adds the bias gradient, and returns the parameter terms
+// (T, eps, alpha) in s3 (FP64, per thread).
 template <class S>
-__global__ void __launch_bounds__(256) k_adj_vjp(NsVol V, const float* __restrict__ phi,
-                                                 const unsigned long long* __restrict__ act,
-                                                 const uint32_t* __restrict__ list, const uint32_t* count,
-                                                 const float* __restrict__ U, float* lam, float* dbias,
-                                                 double* gpart) {
+__device__ void adj_vjp(const NsVol& V, const float* phi, const unsigned long long* act, const uint32_t* list,
+                        const uint32_t* count, const float* U, float* lam, float* dbias, double* s3) {
     const uint32_t n = *count;
-    double sT = 0.0, sE = 0.0, sA = 0.0;
     for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
         const uint32_t b = list[i];
         for (int j = threadIdx.x; j < S::VOX; j += blockDim.x) {
@@ -381,55 +434,108 @@ __global__ void __launch_bounds__(256) k_adj_vjp(NsVol V, const float* __restric
             };
             float g4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
             ns_update_vjp_f32(P, add, V.img[idx], V.bias ? V.bias[idx] : 0.0f, V, u, g4);
-            sT += g4[0];
-            sE += g4[1];
-            sA += g4[2];
+            s3[0] += g4[0];
+            s3[1] += g4[1];
+            s3[2] += g4[2];
             if (dbias) dbias[idx] += g4[3];
         }
     }
-    block_sum3<true>(sT, sE, sA, gpart + 3 * (size_t)blockIdx.x);  // every thread of the block reaches it
 }
 
-// Soft-Dice sums over the volume: gsum[0..2] = (sum s, sum t, sum s t).
-// Per voxel in fp32 (a thread sums a few tens of voxels); the block and grid
-// reduction in FP64.
-__global__ void __launch_bounds__(256) k_adj_dice_sums(NsVol V, const float* __restrict__ phi,
-                                                       const uint8_t* __restrict__ target, float tau,
-                                                       double* gsum) {
-    const uint32_t rows = (uint32_t)V.ny * (uint32_t)V.nz;
-    float ss = 0.0f, tt = 0.0f, st = 0.0f;
-    // Block per row (y, z), threads over x (every thread reaches block_sum3).
-    for (uint32_t r = blockIdx.x; r < rows; r += gridDim.x) {
-        const uint32_t z = r / (uint32_t)V.ny, y = r - z * (uint32_t)V.ny;
-        const size_t row = ((size_t)z * V.py + y) * V.px;
-        for (int x = threadIdx.x; x < V.nx; x += blockDim.x) {
-            const float s = 1.0f / (1.0f + expf(phi[row + x] / tau));
-            const float tv = target[row + x] ? 1.0f : 0.0f;
-            ss += s;
-            tt += tv;
-            st += s * tv;
-        }
+// The forward: list_0, then K iterations, phi checkpointed every `every`.
+template <class S>
+__global__ void __launch_bounds__(kAdjThreads) k_adj_forward(const AdjPlan a) {
+    cg::grid_group grid = cg::this_grid();
+    const NsVol& V = a.V;
+    adj_list0<S>(plan_act(a, 0), plan_flag(a, 0), plan_list(a, 0), &a.counts[0], a.nb);
+    grid.sync();
+    uint32_t mine = 0;
+    for (int k = 0; k < a.K; ++k) {
+        const float* src = a.fw[k & 1];
+        float* dst = a.fw[(k + 1) & 1];
+        mine += adj_update<S>(V, src, dst, plan_act(a, k), plan_list(a, k), &a.counts[k],
+                              k ? plan_list(a, k - 1) : nullptr, k ? &a.counts[k - 1] : nullptr, plan_flag(a, k),
+                              plan_act(a, k + 1), plan_flag(a, k + 1), plan_list(a, k + 1), &a.counts[k + 1]);
+        grid.sync();
+        // The next iteration reads dst and writes the other buffer: the copy
+        // needs no barrier of its own (the reverse pass is another launch).
+        if ((k + 1) % a.every == 0 && k + 1 < a.K)
+            adj_copy_field(dst, a.ck0 + (uint64_t)((k + 1) / a.every) * a.fstride, a.P);
     }
-    block_sum3(ss, tt, st, gsum);
+    __shared__ uint32_t s_cnt;
+    if (threadIdx.x == 0) s_cnt = 0u;
+    __syncthreads();
+    mine = __reduce_add_sync(0xffffffffu, mine);
+    if ((threadIdx.x & 31) == 0 && mine) atomicAdd(&s_cnt, mine);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_cnt) atomicAdd(a.nact, (unsigned long long)s_cnt);
 }
 
-// lambda_K = dloss/dphi_K of the soft-Dice loss, per voxel in fp32 from the
-// FP64 sums: dloss/ds = (2 st - 2 t den) / den^2.
-__global__ void __launch_bounds__(256) k_adj_dice_grad(NsVol V, const float* __restrict__ phi,
-                                                       const uint8_t* __restrict__ target, float tau,
-                                                       const double* __restrict__ sums, float* lam) {
-    const double den = sums[0] + sums[1], st = sums[2];
-    const float c_out = (float)(2.0 * st / (den * den)), c_in = (float)(2.0 * st / (den * den) - 2.0 / den);
+// The reverse: the loss and lambda_K, then the segments from the last.
+template <class S>
+__global__ void __launch_bounds__(kAdjThreads) k_adj_reverse(const AdjPlan a) {
+    cg::grid_group grid = cg::this_grid();
+    const NsVol& V = a.V;
+    const float* phiK = a.fw[a.K & 1];
     const uint32_t rows = (uint32_t)V.ny * (uint32_t)V.nz;
-    for (uint32_t r = blockIdx.x; r < rows; r += gridDim.x) {
-        const uint32_t z = r / (uint32_t)V.ny, y = r - z * (uint32_t)V.ny;
-        const size_t row = ((size_t)z * V.py + y) * V.px;
-        for (int x = threadIdx.x; x < V.nx; x += blockDim.x) {
-            const float s = 1.0f / (1.0f + expf(phi[row + x] / tau));
-            const float dl_ds = target[row + x] ? c_in : c_out;
-            lam[row + x] = dl_ds * (-s * (1.0f - s) / tau);
+    // Soft-Dice sums (s, t, s t): per voxel in fp32, per block and grid in FP64.
+    {
+        float ss = 0.0f, tt = 0.0f, st = 0.0f;
+        for (uint32_t r = blockIdx.x; r < rows; r += gridDim.x) {
+            const uint32_t z = r / (uint32_t)V.ny, y = r - z * (uint32_t)V.ny;
+            const size_t row = ((size_t)z * V.py + y) * V.px;
+            for (int x = threadIdx.x; x < V.nx; x += blockDim.x) {
+                const float s = 1.0f / (1.0f + expf(phiK[row + x] / a.tau));
+                const float tv = a.tgt[row + x] ? 1.0f : 0.0f;
+                ss += s;
+                tt += tv;
+                st += s * tv;
+            }
+        }
+        block_sum3(ss, tt, st, a.gsum + 4);
+    }
+    grid.sync();
+    // lambda_K = dloss/dphi_K: dloss/ds = (2 st - 2 t den) / den^2.
+    {
+        const double den = a.gsum[4] + a.gsum[5], sst = a.gsum[6];
+        const float c_out = (float)(2.0 * sst / (den * den)), c_in = (float)(2.0 * sst / (den * den) - 2.0 / den);
+        for (uint32_t r = blockIdx.x; r < rows; r += gridDim.x) {
+            const uint32_t z = r / (uint32_t)V.ny, y = r - z * (uint32_t)V.ny;
+            const size_t row = ((size_t)z * V.py + y) * V.px;
+            for (int x = threadIdx.x; x < V.nx; x += blockDim.x) {
+                const float s = 1.0f / (1.0f + expf(phiK[row + x] / a.tau));
+                a.lam[row + x] = (a.tgt[row + x] ? c_in : c_out) * (-s * (1.0f - s) / a.tau);
+            }
         }
     }
+    grid.sync();
+    double s3[3] = {0.0, 0.0, 0.0};
+    for (int sgi = a.nck - 1; sgi >= 0; --sgi) {
+        const int s0 = sgi * a.every, s1 = min(a.K, s0 + a.every);
+        // Buffer i held phi_{(sgi+1)*every + i} for the later segment when that
+        // segment reached it (every segment but the last, processed first, is
+        // `every` long); otherwise nothing of this call.
+        const int later = sgi + 1, later_len = later < a.nck ? min(a.K, (later + 1) * a.every) - later * a.every : 0;
+        for (int k = s0; k + 1 < s1; ++k) {
+            const int i = k - s0 + 1;
+            const float* src = plan_seg(a, sgi, i - 1);
+            float* d = plan_seg(a, sgi, i);
+            const int held = i < later_len ? later * a.every + i : -1;
+            if (held < 0) adj_copy_bricks<S>(a, src, d, 0, -1, plan_flag(a, k), true);
+            else if (held - 1 >= k + 1) adj_copy_bricks<S>(a, src, d, k + 1, held - 1, plan_flag(a, k), false);
+            adj_update<S>(V, src, d, plan_act(a, k), plan_list(a, k), &a.counts[k], nullptr, nullptr, nullptr,
+                          nullptr, nullptr, nullptr, nullptr);
+            grid.sync();
+        }
+        for (int k = s1 - 1; k >= s0; --k) {
+            adj_take<S>(V, plan_act(a, k), plan_list(a, k), &a.counts[k], a.lam, a.U);
+            grid.sync();
+            adj_vjp<S>(V, plan_seg(a, sgi, k - s0), plan_act(a, k), plan_list(a, k), &a.counts[k], a.U, a.lam,
+                       a.dbias, s3);
+            grid.sync();
+        }
+    }
+    block_sum3<true>(s3[0], s3[1], s3[2], a.gpart + 3 * (size_t)blockIdx.x);
 }
 
 template <class S>
@@ -443,40 +549,65 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     const uint64_t P = (uint64_t)V.px * V.py * V.pz;
     const size_t mwords = (size_t)nb * S::WORDS;
     const int nck = (K + every - 1) / every;
-    const int grid = owner->num_sms * 8;        // element-wise kernels
-    const int bgrid = owner->num_sms * 4;       // block-per-brick kernels
+    const int grid = owner->num_sms * 8;  // the upload and download kernels
+    const void* kf = (const void*)&k_adj_forward<S>;
+    const void* kr = (const void*)&k_adj_reverse<S>;
+    // Cooperative grids: every block resident.
+    auto coop = [&](const void* k) {
+        int per_sm = 0;
+        LSS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kAdjThreads, 0));
+        LSS_REQUIRE(per_sm > 0, LSS_ERR_CUDA, "adjoint kernel does not fit on an SM");
+        return owner->num_sms * std::min(per_sm, kAdjBlocksPerSm);
+    };
+    const int gf = coop(kf), gr = coop(kr);
     // One device workspace (kept by the engine between calls), carved into
     // 256-byte aligned parts.
     auto al = [](uint64_t b) { return (b + 255) / 256 * 256; };
     const uint64_t nfields = (uint64_t)nck + (every - 1) + 4 + (dbias ? 1 : 0) + (bias ? 1 : 0);
     const uint64_t total = nfields * al(P * 4) + (uint64_t)(K + 1) * al(mwords * 8) +
-                           2 * (uint64_t)(K + 1) * al((uint64_t)nb * 4) + al((uint64_t)(K + 1) * 4) + al(P) + 256 +
-                           al((uint64_t)bgrid * 3 * sizeof(double));
+                           2 * (uint64_t)(K + 1) * al((uint64_t)nb * 4) + al((uint64_t)(K + 1) * 4) + al(P) +
+                           al(8 * sizeof(double) + 8) + al((uint64_t)gr * 3 * sizeof(double));
     char* base = (char*)core.workspace(total);
+    char* const end = base + total;
     auto carve = [&](uint64_t bytes) {
         char* p = base;
         base += al(bytes);
+        LSS_REQUIRE(base <= end, LSS_ERR_CAPACITY, "adjoint workspace layout");
         return p;
     };
     auto F = [&]() { return (float*)carve(P * 4); };
-    std::vector<float*> ck(nck), seg(every);
-    for (auto& p : ck) p = F();
-    for (int i = 1; i < every; ++i) seg[i] = F();
-    float* fw[2] = {F(), F()};  // the forward's ping-pong pair
-    float* lam = F();
-    float* U = F();
-    std::vector<unsigned long long*> act(K + 1);
-    for (auto& a : act) a = (unsigned long long*)carve(mwords * 8);
-    std::vector<uint32_t*> list(K + 1), flag(K + 1);
-    for (auto& l : list) l = (uint32_t*)carve((uint64_t)nb * 4);
-    for (auto& f : flag) f = (uint32_t*)carve((uint64_t)nb * 4);
-    uint32_t* counts = (uint32_t*)carve((uint64_t)(K + 1) * 4);
+    AdjPlan a;
+    std::memset(&a, 0, sizeof(a));
+    a.fstride = al(P * 4) / 4;
+    a.ck0 = F();
+    for (int s = 1; s < nck; ++s) F();
+    a.seg1 = every > 1 ? F() : nullptr;
+    for (int i = 2; i < every; ++i) F();
+    a.fw[0] = F();
+    a.fw[1] = F();
+    a.lam = F();
+    a.U = F();
+    a.astride = al(mwords * 8) / 8;
+    a.act0 = (unsigned long long*)carve(mwords * 8);
+    for (int k = 1; k <= K; ++k) carve(mwords * 8);
+    a.lstride = al((uint64_t)nb * 4) / 4;
+    a.list0 = (uint32_t*)carve((uint64_t)nb * 4);
+    for (int k = 1; k <= K; ++k) carve((uint64_t)nb * 4);
+    a.flag0 = (uint32_t*)carve((uint64_t)nb * 4);
+    for (int k = 1; k <= K; ++k) carve((uint64_t)nb * 4);
+    a.counts = (uint32_t*)carve((uint64_t)(K + 1) * 4);
     uint8_t* tgt = (uint8_t*)carve(P);
-    double* gsum = (double*)carve(8 * sizeof(double) + 8);
-    unsigned long long* nact = (unsigned long long*)(gsum + 8);
-    double* gpart = (double*)carve((uint64_t)bgrid * 3 * sizeof(double));  // per-block dT, deps, dalpha
-    float* dbias_d = dbias ? F() : nullptr;
-    auto count_k = [&](int k) { return counts + k; };
+    a.gsum = (double*)carve(8 * sizeof(double) + 8);
+    a.nact = (unsigned long long*)(a.gsum + 8);
+    a.gpart = (double*)carve((uint64_t)gr * 3 * sizeof(double));
+    a.dbias = dbias ? F() : nullptr;
+    a.tgt = tgt;
+    a.P = P;
+    a.nb = nb;
+    a.K = K;
+    a.every = every;
+    a.nck = nck;
+    a.tau = tau;
     // Target and bias into the padded layout on the device (pinned host
     // buffers are read in place, pageable ones through the copy engine into
     // fw[0], which is free until the forward starts).
@@ -485,7 +616,7 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
         using T = std::remove_cv_t<std::remove_pointer_t<decltype(host)>>;
         const T* src = (const T*)pinned_device_ptr(host);
         if (!src) {
-            T* stage = (T*)(void*)fw[0];
+            T* stage = (T*)(void*)a.fw[0];
             LSS_CUDA(cudaMemcpyAsync(stage, host, n * sizeof(T), cudaMemcpyHostToDevice, st));
             src = stage;
         }
@@ -500,86 +631,41 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
         upload(bd, bias);
         V.bias = bd;
     }
-    if (dbias_d) LSS_CUDA(cudaMemsetAsync(dbias_d, 0, P * 4, st));
-    LSS_CUDA(cudaMemsetAsync(gsum, 0, 8 * sizeof(double) + 8, st));
-    LSS_CUDA(cudaMemsetAsync(gpart, 0, (uint64_t)bgrid * 3 * sizeof(double), st));
-    LSS_CUDA(cudaMemsetAsync(act[1], 0, (uint64_t)K * al(mwords * 8), st));  // act[1..K] are contiguous
-    LSS_CUDA(cudaMemsetAsync(flag[0], 0, (uint64_t)(K + 1) * al((uint64_t)nb * 4), st));
-    LSS_CUDA(cudaMemsetAsync(counts, 0, (uint64_t)(K + 1) * 4, st));
-    auto count = [&]() { count_launch(owner); };
+    a.V = V;
+    if (a.dbias) LSS_CUDA(cudaMemsetAsync(a.dbias, 0, P * 4, st));
+    LSS_CUDA(cudaMemsetAsync(a.gsum, 0, 8 * sizeof(double) + 8, st));
+    LSS_CUDA(cudaMemsetAsync(a.gpart, 0, (uint64_t)gr * 3 * sizeof(double), st));
+    LSS_CUDA(cudaMemsetAsync(a.act0 + a.astride, 0, (uint64_t)K * al(mwords * 8), st));  // act[1..K]
+    LSS_CUDA(cudaMemsetAsync(a.flag0, 0, (uint64_t)(K + 1) * al((uint64_t)nb * 4), st));
+    LSS_CUDA(cudaMemsetAsync(a.counts, 0, (uint64_t)(K + 1) * 4, st));
     // Forward from the engine's current phi and active set: both buffers of
     // the pair and the first checkpoint hold phi_0.
     const float* phi0 = V.phi[core.parity()];
-    for (float* d : {ck[0], fw[0], fw[1]})
+    for (float* d : {a.ck0, a.fw[0], a.fw[1]})
         LSS_CUDA(cudaMemcpyAsync(d, phi0, P * 4, cudaMemcpyDeviceToDevice, st));
-    LSS_CUDA(cudaMemcpyAsync(act[0], core.masks(core.parity()), mwords * 8, cudaMemcpyDeviceToDevice, st));
-    k_adj_list0<S><<<(nb + 255) / 256, 256, 0, st>>>(act[0], flag[0], list[0], count_k(0), nb);
-    count();
-    for (int k = 0; k < K; ++k) {
-        const float* src = fw[k & 1];
-        float* dst = fw[(k + 1) & 1];
-        k_adj_update<S><<<bgrid, 256, 0, st>>>(V, src, dst, act[k], list[k], count_k(k),
-                                               k ? list[k - 1] : nullptr, k ? count_k(k - 1) : nullptr, flag[k],
-                                               act[k + 1], flag[k + 1], list[k + 1], count_k(k + 1), nact);
-        count();
-        if ((k + 1) % every == 0 && k + 1 < K)
-            LSS_CUDA(cudaMemcpyAsync(ck[(k + 1) / every], dst, P * 4, cudaMemcpyDeviceToDevice, st));
-    }
-    const float* phiK = fw[K & 1];
-    // Loss and lambda_K.
-    k_adj_dice_sums<<<grid, 256, 0, st>>>(V, phiK, tgt, tau, gsum + 4);
-    count();
-    k_adj_dice_grad<<<grid, 256, 0, st>>>(V, phiK, tgt, tau, gsum + 4, lam);
-    count();
-    // Reverse, segment by segment from the last checkpoint.  seg[i] holds
-    // phi_{held[i]} (-1: nothing of this call): to turn it into phi_{k+1}
-    // only the bricks of lists k+1 .. held[i]-1 can differ from phi_k (the
-    // bricks of list_k are rewritten whole by the update), so only those are
-    // copied from seg[i-1] = phi_k; the first use copies the whole field.
-    const uint64_t lstride = al((uint64_t)nb * 4) / 4;
-    std::vector<int> held(every, -1);
-    for (int sgi = nck - 1; sgi >= 0; --sgi) {
-        const int s0 = sgi * every, s1 = std::min(K, s0 + every);
-        seg[0] = ck[sgi];
-        for (int k = s0; k + 1 < s1; ++k) {
-            const int i = k - s0 + 1;
-            float* d = seg[i];
-            if (held[i] < 0) {
-                LSS_CUDA(cudaMemcpyAsync(d, seg[i - 1], P * 4, cudaMemcpyDeviceToDevice, st));
-            } else if (held[i] - 1 >= k + 1) {
-                k_adj_copy_bricks<S><<<bgrid, 256, 0, st>>>(V, seg[i - 1], d, list[0], lstride, counts, k + 1,
-                                                            held[i] - 1);
-                count();
-            }
-            k_adj_update<S><<<bgrid, 256, 0, st>>>(V, seg[i - 1], d, act[k], list[k], count_k(k), nullptr,
-                                                   nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
-            count();
-            held[i] = k + 1;
-        }
-        for (int k = s1 - 1; k >= s0; --k) {
-            k_adj_take<S><<<bgrid, 256, 0, st>>>(V, act[k], list[k], count_k(k), lam, U);
-            count();
-            k_adj_vjp<S><<<bgrid, 256, 0, st>>>(V, seg[k - s0], act[k], list[k], count_k(k), U, lam, dbias_d, gpart);
-            count();
-        }
-    }
+    LSS_CUDA(cudaMemcpyAsync(a.act0, core.masks(core.parity()), mwords * 8, cudaMemcpyDeviceToDevice, st));
+    void* params[] = {(void*)&a};
+    LSS_CUDA(cudaLaunchCooperativeKernel(kf, dim3(gf), dim3(kAdjThreads), params, 0, st));
+    count_launch(owner);
+    LSS_CUDA(cudaLaunchCooperativeKernel(kr, dim3(gr), dim3(kAdjThreads), params, 0, st));
+    count_launch(owner);
     // d_bias back to the caller's unpadded layout (in place when pinned).
     if (dbias) {
         float* dev = (float*)pinned_device_ptr(dbias);
-        k_ns_gather<<<grid, 256, 0, st>>>(dev ? dev : fw[0], dbias_d, V.nx, V.ny, V.nz, V.px, V.py);
-        count();
-        if (!dev) LSS_CUDA(cudaMemcpyAsync(dbias, fw[0], n * 4, cudaMemcpyDeviceToHost, st));
+        k_ns_gather<<<grid, 256, 0, st>>>(dev ? dev : a.fw[0], a.dbias, V.nx, V.ny, V.nz, V.px, V.py);
+        count_launch(owner);
+        if (!dev) LSS_CUDA(cudaMemcpyAsync(dbias, a.fw[0], n * 4, cudaMemcpyDeviceToHost, st));
     }
     double h[8];
     unsigned long long na = 0;
-    std::vector<double> parts((size_t)bgrid * 3);
-    LSS_CUDA(cudaMemcpyAsync(h, gsum, sizeof(h), cudaMemcpyDeviceToHost, st));
-    LSS_CUDA(cudaMemcpyAsync(&na, nact, 8, cudaMemcpyDeviceToHost, st));
-    LSS_CUDA(cudaMemcpyAsync(parts.data(), gpart, parts.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    std::vector<double> parts((size_t)gr * 3);
+    LSS_CUDA(cudaMemcpyAsync(h, a.gsum, sizeof(h), cudaMemcpyDeviceToHost, st));
+    LSS_CUDA(cudaMemcpyAsync(&na, a.nact, 8, cudaMemcpyDeviceToHost, st));
+    LSS_CUDA(cudaMemcpyAsync(parts.data(), a.gpart, parts.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
     owner->sync();
     // The blocks' parameter sums, added in block order (the same every call).
     double g3[3] = {0.0, 0.0, 0.0};
-    for (int b = 0; b < bgrid; ++b)
+    for (int b = 0; b < gr; ++b)
         for (int q = 0; q < 3; ++q) g3[q] += parts[(size_t)3 * b + q];
     const double den = h[4] + h[5];
     out->loss = 1.0 - 2.0 * h[6] / den;
