@@ -17,16 +17,27 @@
 // copied) and copies across the bricks of A_{k-1} that left the set; the
 // changed voxels' ballot words are dilated into A_{k+1} exactly as in the
 // persistent kernel, so the recorded sets are the sparse engine's sets.  phi
-// is checkpointed every `every` iterations.
+// is checkpointed at the start of every segment of `every` iterations but
+// the last; over the last segment the forward instead logs, per iteration
+// k, the bricks of A_k as they were before the update (phi_k there).
+//
+// States without dense copies.  phi_k and phi_{k+1} differ only inside the
+// bricks of A_k, so a field that holds phi_{k+2} becomes phi_k by writing
+// back the logged bricks of A_k (phi_k) and those of A_{k+1} outside A_k
+// (phi_{k+1} = phi_k there).  A segment's states live in a pair of fields,
+// state t in pair[(t - base) & 1], that starts with its two highest states
+// and walks down two states at a time.
 //
 // Reverse (k_adj_reverse).  The soft-Dice sums and lambda_K, then segment by
-// segment from the last checkpoint: the segment's states are recomputed from
-// its checkpoint (bit-identical, the arithmetic is deterministic) into
-// `every` - 1 buffers, copying into each only the bricks that can differ
-// from what it held for the later segment, and the segment's iterations run
-// backwards on one lambda field, in place:
+// segment from the last: the last segment runs on the forward's pair (phi_K,
+// phi_{K-1}) and its log.  Every other segment is recomputed from its
+// checkpoint (bit-identical, the arithmetic is deterministic) while the
+// segment after it runs backwards: the checkpoint and a copy of it form the
+// pair of a forward-style ping-pong that logs its bricks as it goes.  The
+// segment's iterations run backwards on one lambda field, in place:
 //   take:  U = lambda_{k+1} at the voxels of A_k, lambda = 0 there (lambda
-//          keeps lambda_{k+1} everywhere else: the pass-through);
+//          keeps lambda_{k+1} everywhere else: the pass-through), and the
+//          pair's other field stepped down to phi_k;
 //   vjp:   every active voxel v scatters U[v] through the transposed stencil
 //          Jacobian of the update onto its 19 stencil voxels (fp32 atomics);
 // the parameter gradients are summed per block in FP64 (the gradient-check
@@ -79,9 +90,10 @@ __device__ __forceinline__ int3 voxel_of(const NsVol& V, uint32_t b, int j) {
 // recompute buffers, the forward's pair) are fstride floats apart.
 struct AdjPlan {
     NsVol V;                    // the one volume (brick_base 0)
-    float* ck0;                 // checkpoint s = ck0 + s * fstride (phi_{s * every})
-    float* seg1;                // recompute buffer i >= 1 = seg1 + (i - 1) * fstride
+    float* ck0;                 // checkpoint s < nck - 1 = ck0 + s * fstride (phi_{s * every})
+    float* qb[2];               // second field of a recomputed segment's pair (by parity)
     float* fw[2];               // the forward's ping-pong pair
+    float* log0;                // brick logs: set (s & 1), slot t - s * every, lgstride floats each
     float* lam;
     float* U;
     float* dbias;               // nullable
@@ -93,7 +105,7 @@ struct AdjPlan {
     double* gsum;               // [8]: soft-Dice sums in 4..6
     double* gpart;              // [grid][3]: each block's dT, deps, dalpha
     unsigned long long* nact;   // active-voxel updates of the forward
-    uint64_t fstride, astride, lstride, P;
+    uint64_t fstride, astride, lstride, lgstride, P;
     uint32_t nb;
     int32_t K, every, nck;
     float tau;
@@ -102,9 +114,31 @@ struct AdjPlan {
 __device__ __forceinline__ unsigned long long* plan_act(const AdjPlan& a, int k) { return a.act0 + (uint64_t)k * a.astride; }
 __device__ __forceinline__ uint32_t* plan_list(const AdjPlan& a, int k) { return a.list0 + (uint64_t)k * a.lstride; }
 __device__ __forceinline__ uint32_t* plan_flag(const AdjPlan& a, int k) { return a.flag0 + (uint64_t)k * a.lstride; }
-// Recompute buffer i of a segment whose checkpoint is s (i = 0: the checkpoint).
-__device__ __forceinline__ float* plan_seg(const AdjPlan& a, int s, int i) {
-    return i == 0 ? a.ck0 + (uint64_t)s * a.fstride : a.seg1 + (uint64_t)(i - 1) * a.fstride;
+// The log of iteration t of segment s: the bricks of list_t before the
+// update, brick i of the list at i * VOX.
+__device__ __forceinline__ float* plan_log(const AdjPlan& a, int s, int t) {
+    return a.log0 + ((uint64_t)(s & 1) * a.every + (uint64_t)(t - s * a.every)) * a.lgstride;
+}
+
+// The pair of fields segment s runs on in the reverse: state t in
+// f[(t - base) & 1].  The last segment: the forward's pair.  The others:
+// their checkpoint and a second field.
+struct SegPair {
+    float* f[2];
+    int base;
+};
+__device__ __forceinline__ SegPair seg_pair(const AdjPlan& a, int s) {
+    SegPair p;
+    if (s == a.nck - 1) {
+        p.f[0] = a.fw[0];
+        p.f[1] = a.fw[1];
+        p.base = 0;
+    } else {
+        p.f[0] = a.ck0 + (uint64_t)s * a.fstride;
+        p.f[1] = a.qb[s & 1];
+        p.base = s * a.every;
+    }
+    return p;
 }
 
 // Per-iteration brick lists: list[k][0 .. count[k]) = the bricks of A_k in
@@ -157,12 +191,14 @@ __device__ __forceinline__ void adj_dilate_brick(const NsVol& V, uint32_t b, con
 // list_k (flag_k clear) are copied from in to out, so that out equals in
 // outside the bricks of A_k.  With nxt (the recorded forward, not a
 // recomputation): each updated brick's changed voxels are dilated into A_{k+1}
-// by the same block.  Returns the active voxels this thread updated.
+// by the same block.  With log: brick i of list_k is logged as it was before
+// the update (in) at log + i * VOX.  Returns the active voxels this thread
+// updated.
 template <class S>
 __device__ uint32_t adj_update(const NsVol& V, const float* in, float* out, const unsigned long long* act,
                                const uint32_t* list, const uint32_t* count, const uint32_t* prev,
                                const uint32_t* prev_count, const uint32_t* flag_k, unsigned long long* nxt,
-                               uint32_t* flag_next, uint32_t* list_next, uint32_t* count_next) {
+                               uint32_t* flag_next, uint32_t* list_next, uint32_t* count_next, float* log) {
     __shared__ uint32_t chg[S::CHG];
     __shared__ uint32_t any;
     const uint32_t n = *count, np = prev ? *prev_count : 0u;
@@ -183,6 +219,7 @@ __device__ uint32_t adj_update(const NsVol& V, const float* in, float* out, cons
             if (p.x < V.nx && p.y < V.ny && p.z < V.nz) {
                 const size_t idx = ((size_t)p.z * V.py + p.y) * V.px + p.x;
                 const float c = in[idx];
+                if (upd && log) log[(size_t)i * S::VOX + j] = c;
                 if (upd && ((act[(size_t)b * S::WORDS + (j >> 6)] >> (j & 63)) & 1ull)) {
                     auto P = [&](int dx, int dy, int dz) {
                         return in[((size_t)clampi(p.z + dz, V.nz) * V.py + clampi(p.y + dy, V.ny)) * V.px +
@@ -214,32 +251,27 @@ __device__ uint32_t adj_update(const NsVol& V, const float* in, float* out, cons
     return mine;
 }
 
-// Copies src to dst brick by brick: every brick (lists == null) or the bricks
-// of lists k_lo .. k_hi (bricks may repeat); bricks flagged in `skip` (the
-// next update rewrites them whole) are left out, so the copy and that update
-// write disjoint bricks.
+// Steps dst (holding phi_{k+2}) down to phi_k from the logs of segment s:
+// the bricks of list_k from log_k, those of list_{k+1} outside list_k from
+// log_{k+1}.
 template <class S>
-__device__ void adj_copy_bricks(const AdjPlan& a, const float* src, float* dst, int k_lo, int k_hi,
-                                const uint32_t* skip, bool all) {
+__device__ void adj_restore(const AdjPlan& a, int s, int k, float* dst) {
     const NsVol& V = a.V;
-    auto copy = [&](uint32_t b) {
-        if (skip[b]) return;
-        for (int j = threadIdx.x; j < S::VOX; j += blockDim.x) {
-            const int3 p = voxel_of<S>(V, b, j);
-            if (p.x < V.nx && p.y < V.ny && p.z < V.nz) {
-                const size_t idx = ((size_t)p.z * V.py + p.y) * V.px + p.x;
-                dst[idx] = src[idx];
+    const uint32_t* in_k = plan_flag(a, k);
+    for (int q = 0; q < 2; ++q) {
+        const int t = k + q;
+        const uint32_t n = a.counts[t];
+        const uint32_t* list = plan_list(a, t);
+        const float* log = plan_log(a, s, t);
+        for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
+            const uint32_t b = list[i];
+            if (q == 1 && in_k[b]) continue;  // uniform over the block
+            for (int j = threadIdx.x; j < S::VOX; j += blockDim.x) {
+                const int3 p = voxel_of<S>(V, b, j);
+                if (p.x < V.nx && p.y < V.ny && p.z < V.nz)
+                    dst[((size_t)p.z * V.py + p.y) * V.px + p.x] = log[(size_t)i * S::VOX + j];
             }
         }
-    };
-    if (all) {
-        for (uint32_t b = blockIdx.x; b < a.nb; b += gridDim.x) copy(b);
-        return;
-    }
-    for (int k = k_lo; k <= k_hi; ++k) {
-        const uint32_t n = a.counts[k];
-        const uint32_t* list = plan_list(a, k);
-        for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) copy(list[i]);
     }
 }
 
@@ -442,7 +474,8 @@ __device__ void adj_vjp(const NsVol& V, const float* phi, const unsigned long lo
     }
 }
 
-// The forward: list_0, then K iterations, phi checkpointed every `every`.
+// The forward: list_0, then K iterations; phi checkpointed at the start of
+// every segment but the first (the caller's copy) and the last (logged).
 template <class S>
 __global__ void __launch_bounds__(kAdjThreads) k_adj_forward(const AdjPlan a) {
     cg::grid_group grid = cg::this_grid();
@@ -450,17 +483,19 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_forward(const AdjPlan a) {
     adj_list0<S>(plan_act(a, 0), plan_flag(a, 0), plan_list(a, 0), &a.counts[0], a.nb);
     grid.sync();
     uint32_t mine = 0;
+    const int last = a.nck - 1;
     for (int k = 0; k < a.K; ++k) {
         const float* src = a.fw[k & 1];
         float* dst = a.fw[(k + 1) & 1];
         mine += adj_update<S>(V, src, dst, plan_act(a, k), plan_list(a, k), &a.counts[k],
                               k ? plan_list(a, k - 1) : nullptr, k ? &a.counts[k - 1] : nullptr, plan_flag(a, k),
-                              plan_act(a, k + 1), plan_flag(a, k + 1), plan_list(a, k + 1), &a.counts[k + 1]);
+                              plan_act(a, k + 1), plan_flag(a, k + 1), plan_list(a, k + 1), &a.counts[k + 1],
+                              k >= last * a.every ? plan_log(a, last, k) : nullptr);
         grid.sync();
         // The next iteration reads dst and writes the other buffer: the copy
         // needs no barrier of its own (the reverse pass is another launch).
-        if ((k + 1) % a.every == 0 && k + 1 < a.K)
-            adj_copy_field(dst, a.ck0 + (uint64_t)((k + 1) / a.every) * a.fstride, a.P);
+        const int m = (k + 1) / a.every;
+        if ((k + 1) % a.every == 0 && m < last) adj_copy_field(dst, a.ck0 + (uint64_t)m * a.fstride, a.P);
     }
     __shared__ uint32_t s_cnt;
     if (threadIdx.x == 0) s_cnt = 0u;
@@ -471,67 +506,135 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_forward(const AdjPlan a) {
     if (threadIdx.x == 0 && s_cnt) atomicAdd(a.nact, (unsigned long long)s_cnt);
 }
 
+// The padded field in groups of four voxels of one row (px is a multiple of
+// 4): group g covers x = 4 (g mod px/4) .. + 3 of row g div px/4, row
+// (y, z) = (row mod py, row div py).  Returns the first x, or -1 for a group
+// outside the volume (a padding row or padding columns).
+__device__ __forceinline__ int group_x(const NsVol& V, uint64_t g) {
+    const uint64_t q = (uint64_t)V.px / 4, r = g / q;
+    const int x0 = (int)(g - r * q) * 4;
+    const uint64_t y = r % (uint64_t)V.py, z = r / (uint64_t)V.py;
+    return (y < (uint64_t)V.ny && z < (uint64_t)V.nz && x0 < V.nx) ? x0 : -1;
+}
+
+// The soft-Dice terms of one voxel: s = sigmoid(-phi / tau), t = target.
+__device__ __forceinline__ float soft_mask(float phi, float tau) { return 1.0f / (1.0f + expf(phi / tau)); }
+
 // The reverse: the loss and lambda_K, then the segments from the last.
 template <class S>
 __global__ void __launch_bounds__(kAdjThreads) k_adj_reverse(const AdjPlan a) {
     cg::grid_group grid = cg::this_grid();
     const NsVol& V = a.V;
     const float* phiK = a.fw[a.K & 1];
-    const uint32_t rows = (uint32_t)V.ny * (uint32_t)V.nz;
+    const float4* phi4 = reinterpret_cast<const float4*>(phiK);
+    const uchar4* tgt4 = reinterpret_cast<const uchar4*>(a.tgt);
+    const uint64_t ng = a.P / 4, t0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x,
+                   nt = (uint64_t)gridDim.x * blockDim.x;
+    constexpr int G = 4;  // groups in flight per thread
     // Soft-Dice sums (s, t, s t): per voxel in fp32, per block and grid in FP64.
     {
         float ss = 0.0f, tt = 0.0f, st = 0.0f;
-        for (uint32_t r = blockIdx.x; r < rows; r += gridDim.x) {
-            const uint32_t z = r / (uint32_t)V.ny, y = r - z * (uint32_t)V.ny;
-            const size_t row = ((size_t)z * V.py + y) * V.px;
-            for (int x = threadIdx.x; x < V.nx; x += blockDim.x) {
-                const float s = 1.0f / (1.0f + expf(phiK[row + x] / a.tau));
-                const float tv = a.tgt[row + x] ? 1.0f : 0.0f;
-                ss += s;
-                tt += tv;
-                st += s * tv;
+        for (uint64_t g0 = t0; g0 < ng; g0 += G * nt) {
+            float4 f[G];
+            uchar4 m[G];
+#pragma unroll
+            for (int u = 0; u < G; ++u) {
+                const uint64_t g = g0 + u * nt;
+                if (g < ng) {
+                    f[u] = phi4[g];
+                    m[u] = tgt4[g];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < G; ++u) {
+                const uint64_t g = g0 + u * nt;
+                const int x0 = g < ng ? group_x(V, g) : -1;
+                if (x0 < 0) continue;
+                const float fv[4] = {f[u].x, f[u].y, f[u].z, f[u].w};
+                const unsigned char mv[4] = {m[u].x, m[u].y, m[u].z, m[u].w};
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    if (x0 + e >= V.nx) break;
+                    const float s = soft_mask(fv[e], a.tau);
+                    const float tv = mv[e] ? 1.0f : 0.0f;
+                    ss += s;
+                    tt += tv;
+                    st += s * tv;
+                }
             }
         }
         block_sum3(ss, tt, st, a.gsum + 4);
     }
     grid.sync();
-    // lambda_K = dloss/dphi_K: dloss/ds = (2 st - 2 t den) / den^2.
+    // lambda_K = dloss/dphi_K: dloss/ds = (2 st - 2 t den) / den^2; 0 in the padding.
     {
         const double den = a.gsum[4] + a.gsum[5], sst = a.gsum[6];
         const float c_out = (float)(2.0 * sst / (den * den)), c_in = (float)(2.0 * sst / (den * den) - 2.0 / den);
-        for (uint32_t r = blockIdx.x; r < rows; r += gridDim.x) {
-            const uint32_t z = r / (uint32_t)V.ny, y = r - z * (uint32_t)V.ny;
-            const size_t row = ((size_t)z * V.py + y) * V.px;
-            for (int x = threadIdx.x; x < V.nx; x += blockDim.x) {
-                const float s = 1.0f / (1.0f + expf(phiK[row + x] / a.tau));
-                a.lam[row + x] = (a.tgt[row + x] ? c_in : c_out) * (-s * (1.0f - s) / a.tau);
+        float4* lam4 = reinterpret_cast<float4*>(a.lam);
+        for (uint64_t g0 = t0; g0 < ng; g0 += G * nt) {
+            float4 f[G];
+            uchar4 m[G];
+#pragma unroll
+            for (int u = 0; u < G; ++u) {
+                const uint64_t g = g0 + u * nt;
+                if (g < ng) {
+                    f[u] = phi4[g];
+                    m[u] = tgt4[g];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < G; ++u) {
+                const uint64_t g = g0 + u * nt;
+                if (g >= ng) continue;
+                const int x0 = group_x(V, g);
+                const float fv[4] = {f[u].x, f[u].y, f[u].z, f[u].w};
+                const unsigned char mv[4] = {m[u].x, m[u].y, m[u].z, m[u].w};
+                float l[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const float s = soft_mask(fv[e], a.tau);
+                    l[e] = (x0 >= 0 && x0 + e < V.nx) ? (mv[e] ? c_in : c_out) * (-s * (1.0f - s) / a.tau) : 0.0f;
+                }
+                lam4[g] = make_float4(l[0], l[1], l[2], l[3]);
             }
         }
     }
     grid.sync();
     double s3[3] = {0.0, 0.0, 0.0};
-    for (int sgi = a.nck - 1; sgi >= 0; --sgi) {
-        const int s0 = sgi * a.every, s1 = min(a.K, s0 + a.every);
-        // Buffer i held phi_{(sgi+1)*every + i} for the later segment when that
-        // segment reached it (every segment but the last, processed first, is
-        // `every` long); otherwise nothing of this call.
-        const int later = sgi + 1, later_len = later < a.nck ? min(a.K, (later + 1) * a.every) - later * a.every : 0;
-        for (int k = s0; k + 1 < s1; ++k) {
-            const int i = k - s0 + 1;
-            const float* src = plan_seg(a, sgi, i - 1);
-            float* d = plan_seg(a, sgi, i);
-            const int held = i < later_len ? later * a.every + i : -1;
-            if (held < 0) adj_copy_bricks<S>(a, src, d, 0, -1, plan_flag(a, k), true);
-            else if (held - 1 >= k + 1) adj_copy_bricks<S>(a, src, d, k + 1, held - 1, plan_flag(a, k), false);
-            adj_update<S>(V, src, d, plan_act(a, k), plan_list(a, k), &a.counts[k], nullptr, nullptr, nullptr,
-                          nullptr, nullptr, nullptr, nullptr);
-            grid.sync();
-        }
-        for (int k = s1 - 1; k >= s0; --k) {
-            adj_take<S>(V, plan_act(a, k), plan_list(a, k), &a.counts[k], a.lam, a.U);
-            grid.sync();
-            adj_vjp<S>(V, plan_seg(a, sgi, k - s0), plan_act(a, k), plan_list(a, k), &a.counts[k], a.U, a.lam,
-                       a.dbias, s3);
+    for (int s = a.nck - 1; s >= 0; --s) {
+        const int s0 = s * a.every, s1 = min(a.K, s0 + a.every), len = s1 - s0;
+        const SegPair pr = seg_pair(a, s);
+        // The highest state the pair holds (with the one below it): phi_K for
+        // the last segment, phi_{s1 - 1} after a recomputation.
+        const int top = s == a.nck - 1 ? a.K : s1 - 1;
+        // Segment s - 1 (full length) is recomputed beside this one, one step
+        // in each take phase: its checkpoint copied into the pair's second
+        // field, then its iterations s0' .. s0' + every - 2, logged.
+        const int recn = (s > 0 && a.every > 1) ? a.every : 0;
+        const SegPair rp = s > 0 ? seg_pair(a, s - 1) : pr;
+        const int J = max(2 * len, 2 * recn - 1);
+        for (int j = 0; j < J; ++j) {
+            if (j < 2 * len) {
+                const int k = s1 - 1 - j / 2;
+                if ((j & 1) == 0) {
+                    adj_take<S>(V, plan_act(a, k), plan_list(a, k), &a.counts[k], a.lam, a.U);
+                    if (k < top - 1) adj_restore<S>(a, s, k, pr.f[(k - pr.base) & 1]);
+                } else {
+                    adj_vjp<S>(V, pr.f[(k - pr.base) & 1], plan_act(a, k), plan_list(a, k), &a.counts[k], a.U,
+                               a.lam, a.dbias, s3);
+                }
+            }
+            const int r = j / 2;
+            if ((j & 1) == 0 && r < recn) {
+                if (r == 0) {
+                    adj_copy_field(rp.f[0], rp.f[1], a.P);
+                } else {
+                    const int t = rp.base + r - 1;
+                    adj_update<S>(V, rp.f[(r - 1) & 1], rp.f[r & 1], plan_act(a, t), plan_list(a, t), &a.counts[t],
+                                  r >= 2 ? plan_list(a, t - 1) : nullptr, r >= 2 ? &a.counts[t - 1] : nullptr,
+                                  plan_flag(a, t), nullptr, nullptr, nullptr, nullptr, plan_log(a, s - 1, t));
+                }
+            }
             grid.sync();
         }
     }
@@ -563,8 +666,14 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     // One device workspace (kept by the engine between calls), carved into
     // 256-byte aligned parts.
     auto al = [](uint64_t b) { return (b + 255) / 256 * 256; };
-    const uint64_t nfields = (uint64_t)nck + (every - 1) + 4 + (dbias ? 1 : 0) + (bias ? 1 : 0);
-    const uint64_t total = nfields * al(P * 4) + (uint64_t)(K + 1) * al(mwords * 8) +
+    // Fields: the checkpoints of every segment but the last, the second
+    // fields of two recomputed segments' pairs, the forward's pair, lambda,
+    // U, d_bias, bias; then two sets of `every` brick logs (one set with a
+    // single segment), a brick list's worth of voxels each.
+    const int nqb = (nck > 1 && every > 1) ? 2 : 0, nsets = std::min(nck, 2);
+    const uint64_t nfields = (uint64_t)(nck - 1) + nqb + 4 + (dbias ? 1 : 0) + (bias ? 1 : 0);
+    const uint64_t logb = al((uint64_t)nb * S::VOX * 4);
+    const uint64_t total = nfields * al(P * 4) + (uint64_t)nsets * every * logb + (uint64_t)(K + 1) * al(mwords * 8) +
                            2 * (uint64_t)(K + 1) * al((uint64_t)nb * 4) + al((uint64_t)(K + 1) * 4) + al(P) +
                            al(8 * sizeof(double) + 8) + al((uint64_t)gr * 3 * sizeof(double));
     char* base = (char*)core.workspace(total);
@@ -579,14 +688,16 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     AdjPlan a;
     std::memset(&a, 0, sizeof(a));
     a.fstride = al(P * 4) / 4;
-    a.ck0 = F();
-    for (int s = 1; s < nck; ++s) F();
-    a.seg1 = every > 1 ? F() : nullptr;
-    for (int i = 2; i < every; ++i) F();
+    a.ck0 = nck > 1 ? F() : nullptr;
+    for (int s = 1; s < nck - 1; ++s) F();
+    for (int q = 0; q < nqb; ++q) a.qb[q] = F();
     a.fw[0] = F();
     a.fw[1] = F();
     a.lam = F();
     a.U = F();
+    a.lgstride = logb / 4;
+    a.log0 = (float*)carve(logb);
+    for (int i = 1; i < nsets * every; ++i) carve(logb);
     a.astride = al(mwords * 8) / 8;
     a.act0 = (unsigned long long*)carve(mwords * 8);
     for (int k = 1; k <= K; ++k) carve(mwords * 8);
@@ -639,10 +750,10 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     LSS_CUDA(cudaMemsetAsync(a.flag0, 0, (uint64_t)(K + 1) * al((uint64_t)nb * 4), st));
     LSS_CUDA(cudaMemsetAsync(a.counts, 0, (uint64_t)(K + 1) * 4, st));
     // Forward from the engine's current phi and active set: both buffers of
-    // the pair and the first checkpoint hold phi_0.
+    // the pair and the first checkpoint (with more than one segment) hold phi_0.
     const float* phi0 = V.phi[core.parity()];
     for (float* d : {a.ck0, a.fw[0], a.fw[1]})
-        LSS_CUDA(cudaMemcpyAsync(d, phi0, P * 4, cudaMemcpyDeviceToDevice, st));
+        if (d) LSS_CUDA(cudaMemcpyAsync(d, phi0, P * 4, cudaMemcpyDeviceToDevice, st));
     LSS_CUDA(cudaMemcpyAsync(a.act0, core.masks(core.parity()), mwords * 8, cudaMemcpyDeviceToDevice, st));
     void* params[] = {(void*)&a};
     LSS_CUDA(cudaLaunchCooperativeKernel(kf, dim3(gf), dim3(kAdjThreads), params, 0, st));
