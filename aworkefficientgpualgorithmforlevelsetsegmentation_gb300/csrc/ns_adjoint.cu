@@ -94,14 +94,15 @@ struct AdjPlan {
     float* qb[2];               // second field of a recomputed segment's pair (by parity)
     float* fw[2];               // the forward's ping-pong pair
     float* log0;                // brick logs: set (s & 1), slot t - s * every, lgstride floats each
-    float* lam;
-    float* U;
+    float* lam;                 // lambda = lam + Z[(k + 1) & 1] entering reverse iteration k
+    float* Z[2];                // lambda contributions of the last reverse iteration, by parity
     float* dbias;               // nullable
     const uint8_t* tgt;
     unsigned long long* act0;   // [K+1][NB * WORDS]: the recorded brick masks of A_k
     uint32_t* list0;            // [K+1][NB]
     uint32_t* flag0;            // [K+1][NB]
     uint32_t* counts;           // [K+1]
+    uint32_t* flagT[2];         // [NB]: bricks reverse iteration k scatters into, in flagT[(k - 1) & 1]
     double* gsum;               // [8]: soft-Dice sums in 4..6
     double* gpart;              // [grid][3]: each block's dT, deps, dalpha
     unsigned long long* nact;   // active-voxel updates of the forward
@@ -159,14 +160,15 @@ __device__ __forceinline__ void adj_list0(const unsigned long long* act, uint32_
     }
 }
 
-// The changed-voxel ballot words of one brick (chg, CHG words) dilated into
-// its 27 neighbours' masks of A_{k+1}; the first thread to put a word into a
-// brick appends the brick to list_{k+1}.  Threads t0, t0 + stride, ... take
-// the (neighbour, mask word) pairs.
+// The voxel bits of one brick (chg, CHG 32-bit words) dilated (nbh = 6 or
+// 26) into its 27 neighbours: with nxt, ORed into their masks of A_{k+1};
+// the first thread to find a word for a brick appends the brick to the list
+// (flag_next, list_next, count_next).  Threads t0, t0 + stride, ... take the
+// (neighbour, mask word) pairs.
 template <class S>
 __device__ __forceinline__ void adj_dilate_brick(const NsVol& V, uint32_t b, const uint32_t* chg, int t0, int stride,
-                                                 unsigned long long* nxt, uint32_t* flag_next, uint32_t* list_next,
-                                                 uint32_t* count_next) {
+                                                 int nbh, unsigned long long* nxt, uint32_t* flag_next,
+                                                 uint32_t* list_next, uint32_t* count_next) {
     const int3 o = brick_origin<S>(V, b + V.brick_base);
     for (int r = t0; r < 27 * S::WORDS; r += stride) {
         const int slot = r / S::WORDS, w = r % S::WORDS;
@@ -174,12 +176,12 @@ __device__ __forceinline__ void adj_dilate_brick(const NsVol& V, uint32_t b, con
         const int bx = o.x / S::X + ox, by = o.y / S::Y + oy, bz = o.z / S::Z + oz;
         const int lx = V.nx - bx * S::X, ly = V.ny - by * S::Y, lz = V.nz - bz * S::Z;
         if (bx < 0 || by < 0 || bz < 0 || lx <= 0 || ly <= 0 || lz <= 0) continue;
-        uint64_t x = dilate_word<S>(chg, ox, oy, oz, w, V.nbh);
+        uint64_t x = dilate_word<S>(chg, ox, oy, oz, w, nbh);
         if (lx < S::X || ly < S::Y || lz < S::Z)
             x &= inside_mask<S>(w, min(lx, S::X), min(ly, S::Y), min(lz, S::Z));
         if (!x) continue;
         const uint32_t nbi = b + (int32_t)((oz * V.nby + oy) * V.nbx + ox);
-        atomicOr(&nxt[(size_t)nbi * S::WORDS + w], (unsigned long long)x);
+        if (nxt) atomicOr(&nxt[(size_t)nbi * S::WORDS + w], (unsigned long long)x);
         if (*(volatile uint32_t*)&flag_next[nbi] == 0u && atomicExch(&flag_next[nbi], 1u) == 0u)
             list_next[atomicAdd(count_next, 1u)] = nbi;
     }
@@ -244,7 +246,8 @@ __device__ uint32_t adj_update(const NsVol& V, const float* in, float* out, cons
         }
         if (dil) {
             __syncthreads();  // chg and any complete
-            if (any) adj_dilate_brick<S>(V, b, chg, threadIdx.x, blockDim.x, nxt, flag_next, list_next, count_next);
+            if (any)
+                adj_dilate_brick<S>(V, b, chg, threadIdx.x, blockDim.x, V.nbh, nxt, flag_next, list_next, count_next);
         }
     }
     __syncthreads();  // chg and any are reused by the next call
@@ -282,26 +285,6 @@ __device__ void adj_copy_field(const float* src, float* dst, uint64_t P) {
     float4* d4 = reinterpret_cast<float4*>(dst);
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n4; i += (uint64_t)gridDim.x * blockDim.x)
         d4[i] = s4[i];
-}
-
-// Reverse iteration k, first half (block per brick of list_k): U =
-// lambda_{k+1} at the voxels of A_k and lambda = 0 there; lambda keeps
-// lambda_{k+1} at every other voxel.
-template <class S>
-__device__ void adj_take(const NsVol& V, const unsigned long long* act, const uint32_t* list, const uint32_t* count,
-                         float* lam, float* U) {
-    const uint32_t n = *count;
-    for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
-        const uint32_t b = list[i];
-        for (int j = threadIdx.x; j < S::VOX; j += blockDim.x) {
-            if (!((act[(size_t)b * S::WORDS + (j >> 6)] >> (j & 63)) & 1ull)) continue;
-            const int3 p = voxel_of<S>(V, b, j);
-            if (p.x >= V.nx || p.y >= V.ny || p.z >= V.nz) continue;
-            const size_t idx = ((size_t)p.z * V.py + p.y) * V.px + p.x;
-            U[idx] = lam[idx];
-            lam[idx] = 0.0f;
-        }
-    }
 }
 
 // Vector-Jacobian product of ns_update_f32 at one voxel with upstream lam:
@@ -439,37 +422,163 @@ __device__ __forceinline__ void block_sum3(double a0, double a1, double a2, doub
     __syncthreads();
 }
 
-// Reverse iteration k, second half (block per brick of list_k): scatters U
-// (lambda_{k+1}) of the voxels of A_k through the update's transposed
-// Jacobian into lam, adds the bias gradient, and returns the parameter terms
-// (T, eps, alpha) in s3 (FP64, per thread).
+// The bricks one brick's reverse iteration scatters into: the 26-dilation of
+// its voxels of A_k (act, a superset of the update's stencil), clipped to
+// the volume; each gets mark[brick] = 1.  Threads t0, t0 + stride, ... take
+// the (neighbour, mask word) pairs.
 template <class S>
-__device__ void adj_vjp(const NsVol& V, const float* phi, const unsigned long long* act, const uint32_t* list,
-                        const uint32_t* count, const float* U, float* lam, float* dbias, double* s3) {
-    const uint32_t n = *count;
-    for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
-        const uint32_t b = list[i];
+__device__ __forceinline__ void adj_mark_brick(const NsVol& V, uint32_t b, const unsigned long long* act, int t0,
+                                               int stride, uint32_t* mark) {
+    const uint32_t* bits = reinterpret_cast<const uint32_t*>(act + (size_t)b * S::WORDS);
+    const int3 o = brick_origin<S>(V, b + V.brick_base);
+    for (int r = t0; r < 27 * S::WORDS; r += stride) {
+        const int slot = r / S::WORDS, w = r % S::WORDS;
+        const int ox = slot % 3 - 1, oy = (slot / 3) % 3 - 1, oz = slot / 9 - 1;
+        const int bx = o.x / S::X + ox, by = o.y / S::Y + oy, bz = o.z / S::Z + oz;
+        const int lx = V.nx - bx * S::X, ly = V.ny - by * S::Y, lz = V.nz - bz * S::Z;
+        if (bx < 0 || by < 0 || bz < 0 || lx <= 0 || ly <= 0 || lz <= 0) continue;
+        uint64_t x = dilate_word<S>(bits, ox, oy, oz, w, 26);
+        if (lx < S::X || ly < S::Y || lz < S::Z)
+            x &= inside_mask<S>(w, min(lx, S::X), min(ly, S::Y), min(lz, S::Z));
+        if (x) mark[b + (int32_t)((oz * V.nby + oy) * V.nbx + ox)] = 1u;
+    }
+}
+
+// What reverse iteration k needs first, loaded before the barrier that
+// precedes it (the recorded lists and masks do not change in the reverse):
+// count_k, the block's first brick of list_k and that brick's mask word of
+// the thread's voxel.
+struct RevPre {
+    uint32_t n, b;
+    unsigned long long w;
+};
+template <class S>
+__device__ __forceinline__ RevPre rev_prefetch(const AdjPlan& a, int k) {
+    RevPre r{0u, 0u, 0ull};
+    if (k < 0) return r;
+    r.n = a.counts[k];
+    if (blockIdx.x < r.n) {
+        r.b = plan_list(a, k)[blockIdx.x];
+        if (threadIdx.x < S::VOX) r.w = plan_act(a, k)[(size_t)r.b * S::WORDS + (threadIdx.x >> 6)];
+    }
+    return r;
+}
+
+// Reverse iteration k.  With p = (k + 1) & 1, lambda_{k+1} = lam + Z[p] on
+// entry, where Z[p] (the previous reverse iteration's scatter) is zero
+// outside the bricks marked in flagT[k & 1], and Z[1-p] is zero everywhere.
+// At each voxel v visited:
+//   lambda_{k+1}[v] = lam[v] + Z[p][v];  Z[p][v] = 0;
+//   v not in A_k: lam[v] = lambda_{k+1}[v] (the pass-through);
+//   v in A_k:     lam[v] = 0, and lambda_{k+1}[v] is scattered through the
+//                 transposed stencil Jacobian of the update into Z[1-p]
+//                 (fp32 atomics), the parameter terms (T, eps, alpha) added
+//                 to s3 (FP64, per thread) and the bias gradient to dbias;
+// so lambda_k = lam + Z[1-p] on exit, with the bricks Z[1-p] reaches marked
+// in flagT[(k - 1) & 1].  Part one (block per brick of A_k) visits the
+// bricks of A_k whole; part two (adj_rev_touched) the marked bricks outside
+// A_k.  Every voxel is read and written by one thread only.
+template <class S>
+__device__ void adj_rev_bricks(const AdjPlan& a, int k, const float* phi, double* s3, const RevPre& pre) {
+    const NsVol& V = a.V;
+    const int p = (k + 1) & 1;
+    float* const lam = a.lam;
+    float* const zin = a.Z[p];
+    float* const zout = a.Z[p ^ 1];
+    const unsigned long long* act = plan_act(a, k);
+    const uint32_t* list = plan_list(a, k);
+    for (uint32_t i = blockIdx.x; i < pre.n; i += gridDim.x) {
+        const bool first = i == blockIdx.x;
+        const uint32_t b = first ? pre.b : list[i];
+        int any = 0;
         for (int j = threadIdx.x; j < S::VOX; j += blockDim.x) {
-            if (!((act[(size_t)b * S::WORDS + (j >> 6)] >> (j & 63)) & 1ull)) continue;
-            const int3 p = voxel_of<S>(V, b, j);
-            if (p.x >= V.nx || p.y >= V.ny || p.z >= V.nz) continue;
-            const size_t idx = ((size_t)p.z * V.py + p.y) * V.px + p.x;
-            const float u = U[idx];
+            const unsigned long long wj = (first && j == (int)threadIdx.x) ? pre.w : act[(size_t)b * S::WORDS + (j >> 6)];
+            const bool in_a = (wj >> (j & 63)) & 1ull;
+            any |= in_a;
+            const int3 pv = voxel_of<S>(V, b, j);
+            if (pv.x >= V.nx || pv.y >= V.ny || pv.z >= V.nz) continue;
+            const size_t idx = ((size_t)pv.z * V.py + pv.y) * V.px + pv.x;
+            const float x = lam[idx], z = zin[idx];
+            const float u = x + z;
+            if (z != 0.0f) zin[idx] = 0.0f;
+            if (!in_a) {
+                if (z != 0.0f) lam[idx] = u;
+                continue;
+            }
+            if (x != 0.0f) lam[idx] = 0.0f;
             if (u == 0.0f) continue;
             auto at = [&](int dx, int dy, int dz) {
-                return ((size_t)clampi(p.z + dz, V.nz) * V.py + clampi(p.y + dy, V.ny)) * V.px +
-                       clampi(p.x + dx, V.nx);
+                return ((size_t)clampi(pv.z + dz, V.nz) * V.py + clampi(pv.y + dy, V.ny)) * V.px +
+                       clampi(pv.x + dx, V.nx);
             };
             auto P = [&](int dx, int dy, int dz) { return phi[at(dx, dy, dz)]; };
             auto add = [&](int dx, int dy, int dz, float g) {
-                if (g != 0.0f) atomicAdd(&lam[at(dx, dy, dz)], g);
+                if (g != 0.0f) atomicAdd(&zout[at(dx, dy, dz)], g);
             };
             float g4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
             ns_update_vjp_f32(P, add, V.img[idx], V.bias ? V.bias[idx] : 0.0f, V, u, g4);
             s3[0] += g4[0];
             s3[1] += g4[1];
             s3[2] += g4[2];
-            if (dbias) dbias[idx] += g4[3];
+            if (a.dbias) a.dbias[idx] += g4[3];
+        }
+        if (__syncthreads_or(any) && k > 0) adj_mark_brick<S>(V, b, act, threadIdx.x, blockDim.x, a.flagT[(k - 1) & 1]);
+    }
+}
+
+// Part two of reverse iteration k: the bricks marked in flagT[k & 1] that
+// are not in A_k hold no active voxel, so lambda_{k+1} passes through:
+// lam += Z[p], Z[p] = 0, four voxels a lane-step (brick rows of 4 or 8
+// voxels are 16-byte aligned: px is a multiple of 8; padding voxels hold
+// Z = 0 and stay as they are).  Warp w scans bricks w + l * NW (lane l; NW
+// warps), so a cluster of consecutive marked bricks spreads over the warps;
+// every mark is cleared for reverse iteration k - 2.
+template <class S>
+__device__ void adj_rev_touched(const AdjPlan& a, int k) {
+    const NsVol& V = a.V;
+    const int p = (k + 1) & 1;
+    float4* const lam4 = reinterpret_cast<float4*>(a.lam);
+    float4* const z4 = reinterpret_cast<float4*>(a.Z[p]);
+    uint32_t* flag = a.flagT[k & 1];
+    const uint32_t* in_a = plan_flag(a, k);
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5, w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    constexpr int G = S::VOX / 4, PER = (G + 31) / 32;
+    for (uint64_t base = 0; base < a.nb; base += 32ull * nw) {
+        const uint64_t bl = base + (uint64_t)lane * nw + w;
+        bool fold = false;
+        if (bl < a.nb && flag[bl]) {
+            flag[bl] = 0u;
+            fold = !in_a[bl];
+        }
+        uint32_t bal = __ballot_sync(0xffffffffu, fold);
+        while (bal) {
+            const int l = __ffs(bal) - 1;
+            bal &= bal - 1u;
+            const uint32_t b = (uint32_t)(base + (uint64_t)l * nw + w);
+            const int3 o = brick_origin<S>(V, b + V.brick_base);
+            size_t g4[PER];
+            float4 zz[PER], xx[PER];
+#pragma unroll
+            for (int u = 0; u < PER; ++u) {
+                const int q = lane + 32 * u, j = 4 * q;
+                g4[u] = q < G ? (((size_t)(o.z + j / (S::X * S::Y)) * V.py + o.y + (j / S::X) % S::Y) * V.px + o.x +
+                                 j % S::X) / 4
+                              : 0;
+                if (q < G) {
+                    zz[u] = z4[g4[u]];
+                    xx[u] = lam4[g4[u]];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < PER; ++u) {
+                if (lane + 32 * u >= G) continue;
+                if (zz[u].x != 0.0f || zz[u].y != 0.0f || zz[u].z != 0.0f || zz[u].w != 0.0f) {
+                    lam4[g4[u]] = make_float4(xx[u].x + zz[u].x, xx[u].y + zz[u].y, xx[u].z + zz[u].z,
+                                              xx[u].w + zz[u].w);
+                    z4[g4[u]] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                }
+            }
         }
     }
 }
@@ -599,6 +708,7 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_reverse(const AdjPlan a) {
             }
         }
     }
+    RevPre pre = rev_prefetch<S>(a, a.K - 1);
     grid.sync();
     double s3[3] = {0.0, 0.0, 0.0};
     for (int s = a.nck - 1; s >= 0; --s) {
@@ -608,24 +718,22 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_reverse(const AdjPlan a) {
         // the last segment, phi_{s1 - 1} after a recomputation.
         const int top = s == a.nck - 1 ? a.K : s1 - 1;
         // Segment s - 1 (full length) is recomputed beside this one, one step
-        // in each take phase: its checkpoint copied into the pair's second
-        // field, then its iterations s0' .. s0' + every - 2, logged.
+        // a phase: its checkpoint copied into the pair's second field, then
+        // its iterations s0' .. s0' + every - 2, logged.
         const int recn = (s > 0 && a.every > 1) ? a.every : 0;
         const SegPair rp = s > 0 ? seg_pair(a, s - 1) : pr;
-        const int J = max(2 * len, 2 * recn - 1);
+        const int J = max(len, recn);
         for (int j = 0; j < J; ++j) {
-            if (j < 2 * len) {
-                const int k = s1 - 1 - j / 2;
-                if ((j & 1) == 0) {
-                    adj_take<S>(V, plan_act(a, k), plan_list(a, k), &a.counts[k], a.lam, a.U);
-                    if (k < top - 1) adj_restore<S>(a, s, k, pr.f[(k - pr.base) & 1]);
-                } else {
-                    adj_vjp<S>(V, pr.f[(k - pr.base) & 1], plan_act(a, k), plan_list(a, k), &a.counts[k], a.U,
-                               a.lam, a.dbias, s3);
-                }
+            const int k = s1 - 1 - j;
+            if (j < len) {
+                // Reverse iteration k on phi_k; beside it the pair's other
+                // field steps down to phi_{k-1} (unless it holds it already).
+                adj_rev_bricks<S>(a, k, pr.f[(k - pr.base) & 1], s3, pre);
+                adj_rev_touched<S>(a, k);
+                if (k - 1 >= s0 && k - 1 < top - 1) adj_restore<S>(a, s, k - 1, pr.f[(k - 1 - pr.base) & 1]);
             }
-            const int r = j / 2;
-            if ((j & 1) == 0 && r < recn) {
+            const int r = j;
+            if (r < recn) {
                 if (r == 0) {
                     adj_copy_field(rp.f[0], rp.f[1], a.P);
                 } else {
@@ -635,6 +743,7 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_reverse(const AdjPlan a) {
                                   plan_flag(a, t), nullptr, nullptr, nullptr, nullptr, plan_log(a, s - 1, t));
                 }
             }
+            if (j < len) pre = rev_prefetch<S>(a, k - 1);
             grid.sync();
         }
     }
@@ -667,14 +776,16 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     // 256-byte aligned parts.
     auto al = [](uint64_t b) { return (b + 255) / 256 * 256; };
     // Fields: the checkpoints of every segment but the last, the second
-    // fields of two recomputed segments' pairs, the forward's pair, lambda,
-    // U, d_bias, bias; then two sets of `every` brick logs (one set with a
-    // single segment), a brick list's worth of voxels each.
+    // fields of two recomputed segments' pairs, the forward's pair, lambda
+    // and its two contribution fields, d_bias, bias; then two sets of
+    // `every` brick logs (one set with a single segment), a brick list's
+    // worth of voxels each.
     const int nqb = (nck > 1 && every > 1) ? 2 : 0, nsets = std::min(nck, 2);
-    const uint64_t nfields = (uint64_t)(nck - 1) + nqb + 4 + (dbias ? 1 : 0) + (bias ? 1 : 0);
+    const uint64_t nfields = (uint64_t)(nck - 1) + nqb + 5 + (dbias ? 1 : 0) + (bias ? 1 : 0);
     const uint64_t logb = al((uint64_t)nb * S::VOX * 4);
     const uint64_t total = nfields * al(P * 4) + (uint64_t)nsets * every * logb + (uint64_t)(K + 1) * al(mwords * 8) +
                            2 * (uint64_t)(K + 1) * al((uint64_t)nb * 4) + al((uint64_t)(K + 1) * 4) + al(P) +
+                           2 * al((uint64_t)nb * 4) +
                            al(8 * sizeof(double) + 8) + al((uint64_t)gr * 3 * sizeof(double));
     char* base = (char*)core.workspace(total);
     char* const end = base + total;
@@ -694,7 +805,8 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     a.fw[0] = F();
     a.fw[1] = F();
     a.lam = F();
-    a.U = F();
+    a.Z[0] = F();
+    a.Z[1] = F();
     a.lgstride = logb / 4;
     a.log0 = (float*)carve(logb);
     for (int i = 1; i < nsets * every; ++i) carve(logb);
@@ -707,6 +819,7 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     a.flag0 = (uint32_t*)carve((uint64_t)nb * 4);
     for (int k = 1; k <= K; ++k) carve((uint64_t)nb * 4);
     a.counts = (uint32_t*)carve((uint64_t)(K + 1) * 4);
+    for (int q = 0; q < 2; ++q) a.flagT[q] = (uint32_t*)carve((uint64_t)nb * 4);
     uint8_t* tgt = (uint8_t*)carve(P);
     a.gsum = (double*)carve(8 * sizeof(double) + 8);
     a.nact = (unsigned long long*)(a.gsum + 8);
@@ -749,6 +862,10 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     LSS_CUDA(cudaMemsetAsync(a.act0 + a.astride, 0, (uint64_t)K * al(mwords * 8), st));  // act[1..K]
     LSS_CUDA(cudaMemsetAsync(a.flag0, 0, (uint64_t)(K + 1) * al((uint64_t)nb * 4), st));
     LSS_CUDA(cudaMemsetAsync(a.counts, 0, (uint64_t)(K + 1) * 4, st));
+    for (int q = 0; q < 2; ++q) {
+        LSS_CUDA(cudaMemsetAsync(a.Z[q], 0, P * 4, st));
+        LSS_CUDA(cudaMemsetAsync(a.flagT[q], 0, (uint64_t)nb * 4, st));
+    }
     // Forward from the engine's current phi and active set: both buffers of
     // the pair and the first checkpoint (with more than one segment) hold phi_0.
     const float* phi0 = V.phi[core.parity()];
