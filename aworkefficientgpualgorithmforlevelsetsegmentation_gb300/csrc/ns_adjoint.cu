@@ -254,27 +254,88 @@ __device__ uint32_t adj_update(const NsVol& V, const float* in, float* out, cons
     return mine;
 }
 
+// Brick parts, the work split of the reverse: a brick's voxels in N runs
+// of TPG consecutive voxels (whole z-planes), one voxel a thread.  A block
+// holds GROUPS groups of TPG threads; item i of a phase (brick i / N, part
+// i mod N) goes to the group whose slot is i mod (GROUPS * grid), slot =
+// group * grid + (block + offset) mod grid.  So the parts of one brick run
+// on different SMs (an iteration holds a few dozen bricks of ~150 active
+// voxels each: one SM a brick would leave most SMs idle), and each kind of
+// work of a phase, with its own offset, starts on its own block.
+template <class S>
+struct Parts {
+    static constexpr int TPG = S::VOX < 128 ? S::VOX : 128;
+    static constexpr int N = S::VOX / TPG;
+    static constexpr int GROUPS = kAdjThreads / TPG;
+    static_assert(kAdjThreads % TPG == 0, "groups tile the block");
+    uint32_t slot, nslots;
+    int t;
+    __device__ __forceinline__ explicit Parts(uint32_t offset) {
+        const uint32_t g = threadIdx.x / TPG;
+        t = (int)(threadIdx.x % TPG);
+        slot = g * gridDim.x + (blockIdx.x + offset) % gridDim.x;
+        nslots = GROUPS * gridDim.x;
+    }
+    // Brick voxel of item i for this thread.
+    __device__ __forceinline__ int voxel(uint32_t i) const { return (int)(i % N) * TPG + t; }
+};
+
 // Steps dst (holding phi_{k+2}) down to phi_k from the logs of segment s:
 // the bricks of list_k from log_k, those of list_{k+1} outside list_k from
 // log_{k+1}.
 template <class S>
 __device__ void adj_restore(const AdjPlan& a, int s, int k, float* dst) {
     const NsVol& V = a.V;
+    const Parts<S> pt(gridDim.x / 3);
     const uint32_t* in_k = plan_flag(a, k);
-    for (int q = 0; q < 2; ++q) {
-        const int t = k + q;
-        const uint32_t n = a.counts[t];
-        const uint32_t* list = plan_list(a, t);
-        const float* log = plan_log(a, s, t);
-        for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
-            const uint32_t b = list[i];
-            if (q == 1 && in_k[b]) continue;  // uniform over the block
-            for (int j = threadIdx.x; j < S::VOX; j += blockDim.x) {
-                const int3 p = voxel_of<S>(V, b, j);
-                if (p.x < V.nx && p.y < V.ny && p.z < V.nz)
-                    dst[((size_t)p.z * V.py + p.y) * V.px + p.x] = log[(size_t)i * S::VOX + j];
-            }
+    const uint32_t n0 = a.counts[k], n1 = a.counts[k + 1];
+    const uint32_t* l0 = plan_list(a, k);
+    const uint32_t* l1 = plan_list(a, k + 1);
+    const float* g0 = plan_log(a, s, k);
+    const float* g1 = plan_log(a, s, k + 1);
+    for (uint32_t it = pt.slot; it < (n0 + n1) * Parts<S>::N; it += pt.nslots) {
+        const uint32_t bi = it / Parts<S>::N;
+        const bool first = bi < n0;
+        const uint32_t pos = first ? bi : bi - n0;
+        const uint32_t b = first ? l0[pos] : l1[pos];
+        if (!first && in_k[b]) continue;
+        const int j = pt.voxel(it);
+        const int3 p = voxel_of<S>(V, b, j);
+        if (p.x < V.nx && p.y < V.ny && p.z < V.nz)
+            dst[((size_t)p.z * V.py + p.y) * V.px + p.x] = (first ? g0 : g1)[(size_t)pos * S::VOX + j];
+    }
+}
+
+// One recomputed iteration t (in brick parts): the bricks of list_t written
+// whole into out (active voxels updated from in, the others copied) and
+// logged as they were (brick i at log + i * VOX); the bricks of prev
+// (list_{t-1}, np of them) outside list_t copied from in to out.
+template <class S>
+__device__ void adj_recompute(const NsVol& V, const float* in, float* out, const unsigned long long* act,
+                              const uint32_t* list, uint32_t n, const uint32_t* prev, uint32_t np,
+                              const uint32_t* flag_t, float* log) {
+    const Parts<S> pt(2 * gridDim.x / 3);
+    for (uint32_t it = pt.slot; it < (n + np) * Parts<S>::N; it += pt.nslots) {
+        const uint32_t bi = it / Parts<S>::N;
+        const bool upd = bi < n;
+        const uint32_t b = upd ? list[bi] : prev[bi - n];
+        if (!upd && flag_t[b]) continue;
+        const int j = pt.voxel(it);
+        const int3 p = voxel_of<S>(V, b, j);
+        if (p.x >= V.nx || p.y >= V.ny || p.z >= V.nz) continue;
+        const size_t idx = ((size_t)p.z * V.py + p.y) * V.px + p.x;
+        const float c = in[idx];
+        if (!upd || !((act[(size_t)b * S::WORDS + (j >> 6)] >> (j & 63)) & 1ull)) {
+            out[idx] = c;
+            if (upd) log[(size_t)bi * S::VOX + j] = c;
+            continue;
         }
+        log[(size_t)bi * S::VOX + j] = c;
+        auto P = [&](int dx, int dy, int dz) {
+            return in[((size_t)clampi(p.z + dz, V.nz) * V.py + clampi(p.y + dy, V.ny)) * V.px +
+                      clampi(p.x + dx, V.nx)];
+        };
+        out[idx] = ns_update_f32(P, V.img[idx], V.bias ? V.bias[idx] : 0.0f, V);
     }
 }
 
@@ -446,8 +507,8 @@ __device__ __forceinline__ void adj_mark_brick(const NsVol& V, uint32_t b, const
 
 // What reverse iteration k needs first, loaded before the barrier that
 // precedes it (the recorded lists and masks do not change in the reverse):
-// count_k, the block's first brick of list_k and that brick's mask word of
-// the thread's voxel.
+// count_k, the brick of the thread's first item of list_k and that brick's
+// mask word of the thread's voxel.
 struct RevPre {
     uint32_t n, b;
     unsigned long long w;
@@ -456,10 +517,11 @@ template <class S>
 __device__ __forceinline__ RevPre rev_prefetch(const AdjPlan& a, int k) {
     RevPre r{0u, 0u, 0ull};
     if (k < 0) return r;
+    const Parts<S> pt(0);
     r.n = a.counts[k];
-    if (blockIdx.x < r.n) {
-        r.b = plan_list(a, k)[blockIdx.x];
-        if (threadIdx.x < S::VOX) r.w = plan_act(a, k)[(size_t)r.b * S::WORDS + (threadIdx.x >> 6)];
+    if (pt.slot < r.n * Parts<S>::N) {
+        r.b = plan_list(a, k)[pt.slot / Parts<S>::N];
+        r.w = plan_act(a, k)[(size_t)r.b * S::WORDS + (pt.voxel(pt.slot) >> 6)];
     }
     return r;
 }
@@ -475,54 +537,57 @@ __device__ __forceinline__ RevPre rev_prefetch(const AdjPlan& a, int k) {
 //                 (fp32 atomics), the parameter terms (T, eps, alpha) added
 //                 to s3 (FP64, per thread) and the bias gradient to dbias;
 // so lambda_k = lam + Z[1-p] on exit, with the bricks Z[1-p] reaches marked
-// in flagT[(k - 1) & 1].  Part one (block per brick of A_k) visits the
-// bricks of A_k whole; part two (adj_rev_touched) the marked bricks outside
-// A_k.  Every voxel is read and written by one thread only.
+// in flagT[(k - 1) & 1] (by each brick's part 0).  Part one (brick parts of
+// A_k) visits the bricks of A_k whole; part two (adj_rev_touched) the
+// marked bricks outside A_k.  Every voxel is read and written by one thread
+// only.
+template <class S>
+__device__ __forceinline__ void rev_voxel(const AdjPlan& a, const float* phi, float* zin, float* zout, uint32_t b,
+                                          int j, bool in_a, double* s3) {
+    const NsVol& V = a.V;
+    const int3 pv = voxel_of<S>(V, b, j);
+    if (pv.x >= V.nx || pv.y >= V.ny || pv.z >= V.nz) return;
+    const size_t idx = ((size_t)pv.z * V.py + pv.y) * V.px + pv.x;
+    const float x = a.lam[idx], z = zin[idx];
+    const float u = x + z;
+    if (z != 0.0f) zin[idx] = 0.0f;
+    if (!in_a) {
+        if (z != 0.0f) a.lam[idx] = u;
+        return;
+    }
+    if (x != 0.0f) a.lam[idx] = 0.0f;
+    if (u == 0.0f) return;
+    auto at = [&](int dx, int dy, int dz) {
+        return ((size_t)clampi(pv.z + dz, V.nz) * V.py + clampi(pv.y + dy, V.ny)) * V.px + clampi(pv.x + dx, V.nx);
+    };
+    auto P = [&](int dx, int dy, int dz) { return phi[at(dx, dy, dz)]; };
+    auto add = [&](int dx, int dy, int dz, float g) {
+        if (g != 0.0f) atomicAdd(&zout[at(dx, dy, dz)], g);
+    };
+    float g4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    ns_update_vjp_f32(P, add, V.img[idx], V.bias ? V.bias[idx] : 0.0f, V, u, g4);
+    s3[0] += g4[0];
+    s3[1] += g4[1];
+    s3[2] += g4[2];
+    if (a.dbias) a.dbias[idx] += g4[3];
+}
+
 template <class S>
 __device__ void adj_rev_bricks(const AdjPlan& a, int k, const float* phi, double* s3, const RevPre& pre) {
-    const NsVol& V = a.V;
     const int p = (k + 1) & 1;
-    float* const lam = a.lam;
+    const Parts<S> pt(0);
     float* const zin = a.Z[p];
     float* const zout = a.Z[p ^ 1];
     const unsigned long long* act = plan_act(a, k);
     const uint32_t* list = plan_list(a, k);
-    for (uint32_t i = blockIdx.x; i < pre.n; i += gridDim.x) {
-        const bool first = i == blockIdx.x;
-        const uint32_t b = first ? pre.b : list[i];
-        int any = 0;
-        for (int j = threadIdx.x; j < S::VOX; j += blockDim.x) {
-            const unsigned long long wj = (first && j == (int)threadIdx.x) ? pre.w : act[(size_t)b * S::WORDS + (j >> 6)];
-            const bool in_a = (wj >> (j & 63)) & 1ull;
-            any |= in_a;
-            const int3 pv = voxel_of<S>(V, b, j);
-            if (pv.x >= V.nx || pv.y >= V.ny || pv.z >= V.nz) continue;
-            const size_t idx = ((size_t)pv.z * V.py + pv.y) * V.px + pv.x;
-            const float x = lam[idx], z = zin[idx];
-            const float u = x + z;
-            if (z != 0.0f) zin[idx] = 0.0f;
-            if (!in_a) {
-                if (z != 0.0f) lam[idx] = u;
-                continue;
-            }
-            if (x != 0.0f) lam[idx] = 0.0f;
-            if (u == 0.0f) continue;
-            auto at = [&](int dx, int dy, int dz) {
-                return ((size_t)clampi(pv.z + dz, V.nz) * V.py + clampi(pv.y + dy, V.ny)) * V.px +
-                       clampi(pv.x + dx, V.nx);
-            };
-            auto P = [&](int dx, int dy, int dz) { return phi[at(dx, dy, dz)]; };
-            auto add = [&](int dx, int dy, int dz, float g) {
-                if (g != 0.0f) atomicAdd(&zout[at(dx, dy, dz)], g);
-            };
-            float g4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-            ns_update_vjp_f32(P, add, V.img[idx], V.bias ? V.bias[idx] : 0.0f, V, u, g4);
-            s3[0] += g4[0];
-            s3[1] += g4[1];
-            s3[2] += g4[2];
-            if (a.dbias) a.dbias[idx] += g4[3];
-        }
-        if (__syncthreads_or(any) && k > 0) adj_mark_brick<S>(V, b, act, threadIdx.x, blockDim.x, a.flagT[(k - 1) & 1]);
+    for (uint32_t it = pt.slot; it < pre.n * Parts<S>::N; it += pt.nslots) {
+        const bool first = it == pt.slot;
+        const uint32_t b = first ? pre.b : list[it / Parts<S>::N];
+        const int j = pt.voxel(it);
+        const unsigned long long wj = first ? pre.w : act[(size_t)b * S::WORDS + (j >> 6)];
+        rev_voxel<S>(a, phi, zin, zout, b, j, (wj >> (j & 63)) & 1ull, s3);
+        if (it % Parts<S>::N == 0 && k > 0)
+            adj_mark_brick<S>(a.V, b, act, pt.t, Parts<S>::TPG, a.flagT[(k - 1) & 1]);
     }
 }
 
@@ -738,9 +803,9 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_reverse(const AdjPlan a) {
                     adj_copy_field(rp.f[0], rp.f[1], a.P);
                 } else {
                     const int t = rp.base + r - 1;
-                    adj_update<S>(V, rp.f[(r - 1) & 1], rp.f[r & 1], plan_act(a, t), plan_list(a, t), &a.counts[t],
-                                  r >= 2 ? plan_list(a, t - 1) : nullptr, r >= 2 ? &a.counts[t - 1] : nullptr,
-                                  plan_flag(a, t), nullptr, nullptr, nullptr, nullptr, plan_log(a, s - 1, t));
+                    adj_recompute<S>(V, rp.f[(r - 1) & 1], rp.f[r & 1], plan_act(a, t), plan_list(a, t), a.counts[t],
+                                     r >= 2 ? plan_list(a, t - 1) : nullptr, r >= 2 ? a.counts[t - 1] : 0u,
+                                     plan_flag(a, t), plan_log(a, s - 1, t));
                 }
             }
             if (j < len) pre = rev_prefetch<S>(a, k - 1);
