@@ -280,63 +280,56 @@ struct Parts {
     __device__ __forceinline__ int voxel(uint32_t i) const { return (int)(i % N) * TPG + t; }
 };
 
-// Steps dst (holding phi_{k+2}) down to phi_k from the logs of segment s:
-// the bricks of list_k from log_k, those of list_{k+1} outside list_k from
-// log_{k+1}.
+// One item of the restore of phi_kr into dst (holding phi_{kr+2}) from the
+// logs of segment s: the bricks of list_kr from log_kr, those of
+// list_{kr+1} outside list_kr from log_{kr+1}; n0 = count_kr.  Item i:
+// brick i / N of list_kr followed by list_{kr+1}.
 template <class S>
-__device__ void adj_restore(const AdjPlan& a, int s, int k, float* dst) {
+__device__ __forceinline__ void restore_item(const AdjPlan& a, int s, int kr, float* dst, uint32_t n0, uint32_t i,
+                                             const Parts<S>& pt) {
     const NsVol& V = a.V;
-    const Parts<S> pt(gridDim.x / 3);
-    const uint32_t* in_k = plan_flag(a, k);
-    const uint32_t n0 = a.counts[k], n1 = a.counts[k + 1];
-    const uint32_t* l0 = plan_list(a, k);
-    const uint32_t* l1 = plan_list(a, k + 1);
-    const float* g0 = plan_log(a, s, k);
-    const float* g1 = plan_log(a, s, k + 1);
-    for (uint32_t it = pt.slot; it < (n0 + n1) * Parts<S>::N; it += pt.nslots) {
-        const uint32_t bi = it / Parts<S>::N;
-        const bool first = bi < n0;
-        const uint32_t pos = first ? bi : bi - n0;
-        const uint32_t b = first ? l0[pos] : l1[pos];
-        if (!first && in_k[b]) continue;
-        const int j = pt.voxel(it);
-        const int3 p = voxel_of<S>(V, b, j);
-        if (p.x < V.nx && p.y < V.ny && p.z < V.nz)
-            dst[((size_t)p.z * V.py + p.y) * V.px + p.x] = (first ? g0 : g1)[(size_t)pos * S::VOX + j];
-    }
+    const uint32_t bi = i / Parts<S>::N;
+    const bool first = bi < n0;
+    const uint32_t pos = first ? bi : bi - n0;
+    const uint32_t b = plan_list(a, first ? kr : kr + 1)[pos];
+    if (!first && plan_flag(a, kr)[b]) return;
+    const int j = pt.voxel(i);
+    const int3 p = voxel_of<S>(V, b, j);
+    if (p.x < V.nx && p.y < V.ny && p.z < V.nz)
+        dst[((size_t)p.z * V.py + p.y) * V.px + p.x] = plan_log(a, s, first ? kr : kr + 1)[(size_t)pos * S::VOX + j];
 }
 
-// One recomputed iteration t (in brick parts): the bricks of list_t written
-// whole into out (active voxels updated from in, the others copied) and
-// logged as they were (brick i at log + i * VOX); the bricks of prev
-// (list_{t-1}, np of them) outside list_t copied from in to out.
+// One item of recomputed iteration t of segment s (list_t then, for t past
+// the segment's first iteration, list_{t-1}; n = count_t): the bricks of
+// list_t written whole into out (active voxels updated from in, the others
+// copied) and logged as they were (brick i at log_t + i * VOX); the bricks
+// of list_{t-1} outside list_t copied from in to out.
 template <class S>
-__device__ void adj_recompute(const NsVol& V, const float* in, float* out, const unsigned long long* act,
-                              const uint32_t* list, uint32_t n, const uint32_t* prev, uint32_t np,
-                              const uint32_t* flag_t, float* log) {
-    const Parts<S> pt(2 * gridDim.x / 3);
-    for (uint32_t it = pt.slot; it < (n + np) * Parts<S>::N; it += pt.nslots) {
-        const uint32_t bi = it / Parts<S>::N;
-        const bool upd = bi < n;
-        const uint32_t b = upd ? list[bi] : prev[bi - n];
-        if (!upd && flag_t[b]) continue;
-        const int j = pt.voxel(it);
-        const int3 p = voxel_of<S>(V, b, j);
-        if (p.x >= V.nx || p.y >= V.ny || p.z >= V.nz) continue;
-        const size_t idx = ((size_t)p.z * V.py + p.y) * V.px + p.x;
-        const float c = in[idx];
-        if (!upd || !((act[(size_t)b * S::WORDS + (j >> 6)] >> (j & 63)) & 1ull)) {
-            out[idx] = c;
-            if (upd) log[(size_t)bi * S::VOX + j] = c;
-            continue;
-        }
-        log[(size_t)bi * S::VOX + j] = c;
-        auto P = [&](int dx, int dy, int dz) {
-            return in[((size_t)clampi(p.z + dz, V.nz) * V.py + clampi(p.y + dy, V.ny)) * V.px +
-                      clampi(p.x + dx, V.nx)];
-        };
-        out[idx] = ns_update_f32(P, V.img[idx], V.bias ? V.bias[idx] : 0.0f, V);
+__device__ __forceinline__ void rec_item(const AdjPlan& a, int s, int t, const float* in, float* out, uint32_t n,
+                                         uint32_t i, const Parts<S>& pt) {
+    const NsVol& V = a.V;
+    const uint32_t bi = i / Parts<S>::N;
+    const bool upd = bi < n;
+    const uint32_t b = upd ? plan_list(a, t)[bi] : plan_list(a, t - 1)[bi - n];
+    if (!upd && plan_flag(a, t)[b]) return;
+    const int j = pt.voxel(i);
+    const int3 p = voxel_of<S>(V, b, j);
+    if (p.x >= V.nx || p.y >= V.ny || p.z >= V.nz) return;
+    const size_t idx = ((size_t)p.z * V.py + p.y) * V.px + p.x;
+    const float c = in[idx];
+    if (!upd) {
+        out[idx] = c;
+        return;
     }
+    plan_log(a, s, t)[(size_t)bi * S::VOX + j] = c;
+    if (!((plan_act(a, t)[(size_t)b * S::WORDS + (j >> 6)] >> (j & 63)) & 1ull)) {
+        out[idx] = c;
+        return;
+    }
+    auto P = [&](int dx, int dy, int dz) {
+        return in[((size_t)clampi(p.z + dz, V.nz) * V.py + clampi(p.y + dy, V.ny)) * V.px + clampi(p.x + dx, V.nx)];
+    };
+    out[idx] = ns_update_f32(P, V.img[idx], V.bias ? V.bias[idx] : 0.0f, V);
 }
 
 // The whole padded field src -> dst (grid-stride, float4).
@@ -505,27 +498,6 @@ __device__ __forceinline__ void adj_mark_brick(const NsVol& V, uint32_t b, const
     }
 }
 
-// What reverse iteration k needs first, loaded before the barrier that
-// precedes it (the recorded lists and masks do not change in the reverse):
-// count_k, the brick of the thread's first item of list_k and that brick's
-// mask word of the thread's voxel.
-struct RevPre {
-    uint32_t n, b;
-    unsigned long long w;
-};
-template <class S>
-__device__ __forceinline__ RevPre rev_prefetch(const AdjPlan& a, int k) {
-    RevPre r{0u, 0u, 0ull};
-    if (k < 0) return r;
-    const Parts<S> pt(0);
-    r.n = a.counts[k];
-    if (pt.slot < r.n * Parts<S>::N) {
-        r.b = plan_list(a, k)[pt.slot / Parts<S>::N];
-        r.w = plan_act(a, k)[(size_t)r.b * S::WORDS + (pt.voxel(pt.slot) >> 6)];
-    }
-    return r;
-}
-
 // Reverse iteration k.  With p = (k + 1) & 1, lambda_{k+1} = lam + Z[p] on
 // entry, where Z[p] (the previous reverse iteration's scatter) is zero
 // outside the bricks marked in flagT[k & 1], and Z[1-p] is zero everywhere.
@@ -572,24 +544,89 @@ __device__ __forceinline__ void rev_voxel(const AdjPlan& a, const float* phi, fl
     if (a.dbias) a.dbias[idx] += g4[3];
 }
 
+// One phase of the reverse: reverse iteration k of segment s (k < 0:
+// none), with the restore of phi_kr beside it (kr < 0: none) and step r of
+// the recomputation of segment rs (r < 0: none; r = 0 seeds the pair's
+// second field with the checkpoint, r >= 1 runs iteration t = rs * every +
+// r - 1).  Its work items (brick parts: reverse iteration, then the
+// recomputed iteration, then the restore) share one item space, so the
+// kinds run side by side on different SMs.  Everything here is read from
+// the recorded lists before the barrier that precedes the phase.
+struct RevPhase {
+    int k, s, kr, rs, r, t;
+    const float* phi;   // phi_k
+    float* rdst;        // the field restored to phi_kr
+    const float* rin;   // the recomputation's fields
+    float* rout;
+    uint32_t nA, nC, nR;  // items of each kind
+    uint32_t cnt_t, cnt_kr;
+    uint32_t b0;          // brick of this thread's first item (reverse iteration)
+    unsigned long long w0;  // and its mask word of the thread's voxel
+};
+
 template <class S>
-__device__ void adj_rev_bricks(const AdjPlan& a, int k, const float* phi, double* s3, const RevPre& pre) {
-    const int p = (k + 1) & 1;
-    const Parts<S> pt(0);
-    float* const zin = a.Z[p];
-    float* const zout = a.Z[p ^ 1];
-    const unsigned long long* act = plan_act(a, k);
-    const uint32_t* list = plan_list(a, k);
-    for (uint32_t it = pt.slot; it < pre.n * Parts<S>::N; it += pt.nslots) {
-        const bool first = it == pt.slot;
-        const uint32_t b = first ? pre.b : list[it / Parts<S>::N];
-        const int j = pt.voxel(it);
-        const unsigned long long wj = first ? pre.w : act[(size_t)b * S::WORDS + (j >> 6)];
-        rev_voxel<S>(a, phi, zin, zout, b, j, (wj >> (j & 63)) & 1ull, s3);
-        if (it % Parts<S>::N == 0 && k > 0)
-            adj_mark_brick<S>(a.V, b, act, pt.t, Parts<S>::TPG, a.flagT[(k - 1) & 1]);
-    }
+__device__ __forceinline__ int rev_phases(const AdjPlan& a, int s) {
+    const int len = min(a.K, (s + 1) * a.every) - s * a.every;
+    return max(len, (s > 0 && a.every > 1) ? a.every : 0);
 }
+
+template <class S>
+__device__ RevPhase rev_phase(const AdjPlan& a, int s, int j) {
+    constexpr uint32_t N = Parts<S>::N;
+    RevPhase ph;
+    ph.k = ph.kr = ph.rs = ph.r = ph.t = -1;
+    ph.s = s;
+    ph.phi = nullptr;
+    ph.rdst = ph.rout = nullptr;
+    ph.rin = nullptr;
+    ph.nA = ph.nC = ph.nR = ph.cnt_t = ph.cnt_kr = ph.b0 = 0u;
+    ph.w0 = 0ull;
+    const int s0 = s * a.every, s1 = min(a.K, s0 + a.every);
+    const SegPair pr = seg_pair(a, s);
+    // The highest state the pair holds (with the one below it): phi_K for
+    // the last segment, phi_{s1 - 1} after a recomputation.
+    const int top = s == a.nck - 1 ? a.K : s1 - 1;
+    if (j < s1 - s0) {
+        const int k = s1 - 1 - j;
+        ph.k = k;
+        ph.phi = pr.f[(k - pr.base) & 1];
+        ph.nA = a.counts[k] * N;
+        const Parts<S> pt(0);
+        if (pt.slot < ph.nA) {
+            ph.b0 = plan_list(a, k)[pt.slot / N];
+            ph.w0 = plan_act(a, k)[(size_t)ph.b0 * S::WORDS + (pt.voxel(pt.slot) >> 6)];
+        }
+        // The pair's other field steps down to phi_{k-1} unless it holds it.
+        if (k - 1 >= s0 && k - 1 < top - 1) {
+            ph.kr = k - 1;
+            ph.rdst = pr.f[(k - 1 - pr.base) & 1];
+            ph.cnt_kr = a.counts[k - 1];
+            ph.nR = (ph.cnt_kr + a.counts[k]) * N;
+        }
+    }
+    // Segment s - 1 (full length) is recomputed beside this one, one step a
+    // phase: its checkpoint copied into the pair's second field, then its
+    // iterations s0' .. s0' + every - 2, logged.
+    if (s > 0 && a.every > 1 && j < a.every) {
+        const SegPair rp = seg_pair(a, s - 1);
+        ph.rs = s - 1;
+        ph.r = j;
+        if (j == 0) {
+            ph.rin = rp.f[0];
+            ph.rout = rp.f[1];
+        } else {
+            ph.t = rp.base + j - 1;
+            ph.rin = rp.f[(j - 1) & 1];
+            ph.rout = rp.f[j & 1];
+            ph.cnt_t = a.counts[ph.t];
+            ph.nC = (ph.cnt_t + (j >= 2 ? a.counts[ph.t - 1] : 0u)) * N;
+        }
+    }
+    return ph;
+}
+
+template <class S>
+__device__ void adj_rev_phase(const AdjPlan& a, const RevPhase& ph, double* s3);
 
 // Part two of reverse iteration k: the bricks marked in flagT[k & 1] that
 // are not in A_k hold no active voxel, so lambda_{k+1} passes through:
@@ -644,6 +681,31 @@ __device__ void adj_rev_touched(const AdjPlan& a, int k) {
                     z4[g4[u]] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                 }
             }
+        }
+    }
+}
+
+template <class S>
+__device__ void adj_rev_phase(const AdjPlan& a, const RevPhase& ph, double* s3) {
+    if (ph.k >= 0) adj_rev_touched<S>(a, ph.k);
+    if (ph.r == 0) adj_copy_field(ph.rin, ph.rout, a.P);
+    const Parts<S> pt(0);
+    const uint32_t nAC = ph.nA + ph.nC, total = nAC + ph.nR;
+    for (uint32_t it = pt.slot; it < total; it += pt.nslots) {
+        if (it < ph.nA) {
+            const int k = ph.k, p = (k + 1) & 1;
+            const bool first = it == pt.slot;
+            const unsigned long long* act = plan_act(a, k);
+            const uint32_t b = first ? ph.b0 : plan_list(a, k)[it / Parts<S>::N];
+            const int jv = pt.voxel(it);
+            const unsigned long long wj = first ? ph.w0 : act[(size_t)b * S::WORDS + (jv >> 6)];
+            rev_voxel<S>(a, ph.phi, a.Z[p], a.Z[p ^ 1], b, jv, (wj >> (jv & 63)) & 1ull, s3);
+            if (it % Parts<S>::N == 0 && k > 0)
+                adj_mark_brick<S>(a.V, b, act, pt.t, Parts<S>::TPG, a.flagT[(k - 1) & 1]);
+        } else if (it < nAC) {
+            rec_item<S>(a, ph.rs, ph.t, ph.rin, ph.rout, ph.cnt_t, it - ph.nA, pt);
+        } else {
+            restore_item<S>(a, ph.s, ph.kr, ph.rdst, ph.cnt_kr, it - nAC, pt);
         }
     }
 }
@@ -773,44 +835,21 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_reverse(const AdjPlan a) {
             }
         }
     }
-    RevPre pre = rev_prefetch<S>(a, a.K - 1);
+    // Segments from the last; each phase's descriptor is read before the
+    // barrier that precedes it.
+    int s = a.nck - 1, j = 0;
+    RevPhase ph = rev_phase<S>(a, s, j);
     grid.sync();
     double s3[3] = {0.0, 0.0, 0.0};
-    for (int s = a.nck - 1; s >= 0; --s) {
-        const int s0 = s * a.every, s1 = min(a.K, s0 + a.every), len = s1 - s0;
-        const SegPair pr = seg_pair(a, s);
-        // The highest state the pair holds (with the one below it): phi_K for
-        // the last segment, phi_{s1 - 1} after a recomputation.
-        const int top = s == a.nck - 1 ? a.K : s1 - 1;
-        // Segment s - 1 (full length) is recomputed beside this one, one step
-        // a phase: its checkpoint copied into the pair's second field, then
-        // its iterations s0' .. s0' + every - 2, logged.
-        const int recn = (s > 0 && a.every > 1) ? a.every : 0;
-        const SegPair rp = s > 0 ? seg_pair(a, s - 1) : pr;
-        const int J = max(len, recn);
-        for (int j = 0; j < J; ++j) {
-            const int k = s1 - 1 - j;
-            if (j < len) {
-                // Reverse iteration k on phi_k; beside it the pair's other
-                // field steps down to phi_{k-1} (unless it holds it already).
-                adj_rev_bricks<S>(a, k, pr.f[(k - pr.base) & 1], s3, pre);
-                adj_rev_touched<S>(a, k);
-                if (k - 1 >= s0 && k - 1 < top - 1) adj_restore<S>(a, s, k - 1, pr.f[(k - 1 - pr.base) & 1]);
-            }
-            const int r = j;
-            if (r < recn) {
-                if (r == 0) {
-                    adj_copy_field(rp.f[0], rp.f[1], a.P);
-                } else {
-                    const int t = rp.base + r - 1;
-                    adj_recompute<S>(V, rp.f[(r - 1) & 1], rp.f[r & 1], plan_act(a, t), plan_list(a, t), a.counts[t],
-                                     r >= 2 ? plan_list(a, t - 1) : nullptr, r >= 2 ? a.counts[t - 1] : 0u,
-                                     plan_flag(a, t), plan_log(a, s - 1, t));
-                }
-            }
-            if (j < len) pre = rev_prefetch<S>(a, k - 1);
-            grid.sync();
+    for (;;) {
+        adj_rev_phase<S>(a, ph, s3);
+        if (++j == rev_phases<S>(a, s)) {
+            --s;
+            j = 0;
         }
+        if (s < 0) break;  // the sums below are the block's own
+        ph = rev_phase<S>(a, s, j);
+        grid.sync();
     }
     block_sum3<true>(s3[0], s3[1], s3[2], a.gpart + 3 * (size_t)blockIdx.x);
 }
