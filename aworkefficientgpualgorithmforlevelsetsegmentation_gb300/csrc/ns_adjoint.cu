@@ -90,7 +90,7 @@ __device__ __forceinline__ int3 voxel_of(const NsVol& V, uint32_t b, int j) {
 // recompute buffers, the forward's pair) are fstride floats apart.
 struct AdjPlan {
     NsVol V;                    // the one volume (brick_base 0)
-    float* ck0;                 // checkpoint s < nck - 1 = ck0 + s * fstride (phi_{s * every})
+    float* ck0;                 // checkpoint s < nck - 1 = ck0 + s * fstride (phi_{s * every}, sparse)
     float* qb[2];               // second field of a recomputed segment's pair (by parity)
     float* fw[2];               // the forward's ping-pong pair
     float* log0;                // brick logs: set (s & 1), slot t - s * every, lgstride floats each
@@ -103,6 +103,9 @@ struct AdjPlan {
     uint32_t* flag0;            // [K+1][NB]
     uint32_t* counts;           // [K+1]
     uint32_t* flagT[2];         // [NB]: bricks reverse iteration k scatters into, in flagT[(k - 1) & 1]
+    uint32_t* need;             // [NB]: s + 1 once segment s's checkpoint holds the brick
+    uint32_t* nlist0;           // [nck - 1][NB]: the bricks of checkpoint s
+    uint32_t* ncount;           // [nck]
     double* gsum;               // [8]: soft-Dice sums in 4..6
     double* gpart;              // [grid][3]: each block's dT, deps, dalpha
     unsigned long long* nact;   // active-voxel updates of the forward
@@ -115,6 +118,7 @@ struct AdjPlan {
 __device__ __forceinline__ unsigned long long* plan_act(const AdjPlan& a, int k) { return a.act0 + (uint64_t)k * a.astride; }
 __device__ __forceinline__ uint32_t* plan_list(const AdjPlan& a, int k) { return a.list0 + (uint64_t)k * a.lstride; }
 __device__ __forceinline__ uint32_t* plan_flag(const AdjPlan& a, int k) { return a.flag0 + (uint64_t)k * a.lstride; }
+__device__ __forceinline__ uint32_t* plan_need(const AdjPlan& a, int s) { return a.nlist0 + (uint64_t)s * a.lstride; }
 // The log of iteration t of segment s: the bricks of list_t before the
 // update, brick i of the list at i * VOX.
 __device__ __forceinline__ float* plan_log(const AdjPlan& a, int s, int t) {
@@ -187,36 +191,61 @@ __device__ __forceinline__ void adj_dilate_brick(const NsVol& V, uint32_t b, con
     }
 }
 
-// Iteration k, block per brick.  The bricks of list_k are written whole into
-// out (active voxels updated from in, the others copied); with `prev` (the
-// recorded forward's ping-pong pair), the bricks of list_{k-1} not in
-// list_k (flag_k clear) are copied from in to out, so that out equals in
-// outside the bricks of A_k.  With nxt (the recorded forward, not a
-// recomputation): each updated brick's changed voxels are dilated into A_{k+1}
-// by the same block.  With log: brick i of list_k is logged as it was before
-// the update (in) at log + i * VOX.  Returns the active voxels this thread
-// updated.
+// Forward iteration k, block per brick.  The bricks of list_k are written
+// whole into out (active voxels updated from in, the others copied), and
+// the bricks of list_{k-1} not in list_k (flag_k clear) are copied from in
+// to out, so that out equals in outside the bricks of A_k (both fields of
+// the pair stay current).  Each updated brick's changed voxels are dilated
+// into A_{k+1} by the same block.  With log (the last segment): brick i of
+// list_k is logged as it was before the update (in) at log + i * VOX.  With
+// cap = s + 1 (segment s has a checkpoint): the 27 bricks around each brick
+// of list_k (the update's reads and writes, a superset) join the segment's
+// checkpoint the first time the segment reaches them, copied from in: a
+// brick no earlier iteration of the segment reached still holds phi at the
+// segment's start.  The checkpoint is that sparse field ck, and the bricks
+// it holds are listed for the reverse.  Returns the active voxels this
+// thread updated.
 template <class S>
-__device__ uint32_t adj_update(const NsVol& V, const float* in, float* out, const unsigned long long* act,
-                               const uint32_t* list, const uint32_t* count, const uint32_t* prev,
-                               const uint32_t* prev_count, const uint32_t* flag_k, unsigned long long* nxt,
-                               uint32_t* flag_next, uint32_t* list_next, uint32_t* count_next, float* log) {
+__device__ uint32_t adj_forward_step(const AdjPlan& a, int k, const float* in, float* out, float* log, uint32_t cap,
+                                     float* ck) {
+    const NsVol& V = a.V;
     __shared__ uint32_t chg[S::CHG];
-    __shared__ uint32_t any;
-    const uint32_t n = *count, np = prev ? *prev_count : 0u;
+    __shared__ uint32_t any, ncap;
+    __shared__ uint32_t capl[27];
+    constexpr int G = S::VOX / 4;
+    const unsigned long long* act = plan_act(a, k);
+    const uint32_t* list = plan_list(a, k);
+    const uint32_t* prev = k ? plan_list(a, k - 1) : nullptr;
+    const uint32_t* flag_k = plan_flag(a, k);
+    const uint32_t n = a.counts[k], np = k ? a.counts[k - 1] : 0u;
     uint32_t mine = 0;
     for (uint32_t i = blockIdx.x; i < n + np; i += gridDim.x) {
         const bool upd = i < n;
         const uint32_t b = upd ? list[i] : prev[i - n];
-        if (!upd && flag_k[b]) continue;  // also in list_k: written above (uniform over the block)
-        const bool dil = nxt && upd;      // uniform over the block
-        if (dil) {
-            __syncthreads();  // chg and any free: the previous brick's dilation is done
-            if (threadIdx.x == 0) any = 0u;
+        if (!upd && flag_k[b]) continue;  // also in list_k: written whole (uniform over the block)
+        const int3 o = brick_origin<S>(V, b + V.brick_base);
+        if (upd) {
+            __syncthreads();  // chg, any, ncap and capl free: the previous brick is done
+            if (threadIdx.x == 0) {
+                any = 0u;
+                ncap = 0u;
+            }
             __syncthreads();
         }
+        // Thread r < 27 checks neighbour r for the checkpoint before the
+        // update (the check's latency hides behind it) and claims it after.
+        uint32_t nbr = 0u;
+        bool fresh = false;
+        if (upd && cap && threadIdx.x < 27) {
+            const int ox = (int)threadIdx.x % 3 - 1, oy = ((int)threadIdx.x / 3) % 3 - 1, oz = (int)threadIdx.x / 9 - 1;
+            const int bx = o.x / S::X + ox, by = o.y / S::Y + oy, bz = o.z / S::Z + oz;
+            if (bx >= 0 && by >= 0 && bz >= 0 && bx < V.nbx && by < V.nby && bz < V.nbz) {
+                nbr = b + (uint32_t)((oz * V.nby + oy) * V.nbx + ox);
+                fresh = *(volatile uint32_t*)&a.need[nbr] != cap;
+            }
+        }
         for (int j = threadIdx.x; j < S::VOX; j += blockDim.x) {
-            const int3 p = voxel_of<S>(V, b, j);
+            const int3 p = make_int3(o.x + j % S::X, o.y + (j / S::X) % S::Y, o.z + j / (S::X * S::Y));
             bool changed = false;
             if (p.x < V.nx && p.y < V.ny && p.z < V.nz) {
                 const size_t idx = ((size_t)p.z * V.py + p.y) * V.px + p.x;
@@ -236,7 +265,7 @@ __device__ uint32_t adj_update(const NsVol& V, const float* in, float* out, cons
                 }
             }
             // VOX is a multiple of 32: a warp's slots are all in or all out.
-            if (dil) {
+            if (upd) {
                 const uint32_t bal = __ballot_sync(0xffffffffu, changed);
                 if ((threadIdx.x & 31) == 0) {
                     chg[j >> 5] = bal;
@@ -244,13 +273,32 @@ __device__ uint32_t adj_update(const NsVol& V, const float* in, float* out, cons
                 }
             }
         }
-        if (dil) {
+        if (upd) {
             __syncthreads();  // chg and any complete
             if (any)
-                adj_dilate_brick<S>(V, b, chg, threadIdx.x, blockDim.x, V.nbh, nxt, flag_next, list_next, count_next);
+                adj_dilate_brick<S>(V, b, chg, threadIdx.x, blockDim.x, V.nbh, plan_act(a, k + 1), plan_flag(a, k + 1),
+                                    plan_list(a, k + 1), &a.counts[k + 1]);
+            if (cap) {
+                if (fresh && atomicExch(&a.need[nbr], cap) != cap) {
+                    capl[atomicAdd(&ncap, 1u)] = nbr;
+                    plan_need(a, (int)cap - 1)[atomicAdd(&a.ncount[cap - 1], 1u)] = nbr;
+                }
+                __syncthreads();  // capl complete
+                const uint32_t nc = ncap;
+                const float4* in4 = reinterpret_cast<const float4*>(in);
+                float4* ck4 = reinterpret_cast<float4*>(ck);
+                for (uint32_t q = threadIdx.x; q < nc * G; q += blockDim.x) {
+                    const uint32_t cb = capl[q / G];
+                    const int jj = (int)(q % G) * 4;
+                    const int3 c = brick_origin<S>(V, cb + V.brick_base);
+                    const size_t idx = ((size_t)(c.z + jj / (S::X * S::Y)) * V.py + c.y + (jj / S::X) % S::Y) * V.px +
+                                       c.x + jj % S::X;
+                    ck4[idx / 4] = in4[idx / 4];
+                }
+            }
         }
     }
-    __syncthreads();  // chg and any are reused by the next call
+    __syncthreads();  // the shared words are reused by the next call
     return mine;
 }
 
@@ -332,13 +380,18 @@ __device__ __forceinline__ void rec_item(const AdjPlan& a, int s, int t, const f
     out[idx] = ns_update_f32(P, V.img[idx], V.bias ? V.bias[idx] : 0.0f, V);
 }
 
-// The whole padded field src -> dst (grid-stride, float4).
-__device__ void adj_copy_field(const float* src, float* dst, uint64_t P) {
-    const uint64_t n4 = P / 4;  // P is a multiple of 8 (padded dims)
-    const float4* s4 = reinterpret_cast<const float4*>(src);
-    float4* d4 = reinterpret_cast<float4*>(dst);
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n4; i += (uint64_t)gridDim.x * blockDim.x)
-        d4[i] = s4[i];
+// One item of the seeding of a recomputed segment's pair: brick i / N of
+// segment s's checkpoint list copied from the checkpoint ck to its second
+// field q (the recomputation reads and writes no other brick).
+template <class S>
+__device__ __forceinline__ void seed_item(const AdjPlan& a, int s, const float* ck, float* q, uint32_t i,
+                                          const Parts<S>& pt) {
+    const NsVol& V = a.V;
+    const int3 p = voxel_of<S>(V, plan_need(a, s)[i / Parts<S>::N], pt.voxel(i));
+    if (p.x < V.nx && p.y < V.ny && p.z < V.nz) {
+        const size_t idx = ((size_t)p.z * V.py + p.y) * V.px + p.x;
+        q[idx] = ck[idx];
+    }
 }
 
 // Vector-Jacobian product of ns_update_f32 at one voxel with upstream lam:
@@ -605,8 +658,8 @@ __device__ RevPhase rev_phase(const AdjPlan& a, int s, int j) {
         }
     }
     // Segment s - 1 (full length) is recomputed beside this one, one step a
-    // phase: its checkpoint copied into the pair's second field, then its
-    // iterations s0' .. s0' + every - 2, logged.
+    // phase: its checkpoint's bricks copied into the pair's second field,
+    // then its iterations s0' .. s0' + every - 2, logged.
     if (s > 0 && a.every > 1 && j < a.every) {
         const SegPair rp = seg_pair(a, s - 1);
         ph.rs = s - 1;
@@ -614,6 +667,7 @@ __device__ RevPhase rev_phase(const AdjPlan& a, int s, int j) {
         if (j == 0) {
             ph.rin = rp.f[0];
             ph.rout = rp.f[1];
+            ph.nC = a.ncount[s - 1] * N;
         } else {
             ph.t = rp.base + j - 1;
             ph.rin = rp.f[(j - 1) & 1];
@@ -688,7 +742,6 @@ __device__ void adj_rev_touched(const AdjPlan& a, int k) {
 template <class S>
 __device__ void adj_rev_phase(const AdjPlan& a, const RevPhase& ph, double* s3) {
     if (ph.k >= 0) adj_rev_touched<S>(a, ph.k);
-    if (ph.r == 0) adj_copy_field(ph.rin, ph.rout, a.P);
     const Parts<S> pt(0);
     const uint32_t nAC = ph.nA + ph.nC, total = nAC + ph.nR;
     for (uint32_t it = pt.slot; it < total; it += pt.nslots) {
@@ -703,7 +756,11 @@ __device__ void adj_rev_phase(const AdjPlan& a, const RevPhase& ph, double* s3) 
             if (it % Parts<S>::N == 0 && k > 0)
                 adj_mark_brick<S>(a.V, b, act, pt.t, Parts<S>::TPG, a.flagT[(k - 1) & 1]);
         } else if (it < nAC) {
-            rec_item<S>(a, ph.rs, ph.t, ph.rin, ph.rout, ph.cnt_t, it - ph.nA, pt);
+            if (ph.r == 0) {
+                seed_item<S>(a, ph.rs, ph.rin, ph.rout, it - ph.nA, pt);
+            } else {
+                rec_item<S>(a, ph.rs, ph.t, ph.rin, ph.rout, ph.cnt_t, it - ph.nA, pt);
+            }
         } else {
             restore_item<S>(a, ph.s, ph.kr, ph.rdst, ph.cnt_kr, it - nAC, pt);
         }
@@ -723,15 +780,11 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_forward(const AdjPlan a) {
     for (int k = 0; k < a.K; ++k) {
         const float* src = a.fw[k & 1];
         float* dst = a.fw[(k + 1) & 1];
-        mine += adj_update<S>(V, src, dst, plan_act(a, k), plan_list(a, k), &a.counts[k],
-                              k ? plan_list(a, k - 1) : nullptr, k ? &a.counts[k - 1] : nullptr, plan_flag(a, k),
-                              plan_act(a, k + 1), plan_flag(a, k + 1), plan_list(a, k + 1), &a.counts[k + 1],
-                              k >= last * a.every ? plan_log(a, last, k) : nullptr);
+        const int s = k / a.every;
+        mine += adj_forward_step<S>(a, k, src, dst, s == last ? plan_log(a, last, k) : nullptr,
+                                    s < last ? (uint32_t)s + 1u : 0u,
+                                    s < last ? a.ck0 + (uint64_t)s * a.fstride : nullptr);
         grid.sync();
-        // The next iteration reads dst and writes the other buffer: the copy
-        // needs no barrier of its own (the reverse pass is another launch).
-        const int m = (k + 1) / a.every;
-        if ((k + 1) % a.every == 0 && m < last) adj_copy_field(dst, a.ck0 + (uint64_t)m * a.fstride, a.P);
     }
     __shared__ uint32_t s_cnt;
     if (threadIdx.x == 0) s_cnt = 0u;
@@ -889,7 +942,7 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     const uint64_t logb = al((uint64_t)nb * S::VOX * 4);
     const uint64_t total = nfields * al(P * 4) + (uint64_t)nsets * every * logb + (uint64_t)(K + 1) * al(mwords * 8) +
                            2 * (uint64_t)(K + 1) * al((uint64_t)nb * 4) + al((uint64_t)(K + 1) * 4) + al(P) +
-                           2 * al((uint64_t)nb * 4) +
+                           2 * al((uint64_t)nb * 4) + (uint64_t)(nck + 1) * al((uint64_t)nb * 4) + al((uint64_t)nck * 4) +
                            al(8 * sizeof(double) + 8) + al((uint64_t)gr * 3 * sizeof(double));
     char* base = (char*)core.workspace(total);
     char* const end = base + total;
@@ -924,6 +977,10 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     for (int k = 1; k <= K; ++k) carve((uint64_t)nb * 4);
     a.counts = (uint32_t*)carve((uint64_t)(K + 1) * 4);
     for (int q = 0; q < 2; ++q) a.flagT[q] = (uint32_t*)carve((uint64_t)nb * 4);
+    a.need = (uint32_t*)carve((uint64_t)nb * 4);
+    a.nlist0 = (uint32_t*)carve((uint64_t)nb * 4);  // lstride apart, like the brick lists
+    for (int q = 1; q < nck - 1; ++q) carve((uint64_t)nb * 4);
+    a.ncount = (uint32_t*)carve((uint64_t)nck * 4);
     uint8_t* tgt = (uint8_t*)carve(P);
     a.gsum = (double*)carve(8 * sizeof(double) + 8);
     a.nact = (unsigned long long*)(a.gsum + 8);
@@ -970,11 +1027,12 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
         LSS_CUDA(cudaMemsetAsync(a.Z[q], 0, P * 4, st));
         LSS_CUDA(cudaMemsetAsync(a.flagT[q], 0, (uint64_t)nb * 4, st));
     }
+    LSS_CUDA(cudaMemsetAsync(a.need, 0, (uint64_t)nb * 4, st));
+    LSS_CUDA(cudaMemsetAsync(a.ncount, 0, (uint64_t)nck * 4, st));
     // Forward from the engine's current phi and active set: both buffers of
-    // the pair and the first checkpoint (with more than one segment) hold phi_0.
+    // the pair hold phi_0 (the checkpoints fill as the forward reaches bricks).
     const float* phi0 = V.phi[core.parity()];
-    for (float* d : {a.ck0, a.fw[0], a.fw[1]})
-        if (d) LSS_CUDA(cudaMemcpyAsync(d, phi0, P * 4, cudaMemcpyDeviceToDevice, st));
+    for (float* d : {a.fw[0], a.fw[1]}) LSS_CUDA(cudaMemcpyAsync(d, phi0, P * 4, cudaMemcpyDeviceToDevice, st));
     LSS_CUDA(cudaMemcpyAsync(a.act0, core.masks(core.parity()), mwords * 8, cudaMemcpyDeviceToDevice, st));
     void* params[] = {(void*)&a};
     LSS_CUDA(cudaLaunchCooperativeKernel(kf, dim3(gf), dim3(kAdjThreads), params, 0, st));
