@@ -490,12 +490,10 @@ __device__ __forceinline__ void ns_update_vjp_f32(PF P, AF add, float I, float b
     g4[2] += lam * (V.alpha_data ? du_dalpha : -du_dalpha);
 }
 
-// Block sum of three doubles into gsum[0..2]: one atomic each per block (none
-// for a zero sum, which changes nothing), or, with Slot, added into the
-// block's own three words (gsum = its slot; no other block writes them, so
-// no atomics, and launches of the same grid accumulate in a fixed order).
-template <bool Slot = false>
-__device__ __forceinline__ void block_sum3(double a0, double a1, double a2, double* gsum) {
+// Block sum of three doubles added into the block's own three words (slot;
+// no other block writes them, so no atomics, and the host adds the blocks'
+// slots in a fixed order).
+__device__ __forceinline__ void block_sum3(double a0, double a1, double a2, double* slot) {
     __shared__ double s[3][32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
@@ -516,14 +514,10 @@ __device__ __forceinline__ void block_sum3(double a0, double a1, double a2, doub
             a1 += __shfl_down_sync(0xffffffffu, a1, o);
             a2 += __shfl_down_sync(0xffffffffu, a2, o);
         }
-        if (lane == 0 && Slot) {
-            gsum[0] += a0;
-            gsum[1] += a1;
-            gsum[2] += a2;
-        } else if (lane == 0) {
-            if (a0 != 0.0) atomicAdd(&gsum[0], a0);
-            if (a1 != 0.0) atomicAdd(&gsum[1], a1);
-            if (a2 != 0.0) atomicAdd(&gsum[2], a2);
+        if (lane == 0) {
+            slot[0] += a0;
+            slot[1] += a1;
+            slot[2] += a2;
         }
     }
     __syncthreads();
@@ -795,104 +789,137 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_forward(const AdjPlan a) {
     if (threadIdx.x == 0 && s_cnt) atomicAdd(a.nact, (unsigned long long)s_cnt);
 }
 
-// The padded field in groups of four voxels of one row (px is a multiple of
-// 4): group g covers x = 4 (g mod px/4) .. + 3 of row g div px/4, row
-// (y, z) = (row mod py, row div py).  Returns the first x, or -1 for a group
-// outside the volume (a padding row or padding columns).
-__device__ __forceinline__ int group_x(const NsVol& V, uint64_t g) {
-    const uint64_t q = (uint64_t)V.px / 4, r = g / q;
-    const int x0 = (int)(g - r * q) * 4;
-    const uint64_t y = r % (uint64_t)V.py, z = r / (uint64_t)V.py;
-    return (y < (uint64_t)V.ny && z < (uint64_t)V.nz && x0 < V.nx) ? x0 : -1;
-}
+// The soft-Dice passes, two streaming kernels between the forward and the
+// reverse: the volume's rows in groups of four voxels (px is a multiple of
+// 8, so a group stays in its row and is 16-byte aligned): item i is group
+// i mod Q of row i div Q (Q = ceil(nx / 4)), row r = (y, z) = (r mod ny,
+// r div ny); the padding rows are never visited.
+constexpr int kDiceThreads = 256;
 
-// The soft-Dice terms of one voxel: s = sigmoid(-phi / tau), t = target.
+struct DiceArgs {
+    const float* phi;  // phi_K
+    const uint8_t* tgt;
+    float* lam;
+    double* part;      // [nparts][3]: the dice blocks' sums
+    double* gsum;      // [8]: the total in 4..6
+    int nx, ny, nz, px, py;
+    uint32_t nparts;
+    float tau;
+};
+
 __device__ __forceinline__ float soft_mask(float phi, float tau) { return 1.0f / (1.0f + expf(phi / tau)); }
 
-// The reverse: the loss and lambda_K, then the segments from the last.
+// Group i: its first x, and its index among the padded field's groups.
+__device__ __forceinline__ uint32_t dice_group(const DiceArgs& d, uint32_t q4, uint32_t i, uint64_t* g) {
+    const uint32_t r = i / q4, x0 = (i - r * q4) * 4;
+    const uint32_t z = r / (uint32_t)d.ny, y = r - z * (uint32_t)d.ny;
+    *g = (((uint64_t)z * d.py + y) * d.px + x0) / 4;
+    return x0;
+}
+
+// Sums s = sigmoid(-phi_K / tau), t = target and s t over the volume: per
+// voxel in fp32, per thread in fp32, per block in FP64 into part[3 * block].
+__global__ void __launch_bounds__(kDiceThreads) k_adj_dice(const DiceArgs d) {
+    const uint32_t q4 = (uint32_t)(d.nx + 3) / 4, n = (uint32_t)d.ny * (uint32_t)d.nz * q4;
+    float ss = 0.0f, tt = 0.0f, st = 0.0f;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint64_t g;
+        const uint32_t x0 = dice_group(d, q4, i, &g);
+        const float4 f = reinterpret_cast<const float4*>(d.phi)[g];
+        const uchar4 m = reinterpret_cast<const uchar4*>(d.tgt)[g];
+        const float fv[4] = {f.x, f.y, f.z, f.w};
+        const unsigned char mv[4] = {m.x, m.y, m.z, m.w};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            if (x0 + e >= (uint32_t)d.nx) break;
+            const float s = soft_mask(fv[e], d.tau);
+            const float tv = mv[e] ? 1.0f : 0.0f;
+            ss += s;
+            tt += tv;
+            st += s * tv;
+        }
+    }
+    __shared__ double w3[3][kDiceThreads / 32];
+    double a0 = ss, a1 = tt, a2 = st;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        a0 += __shfl_down_sync(0xffffffffu, a0, o);
+        a1 += __shfl_down_sync(0xffffffffu, a1, o);
+        a2 += __shfl_down_sync(0xffffffffu, a2, o);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        w3[0][warp] = a0;
+        w3[1][warp] = a1;
+        w3[2][warp] = a2;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double t = 0.0;
+        for (int q = 0; q < kDiceThreads / 32; ++q) t += w3[threadIdx.x][q];
+        d.part[3 * (size_t)blockIdx.x + threadIdx.x] = t;
+    }
+}
+
+// lambda_K = dloss/dphi_K over the volume.  Every block adds the dice
+// blocks' sums in the same order (the same totals in every block and every
+// call); block 0 publishes them for the loss.
+__global__ void __launch_bounds__(kDiceThreads) k_adj_lamk(const DiceArgs d) {
+    __shared__ double tot[3];
+    if (threadIdx.x < 32) {
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+        for (uint32_t b = threadIdx.x; b < d.nparts; b += 32) {
+            a0 += d.part[3 * (size_t)b];
+            a1 += d.part[3 * (size_t)b + 1];
+            a2 += d.part[3 * (size_t)b + 2];
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            a0 += __shfl_down_sync(0xffffffffu, a0, o);
+            a1 += __shfl_down_sync(0xffffffffu, a1, o);
+            a2 += __shfl_down_sync(0xffffffffu, a2, o);
+        }
+        if (threadIdx.x == 0) {
+            tot[0] = a0;
+            tot[1] = a1;
+            tot[2] = a2;
+            if (blockIdx.x == 0) {
+                d.gsum[4] = a0;
+                d.gsum[5] = a1;
+                d.gsum[6] = a2;
+            }
+        }
+    }
+    __syncthreads();
+    // dloss/ds = (2 st - 2 t den) / den^2 with den = sum s + sum t.
+    const double den = tot[0] + tot[1], sst = tot[2];
+    const float c_out = (float)(2.0 * sst / (den * den)), c_in = (float)(2.0 * sst / (den * den) - 2.0 / den);
+    const uint32_t q4 = (uint32_t)(d.nx + 3) / 4, n = (uint32_t)d.ny * (uint32_t)d.nz * q4;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint64_t g;
+        const uint32_t x0 = dice_group(d, q4, i, &g);
+        const float4 f = reinterpret_cast<const float4*>(d.phi)[g];
+        const uchar4 m = reinterpret_cast<const uchar4*>(d.tgt)[g];
+        const float fv[4] = {f.x, f.y, f.z, f.w};
+        const unsigned char mv[4] = {m.x, m.y, m.z, m.w};
+        float l[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const float s = soft_mask(fv[e], d.tau);
+            l[e] = x0 + e < (uint32_t)d.nx ? (mv[e] ? c_in : c_out) * (-s * (1.0f - s) / d.tau) : 0.0f;
+        }
+        reinterpret_cast<float4*>(d.lam)[g] = make_float4(l[0], l[1], l[2], l[3]);
+    }
+}
+
+// The reverse: the segments from the last (lambda_K is in lam).
 template <class S>
 __global__ void __launch_bounds__(kAdjThreads) k_adj_reverse(const AdjPlan a) {
     cg::grid_group grid = cg::this_grid();
-    const NsVol& V = a.V;
-    const float* phiK = a.fw[a.K & 1];
-    const float4* phi4 = reinterpret_cast<const float4*>(phiK);
-    const uchar4* tgt4 = reinterpret_cast<const uchar4*>(a.tgt);
-    const uint64_t ng = a.P / 4, t0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x,
-                   nt = (uint64_t)gridDim.x * blockDim.x;
-    constexpr int G = 4;  // groups in flight per thread
-    // Soft-Dice sums (s, t, s t): per voxel in fp32, per block and grid in FP64.
-    {
-        float ss = 0.0f, tt = 0.0f, st = 0.0f;
-        for (uint64_t g0 = t0; g0 < ng; g0 += G * nt) {
-            float4 f[G];
-            uchar4 m[G];
-#pragma unroll
-            for (int u = 0; u < G; ++u) {
-                const uint64_t g = g0 + u * nt;
-                if (g < ng) {
-                    f[u] = phi4[g];
-                    m[u] = tgt4[g];
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < G; ++u) {
-                const uint64_t g = g0 + u * nt;
-                const int x0 = g < ng ? group_x(V, g) : -1;
-                if (x0 < 0) continue;
-                const float fv[4] = {f[u].x, f[u].y, f[u].z, f[u].w};
-                const unsigned char mv[4] = {m[u].x, m[u].y, m[u].z, m[u].w};
-#pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    if (x0 + e >= V.nx) break;
-                    const float s = soft_mask(fv[e], a.tau);
-                    const float tv = mv[e] ? 1.0f : 0.0f;
-                    ss += s;
-                    tt += tv;
-                    st += s * tv;
-                }
-            }
-        }
-        block_sum3(ss, tt, st, a.gsum + 4);
-    }
-    grid.sync();
-    // lambda_K = dloss/dphi_K: dloss/ds = (2 st - 2 t den) / den^2; 0 in the padding.
-    {
-        const double den = a.gsum[4] + a.gsum[5], sst = a.gsum[6];
-        const float c_out = (float)(2.0 * sst / (den * den)), c_in = (float)(2.0 * sst / (den * den) - 2.0 / den);
-        float4* lam4 = reinterpret_cast<float4*>(a.lam);
-        for (uint64_t g0 = t0; g0 < ng; g0 += G * nt) {
-            float4 f[G];
-            uchar4 m[G];
-#pragma unroll
-            for (int u = 0; u < G; ++u) {
-                const uint64_t g = g0 + u * nt;
-                if (g < ng) {
-                    f[u] = phi4[g];
-                    m[u] = tgt4[g];
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < G; ++u) {
-                const uint64_t g = g0 + u * nt;
-                if (g >= ng) continue;
-                const int x0 = group_x(V, g);
-                const float fv[4] = {f[u].x, f[u].y, f[u].z, f[u].w};
-                const unsigned char mv[4] = {m[u].x, m[u].y, m[u].z, m[u].w};
-                float l[4];
-#pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    const float s = soft_mask(fv[e], a.tau);
-                    l[e] = (x0 >= 0 && x0 + e < V.nx) ? (mv[e] ? c_in : c_out) * (-s * (1.0f - s) / a.tau) : 0.0f;
-                }
-                lam4[g] = make_float4(l[0], l[1], l[2], l[3]);
-            }
-        }
-    }
     // Segments from the last; each phase's descriptor is read before the
     // barrier that precedes it.
     int s = a.nck - 1, j = 0;
     RevPhase ph = rev_phase<S>(a, s, j);
-    grid.sync();
     double s3[3] = {0.0, 0.0, 0.0};
     for (;;) {
         adj_rev_phase<S>(a, ph, s3);
@@ -904,7 +931,7 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_reverse(const AdjPlan a) {
         ph = rev_phase<S>(a, s, j);
         grid.sync();
     }
-    block_sum3<true>(s3[0], s3[1], s3[2], a.gpart + 3 * (size_t)blockIdx.x);
+    block_sum3(s3[0], s3[1], s3[2], a.gpart + 3 * (size_t)blockIdx.x);
 }
 
 template <class S>
@@ -929,6 +956,7 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
         return owner->num_sms * std::min(per_sm, kAdjBlocksPerSm);
     };
     const int gf = coop(kf), gr = coop(kr);
+    const int ndice = owner->num_sms * 4;  // soft-Dice blocks (per-block partial sums)
     // One device workspace (kept by the engine between calls), carved into
     // 256-byte aligned parts.
     auto al = [](uint64_t b) { return (b + 255) / 256 * 256; };
@@ -943,7 +971,8 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     const uint64_t total = nfields * al(P * 4) + (uint64_t)nsets * every * logb + (uint64_t)(K + 1) * al(mwords * 8) +
                            2 * (uint64_t)(K + 1) * al((uint64_t)nb * 4) + al((uint64_t)(K + 1) * 4) + al(P) +
                            2 * al((uint64_t)nb * 4) + (uint64_t)(nck + 1) * al((uint64_t)nb * 4) + al((uint64_t)nck * 4) +
-                           al(8 * sizeof(double) + 8) + al((uint64_t)gr * 3 * sizeof(double));
+                           al(8 * sizeof(double) + 8) + al((uint64_t)gr * 3 * sizeof(double)) +
+                           al((uint64_t)ndice * 3 * sizeof(double));
     char* base = (char*)core.workspace(total);
     char* const end = base + total;
     auto carve = [&](uint64_t bytes) {
@@ -985,6 +1014,7 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     a.gsum = (double*)carve(8 * sizeof(double) + 8);
     a.nact = (unsigned long long*)(a.gsum + 8);
     a.gpart = (double*)carve((uint64_t)gr * 3 * sizeof(double));
+    double* dpart = (double*)carve((uint64_t)ndice * 3 * sizeof(double));
     a.dbias = dbias ? F() : nullptr;
     a.tgt = tgt;
     a.P = P;
@@ -1036,6 +1066,12 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     LSS_CUDA(cudaMemcpyAsync(a.act0, core.masks(core.parity()), mwords * 8, cudaMemcpyDeviceToDevice, st));
     void* params[] = {(void*)&a};
     LSS_CUDA(cudaLaunchCooperativeKernel(kf, dim3(gf), dim3(kAdjThreads), params, 0, st));
+    count_launch(owner);
+    // The loss and lambda_K between the two.
+    DiceArgs d{a.fw[K & 1], tgt, a.lam, dpart, a.gsum, V.nx, V.ny, V.nz, V.px, V.py, (uint32_t)ndice, tau};
+    k_adj_dice<<<ndice, kDiceThreads, 0, st>>>(d);
+    count_launch(owner);
+    k_adj_lamk<<<owner->num_sms * 8, kDiceThreads, 0, st>>>(d);
     count_launch(owner);
     LSS_CUDA(cudaLaunchCooperativeKernel(kr, dim3(gr), dim3(kAdjThreads), params, 0, st));
     count_launch(owner);
