@@ -203,4 +203,28 @@ inline void* pinned_device_ptr(const void* host) {
     return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
+// Device address of a buffer kernels can read or write in place: pinned host
+// memory (as above), device or managed memory; null for pageable memory.
+inline void* device_view(const void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeHost) return a.devicePointer;
+    if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return const_cast<void*>(p);
+    return nullptr;
+}
+
+// True for device memory of the current device.
+inline bool device_memory(const void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    int dev = -1;
+    return a.type == cudaMemoryTypeDevice && cudaGetDevice(&dev) == cudaSuccess && a.device == dev;
+}
+
 }  // namespace lss

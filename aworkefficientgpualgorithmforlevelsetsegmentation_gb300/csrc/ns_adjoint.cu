@@ -761,12 +761,11 @@ __device__ void adj_rev_phase(const AdjPlan& a, const RevPhase& ph, double* s3) 
     }
 }
 
-// The forward: list_0, then K iterations; phi checkpointed at the start of
-// every segment but the first (the caller's copy) and the last (logged).
+// The forward: list_0, then K iterations; every segment but the last
+// builds its sparse checkpoint as it goes, the last one logs its bricks.
 template <class S>
 __global__ void __launch_bounds__(kAdjThreads) k_adj_forward(const AdjPlan a) {
     cg::grid_group grid = cg::this_grid();
-    const NsVol& V = a.V;
     adj_list0<S>(plan_act(a, 0), plan_flag(a, 0), plan_list(a, 0), &a.counts[0], a.nb);
     grid.sync();
     uint32_t mine = 0;
@@ -817,26 +816,44 @@ __device__ __forceinline__ uint32_t dice_group(const DiceArgs& d, uint32_t q4, u
     return x0;
 }
 
+// Four groups a thread in flight (the loads of a round before its math).
+constexpr int kDiceUnroll = 4;
+
 // Sums s = sigmoid(-phi_K / tau), t = target and s t over the volume: per
 // voxel in fp32, per thread in fp32, per block in FP64 into part[3 * block].
 __global__ void __launch_bounds__(kDiceThreads) k_adj_dice(const DiceArgs d) {
     const uint32_t q4 = (uint32_t)(d.nx + 3) / 4, n = (uint32_t)d.ny * (uint32_t)d.nz * q4;
+    const uint32_t nt = gridDim.x * blockDim.x;
     float ss = 0.0f, tt = 0.0f, st = 0.0f;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint64_t g;
-        const uint32_t x0 = dice_group(d, q4, i, &g);
-        const float4 f = reinterpret_cast<const float4*>(d.phi)[g];
-        const uchar4 m = reinterpret_cast<const uchar4*>(d.tgt)[g];
-        const float fv[4] = {f.x, f.y, f.z, f.w};
-        const unsigned char mv[4] = {m.x, m.y, m.z, m.w};
+    for (uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += kDiceUnroll * nt) {
+        float4 f[kDiceUnroll];
+        uchar4 m[kDiceUnroll];
+        uint32_t x0[kDiceUnroll];
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            if (x0 + e >= (uint32_t)d.nx) break;
-            const float s = soft_mask(fv[e], d.tau);
-            const float tv = mv[e] ? 1.0f : 0.0f;
-            ss += s;
-            tt += tv;
-            st += s * tv;
+        for (int u = 0; u < kDiceUnroll; ++u) {
+            const uint32_t i = i0 + u * nt;
+            x0[u] = 0xFFFFFFFFu;
+            if (i < n) {
+                uint64_t g;
+                x0[u] = dice_group(d, q4, i, &g);
+                f[u] = reinterpret_cast<const float4*>(d.phi)[g];
+                m[u] = reinterpret_cast<const uchar4*>(d.tgt)[g];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kDiceUnroll; ++u) {
+            if (x0[u] == 0xFFFFFFFFu) continue;
+            const float fv[4] = {f[u].x, f[u].y, f[u].z, f[u].w};
+            const unsigned char mv[4] = {m[u].x, m[u].y, m[u].z, m[u].w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                if (x0[u] + e >= (uint32_t)d.nx) break;
+                const float s = soft_mask(fv[e], d.tau);
+                const float tv = mv[e] ? 1.0f : 0.0f;
+                ss += s;
+                tt += tv;
+                st += s * tv;
+            }
         }
     }
     __shared__ double w3[3][kDiceThreads / 32];
@@ -895,20 +912,35 @@ __global__ void __launch_bounds__(kDiceThreads) k_adj_lamk(const DiceArgs d) {
     const double den = tot[0] + tot[1], sst = tot[2];
     const float c_out = (float)(2.0 * sst / (den * den)), c_in = (float)(2.0 * sst / (den * den) - 2.0 / den);
     const uint32_t q4 = (uint32_t)(d.nx + 3) / 4, n = (uint32_t)d.ny * (uint32_t)d.nz * q4;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint64_t g;
-        const uint32_t x0 = dice_group(d, q4, i, &g);
-        const float4 f = reinterpret_cast<const float4*>(d.phi)[g];
-        const uchar4 m = reinterpret_cast<const uchar4*>(d.tgt)[g];
-        const float fv[4] = {f.x, f.y, f.z, f.w};
-        const unsigned char mv[4] = {m.x, m.y, m.z, m.w};
-        float l[4];
+    const uint32_t nt = gridDim.x * blockDim.x;
+    for (uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += kDiceUnroll * nt) {
+        float4 f[kDiceUnroll];
+        uchar4 m[kDiceUnroll];
+        uint64_t g[kDiceUnroll];
+        uint32_t x0[kDiceUnroll];
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            const float s = soft_mask(fv[e], d.tau);
-            l[e] = x0 + e < (uint32_t)d.nx ? (mv[e] ? c_in : c_out) * (-s * (1.0f - s) / d.tau) : 0.0f;
+        for (int u = 0; u < kDiceUnroll; ++u) {
+            const uint32_t i = i0 + u * nt;
+            x0[u] = 0xFFFFFFFFu;
+            if (i < n) {
+                x0[u] = dice_group(d, q4, i, &g[u]);
+                f[u] = reinterpret_cast<const float4*>(d.phi)[g[u]];
+                m[u] = reinterpret_cast<const uchar4*>(d.tgt)[g[u]];
+            }
         }
-        reinterpret_cast<float4*>(d.lam)[g] = make_float4(l[0], l[1], l[2], l[3]);
+#pragma unroll
+        for (int u = 0; u < kDiceUnroll; ++u) {
+            if (x0[u] == 0xFFFFFFFFu) continue;
+            const float fv[4] = {f[u].x, f[u].y, f[u].z, f[u].w};
+            const unsigned char mv[4] = {m[u].x, m[u].y, m[u].z, m[u].w};
+            float l[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const float s = soft_mask(fv[e], d.tau);
+                l[e] = x0[u] + e < (uint32_t)d.nx ? (mv[e] ? c_in : c_out) * (-s * (1.0f - s) / d.tau) : 0.0f;
+            }
+            reinterpret_cast<float4*>(d.lam)[g[u]] = make_float4(l[0], l[1], l[2], l[3]);
+        }
     }
 }
 
@@ -956,7 +988,7 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
         return owner->num_sms * std::min(per_sm, kAdjBlocksPerSm);
     };
     const int gf = coop(kf), gr = coop(kr);
-    const int ndice = owner->num_sms * 4;  // soft-Dice blocks (per-block partial sums)
+    const int ndice = owner->num_sms * 8;  // soft-Dice blocks (per-block partial sums)
     // One device workspace (kept by the engine between calls), carved into
     // 256-byte aligned parts.
     auto al = [](uint64_t b) { return (b + 255) / 256 * 256; };
@@ -1010,44 +1042,59 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     a.nlist0 = (uint32_t*)carve((uint64_t)nb * 4);  // lstride apart, like the brick lists
     for (int q = 1; q < nck - 1; ++q) carve((uint64_t)nb * 4);
     a.ncount = (uint32_t*)carve((uint64_t)nck * 4);
-    uint8_t* tgt = (uint8_t*)carve(P);
+    uint8_t* const tgt_field = (uint8_t*)carve(P);
     a.gsum = (double*)carve(8 * sizeof(double) + 8);
     a.nact = (unsigned long long*)(a.gsum + 8);
     a.gpart = (double*)carve((uint64_t)gr * 3 * sizeof(double));
     double* dpart = (double*)carve((uint64_t)ndice * 3 * sizeof(double));
     a.dbias = dbias ? F() : nullptr;
-    a.tgt = tgt;
     a.P = P;
     a.nb = nb;
     a.K = K;
     a.every = every;
     a.nck = nck;
     a.tau = tau;
-    // Target and bias into the padded layout on the device (pinned host
-    // buffers are read in place, pageable ones through the copy engine into
-    // fw[0], which is free until the forward starts).
+    // Target, bias and the bias gradient.  Device memory of a volume whose
+    // rows need no padding (px = nx, py = ny: the caller's layout is the
+    // padded one up to z = nz, the only part any kernel touches) is used in
+    // place.  Otherwise the padded copies in the workspace: pinned host or
+    // device memory is read (written) in place by the scatter (gather)
+    // kernel, pageable memory goes through the copy engine into fw[0] (free
+    // until the forward starts and after the reverse ends).  The padding of
+    // these fields is never read.
     const uint64_t n = (uint64_t)V.nx * V.ny * V.nz;
+    const bool flat = V.px == V.nx && V.py == V.ny;
+    auto in_place = [&](const void* p) { return flat && device_memory(p) && (uintptr_t)p % 16 == 0; };
     auto upload = [&](auto* dst, const auto* host) {
         using T = std::remove_cv_t<std::remove_pointer_t<decltype(host)>>;
-        const T* src = (const T*)pinned_device_ptr(host);
+        const T* src = (const T*)device_view(host);
         if (!src) {
             T* stage = (T*)(void*)a.fw[0];
-            LSS_CUDA(cudaMemcpyAsync(stage, host, n * sizeof(T), cudaMemcpyHostToDevice, st));
+            LSS_CUDA(cudaMemcpyAsync(stage, host, n * sizeof(T), cudaMemcpyDefault, st));
             src = stage;
         }
         k_ns_scatter<<<grid, 256, 0, st>>>(dst, src, V.nx, V.ny, V.nz, V.px, V.py);
         count_launch(owner);
     };
-    LSS_CUDA(cudaMemsetAsync(tgt, 0, P, st));
-    upload(tgt, target);
+    if (in_place(target)) {
+        a.tgt = target;
+    } else {
+        upload(tgt_field, target);
+        a.tgt = tgt_field;
+    }
     if (bias) {
         float* bd = F();
-        LSS_CUDA(cudaMemsetAsync(bd, 0, P * 4, st));
-        upload(bd, bias);
-        V.bias = bd;
+        if (in_place(bias)) {
+            V.bias = bias;
+        } else {
+            upload(bd, bias);
+            V.bias = bd;
+        }
     }
     a.V = V;
-    if (a.dbias) LSS_CUDA(cudaMemsetAsync(a.dbias, 0, P * 4, st));
+    const bool dbias_in_place = dbias && in_place(dbias);
+    if (dbias_in_place) a.dbias = dbias;
+    if (a.dbias) LSS_CUDA(cudaMemsetAsync(a.dbias, 0, (dbias_in_place ? n : P) * 4, st));
     LSS_CUDA(cudaMemsetAsync(a.gsum, 0, 8 * sizeof(double) + 8, st));
     LSS_CUDA(cudaMemsetAsync(a.gpart, 0, (uint64_t)gr * 3 * sizeof(double), st));
     LSS_CUDA(cudaMemsetAsync(a.act0 + a.astride, 0, (uint64_t)K * al(mwords * 8), st));  // act[1..K]
@@ -1068,19 +1115,20 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     LSS_CUDA(cudaLaunchCooperativeKernel(kf, dim3(gf), dim3(kAdjThreads), params, 0, st));
     count_launch(owner);
     // The loss and lambda_K between the two.
-    DiceArgs d{a.fw[K & 1], tgt, a.lam, dpart, a.gsum, V.nx, V.ny, V.nz, V.px, V.py, (uint32_t)ndice, tau};
+    DiceArgs d{a.fw[K & 1], a.tgt, a.lam, dpart, a.gsum, V.nx, V.ny, V.nz, V.px, V.py, (uint32_t)ndice, tau};
     k_adj_dice<<<ndice, kDiceThreads, 0, st>>>(d);
     count_launch(owner);
     k_adj_lamk<<<owner->num_sms * 8, kDiceThreads, 0, st>>>(d);
     count_launch(owner);
     LSS_CUDA(cudaLaunchCooperativeKernel(kr, dim3(gr), dim3(kAdjThreads), params, 0, st));
     count_launch(owner);
-    // d_bias back to the caller's unpadded layout (in place when pinned).
-    if (dbias) {
-        float* dev = (float*)pinned_device_ptr(dbias);
+    // d_bias back to the caller's unpadded layout (written in place when the
+    // device can address it).
+    if (dbias && !dbias_in_place) {
+        float* dev = (float*)device_view(dbias);
         k_ns_gather<<<grid, 256, 0, st>>>(dev ? dev : a.fw[0], a.dbias, V.nx, V.ny, V.nz, V.px, V.py);
         count_launch(owner);
-        if (!dev) LSS_CUDA(cudaMemcpyAsync(dbias, a.fw[0], n * 4, cudaMemcpyDeviceToHost, st));
+        if (!dev) LSS_CUDA(cudaMemcpyAsync(dbias, a.fw[0], n * 4, cudaMemcpyDefault, st));
     }
     double h[8];
     unsigned long long na = 0;

@@ -40,6 +40,27 @@ def _ptr(a: np.ndarray) -> C.c_void_p:
     return C.c_void_p(a.ctypes.data)
 
 
+def _cuda_ptr(x, shape, dtype, writeable=False):
+    """Device address of a CUDA array (any object with __cuda_array_interface__,
+    e.g. a torch CUDA tensor) after checking its shape, dtype and C layout, or
+    None for anything else (host arrays)."""
+    ai = getattr(x, "__cuda_array_interface__", None)
+    if ai is None:
+        return None
+    shape = tuple(shape)
+    dt = np.dtype(dtype)
+    if tuple(ai["shape"]) != shape or np.dtype(ai["typestr"]) != dt:
+        raise ValueError(f"device array must be {dt} of shape {shape}")
+    strides = ai.get("strides")
+    if strides is not None:
+        want = tuple(int(np.prod(shape[i + 1:])) * dt.itemsize for i in range(len(shape)))
+        if tuple(strides) != want:
+            raise ValueError("device array must be C-contiguous")
+    if writeable and ai["data"][1]:
+        raise ValueError("device array is read-only")
+    return C.c_void_p(ai["data"][0])
+
+
 def _out(out, shape, dtype) -> np.ndarray:
     """A new zeroed array, or the caller's `out` (e.g. a view of pinned host
     memory reused across calls) after checking its shape, dtype and layout."""
@@ -246,15 +267,32 @@ class Segmenter:
         self._chk(self._lib.lss_get_stats(self._h, C.byref(s)))
         return {k: getattr(s, k) for k, _ in L.lss_stats._fields_}
 
-    def adjoint(self, K: int, checkpoint_every: int, target_mask: np.ndarray, sigmoid_scale: float = 0.5,
-                bias: np.ndarray | None = None, want_dbias: bool = True, d_bias_out=None):
-        t = np.ascontiguousarray(target_mask, np.uint8)
-        b = None if bias is None else np.ascontiguousarray(bias, np.float32)
-        db = _out(d_bias_out, self.shape, np.float32) if want_dbias else None
+    def adjoint(self, K: int, checkpoint_every: int, target_mask, sigmoid_scale: float = 0.5,
+                bias=None, want_dbias: bool = True, d_bias_out=None):
+        """lss_adjoint_run.  target_mask, bias and d_bias_out are host arrays or
+        CUDA arrays (device memory is used in place); d_bias_out, when given,
+        receives the bias gradient and is returned as "d_bias"."""
+        keep = []
+
+        def arg(x, dtype, writeable=False):
+            p = _cuda_ptr(x, self.shape, dtype, writeable)
+            if p is not None:
+                return p
+            a = np.ascontiguousarray(x, dtype) if not writeable else _out(x, self.shape, dtype)
+            keep.append(a)
+            return _ptr(a)
+
+        t = arg(target_mask, np.uint8)
+        b = None if bias is None else arg(bias, np.float32)
+        db, dbp = None, None
+        if want_dbias:
+            if d_bias_out is not None and _cuda_ptr(d_bias_out, self.shape, np.float32, True) is not None:
+                db, dbp = d_bias_out, _cuda_ptr(d_bias_out, self.shape, np.float32, True)
+            else:
+                db = _out(d_bias_out, self.shape, np.float32)
+                dbp = _ptr(db)
         g = L.lss_grads()
-        self._chk(self._lib.lss_adjoint_run(self._h, K, checkpoint_every, _ptr(t), sigmoid_scale,
-                                            None if b is None else _ptr(b),
-                                            None if db is None else _ptr(db), C.byref(g)))
+        self._chk(self._lib.lss_adjoint_run(self._h, K, checkpoint_every, t, sigmoid_scale, b, dbp, C.byref(g)))
         return {"loss": g.loss, "d_target": g.d_target, "d_window": g.d_window,
                 "d_curvature": g.d_curvature, "d_bias": db,
                 "active_voxel_iterations": g.active_voxel_iterations}

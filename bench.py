@@ -616,9 +616,11 @@ def measure_adjoint(local, scale, steps, warmup):
     lss_adjoint_run: the forward records the K active sets, the loss, the
     reverse pass recomputes each segment from its checkpoint and scatters the
     transposed stencil Jacobian, giving dloss/dT, deps, dalpha and the bias
-    volume's gradient.  Target, bias and the bias gradient live in pinned host
-    buffers.  The metric is active-voxel iterations (the sum over the forward
-    iterations of the active voxels updated) per second of the whole call;
+    volume's gradient.  The value has target, bias and the bias gradient in
+    device memory (used in place); e2e the same calls with pinned host
+    buffers (the bias and its gradient cross the host link every call).  The
+    metric is active-voxel iterations (the sum over the forward iterations of
+    the active voxels updated) per second of the whole call;
     the roofline counts 28 bytes each (phi, I, bias, lambda in and out, the
     bias gradient read and written)."""
     import ctypes
@@ -640,27 +642,39 @@ def measure_adjoint(local, scale, steps, warmup):
     def pinned(dt):
         return torch.empty(shape, dtype=dt, pin_memory=True).numpy()
 
+    def timed(tgt, bias, dbias):
+        for _ in range(warmup):
+            g = seg.adjoint(K, every, tgt, 0.5, bias=bias, d_bias_out=dbias)
+        torch.cuda.synchronize()
+        ev_ms, nact = [], 0
+        launches0 = seg.stats()["kernel_launches"]
+        for _ in range(steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            g = seg.adjoint(K, every, tgt, 0.5, bias=bias, d_bias_out=dbias)
+            e1.record(stream)
+            e1.synchronize()
+            ev_ms.append(e0.elapsed_time(e1))
+            nact += g["active_voxel_iterations"]
+        return ev_ms, nact, g, (seg.stats()["kernel_launches"] - launches0) // steps
+
+    # Inputs resident in HBM (torch CUDA tensors, used in place): the value.
+    tgt_d = torch.from_numpy(np.ascontiguousarray(cfg["target"], np.uint8)).to(f"cuda:{local}")
+    bias_d = torch.zeros(shape, dtype=torch.float32, device=f"cuda:{local}")
+    dbias_d = torch.empty(shape, dtype=torch.float32, device=f"cuda:{local}")
+    ev_ms, nact, g, launches = timed(tgt_d, bias_d, dbias_d)
+    # Pinned host buffers, the bias in and its gradient out over the host link: e2e.
     tgt, bias, dbias = pinned(torch.uint8), pinned(torch.float32), pinned(torch.float32)
     tgt[...] = cfg["target"]
     bias[...] = 0.0
-    for _ in range(warmup):
-        g = seg.adjoint(K, every, tgt, 0.5, bias=bias, d_bias_out=dbias)
-    torch.cuda.synchronize()
-    ev_ms, nact = [], 0
-    launches0 = seg.stats()["kernel_launches"]
-    for _ in range(steps):
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        g = seg.adjoint(K, every, tgt, 0.5, bias=bias, d_bias_out=dbias)
-        e1.record(stream)
-        e1.synchronize()
-        ev_ms.append(e0.elapsed_time(e1))
-        nact += g["active_voxel_iterations"]
-    launches = (seg.stats()["kernel_launches"] - launches0) // steps
-    tot = sum(ev_ms)
+    ev_h, nact_h, gh, launches_h = timed(tgt, bias, dbias)
+    same = (gh["loss"] == g["loss"] and abs(gh["d_target"] - g["d_target"]) <= 1e-6 * abs(g["d_target"])
+            and bool(np.allclose(dbias, dbias_d.cpu().numpy(), rtol=1e-4, atol=1e-9)))
+    tot, tot_h = sum(ev_ms), sum(ev_h)
     peak, peak_kind = measured_peak()
     achieved = ADJOINT_BYTES * nact / (tot / 1e3) / 1e9
+    n = int(np.prod(shape))
     del seg
     torch.cuda.synchronize()
     return {"workload": cfg["name"] + "_two_shell_adjoint", "K": K, "checkpoint_every": every,
@@ -669,7 +683,12 @@ def measure_adjoint(local, scale, steps, warmup):
             "value": nact / (tot / 1e3), "unit": "active_voxel_iterations/s",
             "loss": g["loss"], "d_target": g["d_target"], "d_window": g["d_window"],
             "d_curvature": g["d_curvature"], "gpu_launches_per_call": int(launches),
-            "host_buffers": "pinned (target, bias, bias gradient)",
+            "buffers": "device (target, bias, bias gradient in HBM, used in place)",
+            "e2e": {"value": nact_h / (tot_h / 1e3), "unit": "active_voxel_iterations/s",
+                    "ms_per_call": tot_h / steps, "ms_per_call_median": statistics.median(ev_h),
+                    "buffers": "pinned host (target, bias, bias gradient)",
+                    "h2d_bytes_per_step": n + 4 * n, "d2h_bytes_per_step": 4 * n,
+                    "gpu_launches_per_call": int(launches_h), "same_result_as_device_buffers": same},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "bytes_per_update": ADJOINT_BYTES}, "steps": steps}
@@ -685,7 +704,8 @@ def run_adjoint(args, ws, rank, local):
                 "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_call"],
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic", "config": {"workload": r["workload"]}, "adjoint": r,
-                "clocks": clk.summary()}
+                "e2e": {k: r["e2e"][k] for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step")},
+                "gpu_launches": r["gpu_launches_per_call"] * args.steps, "clocks": clk.summary()}
         print(json.dumps(line), flush=True)
 
 

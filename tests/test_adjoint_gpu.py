@@ -150,3 +150,38 @@ def test_autograd_wrapper_and_adam_fit():
             alpha.clamp_(0.0, 1.0)
         losses.append(float(loss.detach()))
     assert losses[-1] < losses[0] - 1e-3, losses
+
+
+@pytest.mark.parametrize("shape", [(40, 48, 56), (37, 45, 43)])
+def test_gpu_adjoint_device_buffers_match_host_buffers(shape):
+    """Target, bias and the bias gradient as CUDA arrays (used in place when
+    the rows need no padding, scattered and gathered on the device otherwise)
+    give the host-buffer call's results."""
+    torch = pytest.importorskip("torch")
+    cfg = P.config4(0.5)  # 96^3; a centred crop keeps the seed and the shells
+    crop = tuple(slice((m - c) // 2, (m - c) // 2 + c) for m, c in zip(cfg["image"].shape, shape))
+    img = np.ascontiguousarray(cfg["image"][crop])
+    tgt = np.ascontiguousarray(cfg["target"][crop])
+    phi0 = np.ascontiguousarray(cfg["phi0"][crop])
+    p = cfg["params"]
+    rng = np.random.default_rng(5)
+    bias = (0.02 * rng.standard_normal(shape)).astype(np.float32)
+
+    def run(t, b, db):
+        s = lss.Segmenter(lss.MODE_NS, brick=(8, 8, 8), threads_per_brick=256)
+        s.load_volume(img)
+        s.set_parameters(p.target, p.window, p.curvature, p.time_step, alpha_role=p.alpha_role)
+        s.set_phi(phi0)
+        return s.adjoint(12, 4, t, 0.5, bias=b, d_bias_out=db)
+
+    h = run(tgt, bias, None)
+    dev = torch.device("cuda:0")
+    db = torch.full(shape, 7.0, dtype=torch.float32, device=dev)  # overwritten, not added to
+    d = run(torch.from_numpy(tgt).to(dev), torch.from_numpy(bias).to(dev), db)
+    torch.cuda.synchronize()
+    assert d["d_bias"] is db
+    assert d["loss"] == h["loss"]
+    for key in ("d_target", "d_window", "d_curvature"):
+        assert rel(d[key], h[key]) <= 1e-5, (key, d[key], h[key])
+    assert np.allclose(db.cpu().numpy(), h["d_bias"], rtol=1e-4, atol=1e-9)
+    assert h["active_voxel_iterations"] == d["active_voxel_iterations"] > 0
