@@ -302,9 +302,14 @@ typedef struct lss_grads {
 /* Runs K iterations from the current state with the active set of each
  * iteration recorded and then held fixed, and back-propagates the soft-Dice
  * loss of sigmoid(-phi/sigmoid_scale) against target_mask through them.
- * phi is checkpointed every `checkpoint_every` iterations.  bias (nullable)
- * is a per-voxel speed bias added to D; d_bias (nullable) receives its
- * gradient.  The engine state is restored to the starting state on return. */
+ * phi is checkpointed every `checkpoint_every` iterations (each checkpoint
+ * holds the bricks its segment reaches; the last segment is logged brick by
+ * brick instead).  bias (nullable) is a per-voxel speed bias added to D;
+ * d_bias (nullable) receives its gradient.  target_mask, bias and d_bias
+ * (nx*ny*nz, x fastest) may be host memory (pageable or pinned) or device
+ * memory of the engine's device; device memory is used in place when
+ * nx and ny are multiples of 8 and the pointer is 16-byte aligned.  The
+ * engine state is restored to the starting state on return. */
 lss_status lss_adjoint_run(lss_engine* e, int32_t K, int32_t checkpoint_every,
                            const uint8_t* target_mask, float sigmoid_scale,
                            const float* bias, float* d_bias, lss_grads* out);
