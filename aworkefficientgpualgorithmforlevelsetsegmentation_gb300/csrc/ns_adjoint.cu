@@ -120,7 +120,7 @@ __device__ __forceinline__ uint32_t* plan_list(const AdjPlan& a, int k) { return
 __device__ __forceinline__ uint32_t* plan_flag(const AdjPlan& a, int k) { return a.flag0 + (uint64_t)k * a.lstride; }
 __device__ __forceinline__ uint32_t* plan_need(const AdjPlan& a, int s) { return a.nlist0 + (uint64_t)s * a.lstride; }
 // The log of iteration t of segment s: the bricks of list_t before the
-// update, brick i of the list at i * VOX.
+// update, brick b at b * VOX.
 __device__ __forceinline__ float* plan_log(const AdjPlan& a, int s, int t) {
     return a.log0 + ((uint64_t)(s & 1) * a.every + (uint64_t)(t - s * a.every)) * a.lgstride;
 }
@@ -147,32 +147,29 @@ __device__ __forceinline__ SegPair seg_pair(const AdjPlan& a, int s) {
 }
 
 // Per-iteration brick lists: list[k][0 .. count[k]) = the bricks of A_k in
-// no particular order (each brick once), flag[k][b] = b is in it.
+// no particular order (each brick once), flag[k][b] = b is in it.  Brick
+// logs are indexed by brick: brick b of a log at b * VOX.
 
-// list_0 and flag_0 from the recorded masks of A_0.
+// flag_0 from the recorded masks of A_0 (the first iteration's scan lists
+// its bricks).
 template <class S>
-__device__ __forceinline__ void adj_list0(const unsigned long long* act, uint32_t* flag, uint32_t* list,
-                                          uint32_t* count, uint32_t nb) {
+__device__ __forceinline__ void adj_flag0(const unsigned long long* act, uint32_t* flag, uint32_t nb) {
     for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
         unsigned long long any = 0ull;
 #pragma unroll
         for (int w = 0; w < S::WORDS; ++w) any |= act[(size_t)b * S::WORDS + w];
-        if (any) {
-            flag[b] = 1u;
-            list[atomicAdd(count, 1u)] = b;
-        }
+        if (any) flag[b] = 1u;
     }
 }
 
-// The voxel bits of one brick (chg, CHG 32-bit words) dilated (nbh = 6 or
-// 26) into its 27 neighbours: with nxt, ORed into their masks of A_{k+1};
-// the first thread to find a word for a brick appends the brick to the list
-// (flag_next, list_next, count_next).  Threads t0, t0 + stride, ... take the
-// (neighbour, mask word) pairs.
+// The changed-voxel bits of one brick (chg, CHG 32-bit words) dilated
+// (V.nbh = 6 or 26) into its 27 neighbours' masks of A_{k+1} (nxt); each
+// neighbour reached is marked in flag_next with a plain store (the next
+// iteration finds its bricks by a scan of the flags).  Threads t0, t0 +
+// stride, ... take the (neighbour, mask word) pairs.
 template <class S>
 __device__ __forceinline__ void adj_dilate_brick(const NsVol& V, uint32_t b, const uint32_t* chg, int t0, int stride,
-                                                 int nbh, unsigned long long* nxt, uint32_t* flag_next,
-                                                 uint32_t* list_next, uint32_t* count_next) {
+                                                 unsigned long long* nxt, uint32_t* flag_next) {
     const int3 o = brick_origin<S>(V, b + V.brick_base);
     for (int r = t0; r < 27 * S::WORDS; r += stride) {
         const int slot = r / S::WORDS, w = r % S::WORDS;
@@ -180,106 +177,124 @@ __device__ __forceinline__ void adj_dilate_brick(const NsVol& V, uint32_t b, con
         const int bx = o.x / S::X + ox, by = o.y / S::Y + oy, bz = o.z / S::Z + oz;
         const int lx = V.nx - bx * S::X, ly = V.ny - by * S::Y, lz = V.nz - bz * S::Z;
         if (bx < 0 || by < 0 || bz < 0 || lx <= 0 || ly <= 0 || lz <= 0) continue;
-        uint64_t x = dilate_word<S>(chg, ox, oy, oz, w, nbh);
+        uint64_t x = dilate_word<S>(chg, ox, oy, oz, w, V.nbh);
         if (lx < S::X || ly < S::Y || lz < S::Z)
             x &= inside_mask<S>(w, min(lx, S::X), min(ly, S::Y), min(lz, S::Z));
         if (!x) continue;
         const uint32_t nbi = b + (int32_t)((oz * V.nby + oy) * V.nbx + ox);
-        if (nxt) atomicOr(&nxt[(size_t)nbi * S::WORDS + w], (unsigned long long)x);
-        if (*(volatile uint32_t*)&flag_next[nbi] == 0u && atomicExch(&flag_next[nbi], 1u) == 0u)
-            list_next[atomicAdd(count_next, 1u)] = nbi;
+        atomicOr(&nxt[(size_t)nbi * S::WORDS + w], (unsigned long long)x);
+        flag_next[nbi] = 1u;
     }
 }
 
-// Forward iteration k, block per brick.  The bricks of list_k are written
-// whole into out (active voxels updated from in, the others copied), and
-// the bricks of list_{k-1} not in list_k (flag_k clear) are copied from in
-// to out, so that out equals in outside the bricks of A_k (both fields of
-// the pair stay current).  Each updated brick's changed voxels are dilated
-// into A_{k+1} by the same block.  With log (the last segment): brick i of
-// list_k is logged as it was before the update (in) at log + i * VOX.  With
-// cap = s + 1 (segment s has a checkpoint): the 27 bricks around each brick
-// of list_k (the update's reads and writes, a superset) join the segment's
-// checkpoint the first time the segment reaches them, copied from in: a
-// brick no earlier iteration of the segment reached still holds phi at the
-// segment's start.  The checkpoint is that sparse field ck, and the bricks
-// it holds are listed for the reverse.  Returns the active voxels this
-// thread updated.
+// Forward iteration k.  Its bricks are found by a scan of the flags: block
+// g looks at bricks c + t * grid + g (thread t, chunks c of grid * threads
+// bricks, so consecutive bricks go to different blocks); flag_k set: a brick
+// of A_k, written whole into out (active voxels updated from in, the others
+// copied) and recorded in list_k; else flag_{k-1} set: a brick of A_{k-1}
+// that left the set, copied from in to out.  So out equals in outside the
+// bricks of A_k (both fields of the pair stay current).  Each updated
+// brick's changed voxels are dilated into A_{k+1} by the same block, which
+// marks the bricks reached in flag_{k+1}.  With log (the last segment):
+// brick b of A_k is logged as it was before the update (in) at log + b *
+// VOX.  With cap = s + 1 (segment s has a checkpoint): the 27 bricks around
+// each brick of A_k (the update's reads and writes, a superset) join the
+// segment's checkpoint the first time the segment reaches them, copied from
+// in: a brick no earlier iteration of the segment reached still holds phi at
+// the segment's start.  The checkpoint is that sparse field ck, and the
+// bricks it holds are listed for the reverse.  Returns the active voxels
+// this thread updated.
 template <class S>
 __device__ uint32_t adj_forward_step(const AdjPlan& a, int k, const float* in, float* out, float* log, uint32_t cap,
                                      float* ck) {
     const NsVol& V = a.V;
     __shared__ uint32_t chg[S::CHG];
-    __shared__ uint32_t any, ncap;
+    __shared__ uint32_t any, ncap, nfound;
     __shared__ uint32_t capl[27];
+    __shared__ uint32_t found[kAdjThreads];
     constexpr int G = S::VOX / 4;
+    constexpr uint32_t kUpd = 0x80000000u;
     const unsigned long long* act = plan_act(a, k);
-    const uint32_t* list = plan_list(a, k);
-    const uint32_t* prev = k ? plan_list(a, k - 1) : nullptr;
     const uint32_t* flag_k = plan_flag(a, k);
-    const uint32_t n = a.counts[k], np = k ? a.counts[k - 1] : 0u;
+    const uint32_t* flag_p = k ? plan_flag(a, k - 1) : nullptr;
     uint32_t mine = 0;
-    for (uint32_t i = blockIdx.x; i < n + np; i += gridDim.x) {
-        const bool upd = i < n;
-        const uint32_t b = upd ? list[i] : prev[i - n];
-        if (!upd && flag_k[b]) continue;  // also in list_k: written whole (uniform over the block)
-        const int3 o = brick_origin<S>(V, b + V.brick_base);
-        if (upd) {
-            __syncthreads();  // chg, any, ncap and capl free: the previous brick is done
-            if (threadIdx.x == 0) {
-                any = 0u;
-                ncap = 0u;
-            }
-            __syncthreads();
+    const uint64_t chunk = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t c0 = 0; c0 < a.nb; c0 += chunk) {
+        __syncthreads();  // found and nfound free
+        if (threadIdx.x == 0) nfound = 0u;
+        __syncthreads();
+        const uint64_t mb = c0 + (uint64_t)threadIdx.x * gridDim.x + blockIdx.x;
+        bool upd_mine = false;
+        uint32_t pos = 0u;
+        if (mb < a.nb) {
+            const uint32_t b = (uint32_t)mb;
+            upd_mine = flag_k[b] != 0u;
+            if (upd_mine || (flag_p && flag_p[b] != 0u)) found[atomicAdd(&nfound, 1u)] = b | (upd_mine ? kUpd : 0u);
+            // The list position is stored at the end of the chunk: the
+            // atomic's latency hides behind the bricks' work.
+            if (upd_mine) pos = atomicAdd(&a.counts[k], 1u);
         }
-        // Thread r < 27 checks neighbour r for the checkpoint before the
-        // update (the check's latency hides behind it) and claims it after.
-        uint32_t nbr = 0u;
-        bool fresh = false;
-        if (upd && cap && threadIdx.x < 27) {
-            const int ox = (int)threadIdx.x % 3 - 1, oy = ((int)threadIdx.x / 3) % 3 - 1, oz = (int)threadIdx.x / 9 - 1;
-            const int bx = o.x / S::X + ox, by = o.y / S::Y + oy, bz = o.z / S::Z + oz;
-            if (bx >= 0 && by >= 0 && bz >= 0 && bx < V.nbx && by < V.nby && bz < V.nbz) {
-                nbr = b + (uint32_t)((oz * V.nby + oy) * V.nbx + ox);
-                fresh = *(volatile uint32_t*)&a.need[nbr] != cap;
-            }
-        }
-        for (int j = threadIdx.x; j < S::VOX; j += blockDim.x) {
-            const int3 p = make_int3(o.x + j % S::X, o.y + (j / S::X) % S::Y, o.z + j / (S::X * S::Y));
-            bool changed = false;
-            if (p.x < V.nx && p.y < V.ny && p.z < V.nz) {
-                const size_t idx = ((size_t)p.z * V.py + p.y) * V.px + p.x;
-                const float c = in[idx];
-                if (upd && log) log[(size_t)i * S::VOX + j] = c;
-                if (upd && ((act[(size_t)b * S::WORDS + (j >> 6)] >> (j & 63)) & 1ull)) {
-                    auto P = [&](int dx, int dy, int dz) {
-                        return in[((size_t)clampi(p.z + dz, V.nz) * V.py + clampi(p.y + dy, V.ny)) * V.px +
-                                  clampi(p.x + dx, V.nx)];
-                    };
-                    const float nv = ns_update_f32(P, V.img[idx], V.bias ? V.bias[idx] : 0.0f, V);
-                    changed = fabsf(nv - c) > V.thr_t;
-                    out[idx] = nv;
-                    ++mine;
-                } else {
-                    out[idx] = c;
-                }
-            }
-            // VOX is a multiple of 32: a warp's slots are all in or all out.
+        __syncthreads();  // found complete
+        const uint32_t nf = nfound;
+        for (uint32_t f = 0; f < nf; ++f) {
+            const bool upd = (found[f] & kUpd) != 0u;
+            const uint32_t b = found[f] & ~kUpd;
+            const int3 o = brick_origin<S>(V, b + V.brick_base);
             if (upd) {
-                const uint32_t bal = __ballot_sync(0xffffffffu, changed);
-                if ((threadIdx.x & 31) == 0) {
-                    chg[j >> 5] = bal;
-                    if (bal) any = 1u;
+                __syncthreads();  // chg, any, ncap and capl free: the previous brick is done
+                if (threadIdx.x == 0) {
+                    any = 0u;
+                    ncap = 0u;
+                }
+                __syncthreads();
+            }
+            // Thread r < 27 claims neighbour r for the checkpoint before the
+            // update (the atomic's latency hides behind it).
+            uint32_t nbr = 0u;
+            bool won = false;
+            if (upd && cap && threadIdx.x < 27) {
+                const int ox = (int)threadIdx.x % 3 - 1, oy = ((int)threadIdx.x / 3) % 3 - 1,
+                          oz = (int)threadIdx.x / 9 - 1;
+                const int bx = o.x / S::X + ox, by = o.y / S::Y + oy, bz = o.z / S::Z + oz;
+                if (bx >= 0 && by >= 0 && bz >= 0 && bx < V.nbx && by < V.nby && bz < V.nbz) {
+                    nbr = b + (uint32_t)((oz * V.nby + oy) * V.nbx + ox);
+                    won = atomicExch(&a.need[nbr], cap) != cap;
                 }
             }
-        }
-        if (upd) {
+            for (int j = threadIdx.x; j < S::VOX; j += blockDim.x) {
+                const int3 p = make_int3(o.x + j % S::X, o.y + (j / S::X) % S::Y, o.z + j / (S::X * S::Y));
+                bool changed = false;
+                if (p.x < V.nx && p.y < V.ny && p.z < V.nz) {
+                    const size_t idx = ((size_t)p.z * V.py + p.y) * V.px + p.x;
+                    const float c = in[idx];
+                    if (upd && log) log[(size_t)b * S::VOX + j] = c;
+                    if (upd && ((act[(size_t)b * S::WORDS + (j >> 6)] >> (j & 63)) & 1ull)) {
+                        auto P = [&](int dx, int dy, int dz) {
+                            return in[((size_t)clampi(p.z + dz, V.nz) * V.py + clampi(p.y + dy, V.ny)) * V.px +
+                                      clampi(p.x + dx, V.nx)];
+                        };
+                        const float nv = ns_update_f32(P, V.img[idx], V.bias ? V.bias[idx] : 0.0f, V);
+                        changed = fabsf(nv - c) > V.thr_t;
+                        out[idx] = nv;
+                        ++mine;
+                    } else {
+                        out[idx] = c;
+                    }
+                }
+                // VOX is a multiple of 32: a warp's slots are all in or all out.
+                if (upd) {
+                    const uint32_t bal = __ballot_sync(0xffffffffu, changed);
+                    if ((threadIdx.x & 31) == 0) {
+                        chg[j >> 5] = bal;
+                        if (bal) any = 1u;
+                    }
+                }
+            }
+            if (!upd) continue;
             __syncthreads();  // chg and any complete
-            if (any)
-                adj_dilate_brick<S>(V, b, chg, threadIdx.x, blockDim.x, V.nbh, plan_act(a, k + 1), plan_flag(a, k + 1),
-                                    plan_list(a, k + 1), &a.counts[k + 1]);
+            if (any) adj_dilate_brick<S>(V, b, chg, threadIdx.x, blockDim.x, plan_act(a, k + 1), plan_flag(a, k + 1));
             if (cap) {
-                if (fresh && atomicExch(&a.need[nbr], cap) != cap) {
+                if (won) {
                     capl[atomicAdd(&ncap, 1u)] = nbr;
                     plan_need(a, (int)cap - 1)[atomicAdd(&a.ncount[cap - 1], 1u)] = nbr;
                 }
@@ -297,6 +312,7 @@ __device__ uint32_t adj_forward_step(const AdjPlan& a, int k, const float* in, f
                 }
             }
         }
+        if (upd_mine) plan_list(a, k)[pos] = (uint32_t)mb;
     }
     __syncthreads();  // the shared words are reused by the next call
     return mine;
@@ -344,13 +360,13 @@ __device__ __forceinline__ void restore_item(const AdjPlan& a, int s, int kr, fl
     const int j = pt.voxel(i);
     const int3 p = voxel_of<S>(V, b, j);
     if (p.x < V.nx && p.y < V.ny && p.z < V.nz)
-        dst[((size_t)p.z * V.py + p.y) * V.px + p.x] = plan_log(a, s, first ? kr : kr + 1)[(size_t)pos * S::VOX + j];
+        dst[((size_t)p.z * V.py + p.y) * V.px + p.x] = plan_log(a, s, first ? kr : kr + 1)[(size_t)b * S::VOX + j];
 }
 
 // One item of recomputed iteration t of segment s (list_t then, for t past
 // the segment's first iteration, list_{t-1}; n = count_t): the bricks of
 // list_t written whole into out (active voxels updated from in, the others
-// copied) and logged as they were (brick i at log_t + i * VOX); the bricks
+// copied) and logged as they were (brick b at log_t + b * VOX); the bricks
 // of list_{t-1} outside list_t copied from in to out.
 template <class S>
 __device__ __forceinline__ void rec_item(const AdjPlan& a, int s, int t, const float* in, float* out, uint32_t n,
@@ -369,7 +385,7 @@ __device__ __forceinline__ void rec_item(const AdjPlan& a, int s, int t, const f
         out[idx] = c;
         return;
     }
-    plan_log(a, s, t)[(size_t)bi * S::VOX + j] = c;
+    plan_log(a, s, t)[(size_t)b * S::VOX + j] = c;
     if (!((plan_act(a, t)[(size_t)b * S::WORDS + (j >> 6)] >> (j & 63)) & 1ull)) {
         out[idx] = c;
         return;
@@ -766,7 +782,7 @@ __device__ void adj_rev_phase(const AdjPlan& a, const RevPhase& ph, double* s3) 
 template <class S>
 __global__ void __launch_bounds__(kAdjThreads) k_adj_forward(const AdjPlan a) {
     cg::grid_group grid = cg::this_grid();
-    adj_list0<S>(plan_act(a, 0), plan_flag(a, 0), plan_list(a, 0), &a.counts[0], a.nb);
+    adj_flag0<S>(plan_act(a, 0), plan_flag(a, 0), a.nb);
     grid.sync();
     uint32_t mine = 0;
     const int last = a.nck - 1;
