@@ -583,6 +583,22 @@ __device__ __forceinline__ void rev_voxel(const AdjPlan& a, const float* phi, fl
     const int3 pv = voxel_of<S>(V, b, j);
     if (pv.x >= V.nx || pv.y >= V.ny || pv.z >= V.nz) return;
     const size_t idx = ((size_t)pv.z * V.py + pv.y) * V.px + pv.x;
+    auto at = [&](int dx, int dy, int dz) {
+        return ((size_t)clampi(pv.z + dz, V.nz) * V.py + clampi(pv.y + dy, V.ny)) * V.px + clampi(pv.x + dx, V.nx);
+    };
+    // Every load of the voxel is issued before any store or branch, by the
+    // lanes outside A_k too (a warp runs both kinds of lane one after the
+    // other, so this keeps it to one round trip): the stencil of phi_k (the
+    // update's 19 points), I, the bias, lambda's two parts.
+    float st[3][3][3];
+#pragma unroll
+    for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+        for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+            for (int dx = -1; dx <= 1; ++dx)
+                st[dz + 1][dy + 1][dx + 1] = (dx != 0 && dy != 0 && dz != 0) ? 0.0f : phi[at(dx, dy, dz)];
+    const float I = V.img[idx], bias = V.bias ? V.bias[idx] : 0.0f;
     const float x = a.lam[idx], z = zin[idx];
     const float u = x + z;
     if (z != 0.0f) zin[idx] = 0.0f;
@@ -592,15 +608,12 @@ __device__ __forceinline__ void rev_voxel(const AdjPlan& a, const float* phi, fl
     }
     if (x != 0.0f) a.lam[idx] = 0.0f;
     if (u == 0.0f) return;
-    auto at = [&](int dx, int dy, int dz) {
-        return ((size_t)clampi(pv.z + dz, V.nz) * V.py + clampi(pv.y + dy, V.ny)) * V.px + clampi(pv.x + dx, V.nx);
-    };
-    auto P = [&](int dx, int dy, int dz) { return phi[at(dx, dy, dz)]; };
+    auto P = [&](int dx, int dy, int dz) { return st[dz + 1][dy + 1][dx + 1]; };
     auto add = [&](int dx, int dy, int dz, float g) {
         if (g != 0.0f) atomicAdd(&zout[at(dx, dy, dz)], g);
     };
     float g4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-    ns_update_vjp_f32(P, add, V.img[idx], V.bias ? V.bias[idx] : 0.0f, V, u, g4);
+    ns_update_vjp_f32(P, add, I, bias, V, u, g4);
     s3[0] += g4[0];
     s3[1] += g4[1];
     s3[2] += g4[2];
@@ -698,16 +711,16 @@ __device__ void adj_rev_phase(const AdjPlan& a, const RevPhase& ph, double* s3);
 // voxels are 16-byte aligned: px is a multiple of 8; padding voxels hold
 // Z = 0 and stay as they are).  Warp w scans bricks w + l * NW (lane l; NW
 // warps), so a cluster of consecutive marked bricks spreads over the warps;
-// every mark is cleared for reverse iteration k - 2.
+// every mark is cleared for reverse iteration k - 2.  Warp w of the nw
+// warps doing this part.
 template <class S>
-__device__ void adj_rev_touched(const AdjPlan& a, int k) {
+__device__ void adj_rev_touched(const AdjPlan& a, int k, uint32_t w, uint32_t nw) {
     const NsVol& V = a.V;
     const int p = (k + 1) & 1;
     float4* const lam4 = reinterpret_cast<float4*>(a.lam);
     float4* const z4 = reinterpret_cast<float4*>(a.Z[p]);
     uint32_t* flag = a.flagT[k & 1];
     const uint32_t* in_a = plan_flag(a, k);
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5, w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     constexpr int G = S::VOX / 4, PER = (G + 31) / 32;
     for (uint64_t base = 0; base < a.nb; base += 32ull * nw) {
@@ -751,8 +764,19 @@ __device__ void adj_rev_touched(const AdjPlan& a, int k) {
 
 template <class S>
 __device__ void adj_rev_phase(const AdjPlan& a, const RevPhase& ph, double* s3) {
-    if (ph.k >= 0) adj_rev_touched<S>(a, ph.k);
     const Parts<S> pt(0);
+    // Part two of the reverse iteration goes to the warps of the groups
+    // without a brick part of A_k (all warps when every group has one), so
+    // the parts of A_k, the longest work of the phase, start at once.
+    if (ph.k >= 0) {
+        constexpr uint32_t WPG = Parts<S>::TPG / 32;
+        const uint32_t wig = (uint32_t)pt.t / 32;
+        if (ph.nA < pt.nslots) {
+            if (pt.slot >= ph.nA) adj_rev_touched<S>(a, ph.k, (pt.slot - ph.nA) * WPG + wig, (pt.nslots - ph.nA) * WPG);
+        } else {
+            adj_rev_touched<S>(a, ph.k, pt.slot * WPG + wig, pt.nslots * WPG);
+        }
+    }
     const uint32_t nAC = ph.nA + ph.nC, total = nAC + ph.nR;
     for (uint32_t it = pt.slot; it < total; it += pt.nslots) {
         if (it < ph.nA) {
