@@ -142,7 +142,8 @@ def sum_over_ranks(ws, value: float) -> float:
 # the key's first field (profiles/k_ns_persistent_config2_256.md gives the
 # capture); a build from other sources reports null rather than a stale
 # figure.
-DRAM_TRAFFIC = {("06ccbd0ddc59", "config2_256", 8, 8, 8, 256): 16036864}
+DRAM_TRAFFIC = {("06ccbd0ddc59", "config2_256", 8, 8, 8, 256): 16036864,
+                ("d62cdf76a89c", "config2_256", 8, 8, 8, 256): 15937792}
 KERNEL_SOURCES = ("ns_kernels.cuh", "ns_engine.cu", "tma.cuh", "common.cuh")
 
 
