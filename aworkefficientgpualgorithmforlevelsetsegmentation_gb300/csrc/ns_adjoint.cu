@@ -104,6 +104,7 @@ struct AdjPlan {
     uint32_t* counts;           // [K+1]
     uint32_t* flagT[2];         // [NB]: bricks reverse iteration k scatters into, in flagT[(k - 1) & 1]
     uint32_t* need;             // [NB]: s + 1 once segment s's checkpoint holds the brick
+    uint32_t* reached;          // [NB]: within one brick of some A_k (lambda is read there only)
     uint32_t* nlist0;           // [nck - 1][NB]: the bricks of checkpoint s
     uint32_t* ncount;           // [nck]
     double* gsum;               // [8]: soft-Dice sums in 4..6
@@ -197,7 +198,8 @@ __device__ __forceinline__ void adj_dilate_brick(const NsVol& V, uint32_t b, con
 // brick's changed voxels are dilated into A_{k+1} by the same block, which
 // marks the bricks reached in flag_{k+1}.  With log (the last segment):
 // brick b of A_k is logged as it was before the update (in) at log + b *
-// VOX.  With cap = s + 1 (segment s has a checkpoint): the 27 bricks around
+// VOX.  Every brick within one brick of A_k is marked in `reached`.  With
+// cap = s + 1 (segment s has a checkpoint): the 27 bricks around
 // each brick of A_k (the update's reads and writes, a superset) join the
 // segment's checkpoint the first time the segment reaches them, copied from
 // in: a brick no earlier iteration of the segment reached still holds phi at
@@ -250,15 +252,18 @@ __device__ uint32_t adj_forward_step(const AdjPlan& a, int k, const float* in, f
             }
             // Thread r < 27 claims neighbour r for the checkpoint before the
             // update (the atomic's latency hides behind it).
+            // The 27 bricks around are marked as reached (the reverse reads
+            // lambda there only).
             uint32_t nbr = 0u;
             bool won = false;
-            if (upd && cap && threadIdx.x < 27) {
+            if (upd && threadIdx.x < 27) {
                 const int ox = (int)threadIdx.x % 3 - 1, oy = ((int)threadIdx.x / 3) % 3 - 1,
                           oz = (int)threadIdx.x / 9 - 1;
                 const int bx = o.x / S::X + ox, by = o.y / S::Y + oy, bz = o.z / S::Z + oz;
                 if (bx >= 0 && by >= 0 && bz >= 0 && bx < V.nbx && by < V.nby && bz < V.nbz) {
                     nbr = b + (uint32_t)((oz * V.nby + oy) * V.nbx + ox);
-                    won = atomicExch(&a.need[nbr], cap) != cap;
+                    a.reached[nbr] = 1u;
+                    if (cap) won = atomicExch(&a.need[nbr], cap) != cap;
                 }
             }
             for (int j = threadIdx.x; j < S::VOX; j += blockDim.x) {
@@ -844,6 +849,9 @@ struct DiceArgs {
     int nx, ny, nz, px, py;
     uint32_t nparts;
     float tau;
+    const uint32_t* reached;  // [nb]: the bricks whose lambda_K is needed
+    uint32_t nb;
+    int bx, by, bz, nbx, nby;  // brick shape and grid
 };
 
 __device__ __forceinline__ float soft_mask(float phi, float tau) { return 1.0f / (1.0f + expf(phi / tau)); }
@@ -918,9 +926,12 @@ __global__ void __launch_bounds__(kDiceThreads) k_adj_dice(const DiceArgs d) {
     }
 }
 
-// lambda_K = dloss/dphi_K over the volume.  Every block adds the dice
-// blocks' sums in the same order (the same totals in every block and every
-// call); block 0 publishes them for the loss.
+// lambda_K = dloss/dphi_K on the bricks the reverse reads it at (those
+// within one brick of some A_k; elsewhere lambda passes through untouched to
+// lambda_0, which nothing reads).  Item i: group i mod G (four voxels of a
+// brick row) of brick i div G.  Every block adds the dice blocks' sums in
+// the same order (the same totals in every block and every call); block 0
+// publishes them for the loss.
 __global__ void __launch_bounds__(kDiceThreads) k_adj_lamk(const DiceArgs d) {
     __shared__ double tot[3];
     if (threadIdx.x < 32) {
@@ -951,7 +962,7 @@ __global__ void __launch_bounds__(kDiceThreads) k_adj_lamk(const DiceArgs d) {
     // dloss/ds = (2 st - 2 t den) / den^2 with den = sum s + sum t.
     const double den = tot[0] + tot[1], sst = tot[2];
     const float c_out = (float)(2.0 * sst / (den * den)), c_in = (float)(2.0 * sst / (den * den) - 2.0 / den);
-    const uint32_t q4 = (uint32_t)(d.nx + 3) / 4, n = (uint32_t)d.ny * (uint32_t)d.nz * q4;
+    const uint32_t G = (uint32_t)(d.bx * d.by * d.bz) / 4, n = d.nb * G;
     const uint32_t nt = gridDim.x * blockDim.x;
     for (uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += kDiceUnroll * nt) {
         float4 f[kDiceUnroll];
@@ -962,10 +973,18 @@ __global__ void __launch_bounds__(kDiceThreads) k_adj_lamk(const DiceArgs d) {
         for (int u = 0; u < kDiceUnroll; ++u) {
             const uint32_t i = i0 + u * nt;
             x0[u] = 0xFFFFFFFFu;
-            if (i < n) {
-                x0[u] = dice_group(d, q4, i, &g[u]);
-                f[u] = reinterpret_cast<const float4*>(d.phi)[g[u]];
-                m[u] = reinterpret_cast<const uchar4*>(d.tgt)[g[u]];
+            if (i < n && d.reached[i / G]) {
+                const uint32_t b = i / G, j = (i - b * G) * 4;
+                const uint32_t kx = b % (uint32_t)d.nbx, r = b / (uint32_t)d.nbx;
+                const uint32_t ky = r % (uint32_t)d.nby, kz = r / (uint32_t)d.nby;
+                const uint32_t x = kx * d.bx + j % d.bx, y = ky * d.by + (j / d.bx) % d.by,
+                               z = kz * d.bz + j / (d.bx * d.by);
+                if (y < (uint32_t)d.ny && z < (uint32_t)d.nz) {
+                    x0[u] = x;
+                    g[u] = (((uint64_t)z * d.py + y) * d.px + x) / 4;
+                    f[u] = reinterpret_cast<const float4*>(d.phi)[g[u]];
+                    m[u] = reinterpret_cast<const uchar4*>(d.tgt)[g[u]];
+                }
             }
         }
 #pragma unroll
@@ -1042,7 +1061,7 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     const uint64_t logb = al((uint64_t)nb * S::VOX * 4);
     const uint64_t total = nfields * al(P * 4) + (uint64_t)nsets * every * logb + (uint64_t)(K + 1) * al(mwords * 8) +
                            2 * (uint64_t)(K + 1) * al((uint64_t)nb * 4) + al((uint64_t)(K + 1) * 4) + al(P) +
-                           2 * al((uint64_t)nb * 4) + (uint64_t)(nck + 1) * al((uint64_t)nb * 4) + al((uint64_t)nck * 4) +
+                           2 * al((uint64_t)nb * 4) + (uint64_t)(nck + 2) * al((uint64_t)nb * 4) + al((uint64_t)nck * 4) +
                            al(8 * sizeof(double) + 8) + al((uint64_t)gr * 3 * sizeof(double)) +
                            al((uint64_t)ndice * 3 * sizeof(double));
     char* base = (char*)core.workspace(total);
@@ -1079,6 +1098,7 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     a.counts = (uint32_t*)carve((uint64_t)(K + 1) * 4);
     for (int q = 0; q < 2; ++q) a.flagT[q] = (uint32_t*)carve((uint64_t)nb * 4);
     a.need = (uint32_t*)carve((uint64_t)nb * 4);
+    a.reached = (uint32_t*)carve((uint64_t)nb * 4);
     a.nlist0 = (uint32_t*)carve((uint64_t)nb * 4);  // lstride apart, like the brick lists
     for (int q = 1; q < nck - 1; ++q) carve((uint64_t)nb * 4);
     a.ncount = (uint32_t*)carve((uint64_t)nck * 4);
@@ -1145,6 +1165,7 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
         LSS_CUDA(cudaMemsetAsync(a.flagT[q], 0, (uint64_t)nb * 4, st));
     }
     LSS_CUDA(cudaMemsetAsync(a.need, 0, (uint64_t)nb * 4, st));
+    LSS_CUDA(cudaMemsetAsync(a.reached, 0, (uint64_t)nb * 4, st));
     LSS_CUDA(cudaMemsetAsync(a.ncount, 0, (uint64_t)nck * 4, st));
     // Forward from the engine's current phi and active set: both buffers of
     // the pair hold phi_0 (the checkpoints fill as the forward reaches bricks).
@@ -1155,7 +1176,8 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     LSS_CUDA(cudaLaunchCooperativeKernel(kf, dim3(gf), dim3(kAdjThreads), params, 0, st));
     count_launch(owner);
     // The loss and lambda_K between the two.
-    DiceArgs d{a.fw[K & 1], a.tgt, a.lam, dpart, a.gsum, V.nx, V.ny, V.nz, V.px, V.py, (uint32_t)ndice, tau};
+    DiceArgs d{a.fw[K & 1], a.tgt, a.lam, dpart, a.gsum, V.nx, V.ny, V.nz, V.px, V.py, (uint32_t)ndice, tau,
+               a.reached, nb, S::X, S::Y, S::Z, V.nbx, V.nby};
     k_adj_dice<<<ndice, kDiceThreads, 0, st>>>(d);
     count_launch(owner);
     k_adj_lamk<<<owner->num_sms * 8, kDiceThreads, 0, st>>>(d);
