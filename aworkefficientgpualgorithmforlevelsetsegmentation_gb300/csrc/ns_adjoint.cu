@@ -850,6 +850,8 @@ struct DiceArgs {
     uint32_t nparts;
     float tau;
     const uint32_t* reached;  // [nb]: the bricks whose lambda_K is needed
+    float* z0;                // lambda's contribution fields, cleared there too
+    float* z1;
     uint32_t nb;
     int bx, by, bz, nbx, nby;  // brick shape and grid
 };
@@ -928,10 +930,11 @@ __global__ void __launch_bounds__(kDiceThreads) k_adj_dice(const DiceArgs d) {
 
 // lambda_K = dloss/dphi_K on the bricks the reverse reads it at (those
 // within one brick of some A_k; elsewhere lambda passes through untouched to
-// lambda_0, which nothing reads).  Item i: group i mod G (four voxels of a
-// brick row) of brick i div G.  Every block adds the dice blocks' sums in
-// the same order (the same totals in every block and every call); block 0
-// publishes them for the loss.
+// lambda_0, which nothing reads), with the two contribution fields cleared
+// on the same voxels (the reverse reads and scatters into them there only).
+// Item i: group i mod G (four voxels of a brick row) of brick i div G.
+// Every block adds the dice blocks' sums in the same order (the same totals
+// in every block and every call); block 0 publishes them for the loss.
 __global__ void __launch_bounds__(kDiceThreads) k_adj_lamk(const DiceArgs d) {
     __shared__ double tot[3];
     if (threadIdx.x < 32) {
@@ -999,6 +1002,8 @@ __global__ void __launch_bounds__(kDiceThreads) k_adj_lamk(const DiceArgs d) {
                 l[e] = x0[u] + e < (uint32_t)d.nx ? (mv[e] ? c_in : c_out) * (-s * (1.0f - s) / d.tau) : 0.0f;
             }
             reinterpret_cast<float4*>(d.lam)[g[u]] = make_float4(l[0], l[1], l[2], l[3]);
+            reinterpret_cast<float4*>(d.z0)[g[u]] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            reinterpret_cast<float4*>(d.z1)[g[u]] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         }
     }
 }
@@ -1160,10 +1165,7 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     LSS_CUDA(cudaMemsetAsync(a.act0 + a.astride, 0, (uint64_t)K * al(mwords * 8), st));  // act[1..K]
     LSS_CUDA(cudaMemsetAsync(a.flag0, 0, (uint64_t)(K + 1) * al((uint64_t)nb * 4), st));
     LSS_CUDA(cudaMemsetAsync(a.counts, 0, (uint64_t)(K + 1) * 4, st));
-    for (int q = 0; q < 2; ++q) {
-        LSS_CUDA(cudaMemsetAsync(a.Z[q], 0, P * 4, st));
-        LSS_CUDA(cudaMemsetAsync(a.flagT[q], 0, (uint64_t)nb * 4, st));
-    }
+    for (int q = 0; q < 2; ++q) LSS_CUDA(cudaMemsetAsync(a.flagT[q], 0, (uint64_t)nb * 4, st));
     LSS_CUDA(cudaMemsetAsync(a.need, 0, (uint64_t)nb * 4, st));
     LSS_CUDA(cudaMemsetAsync(a.reached, 0, (uint64_t)nb * 4, st));
     LSS_CUDA(cudaMemsetAsync(a.ncount, 0, (uint64_t)nck * 4, st));
@@ -1177,7 +1179,7 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     count_launch(owner);
     // The loss and lambda_K between the two.
     DiceArgs d{a.fw[K & 1], a.tgt, a.lam, dpart, a.gsum, V.nx, V.ny, V.nz, V.px, V.py, (uint32_t)ndice, tau,
-               a.reached, nb, S::X, S::Y, S::Z, V.nbx, V.nby};
+               a.reached, a.Z[0], a.Z[1], nb, S::X, S::Y, S::Z, V.nbx, V.nby};
     k_adj_dice<<<ndice, kDiceThreads, 0, st>>>(d);
     count_launch(owner);
     k_adj_lamk<<<owner->num_sms * 8, kDiceThreads, 0, st>>>(d);
