@@ -111,6 +111,10 @@ struct AdjPlan {
     double* gpart;              // [grid][3]: each block's dT, deps, dalpha
     unsigned long long* nact;   // active-voxel updates of the forward
     uint64_t fstride, astride, lstride, lgstride, P;
+    const float* phi0;                     // the engine's phi at the start
+    const unsigned long long* act_src;     // and its masks of A_0
+    uint64_t mwords;                       // mask words a set
+    uint64_t dbias_n;                      // floats of d_bias cleared (a multiple of 4)
     uint32_t nb;
     int32_t K, every, nck;
     float tau;
@@ -806,11 +810,50 @@ __device__ void adj_rev_phase(const AdjPlan& a, const RevPhase& ph, double* s3) 
     }
 }
 
+// The call's set-up, grid-stride over the whole grid (one pass instead of a
+// dozen memsets and copies): both fields of the forward's pair <- phi_0, the
+// recorded masks of A_0 <- the engine's, those of A_1..A_K, the membership
+// flags, counts, marks and sums <- 0, and d_bias <- 0.
+__device__ void adj_setup(const AdjPlan& a) {
+    const uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x, nt = (uint64_t)gridDim.x * blockDim.x;
+    const float4* src4 = reinterpret_cast<const float4*>(a.phi0);
+    float4* f0 = reinterpret_cast<float4*>(a.fw[0]);
+    float4* f1 = reinterpret_cast<float4*>(a.fw[1]);
+    for (uint64_t i = t0; i < a.P / 4; i += nt) {
+        const float4 v = src4[i];
+        f0[i] = v;
+        f1[i] = v;
+    }
+    const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+    // act_0 (mwords u64, copied) then act_1 .. act_K (astride u64 each, cleared).
+    for (uint64_t i = t0; i < a.mwords; i += nt) a.act0[i] = a.act_src[i];
+    uint4* act4 = reinterpret_cast<uint4*>(a.act0 + a.astride);
+    for (uint64_t i = t0; i < (uint64_t)a.K * a.astride / 2; i += nt) act4[i] = z;
+    uint4* flag4 = reinterpret_cast<uint4*>(a.flag0);
+    for (uint64_t i = t0; i < (uint64_t)(a.K + 1) * a.lstride / 4; i += nt) flag4[i] = z;
+    if (a.dbias) {
+        float4* d4 = reinterpret_cast<float4*>(a.dbias);
+        for (uint64_t i = t0; i < a.dbias_n / 4; i += nt) d4[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    for (uint64_t i = t0; i < a.nb; i += nt) {
+        a.flagT[0][i] = 0u;
+        a.flagT[1][i] = 0u;
+        a.need[i] = 0u;
+        a.reached[i] = 0u;
+    }
+    for (uint64_t i = t0; i <= (uint64_t)a.K; i += nt) a.counts[i] = 0u;
+    for (uint64_t i = t0; i < (uint64_t)a.nck; i += nt) a.ncount[i] = 0u;
+    for (uint64_t i = t0; i < 9; i += nt) a.gsum[i] = 0.0;  // the sums and the update count
+    for (uint64_t i = t0; i < 3ull * gridDim.x; i += nt) a.gpart[i] = 0.0;  // the reverse's grid is this one
+}
+
 // The forward: list_0, then K iterations; every segment but the last
 // builds its sparse checkpoint as it goes, the last one logs its bricks.
 template <class S>
 __global__ void __launch_bounds__(kAdjThreads) k_adj_forward(const AdjPlan a) {
     cg::grid_group grid = cg::this_grid();
+    adj_setup(a);
+    grid.sync();
     adj_flag0<S>(plan_act(a, 0), plan_flag(a, 0), a.nb);
     grid.sync();
     uint32_t mine = 0;
@@ -1159,21 +1202,13 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     a.V = V;
     const bool dbias_in_place = dbias && in_place(dbias);
     if (dbias_in_place) a.dbias = dbias;
-    if (a.dbias) LSS_CUDA(cudaMemsetAsync(a.dbias, 0, (dbias_in_place ? n : P) * 4, st));
-    LSS_CUDA(cudaMemsetAsync(a.gsum, 0, 8 * sizeof(double) + 8, st));
-    LSS_CUDA(cudaMemsetAsync(a.gpart, 0, (uint64_t)gr * 3 * sizeof(double), st));
-    LSS_CUDA(cudaMemsetAsync(a.act0 + a.astride, 0, (uint64_t)K * al(mwords * 8), st));  // act[1..K]
-    LSS_CUDA(cudaMemsetAsync(a.flag0, 0, (uint64_t)(K + 1) * al((uint64_t)nb * 4), st));
-    LSS_CUDA(cudaMemsetAsync(a.counts, 0, (uint64_t)(K + 1) * 4, st));
-    for (int q = 0; q < 2; ++q) LSS_CUDA(cudaMemsetAsync(a.flagT[q], 0, (uint64_t)nb * 4, st));
-    LSS_CUDA(cudaMemsetAsync(a.need, 0, (uint64_t)nb * 4, st));
-    LSS_CUDA(cudaMemsetAsync(a.reached, 0, (uint64_t)nb * 4, st));
-    LSS_CUDA(cudaMemsetAsync(a.ncount, 0, (uint64_t)nck * 4, st));
-    // Forward from the engine's current phi and active set: both buffers of
-    // the pair hold phi_0 (the checkpoints fill as the forward reaches bricks).
-    const float* phi0 = V.phi[core.parity()];
-    for (float* d : {a.fw[0], a.fw[1]}) LSS_CUDA(cudaMemcpyAsync(d, phi0, P * 4, cudaMemcpyDeviceToDevice, st));
-    LSS_CUDA(cudaMemcpyAsync(a.act0, core.masks(core.parity()), mwords * 8, cudaMemcpyDeviceToDevice, st));
+    // Everything else of the set-up (clears, the pair's copies of phi_0, the
+    // masks of A_0) is the forward kernel's first phase.
+    a.dbias_n = a.dbias ? (dbias_in_place ? n : P) : 0;
+    a.phi0 = V.phi[core.parity()];
+    a.act_src = core.masks(core.parity());
+    a.mwords = mwords;
+    LSS_REQUIRE(gf == gr, LSS_ERR_CUDA, "adjoint grids differ");
     void* params[] = {(void*)&a};
     LSS_CUDA(cudaLaunchCooperativeKernel(kf, dim3(gf), dim3(kAdjThreads), params, 0, st));
     count_launch(owner);
