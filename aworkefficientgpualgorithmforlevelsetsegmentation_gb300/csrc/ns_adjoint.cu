@@ -4,22 +4,28 @@
 // fixed, the soft-Dice loss of sigmoid(-phi/tau) against a target mask, and
 // its gradients with respect to T, eps, alpha and a per-voxel speed bias.
 //
-// Two cooperative launches, one per direction; the phases inside each are
-// separated by the cooperative-groups grid barrier, so a call costs two
-// launches instead of a few hundred dependent ones.  Work-efficient like the
-// forward engine: every iteration touches the bricks of its active set only.
+// A call is four launches: the forward and the reverse (cooperative, the
+// phases inside each separated by the cooperative-groups grid barrier) with
+// the two soft-Dice passes between them.  Work-efficient like the forward
+// engine: every iteration touches the bricks of its active set only.
 //
-// Forward (k_adj_forward).  The brick list of each A_k is built while
-// dilating (the first thread to put a word into a brick appends it; the
-// block that updates a brick dilates it) beside the recorded brick masks.
-// It runs over a ping-pong pair in which both buffers stay current:
-// iteration k writes the bricks of A_k whole (active voxels updated, the rest
-// copied) and copies across the bricks of A_{k-1} that left the set; the
-// changed voxels' ballot words are dilated into A_{k+1} exactly as in the
-// persistent kernel, so the recorded sets are the sparse engine's sets.  phi
-// is checkpointed at the start of every segment of `every` iterations but
-// the last; over the last segment the forward instead logs, per iteration
-// k, the bricks of A_k as they were before the update (phi_k there).
+// Forward (k_adj_forward).  Its first phase sets the call up (clears, the
+// pair's copies of phi_0, the masks of A_0).  Iteration k finds the bricks of
+// A_k by a scan of the flags iteration k-1 marked and records them in list_k
+// beside the recorded brick masks.  It runs over a ping-pong pair in which
+// both buffers stay current: iteration k writes the bricks of A_k whole
+// (active voxels updated, the rest copied) and copies across the bricks of
+// A_{k-1} that left the set; the changed voxels' ballot words are dilated
+// into A_{k+1} exactly as in the persistent kernel, so the recorded sets are
+// the sparse engine's sets.  Checkpoints are sparse: during segment s (of
+// `every` iterations) a brick joins checkpoint s the first time the segment
+// reaches it, copied while it still holds phi at the segment's start; the
+// last segment logs, per iteration k, the bricks of A_k as they were before
+// the update.  The bricks within one brick of some A_k are marked: lambda is
+// read there only.
+//
+// Loss (k_adj_dice, k_adj_lamk).  The soft-Dice sums over the volume, then
+// lambda_K on the marked bricks.
 //
 // States without dense copies.  phi_k and phi_{k+1} differ only inside the
 // bricks of A_k, so a field that holds phi_{k+2} becomes phi_k by writing
@@ -28,20 +34,19 @@
 // state t in pair[(t - base) & 1], that starts with its two highest states
 // and walks down two states at a time.
 //
-// Reverse (k_adj_reverse).  The soft-Dice sums and lambda_K, then segment by
-// segment from the last: the last segment runs on the forward's pair (phi_K,
-// phi_{K-1}) and its log.  Every other segment is recomputed from its
-// checkpoint (bit-identical, the arithmetic is deterministic) while the
-// segment after it runs backwards: the checkpoint and a copy of it form the
-// pair of a forward-style ping-pong that logs its bricks as it goes.  The
-// segment's iterations run backwards on one lambda field, in place:
-//   take:  U = lambda_{k+1} at the voxels of A_k, lambda = 0 there (lambda
-//          keeps lambda_{k+1} everywhere else: the pass-through), and the
-//          pair's other field stepped down to phi_k;
-//   vjp:   every active voxel v scatters U[v] through the transposed stencil
-//          Jacobian of the update onto its 19 stencil voxels (fp32 atomics);
-// the parameter gradients are summed per block in FP64 (the gradient-check
-// reduction) into the block's own slot and the bias gradient per voxel.
+// Reverse (k_adj_reverse).  Segment by segment from the last: the last
+// segment runs on the forward's pair (phi_K, phi_{K-1}) and its log.  Every
+// other segment is recomputed from its sparse checkpoint (bit-identical, the
+// arithmetic is deterministic) while the segment after it runs backwards:
+// the checkpoint and a copy of its bricks form the pair of a forward-style
+// ping-pong that logs its bricks as it goes.  lambda is kept as a base field
+// plus the last reverse iteration's scatter, lambda_{k+1} = lam + Z[(k+1)&1];
+// reverse iteration k folds Z into lam on the bricks it visits, moves
+// lambda_{k+1} of A_k's voxels through the transposed stencil Jacobian of the
+// update into the other Z (fp32 atomics) and marks the bricks it reached
+// (adj_rev_phase).  The parameter gradients are summed per thread and block
+// in FP64 (the gradient-check reduction) into the block's own slot, the bias
+// gradient per voxel.
 //
 // Data other blocks wrote earlier in the same launch is read with plain
 // loads after a grid barrier (its fence orders them), never through the
@@ -710,9 +715,6 @@ __device__ RevPhase rev_phase(const AdjPlan& a, int s, int j) {
     }
     return ph;
 }
-
-template <class S>
-__device__ void adj_rev_phase(const AdjPlan& a, const RevPhase& ph, double* s3);
 
 // Part two of reverse iteration k: the bricks marked in flagT[k & 1] that
 // are not in A_k hold no active voxel, so lambda_{k+1} passes through:
