@@ -18,7 +18,8 @@ struct NsArgs;
 
 struct BrickConfig {
     int bx, by, bz, threads;
-    int min_blocks = 0;  // block per brick: resident blocks per SM the registers allow (0: 1024 threads)
+    int min_blocks = 0;  // block per brick: resident blocks per SM the registers allow
+                         // (0: 1024 threads; 8^3 x 256: 3)
     int groups = 1;      // > 1: one block per SM with this many brick workers of `threads` threads
 };
 

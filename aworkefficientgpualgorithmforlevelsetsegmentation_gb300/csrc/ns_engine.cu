@@ -243,7 +243,8 @@ KernelSet warp_kernels_for() {
 const std::vector<BrickConfig>& brick_configs() {
     static const std::vector<BrickConfig> v = {
         {8, 8, 8, 256}, {8, 8, 8, 128}, {8, 8, 8, 512}, {8, 8, 4, 128}, {8, 8, 4, 256}, {4, 4, 4, 64},
-        {8, 8, 4, 32},  {8, 8, 8, 32},  {4, 4, 4, 32},  {8, 8, 8, 256, 5}, {8, 8, 8, 256, 0, 4}};
+        {8, 8, 4, 32},  {8, 8, 8, 32},  {4, 4, 4, 32},  {8, 8, 8, 256, 5}, {8, 8, 8, 256, 4},
+        {8, 8, 8, 256, 0, 4}};
     return v;
 }
 
@@ -255,7 +256,12 @@ static KernelSet kernels(const BrickConfig& c) {
     }
     if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 256 && c.min_blocks == 5)
         return kernels_for<8, 8, 8, 256, 5>();
-    if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 256) return kernels_for<8, 8, 8, 256>();
+    if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 256 && c.min_blocks == 4)
+        return kernels_for<8, 8, 8, 256, 4>();
+    // 8^3 x 256 by default three blocks per SM: 79 registers and no spill
+    // (four cap a thread at 64 and spill 32 bytes; 2 % slower to converge at
+    // 256^3).
+    if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 256) return kernels_for<8, 8, 8, 256, 3>();
     if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 128) return kernels_for<8, 8, 8, 128>();
     if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 512) return kernels_for<8, 8, 8, 512>();
     if (c.bx == 8 && c.by == 8 && c.bz == 4 && c.threads == 128) return kernels_for<8, 8, 4, 128>();
