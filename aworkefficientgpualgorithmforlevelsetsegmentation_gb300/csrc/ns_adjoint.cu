@@ -1,5 +1,5 @@
 // The differentiation form of LSS_MODE_NS (lss_adjoint_run): K unrolled
-// iterations of the spec update from the engine's current state, with
+// iterations of the LSS_MODE_NS update from the engine's current state, with
 // the active set of every iteration recorded in the forward pass and held
 // fixed, the soft-Dice loss of sigmoid(-phi/tau) against a target mask, and
 // its gradients with respect to T, eps, alpha and a per-voxel speed bias.

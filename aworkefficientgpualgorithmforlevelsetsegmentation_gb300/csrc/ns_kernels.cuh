@@ -145,7 +145,7 @@ struct Brick {
     static_assert(XY == 64 || VOX == 64, "mask word layout");
 };
 
-// The spec update of one voxel from the shared-memory halo tile.
+// The LSS_MODE_NS update of one voxel from the shared-memory halo tile.
 // P(dx,dy,dz) reads the tile around the voxel.  Mirrors ns_update() of the
 // FP64 oracle in fp32, with the central differences kept unscaled:
 //   X = 2 phi_x, Fxx = phi_xx, Fxy = 4 phi_xy, so

@@ -1,7 +1,7 @@
-// ORACLE — test infrastructure only (the FP64 checker of the GPU adjoint in
-// LSS_MODE_NS).  Nothing in the product links it.
+// ORACLE — test infrastructure only (the FP64 parity reference of the GPU
+// adjoint in LSS_MODE_NS).  Nothing in the product links it.
 //
-// Differentiation of K unrolled iterations of the spec update
+// Differentiation of K unrolled iterations of the LSS_MODE_NS update
 // (ns_update in ns_model.hpp) with the active set of every iteration recorded
 // in the forward pass and then held fixed:
 //   phi_{k+1}[v] = ns_update(phi_k)[v]  for v in A_k,   phi_k[v] otherwise;

@@ -1,7 +1,7 @@
-// ORACLE — test infrastructure only (the checker for LSS_MODE_NS, and the
-// timed CPU baseline of bench.py).  Nothing in the product links it.
+// ORACLE — test infrastructure only (the parity reference for LSS_MODE_NS,
+// and the timed CPU baseline of bench.py).  Nothing in the product links it.
 //
-// FP64 restatement of the sparse level-set iteration in its spec form:
+// FP64 restatement of the sparse level-set iteration in its LSS_MODE_NS form:
 //   phi <- clamp(phi + dt * (wc * kappa*|grad phi|  -  F * |grad phi|_upwind),
 //                phi_min, phi_max)
 //   kappa*|grad phi| = div(grad phi/|grad phi|) * |grad phi|  (central differences)

@@ -2,12 +2,13 @@
 
 ctypes wrapper of the CPU oracle (oracle/_build/liboracle.so).  Imported only
 by tests/, __graft_entry__.smoke() and bench.py's CPU legs, always as the
-checker or the timed CPU baseline, never as the thing measured or shipped.
+parity reference or the timed CPU baseline, never as the thing measured or
+shipped.
 
   RefOracle — the reference-faithful solver (ref_model.hpp), either with the
               restated kernels or, where oracle/_ref was built, with the
               reference's own kernel sources compiled for the CPU.
-  NsOracle  — the FP64 spec solver (ns_model.hpp).
+  NsOracle  — the FP64 LSS_MODE_NS solver (ns_model.hpp).
 """
 from __future__ import annotations
 
@@ -224,7 +225,7 @@ class RefOracle:
 
 
 class NsOracle:
-    """FP64 spec solver on the CPU (multi-threaded)."""
+    """FP64 LSS_MODE_NS solver on the CPU (multi-threaded)."""
 
     def __init__(self, image: np.ndarray, brick=(8, 8, 8), threads: int = 1):
         self._L = lib()

@@ -1,6 +1,6 @@
 // ORACLE — test infrastructure only.  Nothing in the product links, imports
 // or runs this file; tests, smoke() and bench.py's CPU legs use it as the
-// checker.
+// parity reference.
 //
 // CPU restatement of the reference's level-set solver path in its
 // reference-faithful form (LSS_MODE_REF):

@@ -14,7 +14,6 @@ Returns None when the reference sources are not mounted (the GPU machines).
 """
 from __future__ import annotations
 
-import json
 import os
 import re
 import subprocess
@@ -43,17 +42,10 @@ def rewrite(text: str) -> str:
 
 
 def reference_root() -> str | None:
-    """The reference checkout: $LSS_REFERENCE_ROOT, else the `reference_path`
-    recorded in the repository's benchmark spec; None when neither names an
-    existing directory."""
-    root = os.environ.get("LSS_REFERENCE_ROOT")
-    if not root:
-        try:
-            with open(os.path.join(REPO, "BASELINE.json")) as f:
-                root = json.load(f).get("reference_path")
-        except (OSError, ValueError):
-            root = None
-    return root if root and os.path.isdir(root) else None
+    """The reference checkout: $LSS_REFERENCE_ROOT, else a directory named
+    `reference` beside the repository; None when neither exists."""
+    root = os.environ.get("LSS_REFERENCE_ROOT") or os.path.join(os.path.dirname(REPO), "reference")
+    return root if os.path.isdir(root) else None
 
 
 def code_root() -> str | None:

@@ -1,6 +1,6 @@
 """LSS_MODE_NS on the GPU against the FP64 oracle (oracle/ns_model.hpp).
 
-Tolerances (spec parity criteria):
+Tolerances (the NS parity criteria):
   * one iteration from an identical state: max |phi_gpu - phi_fp64| <= 1e-4;
   * active lists: bit-exact (order included) given identical phi, i.e. the
     oracle's expansion rule applied to the GPU's own before/after values;

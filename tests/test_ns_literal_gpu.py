@@ -1,4 +1,4 @@
-"""LSS_MODE_NS with the data speed as the spec formula writes it
+"""LSS_MODE_NS with the data speed as the formula is written
 (lss_params.data_term = LSS_DATA_LITERAL: D = eps - |I - T| + bias, no
 division by eps, no clamp) against the FP64 oracle under the same reading.
 
