@@ -74,3 +74,26 @@ def test_oracle_run_covers_the_whole_run_in_segments():
     o.set_phi(cfg["phi0"])
     it = o.run(cfg["conv"]["rel"], cfg["conv"]["patience"], cfg["conv"]["max_iterations"])
     assert (o.updates, it) == (runs[0][0], runs[0][2])
+
+
+def test_kernel_hash_ignores_comments_and_tracks_code(tmp_path, monkeypatch):
+    """The DRAM traffic the bench reports is keyed by a hash of the persistent
+    kernel's sources without their comments: a comment edit keeps a capture,
+    a code edit drops it (the line then reports no traffic until the kernel
+    is captured again)."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    src = os.path.join(ROOT, "aworkefficientgpualgorithmforlevelsetsegmentation_gb300", "csrc")
+    pkg = tmp_path / "aworkefficientgpualgorithmforlevelsetsegmentation_gb300" / "csrc"
+    pkg.mkdir(parents=True)
+    for f in bench.KERNEL_SOURCES:
+        (pkg / f).write_text(open(os.path.join(src, f)).read())
+    monkeypatch.setattr(bench, "ROOT", str(tmp_path))
+    h0 = bench.kernel_source_hash()
+    first = bench.KERNEL_SOURCES[0]
+    text = (pkg / first).read_text()
+    (pkg / first).write_text(text + "\n// a comment\n\n")
+    assert bench.kernel_source_hash() == h0
+    (pkg / first).write_text(text + "\nstatic const int kUnused = 1;\n")
+    assert bench.kernel_source_hash() != h0
