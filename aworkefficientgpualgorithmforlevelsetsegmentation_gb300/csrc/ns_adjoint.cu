@@ -70,8 +70,10 @@ namespace {
 namespace cg = cooperative_groups;
 
 // Threads of the two cooperative launches (a voxel of an 8^3 brick each) and
-// their blocks per SM: an iteration holds a few hundred bricks, so one block
-// an SM keeps every SM busy, and fewer blocks make the grid barrier cheaper.
+// their blocks per SM: one block an SM keeps the grid barrier, paid every
+// phase, at one participant an SM (1.16 us measured at 152 x 512); the
+// reverse spreads its few dozen bricks an iteration over every SM in brick
+// parts.
 constexpr int kAdjThreads = 512;
 constexpr int kAdjBlocksPerSm = 1;
 
@@ -91,8 +93,8 @@ __device__ __forceinline__ int3 voxel_of(const NsVol& V, uint32_t b, int j) {
 
 // Everything one call works on.  Per-iteration arrays are evenly spaced in
 // the workspace: act[k] = act0 + k * astride words, list[k] = list0 +
-// k * lstride, flag[k] = flag0 + k * lstride; fields (checkpoints, the
-// recompute buffers, the forward's pair) are fstride floats apart.
+// k * lstride, flag[k] = flag0 + k * lstride; the checkpoints are fstride
+// floats apart, the brick logs lgstride.
 struct AdjPlan {
     NsVol V;                    // the one volume (brick_base 0)
     float* ck0;                 // checkpoint s < nck - 1 = ck0 + s * fstride (phi_{s * every}, sparse)
@@ -112,7 +114,7 @@ struct AdjPlan {
     uint32_t* reached;          // [NB]: within one brick of some A_k (lambda is read there only)
     uint32_t* nlist0;           // [nck - 1][NB]: the bricks of checkpoint s
     uint32_t* ncount;           // [nck]
-    double* gsum;               // [8]: soft-Dice sums in 4..6
+    double* gsum;               // [8]: the soft-Dice totals in 4..6 (nact follows)
     double* gpart;              // [grid][3]: each block's dT, deps, dalpha
     unsigned long long* nact;   // active-voxel updates of the forward
     uint64_t fstride, astride, lstride, lgstride, P;
@@ -259,10 +261,9 @@ __device__ uint32_t adj_forward_step(const AdjPlan& a, int k, const float* in, f
                 }
                 __syncthreads();
             }
-            // Thread r < 27 claims neighbour r for the checkpoint before the
-            // update (the atomic's latency hides behind it).
-            // The 27 bricks around are marked as reached (the reverse reads
-            // lambda there only).
+            // Thread r < 27 marks neighbour r as reached (the reverse reads
+            // lambda there only) and claims it for the checkpoint before the
+            // update, so the atomic's latency hides behind the update.
             uint32_t nbr = 0u;
             bool won = false;
             if (upd && threadIdx.x < 27) {
@@ -337,9 +338,8 @@ __device__ uint32_t adj_forward_step(const AdjPlan& a, int k, const float* in, f
 // holds GROUPS groups of TPG threads; item i of a phase (brick i / N, part
 // i mod N) goes to the group whose slot is i mod (GROUPS * grid), slot =
 // group * grid + (block + offset) mod grid.  So the parts of one brick run
-// on different SMs (an iteration holds a few dozen bricks of ~150 active
-// voxels each: one SM a brick would leave most SMs idle), and each kind of
-// work of a phase, with its own offset, starts on its own block.
+// on different SMs: an iteration holds a few dozen bricks of ~150 active
+// voxels each, and one SM a brick would leave most SMs idle.
 template <class S>
 struct Parts {
     static constexpr int TPG = S::VOX < 128 ? S::VOX : 128;
