@@ -144,16 +144,21 @@ def sum_over_ranks(ws, value: float) -> float:
 # figure.
 DRAM_TRAFFIC = {("c568962b6489", "config2_256", 8, 8, 8, 256): 15832320}
 KERNEL_SOURCES = ("ns_kernels.cuh", "ns_engine.cu", "tma.cuh", "common.cuh")
+# The same for one adjoint call on config 4 (its four kernels: the forward
+# with the call's set-up phase, the two soft-Dice passes, the reverse), from
+# the capture in profiles/k_adj_config4_192.md.
+ADJOINT_TRAFFIC = {("93bf2fa0813b", "config4_192"): 165688832}
+ADJOINT_SOURCES = ("ns_adjoint.cu", "ns_kernels.cuh", "common.cuh")
 
 
-def kernel_source_hash() -> str:
-    """Hash of the persistent kernel's sources with their // comments and
-    blank lines left out (a comment edit keeps a capture valid)."""
+def kernel_source_hash(files=KERNEL_SOURCES) -> str:
+    """Hash of the kernel sources with their // comments and blank lines
+    left out (a comment edit keeps a capture valid)."""
     import hashlib
     import re
     h = hashlib.sha256()
     csrc = os.path.join(ROOT, "aworkefficientgpualgorithmforlevelsetsegmentation_gb300", "csrc")
-    for f in KERNEL_SOURCES:
+    for f in files:
         with open(os.path.join(csrc, f)) as fh:
             for line in fh:
                 code = re.sub(r"//.*", "", line).rstrip()
@@ -697,7 +702,10 @@ def measure_adjoint(local, scale, steps, warmup):
                     "gpu_launches_per_call": int(launches_h), "same_result_as_device_buffers": same},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
-                         "bytes_per_update": ADJOINT_BYTES}, "steps": steps}
+                         "bytes_per_update": ADJOINT_BYTES,
+                         "algorithmic_bytes_per_call": ADJOINT_BYTES * int(g["active_voxel_iterations"]),
+                         "traffic_per_call": ADJOINT_TRAFFIC.get((kernel_source_hash(ADJOINT_SOURCES), cfg["name"])),
+                         "kernel_source_hash": kernel_source_hash(ADJOINT_SOURCES)}, "steps": steps}
 
 
 def run_adjoint(args, ws, rank, local):
