@@ -162,15 +162,15 @@ __device__ __forceinline__ SegPair seg_pair(const AdjPlan& a, int s) {
 // no particular order (each brick once), flag[k][b] = b is in it.  Brick
 // logs are indexed by brick: brick b of a log at b * VOX.
 
-// flag_0 from the recorded masks of A_0 (the first iteration's scan lists
-// its bricks).
+// flag_0 of every brick from the masks of A_0 (the first iteration's scan
+// lists its bricks).
 template <class S>
 __device__ __forceinline__ void adj_flag0(const unsigned long long* act, uint32_t* flag, uint32_t nb) {
     for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
         unsigned long long any = 0ull;
 #pragma unroll
         for (int w = 0; w < S::WORDS; ++w) any |= act[(size_t)b * S::WORDS + w];
-        if (any) flag[b] = 1u;
+        flag[b] = any ? 1u : 0u;
     }
 }
 
@@ -815,7 +815,7 @@ __device__ void adj_rev_phase(const AdjPlan& a, const RevPhase& ph, double* s3) 
 // The call's set-up, grid-stride over the whole grid (one pass instead of a
 // dozen memsets and copies): both fields of the forward's pair <- phi_0, the
 // recorded masks of A_0 <- the engine's, those of A_1..A_K, the membership
-// flags, counts, marks and sums <- 0, and d_bias <- 0.
+// flags of A_1..A_K, counts, marks and sums <- 0, and d_bias <- 0.
 __device__ void adj_setup(const AdjPlan& a) {
     const uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x, nt = (uint64_t)gridDim.x * blockDim.x;
     const float4* src4 = reinterpret_cast<const float4*>(a.phi0);
@@ -831,8 +831,9 @@ __device__ void adj_setup(const AdjPlan& a) {
     for (uint64_t i = t0; i < a.mwords; i += nt) a.act0[i] = a.act_src[i];
     uint4* act4 = reinterpret_cast<uint4*>(a.act0 + a.astride);
     for (uint64_t i = t0; i < (uint64_t)a.K * a.astride / 2; i += nt) act4[i] = z;
-    uint4* flag4 = reinterpret_cast<uint4*>(a.flag0);
-    for (uint64_t i = t0; i < (uint64_t)(a.K + 1) * a.lstride / 4; i += nt) flag4[i] = z;
+    // flag_1 .. flag_K (flag_0 is written whole by adj_flag0 in this phase).
+    uint4* flag4 = reinterpret_cast<uint4*>(a.flag0 + a.lstride);
+    for (uint64_t i = t0; i < (uint64_t)a.K * a.lstride / 4; i += nt) flag4[i] = z;
     if (a.dbias) {
         float4* d4 = reinterpret_cast<float4*>(a.dbias);
         for (uint64_t i = t0; i < a.dbias_n / 4; i += nt) d4[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -855,8 +856,7 @@ template <class S>
 __global__ void __launch_bounds__(kAdjThreads) k_adj_forward(const AdjPlan a) {
     cg::grid_group grid = cg::this_grid();
     adj_setup(a);
-    grid.sync();
-    adj_flag0<S>(plan_act(a, 0), plan_flag(a, 0), a.nb);
+    adj_flag0<S>(a.act_src, plan_flag(a, 0), a.nb);  // from the engine's masks: no wait for the copy
     grid.sync();
     uint32_t mine = 0;
     const int last = a.nck - 1;
