@@ -346,6 +346,13 @@ struct Parts {
     static constexpr int N = S::VOX / TPG;
     static constexpr int GROUPS = kAdjThreads / TPG;
     static_assert(kAdjThreads % TPG == 0, "groups tile the block");
+    // Items of the reverse iteration proper: with 128-thread groups, 64
+    // voxels an item and two threads a voxel (t and t + 64, in different
+    // warps, each half of the transposed Jacobian); else TPG voxels, one
+    // thread each.
+    static constexpr bool SPLIT = TPG == 128;
+    static constexpr int AV = SPLIT ? 64 : TPG;
+    static constexpr int NA = S::VOX / AV;
     uint32_t slot, nslots;
     int t;
     __device__ __forceinline__ explicit Parts(uint32_t offset) {
@@ -356,6 +363,10 @@ struct Parts {
     }
     // Brick voxel of item i for this thread.
     __device__ __forceinline__ int voxel(uint32_t i) const { return (int)(i % N) * TPG + t; }
+    // Brick voxel of reverse-iteration item i, and this thread's half of the
+    // Jacobian (-1: all of it).
+    __device__ __forceinline__ int avoxel(uint32_t i) const { return (int)(i % NA) * AV + (SPLIT ? (t & 63) : t); }
+    __device__ __forceinline__ int half() const { return SPLIT ? (t >> 6) : -1; }
 };
 
 // One item of the restore of phi_kr into dst (holding phi_{kr+2}) from the
@@ -427,10 +438,12 @@ __device__ __forceinline__ void seed_item(const AdjPlan& a, int s, const float* 
 // Vector-Jacobian product of ns_update_f32 at one voxel with upstream lam:
 // scatters dloss/dphi onto the stencil (add(dx, dy, dz, g)) and returns the
 // parameter terms in g4 = (T, eps, alpha, bias).  Same derivation as the FP64
-// oracle (oracle/ns_adjoint.hpp), in fp32.
+// oracle (oracle/ns_adjoint.hpp), in fp32.  part 0: the centre, face and
+// upwind terms; part 1: the cross-derivative and parameter terms; part 2:
+// all (two threads with parts 0 and 1 together do what one with part 2 does).
 template <class PF, class AF>
 __device__ __forceinline__ void ns_update_vjp_f32(PF P, AF add, float I, float bias, const NsVol& V, float lam,
-                                                  float* g4) {
+                                                  float* g4, int part = 2) {
     const float c = P(0, 0, 0);
     const float xm = P(-1, 0, 0), xp = P(1, 0, 0);
     const float ym = P(0, -1, 0), yp = P(0, 1, 0);
@@ -464,23 +477,29 @@ __device__ __forceinline__ void ns_update_vjp_f32(PF P, AF add, float I, float b
     const float gn = sqrtf(a * a + b * b + e * e + f * f + h * h + k * k);
     const float u = c + V.dt * (V.wc * curv - F * gn);
     if (u < V.lo || u > V.hi) return;  // clamped: no gradient
-    add(0, 0, 0, lam);
+    const bool p0 = part != 1, p1 = part != 0;
+    if (p0) add(0, 0, 0, lam);
     const float gcurv = lam * V.dt * V.wc, gF = -lam * V.dt * gn, ggn = -lam * V.dt * F;
     if (has_curv) {
         const float gnum = gcurv / g2, gg2 = -gcurv * curv / g2;
-        const float gcx = gnum * (2.0f * cx * (fyy + fzz) - 2.0f * (cy * fxy + cz * fxz)) + gg2 * 2.0f * cx;
-        const float gcy = gnum * (2.0f * cy * (fxx + fzz) - 2.0f * (cx * fxy + cz * fyz)) + gg2 * 2.0f * cy;
-        const float gcz = gnum * (2.0f * cz * (fxx + fyy) - 2.0f * (cx * fxz + cy * fyz)) + gg2 * 2.0f * cz;
-        const float gfxx = gnum * (cy * cy + cz * cz), gfyy = gnum * (cx * cx + cz * cz),
-                    gfzz = gnum * (cx * cx + cy * cy);
+        if (p0) {
+            const float gcx = gnum * (2.0f * cx * (fyy + fzz) - 2.0f * (cy * fxy + cz * fxz)) + gg2 * 2.0f * cx;
+            const float gcy = gnum * (2.0f * cy * (fxx + fzz) - 2.0f * (cx * fxy + cz * fyz)) + gg2 * 2.0f * cy;
+            const float gcz = gnum * (2.0f * cz * (fxx + fyy) - 2.0f * (cx * fxz + cy * fyz)) + gg2 * 2.0f * cz;
+            const float gfxx = gnum * (cy * cy + cz * cz), gfyy = gnum * (cx * cx + cz * cz),
+                        gfzz = gnum * (cx * cx + cy * cy);
+            add(1, 0, 0, 0.5f * gcx + gfxx);
+            add(-1, 0, 0, -0.5f * gcx + gfxx);
+            add(0, 1, 0, 0.5f * gcy + gfyy);
+            add(0, -1, 0, -0.5f * gcy + gfyy);
+            add(0, 0, 1, 0.5f * gcz + gfzz);
+            add(0, 0, -1, -0.5f * gcz + gfzz);
+            add(0, 0, 0, -2.0f * (gfxx + gfyy + gfzz));
+        }
+    }
+    if (has_curv && p1) {
+        const float gnum = gcurv / g2;
         const float gfxy = -2.0f * gnum * cx * cy, gfxz = -2.0f * gnum * cx * cz, gfyz = -2.0f * gnum * cy * cz;
-        add(1, 0, 0, 0.5f * gcx + gfxx);
-        add(-1, 0, 0, -0.5f * gcx + gfxx);
-        add(0, 1, 0, 0.5f * gcy + gfyy);
-        add(0, -1, 0, -0.5f * gcy + gfyy);
-        add(0, 0, 1, 0.5f * gcz + gfzz);
-        add(0, 0, -1, -0.5f * gcz + gfzz);
-        add(0, 0, 0, -2.0f * (gfxx + gfyy + gfzz));
         add(1, 1, 0, 0.25f * gfxy);
         add(1, -1, 0, -0.25f * gfxy);
         add(-1, 1, 0, -0.25f * gfxy);
@@ -494,7 +513,7 @@ __device__ __forceinline__ void ns_update_vjp_f32(PF P, AF add, float I, float b
         add(0, -1, 1, -0.25f * gfyz);
         add(0, -1, -1, 0.25f * gfyz);
     }
-    if (gn > 0.0f) {
+    if (p0 && gn > 0.0f) {
         const float s = ggn / gn;
         add(0, 0, 0, s * (a - b + e - f + h - k));
         add(-1, 0, 0, -s * a);
@@ -504,6 +523,7 @@ __device__ __forceinline__ void ns_update_vjp_f32(PF P, AF add, float I, float b
         add(0, 0, -1, -s * h);
         add(0, 0, 1, s * k);
     }
+    if (!p1) return;
     const float gDt = gF * V.wd;
     g4[3] += gDt;
     if (!dclamp) {
@@ -590,13 +610,20 @@ __device__ __forceinline__ void adj_mark_brick(const NsVol& V, uint32_t b, const
 // A_k) visits the bricks of A_k whole; part two (adj_rev_touched) the
 // marked bricks outside A_k.  Every voxel is read and written by one thread
 // only.
+//
+// half (Parts::half): -1, the thread does the voxel alone; 0 or 1, the
+// voxel's two threads of a 128-thread group (in different warps, so the
+// halves run side by side) both load, a barrier of the group orders every
+// load before the folds, then half 0 folds lambda and scatters part 0 of
+// the transposed Jacobian, half 1 scatters part 1 and adds the parameter
+// and bias gradients.  Every thread of a split group reaches the barrier.
 template <class S>
 __device__ __forceinline__ void rev_voxel(const AdjPlan& a, const float* phi, float* zin, float* zout, uint32_t b,
-                                          int j, bool in_a, double* s3) {
+                                          int j, bool in_a, double* s3, int half) {
     const NsVol& V = a.V;
     const int3 pv = voxel_of<S>(V, b, j);
-    if (pv.x >= V.nx || pv.y >= V.ny || pv.z >= V.nz) return;
-    const size_t idx = ((size_t)pv.z * V.py + pv.y) * V.px + pv.x;
+    const bool inside = pv.x < V.nx && pv.y < V.ny && pv.z < V.nz;
+    const size_t idx = inside ? ((size_t)pv.z * V.py + pv.y) * V.px + pv.x : 0;
     auto at = [&](int dx, int dy, int dz) {
         return ((size_t)clampi(pv.z + dz, V.nz) * V.py + clampi(pv.y + dy, V.ny)) * V.px + clampi(pv.x + dx, V.nx);
     };
@@ -605,29 +632,41 @@ __device__ __forceinline__ void rev_voxel(const AdjPlan& a, const float* phi, fl
     // other, so this keeps it to one round trip): the stencil of phi_k (the
     // update's 19 points), I, the bias, lambda's two parts.
     float st[3][3][3];
+    float I = 0.0f, bias = 0.0f, x = 0.0f, z = 0.0f;
+    if (inside) {
 #pragma unroll
-    for (int dz = -1; dz <= 1; ++dz)
+        for (int dz = -1; dz <= 1; ++dz)
 #pragma unroll
-        for (int dy = -1; dy <= 1; ++dy)
+            for (int dy = -1; dy <= 1; ++dy)
 #pragma unroll
-            for (int dx = -1; dx <= 1; ++dx)
-                st[dz + 1][dy + 1][dx + 1] = (dx != 0 && dy != 0 && dz != 0) ? 0.0f : phi[at(dx, dy, dz)];
-    const float I = V.img[idx], bias = V.bias ? V.bias[idx] : 0.0f;
-    const float x = a.lam[idx], z = zin[idx];
-    const float u = x + z;
-    if (z != 0.0f) zin[idx] = 0.0f;
-    if (!in_a) {
-        if (z != 0.0f) a.lam[idx] = u;
-        return;
+                for (int dx = -1; dx <= 1; ++dx)
+                    st[dz + 1][dy + 1][dx + 1] = (dx != 0 && dy != 0 && dz != 0) ? 0.0f : phi[at(dx, dy, dz)];
+        I = V.img[idx];
+        bias = V.bias ? V.bias[idx] : 0.0f;
+        x = a.lam[idx];
+        z = zin[idx];
     }
-    if (x != 0.0f) a.lam[idx] = 0.0f;
-    if (u == 0.0f) return;
+    // The group's 128 threads, barrier 1 + group (the non-aligned form: the
+    // lanes may reach it from the divergent loads above).
+    if (half >= 0) asm volatile("barrier.sync %0, 128;" ::"r"(1 + (int)(threadIdx.x >> 7)) : "memory");
+    if (!inside) return;
+    const float u = x + z;
+    if (half != 1) {
+        if (z != 0.0f) zin[idx] = 0.0f;
+        if (!in_a) {
+            if (z != 0.0f) a.lam[idx] = u;
+            return;
+        }
+        if (x != 0.0f) a.lam[idx] = 0.0f;
+    }
+    if (!in_a || u == 0.0f) return;
     auto P = [&](int dx, int dy, int dz) { return st[dz + 1][dy + 1][dx + 1]; };
     auto add = [&](int dx, int dy, int dz, float g) {
         if (g != 0.0f) atomicAdd(&zout[at(dx, dy, dz)], g);
     };
     float g4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-    ns_update_vjp_f32(P, add, I, bias, V, u, g4);
+    ns_update_vjp_f32(P, add, I, bias, V, u, g4, half < 0 ? 2 : half);
+    if (half == 0) return;
     s3[0] += g4[0];
     s3[1] += g4[1];
     s3[2] += g4[2];
@@ -680,11 +719,11 @@ __device__ RevPhase rev_phase(const AdjPlan& a, int s, int j) {
         const int k = s1 - 1 - j;
         ph.k = k;
         ph.phi = pr.f[(k - pr.base) & 1];
-        ph.nA = a.counts[k] * N;
+        ph.nA = a.counts[k] * (uint32_t)Parts<S>::NA;
         const Parts<S> pt(0);
         if (pt.slot < ph.nA) {
-            ph.b0 = plan_list(a, k)[pt.slot / N];
-            ph.w0 = plan_act(a, k)[(size_t)ph.b0 * S::WORDS + (pt.voxel(pt.slot) >> 6)];
+            ph.b0 = plan_list(a, k)[pt.slot / Parts<S>::NA];
+            ph.w0 = plan_act(a, k)[(size_t)ph.b0 * S::WORDS + (pt.avoxel(pt.slot) >> 6)];
         }
         // The pair's other field steps down to phi_{k-1} unless it holds it.
         if (k - 1 >= s0 && k - 1 < top - 1) {
@@ -794,11 +833,11 @@ __device__ void adj_rev_phase(const AdjPlan& a, const RevPhase& ph, double* s3) 
             const int k = ph.k, p = (k + 1) & 1;
             const bool first = it == pt.slot;
             const unsigned long long* act = plan_act(a, k);
-            const uint32_t b = first ? ph.b0 : plan_list(a, k)[it / Parts<S>::N];
-            const int jv = pt.voxel(it);
+            const uint32_t b = first ? ph.b0 : plan_list(a, k)[it / Parts<S>::NA];
+            const int jv = pt.avoxel(it);
             const unsigned long long wj = first ? ph.w0 : act[(size_t)b * S::WORDS + (jv >> 6)];
-            rev_voxel<S>(a, ph.phi, a.Z[p], a.Z[p ^ 1], b, jv, (wj >> (jv & 63)) & 1ull, s3);
-            if (it % Parts<S>::N == 0 && k > 0)
+            rev_voxel<S>(a, ph.phi, a.Z[p], a.Z[p ^ 1], b, jv, (wj >> (jv & 63)) & 1ull, s3, pt.half());
+            if (it % Parts<S>::NA == 0 && k > 0)
                 adj_mark_brick<S>(a.V, b, act, pt.t, Parts<S>::TPG, a.flagT[(k - 1) & 1]);
         } else if (it < nAC) {
             if (ph.r == 0) {
