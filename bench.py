@@ -147,7 +147,7 @@ KERNEL_SOURCES = ("ns_kernels.cuh", "ns_engine.cu", "tma.cuh", "common.cuh")
 # The same for one adjoint call on config 4 (its four kernels: the forward
 # with the call's set-up phase, the two soft-Dice passes, the reverse), from
 # the capture in profiles/k_adj_config4_192.md.
-ADJOINT_TRAFFIC = {("93bf2fa0813b", "config4_192"): 165688832}
+ADJOINT_TRAFFIC = {("8e47c831e2e6", "config4_192"): 165644595}
 ADJOINT_SOURCES = ("ns_adjoint.cu", "ns_kernels.cuh", "common.cuh")
 
 

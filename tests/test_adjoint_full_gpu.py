@@ -157,4 +157,5 @@ def test_autograd_adam_fit_192(case):
     # target (about 0.5 voxel an iteration at most, so 64 iterations cannot
     # fill the whole ellipsoid at this size).
     assert min(losses[-20:]) < losses[0] - 0.1, (losses[0], losses[-20:])
-    assert float(T) > 0.65, (float(T), float(eps), float(alpha))
+    T, eps, alpha = (float(t.detach()) for t in (T, eps, alpha))
+    assert T > 0.65, (T, eps, alpha)
