@@ -1,5 +1,5 @@
 """bench.py's reference arm (the CPU restatement timed on the host cores)
-prints the benchmark line the driver reads: checked on the CPU at a small
+prints its one-line JSON benchmark record: checked on the CPU at a small
 scale.  The arm names the same workload as the GPU arm (the same `config`
 dict, built by one function for both), times one whole seeding + run to
 convergence, and its process loads the oracle and the input generator but
