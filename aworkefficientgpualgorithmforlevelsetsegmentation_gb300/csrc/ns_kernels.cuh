@@ -618,11 +618,15 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
         tally.add(a.vstate, cnt, v, nact);
     }
     // Dilation of the changed mask into the 27 bricks around (and including)
-    // b: thread t computes word t % WORDS of neighbour t / WORDS and ORs it
-    // into the next masks; one thread per neighbour sets its membership bit
+    // b: each thread computes one word of one neighbour and ORs it into the
+    // next masks; one thread per neighbour sets its membership bit
     // (reductions, no round trip).  With one z-plane per mask word the 9 x
     // WORDS xy-dilated planes are computed once (phase 1) and each neighbour
-    // word is an OR of up to three of them.
+    // word is an OR of up to three of them; a neighbour above or below the
+    // brick then receives one word only (the plane next to the brick), so the
+    // 9 neighbours of the brick's own layer take WORDS threads each and the
+    // 18 others one thread each.  Otherwise thread t computes word t % WORDS
+    // of neighbour t / WORDS.
     if (any) {
         const uint32_t* cw = sm.chg[buf];
         auto W = [&](int q) -> uint64_t { return (uint64_t)cw[2 * q] | ((uint64_t)cw[2 * q + 1] << 32); };
@@ -642,14 +646,27 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
             }
             team.sync();  // uniform: `any` is
         }
-        constexpr int ROUNDS = (27 * S::WORDS + NT - 1) / NT;
+        constexpr int LAYER = kPlanes ? 9 * S::WORDS : 27 * S::WORDS;  // grouped items
+        constexpr int ITEMS = kPlanes ? LAYER + 18 : LAYER;
+        constexpr int ROUNDS = (ITEMS + NT - 1) / NT;
 #pragma unroll
         for (int r = 0; r < ROUNDS; ++r) {
             const int t = tid + r * NT;
-            const int slot = t / S::WORDS, w = t % S::WORDS;
+            // Item t: neighbour (ox, oy, oz), word w; `single`: the only
+            // word of its neighbour.
+            const bool single = t >= LAYER;
+            int slot, w;
+            if (!single) {
+                slot = (kPlanes ? 9 : 0) + t / S::WORDS;  // kPlanes: the layer oz = 0
+                w = t % S::WORDS;
+            } else {
+                const int q = t - LAYER;  // q < 9: the layer below, else above
+                slot = q < 9 ? q : q + 9;
+                w = q < 9 ? S::WORDS - 1 : 0;
+            }
             uint64_t x = 0ull;
             uint32_t nb = 0;
-            if (slot < 27) {
+            if (t < ITEMS) {
                 const int ox = slot % 3 - 1, oy = (slot / 3) % 3 - 1, oz = slot / 9 - 1;
                 const int bx = x0 / S::X + ox, by = y0 / S::Y + oy, bz = z0 / S::Z + oz;
                 // Voxels of the neighbour inside the volume along each axis
@@ -679,11 +696,13 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
                     if (x) atomicOr(&a.masks[p ^ 1u][(size_t)nb * S::WORDS + w], (unsigned long long)x);
                 }
             }
-            // The WORDS threads of a neighbour are adjacent lanes of one warp.
+            // The WORDS threads of a grouped neighbour are adjacent lanes of
+            // one warp (LAYER is a multiple of WORDS).
             const uint32_t bal = __ballot_sync(0xffffffffu, x != 0ull);
             const int lane = tid & 31, g0 = lane & ~(S::WORDS - 1);
             const uint32_t gmask = (S::WORDS >= 32 ? 0xffffffffu : ((1u << S::WORDS) - 1u)) << g0;
-            if (lane == g0 && (bal & gmask)) atomicOr(&a.bits[sn][nb >> 5], 1u << (nb & 31));
+            if (single ? x != 0ull : (lane == g0 && (bal & gmask)))
+                atomicOr(&a.bits[sn][nb >> 5], 1u << (nb & 31));
         }
     }
     // No barrier here: the next brick uses the other buffers, and this
