@@ -502,6 +502,102 @@ __device__ __forceinline__ void ns_fetch_mask(const NsArgs& a, NsSmem<S, NT>& sm
     }
 }
 
+// Phase 1 of a brick's dilation with one z-plane per mask word (XY == 64):
+// the 9 x WORDS xy-dilated planes of the changed mask cw (ballot words),
+// once each, into xy.  Threads t0, t0 + stride, ...
+template <class S>
+__device__ __forceinline__ void dilate_planes(const NsVol& V, const uint32_t* cw, unsigned long long* xy,
+                                              int t0, int stride) {
+    for (int t = t0; t < 9 * S::WORDS; t += stride) {
+        const int pair = t / S::WORDS, w = t % S::WORDS;
+        const int ox = pair % 3 - 1, oy = pair / 3 - 1;
+        const uint64_t c = (uint64_t)cw[2 * w] | ((uint64_t)cw[2 * w + 1] << 32);
+        uint64_t v;
+        if (V.nbh == 26) v = dil_y<S>(dil_x<S>(c, ox), oy);
+        else if (ox == 0 && oy == 0) v = dil_x<S>(c, 0) | dil_y<S>(c, 0);
+        else if (ox == 0 || oy == 0) v = ox ? dil_x<S>(c, ox) : dil_y<S>(c, oy);
+        else v = 0ull;
+        xy[t] = v;
+    }
+}
+
+// Phase 2: each thread computes one word of one neighbour of brick b (origin
+// x0, y0, z0) and ORs it into the next masks (parity p ^ 1); one thread per
+// neighbour sets its membership bit in bits[sn] (reductions, no round trip).
+// With one z-plane per mask word each neighbour word is an OR of up to three
+// xy-dilated planes, and a neighbour above or below the brick receives one
+// word only (the plane next to the brick): the 9 neighbours of the brick's
+// own layer take WORDS threads each and the 18 others one thread each.
+// Otherwise thread t computes word t % WORDS of neighbour t / WORDS.
+// Threads t0, t0 + STRIDE, ...; STRIDE is a multiple of 32 and every lane of
+// a calling warp takes part (ballots).
+template <class S, int STRIDE>
+__device__ __forceinline__ void dilate_scatter(const NsArgs& a, const NsVol& V, const uint32_t* cw,
+                                               const unsigned long long* xyp, uint32_t b, int x0, int y0,
+                                               int z0, uint32_t p, uint32_t sn, int t0) {
+    static_assert(STRIDE % 32 == 0, "whole warps");
+    auto W = [&](int q) -> uint64_t { return (uint64_t)cw[2 * q] | ((uint64_t)cw[2 * q + 1] << 32); };
+    constexpr bool kPlanes = S::XY == 64;  // one z-plane per mask word
+    constexpr int LAYER = kPlanes ? 9 * S::WORDS : 27 * S::WORDS;  // grouped items
+    constexpr int ITEMS = kPlanes ? LAYER + 18 : LAYER;
+    constexpr int ROUNDS = (ITEMS + STRIDE - 1) / STRIDE;
+#pragma unroll
+    for (int r = 0; r < ROUNDS; ++r) {
+        const int t = t0 + r * STRIDE;
+        // Item t: neighbour slot (ox, oy, oz) and word w; `single`: the only
+        // word of its neighbour.
+        const bool single = t >= LAYER;
+        int slot, w;
+        if (!single) {
+            slot = (kPlanes ? 9 : 0) + t / S::WORDS;  // kPlanes: the layer oz = 0
+            w = t % S::WORDS;
+        } else {
+            const int q = t - LAYER;  // q < 9: the layer below, else above
+            slot = q < 9 ? q : q + 9;
+            w = q < 9 ? S::WORDS - 1 : 0;
+        }
+        uint64_t x = 0ull;
+        uint32_t nb = 0;
+        if (t < ITEMS) {
+            const int ox = slot % 3 - 1, oy = (slot / 3) % 3 - 1, oz = slot / 9 - 1;
+            const int bx = x0 / S::X + ox, by = y0 / S::Y + oy, bz = z0 / S::Z + oz;
+            // Voxels of the neighbour inside the volume along each axis
+            // (bricks in the padding beyond the volume hold none).
+            const int lx = V.nx - bx * S::X, ly = V.ny - by * S::Y, lz = V.nz - bz * S::Z;
+            if (bx >= 0 && by >= 0 && bz >= 0 && lx > 0 && ly > 0 && lz > 0) {
+                if constexpr (kPlanes) {
+                    const unsigned long long* xy = xyp + ((oy + 1) * 3 + (ox + 1)) * S::WORDS;
+                    const bool center = ox == 0 && oy == 0;
+                    if (V.nbh == 26) {
+                        x = oz == 0 ? (xy[w] | (w > 0 ? xy[w - 1] : 0ull) | (w < S::WORDS - 1 ? xy[w + 1] : 0ull))
+                                    : (oz < 0 ? (w == S::WORDS - 1 ? xy[0] : 0ull)
+                                              : (w == 0 ? xy[S::WORDS - 1] : 0ull));
+                    } else if (oz == 0) {
+                        x = xy[w] | (center ? ((w > 0 ? W(w - 1) : 0ull) | (w < S::WORDS - 1 ? W(w + 1) : 0ull)) : 0ull);
+                    } else {
+                        x = center ? (oz < 0 ? (w == S::WORDS - 1 ? W(0) : 0ull)
+                                             : (w == 0 ? W(S::WORDS - 1) : 0ull))
+                                   : 0ull;
+                    }
+                } else {
+                    x = dilate_word<S>(cw, ox, oy, oz, w, V.nbh);
+                }
+                if (lx < S::X || ly < S::Y || lz < S::Z)
+                    x &= inside_mask<S>(w, min(lx, S::X), min(ly, S::Y), min(lz, S::Z));
+                nb = b + (int32_t)((oz * V.nby + oy) * V.nbx + ox);
+                if (x) atomicOr(&a.masks[p ^ 1u][(size_t)nb * S::WORDS + w], (unsigned long long)x);
+            }
+        }
+        // The WORDS threads of a grouped neighbour are adjacent lanes of one
+        // warp (LAYER is a multiple of WORDS).
+        const uint32_t bal = __ballot_sync(0xffffffffu, x != 0ull);
+        const int lane = t & 31, g0 = lane & ~(S::WORDS - 1);
+        const uint32_t gmask = (S::WORDS >= 32 ? 0xffffffffu : ((1u << S::WORDS) - 1u)) << g0;
+        if (single ? x != 0ull : (lane == g0 && (bal & gmask)))
+            atomicOr(&a.bits[sn][nb >> 5], 1u << (nb & 31));
+    }
+}
+
 // One brick of A_k by the whole block: wait for its loads, update its active
 // voxels in place of a copy of the tile centre (each thread its own voxels:
 // compacting the active voxels first measured slower, it costs two more block
@@ -618,92 +714,13 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
         tally.add(a.vstate, cnt, v, nact);
     }
     // Dilation of the changed mask into the 27 bricks around (and including)
-    // b: each thread computes one word of one neighbour and ORs it into the
-    // next masks; one thread per neighbour sets its membership bit
-    // (reductions, no round trip).  With one z-plane per mask word the 9 x
-    // WORDS xy-dilated planes are computed once (phase 1) and each neighbour
-    // word is an OR of up to three of them; a neighbour above or below the
-    // brick then receives one word only (the plane next to the brick), so the
-    // 9 neighbours of the brick's own layer take WORDS threads each and the
-    // 18 others one thread each.  Otherwise thread t computes word t % WORDS
-    // of neighbour t / WORDS.
+    // b (dilate_planes, dilate_scatter).
     if (any) {
-        const uint32_t* cw = sm.chg[buf];
-        auto W = [&](int q) -> uint64_t { return (uint64_t)cw[2 * q] | ((uint64_t)cw[2 * q + 1] << 32); };
-        constexpr bool kPlanes = S::XY == 64;  // one z-plane per mask word
-        if constexpr (kPlanes) {
-            // Phase 1: the 9 x WORDS xy-dilated planes, once each.
-            for (int t = tid; t < 9 * S::WORDS; t += NT) {
-                const int pair = t / S::WORDS, w = t % S::WORDS;
-                const int ox = pair % 3 - 1, oy = pair / 3 - 1;
-                const uint64_t c = W(w);
-                uint64_t v;
-                if (V.nbh == 26) v = dil_y<S>(dil_x<S>(c, ox), oy);
-                else if (ox == 0 && oy == 0) v = dil_x<S>(c, 0) | dil_y<S>(c, 0);
-                else if (ox == 0 || oy == 0) v = ox ? dil_x<S>(c, ox) : dil_y<S>(c, oy);
-                else v = 0ull;
-                sm.xy[t] = v;
-            }
+        if constexpr (S::XY == 64) {
+            dilate_planes<S>(V, sm.chg[buf], sm.xy, tid, NT);
             team.sync();  // uniform: `any` is
         }
-        constexpr int LAYER = kPlanes ? 9 * S::WORDS : 27 * S::WORDS;  // grouped items
-        constexpr int ITEMS = kPlanes ? LAYER + 18 : LAYER;
-        constexpr int ROUNDS = (ITEMS + NT - 1) / NT;
-#pragma unroll
-        for (int r = 0; r < ROUNDS; ++r) {
-            const int t = tid + r * NT;
-            // Item t: neighbour (ox, oy, oz), word w; `single`: the only
-            // word of its neighbour.
-            const bool single = t >= LAYER;
-            int slot, w;
-            if (!single) {
-                slot = (kPlanes ? 9 : 0) + t / S::WORDS;  // kPlanes: the layer oz = 0
-                w = t % S::WORDS;
-            } else {
-                const int q = t - LAYER;  // q < 9: the layer below, else above
-                slot = q < 9 ? q : q + 9;
-                w = q < 9 ? S::WORDS - 1 : 0;
-            }
-            uint64_t x = 0ull;
-            uint32_t nb = 0;
-            if (t < ITEMS) {
-                const int ox = slot % 3 - 1, oy = (slot / 3) % 3 - 1, oz = slot / 9 - 1;
-                const int bx = x0 / S::X + ox, by = y0 / S::Y + oy, bz = z0 / S::Z + oz;
-                // Voxels of the neighbour inside the volume along each axis
-                // (bricks in the padding beyond the volume hold none).
-                const int lx = V.nx - bx * S::X, ly = V.ny - by * S::Y, lz = V.nz - bz * S::Z;
-                if (bx >= 0 && by >= 0 && bz >= 0 && lx > 0 && ly > 0 && lz > 0) {
-                    if constexpr (kPlanes) {
-                        const unsigned long long* xy = sm.xy + ((oy + 1) * 3 + (ox + 1)) * S::WORDS;
-                        const bool center = ox == 0 && oy == 0;
-                        if (V.nbh == 26) {
-                            x = oz == 0 ? (xy[w] | (w > 0 ? xy[w - 1] : 0ull) | (w < S::WORDS - 1 ? xy[w + 1] : 0ull))
-                                        : (oz < 0 ? (w == S::WORDS - 1 ? xy[0] : 0ull)
-                                                  : (w == 0 ? xy[S::WORDS - 1] : 0ull));
-                        } else if (oz == 0) {
-                            x = xy[w] | (center ? ((w > 0 ? W(w - 1) : 0ull) | (w < S::WORDS - 1 ? W(w + 1) : 0ull)) : 0ull);
-                        } else {
-                            x = center ? (oz < 0 ? (w == S::WORDS - 1 ? W(0) : 0ull)
-                                                 : (w == 0 ? W(S::WORDS - 1) : 0ull))
-                                       : 0ull;
-                        }
-                    } else {
-                        x = dilate_word<S>(cw, ox, oy, oz, w, V.nbh);
-                    }
-                    if (lx < S::X || ly < S::Y || lz < S::Z)
-                        x &= inside_mask<S>(w, min(lx, S::X), min(ly, S::Y), min(lz, S::Z));
-                    nb = b + (int32_t)((oz * V.nby + oy) * V.nbx + ox);
-                    if (x) atomicOr(&a.masks[p ^ 1u][(size_t)nb * S::WORDS + w], (unsigned long long)x);
-                }
-            }
-            // The WORDS threads of a grouped neighbour are adjacent lanes of
-            // one warp (LAYER is a multiple of WORDS).
-            const uint32_t bal = __ballot_sync(0xffffffffu, x != 0ull);
-            const int lane = tid & 31, g0 = lane & ~(S::WORDS - 1);
-            const uint32_t gmask = (S::WORDS >= 32 ? 0xffffffffu : ((1u << S::WORDS) - 1u)) << g0;
-            if (single ? x != 0ull : (lane == g0 && (bal & gmask)))
-                atomicOr(&a.bits[sn][nb >> 5], 1u << (nb & 31));
-        }
+        dilate_scatter<S, NT>(a, V, sm.chg[buf], sm.xy, b, x0, y0, z0, p, sn, tid);
     }
     // No barrier here: the next brick uses the other buffers, and this
     // brick's buffers are reused two bricks later, behind the next brick's
@@ -1365,67 +1382,11 @@ __device__ __forceinline__ void ns_warp_brick(const NsArgs& a, WarpSlot<S>& sl, 
         tally.add(a.vstate, cnt, v, nact);
     }
     if (any) {
-        const uint32_t* cw = sl.chg;
-        auto W = [&](int q) -> uint64_t { return (uint64_t)cw[2 * q] | ((uint64_t)cw[2 * q + 1] << 32); };
-        constexpr bool kPlanes = S::XY == 64;  // one z-plane per mask word
-        if constexpr (kPlanes) {
-            // Phase 1: the 9 x WORDS xy-dilated planes, once each.
-            for (int t = lane; t < 9 * S::WORDS; t += 32) {
-                const int pair = t / S::WORDS, w = t % S::WORDS;
-                const int ox = pair % 3 - 1, oy = pair / 3 - 1;
-                const uint64_t c = W(w);
-                uint64_t v;
-                if (V.nbh == 26) v = dil_y<S>(dil_x<S>(c, ox), oy);
-                else if (ox == 0 && oy == 0) v = dil_x<S>(c, 0) | dil_y<S>(c, 0);
-                else if (ox == 0 || oy == 0) v = ox ? dil_x<S>(c, ox) : dil_y<S>(c, oy);
-                else v = 0ull;
-                sl.xy[t] = v;
-            }
+        if constexpr (S::XY == 64) {
+            dilate_planes<S>(V, sl.chg, sl.xy, lane, 32);
             __syncwarp();
         }
-        constexpr int ROUNDS = (27 * S::WORDS + 31) / 32;
-#pragma unroll
-        for (int r = 0; r < ROUNDS; ++r) {
-            const int t = lane + r * 32;
-            const int slot = t / S::WORDS, w = t % S::WORDS;
-            uint64_t x = 0ull;
-            uint32_t nb = 0;
-            if (slot < 27) {
-                const int ox = slot % 3 - 1, oy = (slot / 3) % 3 - 1, oz = slot / 9 - 1;
-                const int bx = o.x / S::X + ox, by = o.y / S::Y + oy, bz = o.z / S::Z + oz;
-                // Voxels of the neighbour inside the volume along each axis
-                // (bricks in the padding beyond the volume hold none).
-                const int lx = V.nx - bx * S::X, ly = V.ny - by * S::Y, lz = V.nz - bz * S::Z;
-                if (bx >= 0 && by >= 0 && bz >= 0 && lx > 0 && ly > 0 && lz > 0) {
-                    if constexpr (kPlanes) {
-                        const unsigned long long* xy = sl.xy + ((oy + 1) * 3 + (ox + 1)) * S::WORDS;
-                        const bool center = ox == 0 && oy == 0;
-                        if (V.nbh == 26) {
-                            x = oz == 0 ? (xy[w] | (w > 0 ? xy[w - 1] : 0ull) | (w < S::WORDS - 1 ? xy[w + 1] : 0ull))
-                                        : (oz < 0 ? (w == S::WORDS - 1 ? xy[0] : 0ull)
-                                                  : (w == 0 ? xy[S::WORDS - 1] : 0ull));
-                        } else if (oz == 0) {
-                            x = xy[w] | (center ? ((w > 0 ? W(w - 1) : 0ull) | (w < S::WORDS - 1 ? W(w + 1) : 0ull)) : 0ull);
-                        } else {
-                            x = center ? (oz < 0 ? (w == S::WORDS - 1 ? W(0) : 0ull)
-                                                 : (w == 0 ? W(S::WORDS - 1) : 0ull))
-                                       : 0ull;
-                        }
-                    } else {
-                        x = dilate_word<S>(cw, ox, oy, oz, w, V.nbh);
-                    }
-                    if (lx < S::X || ly < S::Y || lz < S::Z)
-                        x &= inside_mask<S>(w, min(lx, S::X), min(ly, S::Y), min(lz, S::Z));
-                    nb = b + (int32_t)((oz * V.nby + oy) * V.nbx + ox);
-                    if (x) atomicOr(&a.masks[p ^ 1u][(size_t)nb * S::WORDS + w], (unsigned long long)x);
-                }
-            }
-            // The WORDS lanes of a neighbour are adjacent lanes.
-            const uint32_t bal = __ballot_sync(0xffffffffu, x != 0ull);
-            const int g0 = lane & ~(S::WORDS - 1);
-            const uint32_t gmask = (S::WORDS >= 32 ? 0xffffffffu : ((1u << S::WORDS) - 1u)) << g0;
-            if (lane == g0 && (bal & gmask)) atomicOr(&a.bits[sn][nb >> 5], 1u << (nb & 31));
-        }
+        dilate_scatter<S, 32>(a, V, sl.chg, sl.xy, b, o.x, o.y, o.z, p, sn, lane);
     }
     __syncwarp();
 }
