@@ -795,10 +795,11 @@ def run_ref_mode(args, ws, rank, local):
 
 def run_tour(args, ws, rank, local):
     """Every kernel of the library once, on small inputs (for a per-kernel
-    ncu launch list with DRAM bytes): the REF engine (u8 volume: seed, steps
-    on the few- and many-active paths, read-backs, parameter estimate), the
-    NS engine (seed, sparse steps, dense steps, read-backs), the batched
-    form, the adjoint and the kernel-level compaction."""
+    ncu launch list): the REF engine (u8 volume: seed, steps on the few- and
+    many-active paths, read-backs, parameter estimate), the NS engine (seed,
+    sparse steps with a block per brick and with four brick workers a block,
+    dense steps, read-backs), the batched form (a warp per brick), the
+    adjoint and the kernel-level compaction."""
     import ctypes as C
     import torch
     import aworkefficientgpualgorithmforlevelsetsegmentation_gb300 as lss
@@ -826,6 +827,11 @@ def run_tour(args, ws, rank, local):
     s.freeze_current_segmentation()
     s.get_saveable_segmentation()
     s.step_dense(2)
+    w = lss.Segmenter(lss.MODE_NS, brick=(8, 8, 8), threads_per_brick=256, brick_workers=4)
+    w.load_volume(cfg["image"])
+    w.set_parameters(p.target, p.window, p.curvature, p.time_step, alpha_role=p.alpha_role)
+    w.set_seed_spheres(cfg["spheres"])
+    w.step(20)
     c4 = P.config4(0.25)
     a = lss.Segmenter(lss.MODE_NS, brick=(8, 8, 8), threads_per_brick=256)
     a.load_volume(c4["image"])
