@@ -111,7 +111,7 @@ struct AdjPlan {
     uint32_t* counts;           // [K+1]
     uint32_t* flagT[2];         // [NB]: bricks reverse iteration k scatters into, in flagT[(k - 1) & 1]
     uint32_t* need;             // [NB]: s + 1 once segment s's checkpoint holds the brick
-    uint32_t* reached;          // [NB]: within one brick of some A_k (lambda is read there only)
+    uint32_t* reached;          // [NB]: gen once within one brick of some A_k (lambda is read there only)
     uint32_t* nlist0;           // [nck - 1][NB]: the bricks of checkpoint s
     uint32_t* ncount;           // [nck]
     double* gsum;               // [8]: the soft-Dice totals in 4..6 (nact follows)
@@ -122,6 +122,8 @@ struct AdjPlan {
     const unsigned long long* act_src;     // and its masks of A_0
     uint64_t mwords;                       // mask words a set
     uint64_t dbias_n;                      // floats of d_bias cleared (a multiple of 4)
+    uint32_t gen;                          // this call's stamp in `reached` (>= 1)
+    int32_t partial;                       // 1: the pair holds phi_0 but in the bricks stamped gen - 1
     uint32_t nb;
     int32_t K, every, nck;
     float tau;
@@ -272,7 +274,7 @@ __device__ uint32_t adj_forward_step(const AdjPlan& a, int k, const float* in, f
                 const int bx = o.x / S::X + ox, by = o.y / S::Y + oy, bz = o.z / S::Z + oz;
                 if (bx >= 0 && by >= 0 && bz >= 0 && bx < V.nbx && by < V.nby && bz < V.nbz) {
                     nbr = b + (uint32_t)((oz * V.nby + oy) * V.nbx + ox);
-                    a.reached[nbr] = 1u;
+                    a.reached[nbr] = a.gen;
                     if (cap) won = atomicExch(&a.need[nbr], cap) != cap;
                 }
             }
@@ -854,16 +856,38 @@ __device__ void adj_rev_phase(const AdjPlan& a, const RevPhase& ph, double* s3) 
 // The call's set-up, grid-stride over the whole grid (one pass instead of a
 // dozen memsets and copies): both fields of the forward's pair <- phi_0, the
 // recorded masks of A_0 <- the engine's, those of A_1..A_K, the membership
-// flags of A_1..A_K, counts, marks and sums <- 0, and d_bias <- 0.
+// flags of A_1..A_K, counts, marks and sums <- 0, and d_bias <- 0.  A call
+// writes the pair in the bricks of its A_k only, all stamped in `reached`;
+// when the engine's phi and the workspace are those of the previous call
+// (partial), the pair still holds phi_0 elsewhere and only the bricks that
+// call stamped (gen - 1) are copied again, and the stamps stay (this call's
+// are gen); otherwise the whole field is copied and the stamps cleared.
+template <class S>
 __device__ void adj_setup(const AdjPlan& a) {
     const uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x, nt = (uint64_t)gridDim.x * blockDim.x;
     const float4* src4 = reinterpret_cast<const float4*>(a.phi0);
     float4* f0 = reinterpret_cast<float4*>(a.fw[0]);
     float4* f1 = reinterpret_cast<float4*>(a.fw[1]);
-    for (uint64_t i = t0; i < a.P / 4; i += nt) {
-        const float4 v = src4[i];
-        f0[i] = v;
-        f1[i] = v;
+    if (a.partial) {
+        // Item i: float4 q of brick b (rows of X / 4 float4, x fastest).
+        constexpr uint32_t Q = S::X / 4, PER = S::VOX / 4;
+        const uint32_t prev = a.gen - 1u;
+        for (uint64_t i = t0; i < (uint64_t)a.nb * PER; i += nt) {
+            const uint32_t b = (uint32_t)(i / PER), q = (uint32_t)(i % PER);
+            if (a.reached[b] != prev) continue;
+            const int3 o = brick_origin<S>(a.V, b + a.V.brick_base);
+            const uint32_t row = q / Q, ly = row % S::Y, lz = row / S::Y;
+            const uint64_t g = (((uint64_t)(o.z + lz) * a.V.py + (o.y + ly)) * a.V.px + o.x) / 4 + q % Q;
+            const float4 v = src4[g];
+            f0[g] = v;
+            f1[g] = v;
+        }
+    } else {
+        for (uint64_t i = t0; i < a.P / 4; i += nt) {
+            const float4 v = src4[i];
+            f0[i] = v;
+            f1[i] = v;
+        }
     }
     const uint4 z = make_uint4(0u, 0u, 0u, 0u);
     // act_0 (mwords u64, copied) then act_1 .. act_K (astride u64 each, cleared).
@@ -881,7 +905,7 @@ __device__ void adj_setup(const AdjPlan& a) {
         a.flagT[0][i] = 0u;
         a.flagT[1][i] = 0u;
         a.need[i] = 0u;
-        a.reached[i] = 0u;
+        if (!a.partial) a.reached[i] = 0u;
     }
     for (uint64_t i = t0; i <= (uint64_t)a.K; i += nt) a.counts[i] = 0u;
     for (uint64_t i = t0; i < (uint64_t)a.nck; i += nt) a.ncount[i] = 0u;
@@ -894,7 +918,7 @@ __device__ void adj_setup(const AdjPlan& a) {
 template <class S>
 __global__ void __launch_bounds__(kAdjThreads) k_adj_forward(const AdjPlan a) {
     cg::grid_group grid = cg::this_grid();
-    adj_setup(a);
+    adj_setup<S>(a);
     adj_flag0<S>(a.act_src, plan_flag(a, 0), a.nb);  // from the engine's masks: no wait for the copy
     grid.sync();
     uint32_t mine = 0;
@@ -938,6 +962,7 @@ struct DiceArgs {
     float* z1;
     uint32_t nb;
     int bx, by, bz, nbx, nby;  // brick shape and grid
+    uint32_t gen;              // the call's stamp in reached
 };
 
 __device__ __forceinline__ float soft_mask(float phi, float tau) { return 1.0f / (1.0f + expf(phi / tau)); }
@@ -1060,7 +1085,7 @@ __global__ void __launch_bounds__(kDiceThreads) k_adj_lamk(const DiceArgs d) {
         for (int u = 0; u < kDiceUnroll; ++u) {
             const uint32_t i = i0 + u * nt;
             x0[u] = 0xFFFFFFFFu;
-            if (i < n && d.reached[i / G]) {
+            if (i < n && d.reached[i / G] == d.gen) {
                 const uint32_t b = i / G, j = (i - b * G) * 4;
                 const uint32_t kx = b % (uint32_t)d.nbx, r = b / (uint32_t)d.nbx;
                 const uint32_t ky = r % (uint32_t)d.nby, kz = r / (uint32_t)d.nby;
@@ -1214,6 +1239,7 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     const uint64_t n = (uint64_t)V.nx * V.ny * V.nz;
     const bool flat = V.px == V.nx && V.py == V.ny;
     auto in_place = [&](const void* p) { return flat && device_memory(p) && (uintptr_t)p % 16 == 0; };
+    bool staged = false;  // fw[0] used as a staging buffer before the forward
     auto upload = [&](auto* dst, const auto* host) {
         using T = std::remove_cv_t<std::remove_pointer_t<decltype(host)>>;
         const T* src = (const T*)device_view(host);
@@ -1221,6 +1247,7 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
             T* stage = (T*)(void*)a.fw[0];
             LSS_CUDA(cudaMemcpyAsync(stage, host, n * sizeof(T), cudaMemcpyDefault, st));
             src = stage;
+            staged = true;
         }
         k_ns_scatter<<<grid, 256, 0, st>>>(dst, src, V.nx, V.ny, V.nz, V.px, V.py);
         count_launch(owner);
@@ -1249,13 +1276,24 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     a.phi0 = V.phi[core.parity()];
     a.act_src = core.masks(core.parity());
     a.mwords = mwords;
+    // The pair is copied whole unless the previous call left it holding
+    // phi_0 outside its stamped bricks: the engine unchanged since (epoch),
+    // the same fields, stamps and phi_0 (key), and fw[0] not used for
+    // staging since.  The record is void until this call has completed.
+    NsCore::AdjointRecord& rec = core.adjoint_record();
+    const void* key[4] = {a.fw[0], a.fw[1], a.reached, a.phi0};
+    const bool same = rec.valid && rec.epoch == core.epoch() && !staged &&
+                      std::equal(key, key + 4, rec.key) && rec.gen < 0xFFFFFF00u;
+    a.partial = same ? 1 : 0;
+    a.gen = same ? rec.gen + 1u : 1u;
+    rec.valid = false;
     LSS_REQUIRE(gf == gr, LSS_ERR_CUDA, "adjoint grids differ");
     void* params[] = {(void*)&a};
     LSS_CUDA(cudaLaunchCooperativeKernel(kf, dim3(gf), dim3(kAdjThreads), params, 0, st));
     count_launch(owner);
     // The loss and lambda_K between the two.
     DiceArgs d{a.fw[K & 1], a.tgt, a.lam, dpart, a.gsum, V.nx, V.ny, V.nz, V.px, V.py, (uint32_t)ndice, tau,
-               a.reached, a.Z[0], a.Z[1], nb, S::X, S::Y, S::Z, V.nbx, V.nby};
+               a.reached, a.Z[0], a.Z[1], nb, S::X, S::Y, S::Z, V.nbx, V.nby, a.gen};
     k_adj_dice<<<ndice, kDiceThreads, 0, st>>>(d);
     count_launch(owner);
     k_adj_lamk<<<owner->num_sms * 8, kDiceThreads, 0, st>>>(d);
@@ -1264,11 +1302,13 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     count_launch(owner);
     // d_bias back to the caller's unpadded layout (written in place when the
     // device can address it).
+    bool staged_out = false;  // fw[0] used as a staging buffer after the reverse
     if (dbias && !dbias_in_place) {
         float* dev = (float*)device_view(dbias);
         k_ns_gather<<<grid, 256, 0, st>>>(dev ? dev : a.fw[0], a.dbias, V.nx, V.ny, V.nz, V.px, V.py);
         count_launch(owner);
         if (!dev) LSS_CUDA(cudaMemcpyAsync(dbias, a.fw[0], n * 4, cudaMemcpyDefault, st));
+        staged_out = !dev;
     }
     double h[8];
     unsigned long long na = 0;
@@ -1277,6 +1317,10 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     LSS_CUDA(cudaMemcpyAsync(&na, a.nact, 8, cudaMemcpyDeviceToHost, st));
     LSS_CUDA(cudaMemcpyAsync(parts.data(), a.gpart, parts.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
     owner->sync();
+    rec.epoch = core.epoch();
+    std::copy(key, key + 4, rec.key);
+    rec.gen = a.gen;
+    rec.valid = !staged_out;
     // The blocks' parameter sums, added in block order (the same every call).
     double g3[3] = {0.0, 0.0, 0.0};
     for (int b = 0; b < gr; ++b)

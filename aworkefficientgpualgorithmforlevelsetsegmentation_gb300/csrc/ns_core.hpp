@@ -39,7 +39,11 @@ class NsCore {
     // New intensities for volume v (same dimensions): the state after
     // add_volume + configure, the buffers and the configuration kept.
     void reload_volume(int v, const float* data, const lss_params& p);
-    void set_params(int v, const lss_params& p) { vols_.at(v).p = p; upload_descriptors(); }
+    void set_params(int v, const lss_params& p) {
+        ++epoch_;
+        vols_.at(v).p = p;
+        upload_descriptors();
+    }
     void set_bias(int v, const float* bias);
     void configure(const BrickConfig& c);
     void init_active();
@@ -97,7 +101,21 @@ class NsCore {
         bool uniform = false;
         int3 dirty_lo{0, 0, 0}, dirty_hi{0, 0, 0};
     };
-    std::vector<VolHost>& vols() { return vols_; }
+    const std::vector<VolHost>& vols() const { return vols_; }
+    // Counts the calls that may change a volume's phi, masks, parameters or
+    // layout (every member above that is not a read; the adjoint changes
+    // nothing): the adjoint keeps copies of phi in its workspace between
+    // calls only while this count stays the same.
+    uint64_t epoch() const { return epoch_; }
+    // What the adjoint left in its workspace (ns_adjoint.cu): `valid` while
+    // the workspace stays in place (cleared when it is reallocated).
+    struct AdjointRecord {
+        bool valid = false;
+        uint64_t epoch = 0;
+        const void* key[4] = {nullptr, nullptr, nullptr, nullptr};
+        uint32_t gen = 0;
+    };
+    AdjointRecord& adjoint_record() { return adj_rec_; }
 
    private:
     size_t dyn_smem() const;
@@ -133,6 +151,8 @@ class NsCore {
     uint32_t* d_misc_ = nullptr;
     void* ws_ = nullptr;
     uint64_t ws_bytes_ = 0;
+    uint64_t epoch_ = 0;
+    AdjointRecord adj_rec_;
 };
 
 }  // namespace lss

@@ -285,6 +285,7 @@ void* NsCore::workspace(uint64_t bytes) {
         if (ws_) arena_.free_last(ws_);
         ws_ = nullptr;
         ws_bytes_ = 0;
+        adj_rec_ = AdjointRecord{};
         ws_ = arena_.alloc(bytes);
         ws_bytes_ = bytes;
     }
@@ -313,6 +314,7 @@ void NsCore::upload_padded(float* dst, const float* host, const VolHost& V, floa
 }
 
 int NsCore::add_volume(const float* data, int nx, int ny, int nz, const lss_params& p) {
+    ++epoch_;
     LSS_REQUIRE(data && nx > 0 && ny > 0 && nz > 0, LSS_ERR_INVALID_ARGUMENT, "bad volume");
     LSS_REQUIRE(vols_.size() < 4096, LSS_ERR_CAPACITY, "at most 4096 volumes per batch");
     VolHost v;
@@ -339,6 +341,7 @@ int NsCore::add_volume(const float* data, int nx, int ny, int nz, const lss_para
 }
 
 void NsCore::set_bias(int v, const float* bias) {
+    ++epoch_;
     VolHost& V = vols_.at(v);
     const uint64_t P = (uint64_t)V.px * V.py * V.pz;
     if (!bias) {
@@ -353,6 +356,7 @@ void NsCore::set_bias(int v, const float* bias) {
 }
 
 void NsCore::configure(const BrickConfig& c) {
+    ++epoch_;
     LSS_REQUIRE(!vols_.empty(), LSS_ERR_STATE, "no volume");
     owner_->sync();
     cfg_ = c;
@@ -490,6 +494,7 @@ NsArgs NsCore::args(uint32_t k0, int max_iters, const lss_conv* conv) const {
 // paper's initial active set, main.tex:217-231).  Both phi buffers are made
 // equal first.
 void NsCore::init_active() {
+    ++epoch_;
     LSS_REQUIRE(configured_, LSS_ERR_STATE, "not configured");
     cudaStream_t st = owner_->stream;
     // One volume whose phi is uniform outside a box (cleared, then seeded):
@@ -557,6 +562,7 @@ void NsCore::init_active() {
 }
 
 void NsCore::sphere_union(int v, float cx, float cy, float cz, float r) {
+    ++epoch_;
     VolHost& V = vols_.at(v);
     // Voxels farther than r + phi_max from the centre keep phi (<= phi_max).
     const double reach = (double)r + std::max(0.0f, V.p.phi_max) + 1.0;
@@ -583,6 +589,7 @@ void NsCore::sphere_union(int v, float cx, float cy, float cz, float r) {
 }
 
 void NsCore::set_phi(int v, const float* phi) {
+    ++epoch_;
     VolHost& V = vols_.at(v);
     V.uniform = false;
     upload_padded(V.phi[parity_], phi, V, nullptr);
@@ -591,6 +598,7 @@ void NsCore::set_phi(int v, const float* phi) {
 // Both buffers: phi is then uniform, which later seeding and active-set
 // rebuilds exploit (only the seeded box can differ).
 void NsCore::fill_phi(int v, float value) {
+    ++epoch_;
     VolHost& V = vols_.at(v);
     for (int q = 0; q < 2; ++q) {
         k_ns_fill<<<owner_->num_sms * 4, 256, 0, owner_->stream>>>(V.phi[q], (uint64_t)V.px * V.py * V.pz,
@@ -603,6 +611,7 @@ void NsCore::fill_phi(int v, float value) {
 }
 
 int NsCore::run(int max_iters, const lss_conv* conv, float* ms) {
+    ++epoch_;
     LSS_REQUIRE(initialized_, LSS_ERR_STATE, "no seed / phi set");
     if (max_iters <= 0) return 0;
     for (VolHost& v : vols_) v.uniform = false;
@@ -661,6 +670,7 @@ uint32_t NsCore::vol_parity(int v) {
 }
 
 void NsCore::reload_volume(int v, const float* data, const lss_params& p) {
+    ++epoch_;
     LSS_REQUIRE(configured_, LSS_ERR_STATE, "not configured");
     VolHost& V = vols_.at(v);
     cudaStream_t st = owner_->stream;
@@ -704,6 +714,7 @@ void NsCore::read_mask(int v, uint8_t* out) {
 }
 
 void NsCore::freeze(int v) {
+    ++epoch_;
     VolHost& V = vols_.at(v);
     const uint32_t p = vols_.size() == 1 ? parity_ : vol_parity(v);
     const uint64_t n = (uint64_t)V.nx * V.ny * V.nz;
@@ -719,6 +730,7 @@ void NsCore::freeze(int v) {
 }
 
 void NsCore::clear_frozen(int v) {
+    ++epoch_;
     VolHost& V = vols_.at(v);
     if (V.frozen) LSS_CUDA(cudaMemsetAsync(V.frozen, 0, (uint64_t)V.nx * V.ny * V.nz, owner_->stream));
     owner_->sync();
@@ -796,6 +808,7 @@ void NsCore::estimate(int v, float* t, float* w) {
 }
 
 float NsCore::dense_run(int iters) {
+    ++epoch_;
     LSS_REQUIRE(initialized_, LSS_ERR_STATE, "no seed / phi set");
     for (VolHost& v : vols_) v.uniform = false;
     cudaStream_t st = owner_->stream;

@@ -185,3 +185,54 @@ def test_gpu_adjoint_device_buffers_match_host_buffers(shape):
         assert rel(d[key], h[key]) <= 1e-5, (key, d[key], h[key])
     assert np.allclose(db.cpu().numpy(), h["d_bias"], rtol=1e-4, atol=1e-9)
     assert h["active_voxel_iterations"] == d["active_voxel_iterations"] > 0
+
+
+def test_gpu_adjoint_calls_on_one_engine_match_fresh_engines():
+    """Between calls the engine keeps the forward's two copies of phi_0 and
+    copies again only the bricks the previous call touched, while its phi is
+    unchanged and no host staging went through them: device buffers, so the
+    later calls take that path.  Each call equals the same call on a fresh
+    engine: the same call again, a call whose bias reaches other bricks, the
+    first bias once more, and a call after further iterations of the engine
+    (phi changed: full copies)."""
+    torch = pytest.importorskip("torch")
+    cfg = P.config4(0.25)
+    shape = cfg["image"].shape
+    dev = torch.device("cuda:0")
+    rng = np.random.default_rng(11)
+    b1 = (0.05 * rng.standard_normal(shape)).astype(np.float32)
+    b2 = (0.3 * rng.standard_normal(shape) + 0.2).astype(np.float32)
+    tgt = torch.from_numpy(cfg["target"]).to(dev)
+    K, every = 16, 4
+
+    def call(s, bias):
+        db = torch.empty(shape, dtype=torch.float32, device=dev)
+        g = s.adjoint(K, every, tgt, 0.5, bias=torch.from_numpy(bias).to(dev), d_bias_out=db)
+        torch.cuda.synchronize()
+        g["d_bias"] = db.cpu().numpy()
+        return g
+
+    def fresh(bias, steps=0):
+        e = make(cfg)
+        if steps:
+            e.step(steps)
+        return call(e, bias)
+
+    def same(g, h):
+        assert g["loss"] == h["loss"]
+        assert g["active_voxel_iterations"] == h["active_voxel_iterations"] > 0
+        for key in ("d_target", "d_window", "d_curvature"):
+            assert rel(g[key], h[key]) <= 1e-5, (key, g[key], h[key])
+        assert np.allclose(g["d_bias"], h["d_bias"], rtol=1e-4, atol=1e-9)
+
+    s = make(cfg)
+    r1 = call(s, b1)
+    same(r1, fresh(b1))
+    same(call(s, b1), r1)
+    r2 = call(s, b2)
+    assert r2["active_voxel_iterations"] != r1["active_voxel_iterations"]
+    same(r2, fresh(b2))
+    same(call(s, b1), r1)
+    s.step(3)
+    same(call(s, b1), fresh(b1, steps=3))
+    same(call(s, b2), fresh(b2, steps=3))
