@@ -42,9 +42,9 @@ class NsCore {
     void set_params(int v, const lss_params& p) {
         ++epoch_;
         vols_.at(v).p = p;
+        vols_.at(v).speed_stale = true;
         upload_descriptors();
     }
-    void set_bias(int v, const float* bias);
     void configure(const BrickConfig& c);
     void init_active();
     void sphere_union(int v, float cx, float cy, float cz, float r);
@@ -91,8 +91,8 @@ class NsCore {
         uint32_t brick_base = 0;
         float* phi[2] = {nullptr, nullptr};
         float* img = nullptr;
-        float* bias = nullptr;
-        float* bias_buf = nullptr;
+        float* speed = nullptr;     // ns_speed_f32 of every voxel (padded), made by refresh_speed
+        bool speed_stale = true;    // the intensities or parameters changed since
         lss_params p{};
         uint8_t* frozen = nullptr;  // unpadded u8 mask of frozen segmentations (device), once frozen
         unsigned long long iterations = 0;
@@ -120,11 +120,12 @@ class NsCore {
    private:
     size_t dyn_smem() const;
     void upload_descriptors();
+    void refresh_speed();  // the speed of every volume whose speed is stale
     void upload_padded(float* dst, const float* host, const VolHost& V, float* stage);
     NsArgs args(uint32_t k0, int max_iters, const lss_conv* conv) const;
 
     EngineBase* owner_;
-    DeviceArena arena_;        // volumes (phi, intensities, bias)
+    DeviceArena arena_;        // volumes (phi, intensities, speed)
     DeviceArena brick_arena_;  // brick-shape dependent state
     std::vector<VolHost> vols_;
     BrickConfig cfg_{8, 8, 8, 256};

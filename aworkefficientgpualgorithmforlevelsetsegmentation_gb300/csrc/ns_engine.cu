@@ -111,6 +111,21 @@ __global__ void k_ns_sphere_union(float* phi, int nx, int ny, int nz, int px, in
     }
 }
 
+// The speed of every voxel of a padded volume (the padding's intensities
+// are 0 and never updated), four voxels a thread and round: the part of the
+// update no iteration changes, with the update's own arithmetic (no bias:
+// only the adjoint takes one, per call).
+__global__ void k_ns_speed(const NsVol V, float* speed, uint64_t n4) {
+    const float4* I4 = reinterpret_cast<const float4*>(V.img);
+    float4* S4 = reinterpret_cast<float4*>(speed);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n4;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const float4 I = I4[i];
+        S4[i] = make_float4(ns_speed_f32(I.x, 0.0f, V), ns_speed_f32(I.y, 0.0f, V), ns_speed_f32(I.z, 0.0f, V),
+                            ns_speed_f32(I.w, 0.0f, V));
+    }
+}
+
 // Dense all-voxel update with the same arithmetic as the sparse engine: the
 // unconditional update the paper compares against (main.tex:523).  A block
 // covers a 32 x 8 column of the volume over zc planes and marches in z
@@ -164,7 +179,7 @@ __global__ void __launch_bounds__(256) k_ns_dense(const NsVol V, uint32_t p, int
                 const float* pl = dz < 0 ? pm : (dz > 0 ? pp : pc);
                 return pl[c0 + dy * (kDenseX + 2) + dx];
             };
-            dst[k] = ns_update_f32(P, V.img[k], V.bias ? V.bias[k] : 0.0f, V);
+            dst[k] = ns_update_speed_f32(P, V.speed[k], V);
         }
         __syncthreads();
         float* t = pm;
@@ -323,6 +338,7 @@ int NsCore::add_volume(const float* data, int nx, int ny, int nz, const lss_para
     v.p = p;
     const uint64_t P = (uint64_t)v.px * v.py * v.pz;
     v.img = (float*)arena_.alloc(P * 4);
+    v.speed = (float*)arena_.alloc(P * 4);
     v.phi[0] = (float*)arena_.alloc(P * 4);
     v.phi[1] = (float*)arena_.alloc(P * 4);
     cudaStream_t st = owner_->stream;
@@ -338,21 +354,6 @@ int NsCore::add_volume(const float* data, int nx, int ny, int nz, const lss_para
     vols_.push_back(v);
     configured_ = false;
     return (int)vols_.size() - 1;
-}
-
-void NsCore::set_bias(int v, const float* bias) {
-    ++epoch_;
-    VolHost& V = vols_.at(v);
-    const uint64_t P = (uint64_t)V.px * V.py * V.pz;
-    if (!bias) {
-        V.bias = nullptr;
-    } else {
-        if (!V.bias_buf) V.bias_buf = (float*)arena_.alloc(P * 4);
-        LSS_CUDA(cudaMemsetAsync(V.bias_buf, 0, P * 4, owner_->stream));
-        upload_padded(V.bias_buf, bias, V, nullptr);
-        V.bias = V.bias_buf;
-    }
-    upload_descriptors();
 }
 
 void NsCore::configure(const BrickConfig& c) {
@@ -401,7 +402,7 @@ void NsCore::configure(const BrickConfig& c) {
             encode_tmap_f32_3d(&maps[5 * i + 2 + q], v.phi[q], v.nx, v.ny, v.nz, v.px, pxy, c.bx, c.by,
                                c.bz);
         }
-        encode_tmap_f32_3d(&maps[5 * i + 4], v.img, v.nx, v.ny, v.nz, v.px, pxy, c.bx, c.by, c.bz);
+        encode_tmap_f32_3d(&maps[5 * i + 4], v.speed, v.nx, v.ny, v.nz, v.px, pxy, c.bx, c.by, c.bz);
     }
     LSS_CUDA(cudaMemcpyAsync(d_tmaps_, maps.data(), maps.size() * sizeof(CUtensorMap),
                              cudaMemcpyHostToDevice, st));
@@ -421,6 +422,18 @@ void NsCore::configure(const BrickConfig& c) {
     owner_->sync();
 }
 
+void NsCore::refresh_speed() {
+    for (int v = 0; v < (int)vols_.size(); ++v) {
+        VolHost& V = vols_[v];
+        if (!V.speed_stale) continue;
+        const uint64_t n4 = (uint64_t)V.px * V.py * V.pz / 4;
+        k_ns_speed<<<owner_->num_sms * 4, 256, 0, owner_->stream>>>(descriptor(v), V.speed, n4);
+        ++owner_->launches;
+        LSS_CUDA(cudaGetLastError());
+        V.speed_stale = false;
+    }
+}
+
 size_t NsCore::dyn_smem() const {
     return kernels(cfg_).smem_fixed + stop_state_bytes((int)vols_.size());
 }
@@ -437,7 +450,8 @@ NsVol NsCore::descriptor(int i) const {
     o.brick_base = v.brick_base;
     o.phi[0] = v.phi[0]; o.phi[1] = v.phi[1];
     o.img = v.img;
-    o.bias = v.bias;
+    o.bias = nullptr;  // the adjoint sets its own
+    o.speed = v.speed;
     o.T = v.p.target; o.eps = v.p.window; o.alpha = v.p.curvature; o.dt = v.p.time_step;
     o.lo = v.p.phi_min; o.hi = v.p.phi_max;
     o.thr_t = v.p.temporal_threshold; o.thr_s = v.p.spatial_threshold;
@@ -614,6 +628,7 @@ int NsCore::run(int max_iters, const lss_conv* conv, float* ms) {
     ++epoch_;
     LSS_REQUIRE(initialized_, LSS_ERR_STATE, "no seed / phi set");
     if (max_iters <= 0) return 0;
+    refresh_speed();
     for (VolHost& v : vols_) v.uniform = false;
     cudaStream_t st = owner_->stream;
     KernelSet ks = kernels(cfg_);
@@ -681,7 +696,7 @@ void NsCore::reload_volume(int v, const float* data, const lss_params& p) {
         ++owner_->launches;
     }
     V.p = p;
-    V.bias = nullptr;  // a bias belongs to the previous volume
+    V.speed_stale = true;
     V.uniform = true;
     V.dirty_lo = V.dirty_hi = make_int3(0, 0, 0);
     V.iterations = 0;
@@ -810,6 +825,7 @@ void NsCore::estimate(int v, float* t, float* w) {
 float NsCore::dense_run(int iters) {
     ++epoch_;
     LSS_REQUIRE(initialized_, LSS_ERR_STATE, "no seed / phi set");
+    refresh_speed();
     for (VolHost& v : vols_) v.uniform = false;
     cudaStream_t st = owner_->stream;
     cudaEvent_t e0, e1;

@@ -7,9 +7,10 @@
 //     (block i of G): every block gets ceil(n/G) or floor(n/G) bricks, with
 //     no global list and no atomics;
 //   every owned brick of A_k: TMA-load the brick's phi with a one-voxel halo
-//     (and its intensities) into shared memory, with the next brick's loads
-//     and mask words in flight (double buffered); update the active voxels
-//     (upwind |grad phi|, mean curvature, speed D = eps - |I - T|), TMA-store
+//     (and its speed, computed once per volume and parameter set from D =
+//     eps - |I - T|) into shared memory, with the next brick's loads and mask
+//     words in flight (double buffered); update the active voxels (upwind
+//     |grad phi| times the speed, mean curvature), TMA-store
 //     the brick into the other phi buffer, flag changed voxels with warp
 //     ballots, dilate the changed bitmask by the 26- (or 6-) neighbourhood and
 //     OR it into the next masks and membership bits of the brick and its 26
@@ -49,10 +50,11 @@ struct NsVol {
     float* phi[2];          // ping-pong fields, padded, x fastest
     const float* img;       // intensities, padded
     const float* bias;      // per-voxel speed bias (padded) or null
+    const float* speed;     // ns_speed_f32 of every voxel (padded): what the iterations read
     float T, eps, alpha, dt, lo, hi, thr_t, thr_s;
     int32_t alpha_data;     // 1: alpha weights the data term, 0: the curvature term
     int32_t nbh;            // 26 or 6
-    uint32_t tmap_base;     // 5 maps: phi0 halo-load, phi1 halo-load, phi0 store, phi1 store, img
+    uint32_t tmap_base;     // 5 maps: phi0 halo-load, phi1 halo-load, phi0 store, phi1 store, speed
     float inv_eps;          // 1 / eps (LSS_DATA_NORMALISED), 1 (LSS_DATA_LITERAL)
     float dlo, dhi;         // clamp of the data term: -1, 1 or -inf, +inf (literal)
     int32_t data_literal;   // 1: D = eps - |I - T| as written
@@ -145,9 +147,22 @@ struct Brick {
     static_assert(XY == 64 || VOX == 64, "mask word layout");
 };
 
-// The LSS_MODE_NS update of one voxel from the shared-memory halo tile.
-// P(dx,dy,dz) reads the tile around the voxel.  Mirrors ns_update() of the
-// FP64 oracle in fp32, with the central differences kept unscaled:
+// The speed of one voxel, F = w_d (clamp(D(I)) + bias), the part of the
+// LSS_MODE_NS update that no iteration changes: the engine computes it once
+// per volume and parameter set (k_ns_speed, no bias) and the iterations read
+// it; the adjoint, whose bias changes every call, computes it in place.
+// Every operation is an explicit round-to-nearest intrinsic, so both give
+// the same bits.  Literal data term: inv_eps = 1 (an exact product) and an
+// infinite clamp, so both readings share one instruction sequence.
+__device__ __forceinline__ float ns_speed_f32(float I, float bias, const NsVol& V) {
+    float D = __fmul_rn(__fsub_rn(V.eps, fabsf(__fsub_rn(I, V.T))), V.inv_eps);
+    D = __fadd_rn(fminf(fmaxf(D, V.dlo), V.dhi), bias);
+    return __fmul_rn(V.wd, D);
+}
+
+// The LSS_MODE_NS update of one voxel of speed F from the shared-memory halo
+// tile.  P(dx,dy,dz) reads the tile around the voxel.  Mirrors ns_update()
+// of the FP64 oracle in fp32, with the central differences kept unscaled:
 //   X = 2 phi_x, Fxx = phi_xx, Fxy = 4 phi_xy, so
 //   kappa |grad phi| = [Fxx (Y^2+Z^2) + Fyy (X^2+Z^2) + Fzz (X^2+Y^2)
 //                       - (XY Fxy + XZ Fxz + YZ Fyz) / 2] / (X^2+Y^2+Z^2).
@@ -159,7 +174,7 @@ struct Brick {
 // form matched a CPU restatement of the sequence bit for bit.  The
 // evaluation order keeps few values live; it changes no result.
 template <class PF>
-__device__ __forceinline__ float ns_update_f32(PF P, float I, float bias, const NsVol& V) {
+__device__ __forceinline__ float ns_update_speed_f32(PF P, float F, const NsVol& V) {
     const float c = P(0, 0, 0);
     const float xm = P(-1, 0, 0), xp = P(1, 0, 0);
     const float ym = P(0, -1, 0), yp = P(0, 1, 0);
@@ -170,11 +185,6 @@ __device__ __forceinline__ float ns_update_f32(PF P, float I, float bias, const 
     const float Fzz = __fmaf_rn(-2.0f, c, __fadd_rn(zp, zm));
     const float dxm = __fsub_rn(c, xm), dxp = __fsub_rn(xp, c), dym = __fsub_rn(c, ym),
                 dyp = __fsub_rn(yp, c), dzm = __fsub_rn(c, zm), dzp = __fsub_rn(zp, c);
-    // Literal data term: inv_eps = 1 (an exact product) and an infinite
-    // clamp, so both readings share one instruction sequence.
-    float D = __fmul_rn(__fsub_rn(V.eps, fabsf(__fsub_rn(I, V.T))), V.inv_eps);
-    D = __fadd_rn(fminf(fmaxf(D, V.dlo), V.dhi), bias);
-    const float F = __fmul_rn(V.wd, D);
     // Osher-Sethian upwind |grad phi| for the speed F: one-sided differences
     // selected by the sign of F.
     float a, b, e, f, h, k;
@@ -207,6 +217,12 @@ __device__ __forceinline__ float ns_update_f32(PF P, float I, float bias, const 
     return fminf(fmaxf(nv, V.lo), V.hi);
 }
 
+// The update from the intensity and the bias (the speed computed in place).
+template <class PF>
+__device__ __forceinline__ float ns_update_f32(PF P, float I, float bias, const NsVol& V) {
+    return ns_update_speed_f32(P, ns_speed_f32(I, bias, V), V);
+}
+
 // Every TMA destination / source below starts on a 128-byte boundary: the
 // arrays are 128-byte aligned and every per-buffer stride is a multiple of
 // 128 bytes (TILE_PAD floats; VOX floats = 256 B or more).
@@ -218,7 +234,7 @@ struct NsSmem {
     // (9 x WORDS <= NT - 32), so the store issue delays no barrier.
     static constexpr int STORE_TID = NT - 32;
     alignas(128) float phi[2][S::TILE_PAD];  // halo tiles, double buffered
-    alignas(128) float img[2][S::VOX];
+    alignas(128) float spd[2][S::VOX];         // the brick's speed
     alignas(128) float out[2][S::VOX];
     unsigned long long act[2][S::WORDS];     // the brick's active mask, double buffered
     uint32_t chg[2][S::CHG];                 // changed voxels of the brick (ballot words)
@@ -411,7 +427,7 @@ __device__ __forceinline__ void clamp_tile_halo(float* phi, const NsVol& V, int 
     }
 }
 
-// Issues the TMA loads of brick b (halo tile of phi[p] and the intensities)
+// Issues the TMA loads of brick b (halo tile of phi[p] and the speed)
 // into buffer `buf` and records the brick's origin and volume beside them
 // (thread 0 only: the brick's index arithmetic is done once, not by every
 // thread).
@@ -424,7 +440,7 @@ __device__ __forceinline__ void ns_issue_loads(const NsArgs& a, NsSmem<S, NT>& s
     sm.org[buf] = make_int4(o.x, o.y, o.z, (int)vol);
     mbar_expect_tx(&sm.bar[buf], (uint32_t)(S::TILE + S::VOX) * 4u);
     tma_load_3d(sm.phi[buf], &a.tmaps[V.tmap_base + p], o.x - 4, o.y - 1, o.z - 1, &sm.bar[buf]);
-    tma_load_3d(sm.img[buf], &a.tmaps[V.tmap_base + 4], o.x, o.y, o.z, &sm.bar[buf]);
+    tma_load_3d(sm.spd[buf], &a.tmaps[V.tmap_base + 4], o.x, o.y, o.z, &sm.bar[buf]);
 }
 
 // Per-block running totals of updated voxels and bricks of one volume,
@@ -639,12 +655,7 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
     if ((tid >> 5) == (STORE_TID >> 5))
         nact = __reduce_add_sync(0xffffffffu, (tid & 31) < S::WORDS ? __popcll(act[tid & 31]) : 0u);
     constexpr int VPT = (S::VOX + NT - 1) / NT;
-    const float* bias = V.bias;
     bool anyl = false;
-    auto bias_at = [&](int j) {
-        const int lx = j % S::X, ly = (j / S::X) % S::Y, lz = j / (S::X * S::Y);
-        return bias[((size_t)(z0 + lz) * V.py + (y0 + ly)) * V.px + (x0 + lx)];
-    };
     if constexpr (VPT == 2 && S::VOX == 2 * NT && S::Z % 2 == 0) {
         // Two voxels a thread, z-adjacent at the same (x, y): updated in one
         // straight-line block (their chains interleave) when either is
@@ -659,8 +670,8 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
         if (a0 || a1) {
             auto P0 = [&](int dx, int dy, int dz) { return phi[t0 + (dz * S::TY + dy) * S::TX + dx]; };
             auto P1 = [&](int dx, int dy, int dz) { return phi[t1 + (dz * S::TY + dy) * S::TX + dx]; };
-            const float u0 = ns_update_f32(P0, sm.img[buf][j0], bias ? bias_at(j0) : 0.0f, V);
-            const float u1 = ns_update_f32(P1, sm.img[buf][j1], bias ? bias_at(j1) : 0.0f, V);
+            const float u0 = ns_update_speed_f32(P0, sm.spd[buf][j0], V);
+            const float u1 = ns_update_speed_f32(P1, sm.spd[buf][j1], V);
             if (a0) {
                 nv0 = u0;
                 ch0 = fabsf(nv0 - c0) > V.thr_t;
@@ -689,7 +700,7 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
             float nv = c;
             if ((act[j >> 6] >> (j & 63)) & 1ull) {
                 auto P = [&](int dx, int dy, int dz) { return phi[ti + (dz * S::TY + dy) * S::TX + dx]; };
-                nv = ns_update_f32(P, sm.img[buf][j], bias ? bias_at(j) : 0.0f, V);
+                nv = ns_update_speed_f32(P, sm.spd[buf][j], V);
                 chg = fabsf(nv - c) > V.thr_t;
             }
             out[j] = nv;
@@ -705,7 +716,7 @@ __device__ __forceinline__ void ns_process_brick(const NsArgs& a, NsSmem<S, NT>&
     // brick after this barrier) has read its source.
     if (tid == STORE_TID) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
     // The one block barrier of a brick: out[] and chg[buf] complete; after it
-    // nothing reads phi[buf], img[buf] or act[buf] of this brick, so the next
+    // nothing reads phi[buf], spd[buf] or act[buf] of this brick, so the next
     // loads into this buffer may be issued while the dilation below runs.
     const int any = team.sync_or(anyl ? 1 : 0);
     if (tid == STORE_TID) {
@@ -1289,7 +1300,7 @@ template <class S>
 struct WarpSlot {
     static_assert((S::TILE_PAD * 4) % 128 == 0 && (S::VOX * 4) % 128 == 0, "TMA smem alignment");
     alignas(128) float phi[S::TILE_PAD];  // halo tile of phi
-    alignas(128) float img[S::VOX];
+    alignas(128) float spd[S::VOX];  // the brick's speed
     alignas(128) float out[S::VOX];
     unsigned long long act[S::WORDS];
     uint32_t chg[S::CHG];
@@ -1322,7 +1333,7 @@ __device__ __forceinline__ void ns_warp_brick(const NsArgs& a, WarpSlot<S>& sl, 
         fence_proxy_async_smem();  // the warp's generic reads of the slot before the async writes
         mbar_expect_tx(&sl.bar, (uint32_t)(S::TILE + S::VOX) * 4u);
         tma_load_3d(sl.phi, &a.tmaps[V.tmap_base + p], o.x - 4, o.y - 1, o.z - 1, &sl.bar);
-        tma_load_3d(sl.img, &a.tmaps[V.tmap_base + 4], o.x, o.y, o.z, &sl.bar);
+        tma_load_3d(sl.spd, &a.tmaps[V.tmap_base + 4], o.x, o.y, o.z, &sl.bar);
     }
     __syncwarp();
     if (!mbar_wait(&sl.bar, phase)) set_error(&a.ctl->err, ERR_TMA_TIMEOUT);
@@ -1355,13 +1366,8 @@ __device__ __forceinline__ void ns_warp_brick(const NsArgs& a, WarpSlot<S>& sl, 
         const int j = sl.list[i];
         const int ti = tile_index(j);
         auto P = [&](int dx, int dy, int dz) { return phi[ti + (dz * S::TY + dy) * S::TX + dx]; };
-        float bb = 0.0f;
-        if (V.bias) {
-            const int lx = j % S::X, ly = (j / S::X) % S::Y, lz = j / (S::X * S::Y);
-            bb = V.bias[((size_t)(o.z + lz) * V.py + (o.y + ly)) * V.px + (o.x + lx)];
-        }
         const float c = phi[ti];
-        const float nv = ns_update_f32(P, sl.img[j], bb, V);
+        const float nv = ns_update_speed_f32(P, sl.spd[j], V);
         sl.out[j] = nv;
         sl.chgb[j] = fabsf(nv - c) > V.thr_t;
     }
