@@ -825,6 +825,7 @@ __host__ __device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t s)
     return pos;
 }
 constexpr int kScanCache = 4;               // membership words per thread kept in shared memory
+constexpr int kSearchBatch = 8;             // words past the cache loaded at once by a rank search
 
 // Shared state of the iteration driver (static shared memory).
 template <int NT>
@@ -949,12 +950,26 @@ __device__ __forceinline__ void ns_drive(const NsArgs& a, IterShared<NT>& sh, St
                             }
                             s -= c;
                         }
-                        for (uint32_t w = tid + kScanCache * NT; b == 0xFFFFFFFFu && w < a.NW; w += NT) {
-                            const uint32_t cw = cur[w];
-                            const uint32_t bits = fl ? prev[w] & ~cw : cw;
-                            const uint32_t c = __popc(bits);
-                            if (s < c) b = w * 32u + nth_set_bit(bits, s);
-                            else s -= c;
+                        // Words past the cache, kSearchBatch at a time:
+                        // their loads are independent, so a search costs
+                        // one memory round trip per batch, not per word.
+                        for (uint32_t w0 = tid + kScanCache * NT; b == 0xFFFFFFFFu && w0 < a.NW;
+                             w0 += kSearchBatch * NT) {
+                            uint32_t bw[kSearchBatch];
+#pragma unroll
+                            for (int u = 0; u < kSearchBatch; ++u) {
+                                const uint32_t w = w0 + (uint32_t)u * NT;
+                                const uint32_t cw = w < a.NW ? cur[w] : 0u;
+                                bw[u] = fl ? (w < a.NW ? prev[w] : 0u) & ~cw : cw;
+                            }
+#pragma unroll
+                            for (int u = 0; u < kSearchBatch; ++u) {
+                                const uint32_t c = __popc(bw[u]);
+                                if (b == 0xFFFFFFFFu) {
+                                    if (s < c) b = (w0 + (uint32_t)u * NT) * 32u + nth_set_bit(bw[u], s);
+                                    else s -= c;
+                                }
+                            }
                         }
                         const uint32_t slot = divg(q - bi) - c0;
                         if (slot >= (uint32_t)NT || b >= a.NB) {  // a rank outside this chunk: report, skip
