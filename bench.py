@@ -142,12 +142,12 @@ def sum_over_ranks(ws, value: float) -> float:
 # the key's first field (profiles/k_ns_persistent_config2_256.md gives the
 # capture); a build from other sources reports null rather than a stale
 # figure.
-DRAM_TRAFFIC = {("809a5bdef697", "config2_256", 8, 8, 8, 256): 15853312}
+DRAM_TRAFFIC = {("7972d1c57af0", "config2_256", 8, 8, 8, 256): 16057344}
 KERNEL_SOURCES = ("ns_kernels.cuh", "ns_engine.cu", "tma.cuh", "common.cuh")
 # The same for one adjoint call on config 4 (its four kernels: the forward
 # with the call's set-up phase, the two soft-Dice passes, the reverse), from
 # the capture in profiles/k_adj_config4_192.md.
-ADJOINT_TRAFFIC = {("e0d969bb4511", "config4_192"): 84099840}
+ADJOINT_TRAFFIC = {("95ec282ab517", "config4_192"): 84198912}
 ADJOINT_SOURCES = ("ns_adjoint.cu", "ns_kernels.cuh", "common.cuh")
 
 
