@@ -186,6 +186,8 @@ def test_ns_param_change_reinitialises_active_set():
     o.set_phi(phi)  # re-init from the current phi, as the engine does
     o.step(1)
     assert np.array_equal(s.active_linear(), o.active())
+    # The step ran with the new target (the precomputed speed follows it).
+    assert float(np.max(np.abs(s.read_phi().astype(np.float64) - o.read_phi64()))) <= 1e-4
 
 
 def test_ns_seeds_and_readbacks():
