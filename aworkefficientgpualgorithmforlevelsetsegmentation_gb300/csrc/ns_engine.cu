@@ -273,9 +273,9 @@ static KernelSet kernels(const BrickConfig& c) {
         return kernels_for<8, 8, 8, 256, 5>();
     if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 256 && c.min_blocks == 4)
         return kernels_for<8, 8, 8, 256, 4>();
-    // 8^3 x 256 by default three blocks per SM: 79 registers and no spill
-    // (four cap a thread at 64 and spill 32 bytes; 2 % slower to converge at
-    // 256^3).
+    // 8^3 x 256 by default three blocks per SM: 79 registers (four cap a
+    // thread at 64: 3 % slower to converge at 256^3, more blocks each
+    // running a rank selection every iteration).
     if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 256) return kernels_for<8, 8, 8, 256, 3>();
     if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 128) return kernels_for<8, 8, 8, 128>();
     if (c.bx == 8 && c.by == 8 && c.bz == 8 && c.threads == 512) return kernels_for<8, 8, 8, 512>();
