@@ -610,8 +610,9 @@ __device__ __forceinline__ void adj_mark_brick(const NsVol& V, uint32_t b, const
 // so lambda_k = lam + Z[1-p] on exit, with the bricks Z[1-p] reaches marked
 // in flagT[(k - 1) & 1] (by each brick's part 0).  Part one (brick parts of
 // A_k) visits the bricks of A_k whole; part two (adj_rev_touched) the
-// marked bricks outside A_k.  Every voxel is read and written by one thread
-// only.
+// marked bricks outside A_k.  Every field of a voxel is written by one
+// thread only (with two threads a voxel: lambda and Z by half 0, d_bias by
+// half 1).
 //
 // half (Parts::half): -1, the thread does the voxel alone; 0 or 1, the
 // voxel's two threads of a 128-thread group (in different warps, so the
