@@ -187,7 +187,8 @@ def test_gpu_adjoint_device_buffers_match_host_buffers(shape):
     assert h["active_voxel_iterations"] == d["active_voxel_iterations"] > 0
 
 
-def test_gpu_adjoint_calls_on_one_engine_match_fresh_engines():
+@pytest.mark.parametrize("brick,threads", [((8, 8, 8), 256), ((8, 8, 4), 32), ((4, 4, 4), 64)])
+def test_gpu_adjoint_calls_on_one_engine_match_fresh_engines(brick, threads):
     """Between calls the engine keeps the forward's two copies of phi_0 and
     copies again only the bricks the previous call touched, while its phi is
     unchanged and no host staging went through them: device buffers, so the
@@ -213,7 +214,7 @@ def test_gpu_adjoint_calls_on_one_engine_match_fresh_engines():
         return g
 
     def fresh(bias, steps=0):
-        e = make(cfg)
+        e = make(cfg, brick, threads)
         if steps:
             e.step(steps)
         return call(e, bias)
@@ -225,7 +226,7 @@ def test_gpu_adjoint_calls_on_one_engine_match_fresh_engines():
             assert rel(g[key], h[key]) <= 1e-5, (key, g[key], h[key])
         assert np.allclose(g["d_bias"], h["d_bias"], rtol=1e-4, atol=1e-9)
 
-    s = make(cfg)
+    s = make(cfg, brick, threads)
     r1 = call(s, b1)
     same(r1, fresh(b1))
     same(call(s, b1), r1)
