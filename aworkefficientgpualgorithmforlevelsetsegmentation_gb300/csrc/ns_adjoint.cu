@@ -4,10 +4,10 @@
 // fixed, the soft-Dice loss of sigmoid(-phi/tau) against a target mask, and
 // its gradients with respect to T, eps, alpha and a per-voxel speed bias.
 //
-// A call is four launches: the forward and the reverse (cooperative, the
-// phases inside each separated by the cooperative-groups grid barrier) with
-// the two soft-Dice passes between them.  Work-efficient like the forward
-// engine: every iteration touches the bricks of its active set only.
+// A call is two cooperative launches, the forward (its last two phases the
+// loss) and the reverse, the phases inside each separated by the
+// cooperative-groups grid barrier.  Work-efficient like the forward engine:
+// every iteration touches the bricks of its active set only.
 //
 // Forward (k_adj_forward).  Its first phase sets the call up (clears, the
 // pair's copies of phi_0, the masks of A_0).  Iteration k finds the bricks of
@@ -24,8 +24,8 @@
 // the update.  The bricks within one brick of some A_k are marked: lambda is
 // read there only.
 //
-// Loss (k_adj_dice, k_adj_lamk).  The soft-Dice sums over the volume, then
-// lambda_K on the marked bricks.
+// Loss (the forward's last two phases).  The soft-Dice sums over the
+// volume, then lambda_K on the marked bricks.
 //
 // States without dense copies.  phi_k and phi_{k+1} differ only inside the
 // bricks of A_k, so a field that holds phi_{k+2} becomes phi_k by writing
@@ -91,6 +91,184 @@ __device__ __forceinline__ int3 voxel_of(const NsVol& V, uint32_t b, int j) {
     return make_int3(o.x + j % S::X, o.y + (j / S::X) % S::Y, o.z + j / (S::X * S::Y));
 }
 
+// The soft-Dice loss, the last two grid phases of the forward kernel (a
+// grid barrier between them): the sums over the volume's rows in groups of
+// four voxels (px is a multiple of 8, so a group stays in its row and is
+// 16-byte aligned): item i is group i mod Q of row i div Q (Q = ceil(nx /
+// 4)), row r = (y, z) = (r mod ny, r div ny); the padding rows are never
+// visited.  Then lambda_K on the bricks the reverse reads it at.
+
+struct DiceArgs {
+    const float* phi;  // phi_K
+    const uint8_t* tgt;
+    float* lam;
+    double* part;      // [nparts][3]: the dice blocks' sums
+    double* gsum;      // [8]: the total in 4..6
+    int nx, ny, nz, px, py;
+    uint32_t nparts;
+    float tau;
+    const uint32_t* reached;  // [nb]: the bricks whose lambda_K is needed
+    float* z0;                // lambda's contribution fields, cleared there too
+    float* z1;
+    uint32_t nb;
+    int bx, by, bz, nbx, nby;  // brick shape and grid
+    uint32_t gen;              // the call's stamp in reached
+};
+
+__device__ __forceinline__ float soft_mask(float phi, float tau) { return 1.0f / (1.0f + expf(phi / tau)); }
+
+// Group i: its first x, and its index among the padded field's groups.
+__device__ __forceinline__ uint32_t dice_group(const DiceArgs& d, uint32_t q4, uint32_t i, uint64_t* g) {
+    const uint32_t r = i / q4, x0 = (i - r * q4) * 4;
+    const uint32_t z = r / (uint32_t)d.ny, y = r - z * (uint32_t)d.ny;
+    *g = (((uint64_t)z * d.py + y) * d.px + x0) / 4;
+    return x0;
+}
+
+// Four groups a thread in flight (the loads of a round before its math).
+constexpr int kDiceUnroll = 4;
+
+// Sums s = sigmoid(-phi_K / tau), t = target and s t over the volume: per
+// voxel in fp32, per thread in fp32, per block in FP64 into part[3 * block].
+// NTH threads a block.
+template <int NTH>
+__device__ void adj_dice_sums(const DiceArgs& d) {
+    const uint32_t q4 = (uint32_t)(d.nx + 3) / 4, n = (uint32_t)d.ny * (uint32_t)d.nz * q4;
+    const uint32_t nt = gridDim.x * blockDim.x;
+    float ss = 0.0f, tt = 0.0f, st = 0.0f;
+    for (uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += kDiceUnroll * nt) {
+        float4 f[kDiceUnroll];
+        uchar4 m[kDiceUnroll];
+        uint32_t x0[kDiceUnroll];
+#pragma unroll
+        for (int u = 0; u < kDiceUnroll; ++u) {
+            const uint32_t i = i0 + u * nt;
+            x0[u] = 0xFFFFFFFFu;
+            if (i < n) {
+                uint64_t g;
+                x0[u] = dice_group(d, q4, i, &g);
+                f[u] = reinterpret_cast<const float4*>(d.phi)[g];
+                m[u] = reinterpret_cast<const uchar4*>(d.tgt)[g];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kDiceUnroll; ++u) {
+            if (x0[u] == 0xFFFFFFFFu) continue;
+            const float fv[4] = {f[u].x, f[u].y, f[u].z, f[u].w};
+            const unsigned char mv[4] = {m[u].x, m[u].y, m[u].z, m[u].w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                if (x0[u] + e >= (uint32_t)d.nx) break;
+                const float s = soft_mask(fv[e], d.tau);
+                const float tv = mv[e] ? 1.0f : 0.0f;
+                ss += s;
+                tt += tv;
+                st += s * tv;
+            }
+        }
+    }
+    __shared__ double w3[3][NTH / 32];
+    double a0 = ss, a1 = tt, a2 = st;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        a0 += __shfl_down_sync(0xffffffffu, a0, o);
+        a1 += __shfl_down_sync(0xffffffffu, a1, o);
+        a2 += __shfl_down_sync(0xffffffffu, a2, o);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        w3[0][warp] = a0;
+        w3[1][warp] = a1;
+        w3[2][warp] = a2;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double t = 0.0;
+        for (int q = 0; q < NTH / 32; ++q) t += w3[threadIdx.x][q];
+        d.part[3 * (size_t)blockIdx.x + threadIdx.x] = t;
+    }
+}
+
+// lambda_K = dloss/dphi_K on the bricks the reverse reads it at (those
+// within one brick of some A_k; elsewhere lambda passes through untouched to
+// lambda_0, which nothing reads), with the two contribution fields cleared
+// on the same voxels (the reverse reads and scatters into them there only).
+// Item i: group i mod G (four voxels of a brick row) of brick i div G.
+// Every block adds the blocks' sums in the same order (the same totals in
+// every block and every call); block 0 publishes them for the loss.
+__device__ void adj_lambda_k(const DiceArgs& d) {
+    __shared__ double tot[3];
+    if (threadIdx.x < 32) {
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+        for (uint32_t b = threadIdx.x; b < d.nparts; b += 32) {
+            a0 += d.part[3 * (size_t)b];
+            a1 += d.part[3 * (size_t)b + 1];
+            a2 += d.part[3 * (size_t)b + 2];
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            a0 += __shfl_down_sync(0xffffffffu, a0, o);
+            a1 += __shfl_down_sync(0xffffffffu, a1, o);
+            a2 += __shfl_down_sync(0xffffffffu, a2, o);
+        }
+        if (threadIdx.x == 0) {
+            tot[0] = a0;
+            tot[1] = a1;
+            tot[2] = a2;
+            if (blockIdx.x == 0) {
+                d.gsum[4] = a0;
+                d.gsum[5] = a1;
+                d.gsum[6] = a2;
+            }
+        }
+    }
+    __syncthreads();
+    // dloss/ds = (2 st - 2 t den) / den^2 with den = sum s + sum t.
+    const double den = tot[0] + tot[1], sst = tot[2];
+    const float c_out = (float)(2.0 * sst / (den * den)), c_in = (float)(2.0 * sst / (den * den) - 2.0 / den);
+    const uint32_t G = (uint32_t)(d.bx * d.by * d.bz) / 4, n = d.nb * G;
+    const uint32_t nt = gridDim.x * blockDim.x;
+    for (uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += kDiceUnroll * nt) {
+        float4 f[kDiceUnroll];
+        uchar4 m[kDiceUnroll];
+        uint64_t g[kDiceUnroll];
+        uint32_t x0[kDiceUnroll];
+#pragma unroll
+        for (int u = 0; u < kDiceUnroll; ++u) {
+            const uint32_t i = i0 + u * nt;
+            x0[u] = 0xFFFFFFFFu;
+            if (i < n && d.reached[i / G] == d.gen) {
+                const uint32_t b = i / G, j = (i - b * G) * 4;
+                const uint32_t kx = b % (uint32_t)d.nbx, r = b / (uint32_t)d.nbx;
+                const uint32_t ky = r % (uint32_t)d.nby, kz = r / (uint32_t)d.nby;
+                const uint32_t x = kx * d.bx + j % d.bx, y = ky * d.by + (j / d.bx) % d.by,
+                               z = kz * d.bz + j / (d.bx * d.by);
+                if (y < (uint32_t)d.ny && z < (uint32_t)d.nz) {
+                    x0[u] = x;
+                    g[u] = (((uint64_t)z * d.py + y) * d.px + x) / 4;
+                    f[u] = reinterpret_cast<const float4*>(d.phi)[g[u]];
+                    m[u] = reinterpret_cast<const uchar4*>(d.tgt)[g[u]];
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kDiceUnroll; ++u) {
+            if (x0[u] == 0xFFFFFFFFu) continue;
+            const float fv[4] = {f[u].x, f[u].y, f[u].z, f[u].w};
+            const unsigned char mv[4] = {m[u].x, m[u].y, m[u].z, m[u].w};
+            float l[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const float s = soft_mask(fv[e], d.tau);
+                l[e] = x0[u] + e < (uint32_t)d.nx ? (mv[e] ? c_in : c_out) * (-s * (1.0f - s) / d.tau) : 0.0f;
+            }
+            reinterpret_cast<float4*>(d.lam)[g[u]] = make_float4(l[0], l[1], l[2], l[3]);
+            reinterpret_cast<float4*>(d.z0)[g[u]] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            reinterpret_cast<float4*>(d.z1)[g[u]] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+    }
+}
+
 // Everything one call works on.  Per-iteration arrays are evenly spaced in
 // the workspace: act[k] = act0 + k * astride words, list[k] = list0 +
 // k * lstride, flag[k] = flag0 + k * lstride; the checkpoints are fstride
@@ -122,6 +300,7 @@ struct AdjPlan {
     const unsigned long long* act_src;     // and its masks of A_0
     uint64_t mwords;                       // mask words a set
     uint64_t dbias_n;                      // floats of d_bias cleared (a multiple of 4)
+    DiceArgs dice;                         // the loss phases' view (phi_K, target, lambda, sums)
     uint32_t gen;                          // this call's stamp in `reached` (>= 1)
     int32_t partial;                       // 1: the pair holds phi_0 but in the bricks stamped gen - 1
     uint32_t nb;
@@ -940,182 +1119,11 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_forward(const AdjPlan a) {
     if ((threadIdx.x & 31) == 0 && mine) atomicAdd(&s_cnt, mine);
     __syncthreads();
     if (threadIdx.x == 0 && s_cnt) atomicAdd(a.nact, (unsigned long long)s_cnt);
-}
-
-// The soft-Dice passes, two streaming kernels between the forward and the
-// reverse: the volume's rows in groups of four voxels (px is a multiple of
-// 8, so a group stays in its row and is 16-byte aligned): item i is group
-// i mod Q of row i div Q (Q = ceil(nx / 4)), row r = (y, z) = (r mod ny,
-// r div ny); the padding rows are never visited.
-constexpr int kDiceThreads = 256;
-
-struct DiceArgs {
-    const float* phi;  // phi_K
-    const uint8_t* tgt;
-    float* lam;
-    double* part;      // [nparts][3]: the dice blocks' sums
-    double* gsum;      // [8]: the total in 4..6
-    int nx, ny, nz, px, py;
-    uint32_t nparts;
-    float tau;
-    const uint32_t* reached;  // [nb]: the bricks whose lambda_K is needed
-    float* z0;                // lambda's contribution fields, cleared there too
-    float* z1;
-    uint32_t nb;
-    int bx, by, bz, nbx, nby;  // brick shape and grid
-    uint32_t gen;              // the call's stamp in reached
-};
-
-__device__ __forceinline__ float soft_mask(float phi, float tau) { return 1.0f / (1.0f + expf(phi / tau)); }
-
-// Group i: its first x, and its index among the padded field's groups.
-__device__ __forceinline__ uint32_t dice_group(const DiceArgs& d, uint32_t q4, uint32_t i, uint64_t* g) {
-    const uint32_t r = i / q4, x0 = (i - r * q4) * 4;
-    const uint32_t z = r / (uint32_t)d.ny, y = r - z * (uint32_t)d.ny;
-    *g = (((uint64_t)z * d.py + y) * d.px + x0) / 4;
-    return x0;
-}
-
-// Four groups a thread in flight (the loads of a round before its math).
-constexpr int kDiceUnroll = 4;
-
-// Sums s = sigmoid(-phi_K / tau), t = target and s t over the volume: per
-// voxel in fp32, per thread in fp32, per block in FP64 into part[3 * block].
-__global__ void __launch_bounds__(kDiceThreads) k_adj_dice(const DiceArgs d) {
-    const uint32_t q4 = (uint32_t)(d.nx + 3) / 4, n = (uint32_t)d.ny * (uint32_t)d.nz * q4;
-    const uint32_t nt = gridDim.x * blockDim.x;
-    float ss = 0.0f, tt = 0.0f, st = 0.0f;
-    for (uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += kDiceUnroll * nt) {
-        float4 f[kDiceUnroll];
-        uchar4 m[kDiceUnroll];
-        uint32_t x0[kDiceUnroll];
-#pragma unroll
-        for (int u = 0; u < kDiceUnroll; ++u) {
-            const uint32_t i = i0 + u * nt;
-            x0[u] = 0xFFFFFFFFu;
-            if (i < n) {
-                uint64_t g;
-                x0[u] = dice_group(d, q4, i, &g);
-                f[u] = reinterpret_cast<const float4*>(d.phi)[g];
-                m[u] = reinterpret_cast<const uchar4*>(d.tgt)[g];
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < kDiceUnroll; ++u) {
-            if (x0[u] == 0xFFFFFFFFu) continue;
-            const float fv[4] = {f[u].x, f[u].y, f[u].z, f[u].w};
-            const unsigned char mv[4] = {m[u].x, m[u].y, m[u].z, m[u].w};
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                if (x0[u] + e >= (uint32_t)d.nx) break;
-                const float s = soft_mask(fv[e], d.tau);
-                const float tv = mv[e] ? 1.0f : 0.0f;
-                ss += s;
-                tt += tv;
-                st += s * tv;
-            }
-        }
-    }
-    __shared__ double w3[3][kDiceThreads / 32];
-    double a0 = ss, a1 = tt, a2 = st;
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-        a0 += __shfl_down_sync(0xffffffffu, a0, o);
-        a1 += __shfl_down_sync(0xffffffffu, a1, o);
-        a2 += __shfl_down_sync(0xffffffffu, a2, o);
-    }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) {
-        w3[0][warp] = a0;
-        w3[1][warp] = a1;
-        w3[2][warp] = a2;
-    }
-    __syncthreads();
-    if (threadIdx.x < 3) {
-        double t = 0.0;
-        for (int q = 0; q < kDiceThreads / 32; ++q) t += w3[threadIdx.x][q];
-        d.part[3 * (size_t)blockIdx.x + threadIdx.x] = t;
-    }
-}
-
-// lambda_K = dloss/dphi_K on the bricks the reverse reads it at (those
-// within one brick of some A_k; elsewhere lambda passes through untouched to
-// lambda_0, which nothing reads), with the two contribution fields cleared
-// on the same voxels (the reverse reads and scatters into them there only).
-// Item i: group i mod G (four voxels of a brick row) of brick i div G.
-// Every block adds the dice blocks' sums in the same order (the same totals
-// in every block and every call); block 0 publishes them for the loss.
-__global__ void __launch_bounds__(kDiceThreads) k_adj_lamk(const DiceArgs d) {
-    __shared__ double tot[3];
-    if (threadIdx.x < 32) {
-        double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-        for (uint32_t b = threadIdx.x; b < d.nparts; b += 32) {
-            a0 += d.part[3 * (size_t)b];
-            a1 += d.part[3 * (size_t)b + 1];
-            a2 += d.part[3 * (size_t)b + 2];
-        }
-#pragma unroll
-        for (int o = 16; o; o >>= 1) {
-            a0 += __shfl_down_sync(0xffffffffu, a0, o);
-            a1 += __shfl_down_sync(0xffffffffu, a1, o);
-            a2 += __shfl_down_sync(0xffffffffu, a2, o);
-        }
-        if (threadIdx.x == 0) {
-            tot[0] = a0;
-            tot[1] = a1;
-            tot[2] = a2;
-            if (blockIdx.x == 0) {
-                d.gsum[4] = a0;
-                d.gsum[5] = a1;
-                d.gsum[6] = a2;
-            }
-        }
-    }
-    __syncthreads();
-    // dloss/ds = (2 st - 2 t den) / den^2 with den = sum s + sum t.
-    const double den = tot[0] + tot[1], sst = tot[2];
-    const float c_out = (float)(2.0 * sst / (den * den)), c_in = (float)(2.0 * sst / (den * den) - 2.0 / den);
-    const uint32_t G = (uint32_t)(d.bx * d.by * d.bz) / 4, n = d.nb * G;
-    const uint32_t nt = gridDim.x * blockDim.x;
-    for (uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += kDiceUnroll * nt) {
-        float4 f[kDiceUnroll];
-        uchar4 m[kDiceUnroll];
-        uint64_t g[kDiceUnroll];
-        uint32_t x0[kDiceUnroll];
-#pragma unroll
-        for (int u = 0; u < kDiceUnroll; ++u) {
-            const uint32_t i = i0 + u * nt;
-            x0[u] = 0xFFFFFFFFu;
-            if (i < n && d.reached[i / G] == d.gen) {
-                const uint32_t b = i / G, j = (i - b * G) * 4;
-                const uint32_t kx = b % (uint32_t)d.nbx, r = b / (uint32_t)d.nbx;
-                const uint32_t ky = r % (uint32_t)d.nby, kz = r / (uint32_t)d.nby;
-                const uint32_t x = kx * d.bx + j % d.bx, y = ky * d.by + (j / d.bx) % d.by,
-                               z = kz * d.bz + j / (d.bx * d.by);
-                if (y < (uint32_t)d.ny && z < (uint32_t)d.nz) {
-                    x0[u] = x;
-                    g[u] = (((uint64_t)z * d.py + y) * d.px + x) / 4;
-                    f[u] = reinterpret_cast<const float4*>(d.phi)[g[u]];
-                    m[u] = reinterpret_cast<const uchar4*>(d.tgt)[g[u]];
-                }
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < kDiceUnroll; ++u) {
-            if (x0[u] == 0xFFFFFFFFu) continue;
-            const float fv[4] = {f[u].x, f[u].y, f[u].z, f[u].w};
-            const unsigned char mv[4] = {m[u].x, m[u].y, m[u].z, m[u].w};
-            float l[4];
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const float s = soft_mask(fv[e], d.tau);
-                l[e] = x0[u] + e < (uint32_t)d.nx ? (mv[e] ? c_in : c_out) * (-s * (1.0f - s) / d.tau) : 0.0f;
-            }
-            reinterpret_cast<float4*>(d.lam)[g[u]] = make_float4(l[0], l[1], l[2], l[3]);
-            reinterpret_cast<float4*>(d.z0)[g[u]] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            reinterpret_cast<float4*>(d.z1)[g[u]] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        }
-    }
+    // The loss: phi_K is whole (the last iteration's barrier), the sums,
+    // one barrier, lambda_K.
+    adj_dice_sums<kAdjThreads>(a.dice);
+    grid.sync();
+    adj_lambda_k(a.dice);
 }
 
 // The reverse: the segments from the last (lambda_K is in lam).
@@ -1162,7 +1170,6 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
         return owner->num_sms * std::min(per_sm, kAdjBlocksPerSm);
     };
     const int gf = coop(kf), gr = coop(kr);
-    const int ndice = owner->num_sms * 8;  // soft-Dice blocks (per-block partial sums)
     // One device workspace (kept by the engine between calls), carved into
     // 256-byte aligned parts.
     auto al = [](uint64_t b) { return (b + 255) / 256 * 256; };
@@ -1178,7 +1185,7 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
                            2 * (uint64_t)(K + 1) * al((uint64_t)nb * 4) + al((uint64_t)(K + 1) * 4) + al(P) +
                            2 * al((uint64_t)nb * 4) + (uint64_t)(nck + 2) * al((uint64_t)nb * 4) + al((uint64_t)nck * 4) +
                            al(8 * sizeof(double) + 8) + al((uint64_t)gr * 3 * sizeof(double)) +
-                           al((uint64_t)ndice * 3 * sizeof(double));
+                           al((uint64_t)gf * 3 * sizeof(double));
     char* base = (char*)core.workspace(total);
     char* const end = base + total;
     auto carve = [&](uint64_t bytes) {
@@ -1221,7 +1228,7 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     a.gsum = (double*)carve(8 * sizeof(double) + 8);
     a.nact = (unsigned long long*)(a.gsum + 8);
     a.gpart = (double*)carve((uint64_t)gr * 3 * sizeof(double));
-    double* dpart = (double*)carve((uint64_t)ndice * 3 * sizeof(double));
+    double* dpart = (double*)carve((uint64_t)gf * 3 * sizeof(double));  // the loss's block sums
     a.dbias = dbias ? F() : nullptr;
     a.P = P;
     a.nb = nb;
@@ -1290,14 +1297,9 @@ void run_adjoint(NsCore& core, int K, int every, const uint8_t* target, float ta
     rec.valid = false;
     LSS_REQUIRE(gf == gr, LSS_ERR_CUDA, "adjoint grids differ");
     void* params[] = {(void*)&a};
+    a.dice = DiceArgs{a.fw[K & 1], a.tgt, a.lam, dpart, a.gsum, V.nx, V.ny, V.nz, V.px, V.py, (uint32_t)gf, tau,
+                      a.reached, a.Z[0], a.Z[1], nb, S::X, S::Y, S::Z, V.nbx, V.nby, a.gen};
     LSS_CUDA(cudaLaunchCooperativeKernel(kf, dim3(gf), dim3(kAdjThreads), params, 0, st));
-    count_launch(owner);
-    // The loss and lambda_K between the two.
-    DiceArgs d{a.fw[K & 1], a.tgt, a.lam, dpart, a.gsum, V.nx, V.ny, V.nz, V.px, V.py, (uint32_t)ndice, tau,
-               a.reached, a.Z[0], a.Z[1], nb, S::X, S::Y, S::Z, V.nbx, V.nby, a.gen};
-    k_adj_dice<<<ndice, kDiceThreads, 0, st>>>(d);
-    count_launch(owner);
-    k_adj_lamk<<<owner->num_sms * 8, kDiceThreads, 0, st>>>(d);
     count_launch(owner);
     LSS_CUDA(cudaLaunchCooperativeKernel(kr, dim3(gr), dim3(kAdjThreads), params, 0, st));
     count_launch(owner);
