@@ -144,10 +144,10 @@ def sum_over_ranks(ws, value: float) -> float:
 # figure.
 DRAM_TRAFFIC = {("7972d1c57af0", "config2_256", 8, 8, 8, 256): 16057344}
 KERNEL_SOURCES = ("ns_kernels.cuh", "ns_engine.cu", "tma.cuh", "common.cuh")
-# The same for one adjoint call on config 4 (its four kernels: the forward
-# with the call's set-up phase, the two soft-Dice passes, the reverse), from
+# The same for one adjoint call on config 4 (its two kernels: the forward,
+# with the call's set-up and the loss as phases, and the reverse), from
 # the capture in profiles/k_adj_config4_192.md.
-ADJOINT_TRAFFIC = {("95ec282ab517", "config4_192"): 84198912}
+ADJOINT_TRAFFIC = {("b64285c6dd33", "config4_192"): 93274368}
 ADJOINT_SOURCES = ("ns_adjoint.cu", "ns_kernels.cuh", "common.cuh")
 
 
