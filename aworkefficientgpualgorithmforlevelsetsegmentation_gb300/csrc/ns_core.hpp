@@ -40,7 +40,6 @@ class NsCore {
     // add_volume + configure, the buffers and the configuration kept.
     void reload_volume(int v, const float* data, const lss_params& p);
     void set_params(int v, const lss_params& p) {
-        ++epoch_;
         vols_.at(v).p = p;
         vols_.at(v).speed_stale = true;
         upload_descriptors();
@@ -102,10 +101,11 @@ class NsCore {
         int3 dirty_lo{0, 0, 0}, dirty_hi{0, 0, 0};
     };
     const std::vector<VolHost>& vols() const { return vols_; }
-    // Counts the calls that may change a volume's phi, masks, parameters or
-    // layout (every member above that is not a read; the adjoint changes
-    // nothing): the adjoint keeps copies of phi in its workspace between
-    // calls only while this count stays the same.
+    // Counts the calls that may change a volume's phi or the layout
+    // (add_volume, reload_volume, configure, sphere_union, set_phi,
+    // fill_phi, run, dense_run; not parameters, masks or frozen masks): the
+    // adjoint keeps copies of phi in its workspace between calls only while
+    // this count stays the same.
     uint64_t epoch() const { return epoch_; }
     // What the adjoint left in its workspace (ns_adjoint.cu): `valid` while
     // the workspace stays in place (cleared when it is reallocated).

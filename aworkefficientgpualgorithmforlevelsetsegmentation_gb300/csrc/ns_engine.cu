@@ -508,7 +508,6 @@ NsArgs NsCore::args(uint32_t k0, int max_iters, const lss_conv* conv) const {
 // paper's initial active set, main.tex:217-231).  Both phi buffers are made
 // equal first.
 void NsCore::init_active() {
-    ++epoch_;
     LSS_REQUIRE(configured_, LSS_ERR_STATE, "not configured");
     cudaStream_t st = owner_->stream;
     // One volume whose phi is uniform outside a box (cleared, then seeded):
@@ -729,7 +728,6 @@ void NsCore::read_mask(int v, uint8_t* out) {
 }
 
 void NsCore::freeze(int v) {
-    ++epoch_;
     VolHost& V = vols_.at(v);
     const uint32_t p = vols_.size() == 1 ? parity_ : vol_parity(v);
     const uint64_t n = (uint64_t)V.nx * V.ny * V.nz;
@@ -745,7 +743,6 @@ void NsCore::freeze(int v) {
 }
 
 void NsCore::clear_frozen(int v) {
-    ++epoch_;
     VolHost& V = vols_.at(v);
     if (V.frozen) LSS_CUDA(cudaMemsetAsync(V.frozen, 0, (uint64_t)V.nx * V.ny * V.nz, owner_->stream));
     owner_->sync();

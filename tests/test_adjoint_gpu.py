@@ -194,8 +194,9 @@ def test_gpu_adjoint_calls_on_one_engine_match_fresh_engines(brick, threads):
     unchanged and no host staging went through them: device buffers, so the
     later calls take that path.  Each call equals the same call on a fresh
     engine: the same call again, a call whose bias reaches other bricks, the
-    first bias once more, and a call after further iterations of the engine
-    (phi changed: full copies)."""
+    first bias once more, a call after new parameters (phi unchanged: still
+    partial copies), and a call after further iterations of the engine (phi
+    changed: full copies)."""
     torch = pytest.importorskip("torch")
     cfg = P.config4(0.25)
     shape = cfg["image"].shape
@@ -213,8 +214,10 @@ def test_gpu_adjoint_calls_on_one_engine_match_fresh_engines(brick, threads):
         g["d_bias"] = db.cpu().numpy()
         return g
 
-    def fresh(bias, steps=0):
+    def fresh(bias, steps=0, target=None):
         e = make(cfg, brick, threads)
+        if target is not None:
+            e.set_parameters(target=target)
         if steps:
             e.step(steps)
         return call(e, bias)
@@ -233,6 +236,11 @@ def test_gpu_adjoint_calls_on_one_engine_match_fresh_engines(brick, threads):
     r2 = call(s, b2)
     assert r2["active_voxel_iterations"] != r1["active_voxel_iterations"]
     same(r2, fresh(b2))
+    same(call(s, b1), r1)
+    t2 = cfg["params"].target - 0.03
+    s.set_parameters(target=t2)
+    same(call(s, b1), fresh(b1, target=t2))
+    s.set_parameters(target=cfg["params"].target)
     same(call(s, b1), r1)
     s.step(3)
     same(call(s, b1), fresh(b1, steps=3))
