@@ -142,7 +142,7 @@ def sum_over_ranks(ws, value: float) -> float:
 # the key's first field (profiles/k_ns_persistent_config2_256.md gives the
 # capture); a build from other sources reports null rather than a stale
 # figure.
-DRAM_TRAFFIC = {("7972d1c57af0", "config2_256", 8, 8, 8, 256): 16057344}
+DRAM_TRAFFIC = {("6b9bb85714f5", "config2_256", 8, 8, 8, 256): 15818240}
 KERNEL_SOURCES = ("ns_kernels.cuh", "ns_engine.cu", "tma.cuh", "common.cuh")
 # The same for one adjoint call on config 4 (its two kernels: the forward,
 # with the call's set-up and the loss as phases, and the reverse), from
