@@ -45,6 +45,10 @@ struct RefDims {
     uint32_t x, y, z;
 };
 
+// Iterations a run to convergence launches between two reads of the rule's
+// state (an iteration launched after the rule stopped costs its launches).
+constexpr int kRuleChunk = 16;
+
 struct RefCtl {
     unsigned long long n;        // active count (the list length)
     unsigned long long updates;  // sum of n over updates
@@ -57,6 +61,14 @@ struct RefCtl {
     uint32_t clear;              // compaction clears consumed valid flags
     uint32_t ntiles;
     uint32_t tile_counter;
+    // The stopping rule on the device (k_ref_rule_start, k_ref_rule): once
+    // `halt` is set every iteration kernel returns at entry, so iterations
+    // launched after the rule stopped change nothing.
+    uint32_t halt;
+    int32_t conv, streak, patience;
+    unsigned long long done;     // iterations run since k_ref_rule_start
+    unsigned long long n0, abs_thr;
+    double rel;
 };
 
 __device__ __forceinline__ uint32_t d_tiled(uint32_t x, uint32_t y, uint32_t z, RefDims d) {
@@ -146,6 +158,7 @@ __global__ void __launch_bounds__(kThreads) k_ref_update(
     int8_t* __restrict__ wr, uint8_t* __restrict__ ex, uint8_t* __restrict__ tag,
     const int8_t* __restrict__ rd, const uint32_t* __restrict__ active, const void* src,
     RefDims d, RefCtl* ctl, int32_t target, int32_t window, float alpha, float dt_in) {
+    if (ctl->halt) return;
     const uint64_t n = ctl->n;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x) {
@@ -195,6 +208,7 @@ __global__ void __launch_bounds__(kThreads) k_ref_update(
 
 // Path choice, compaction sizing, status reset (one block).
 __global__ void k_ref_plan(RefCtl* c, uint64_t* status, uint32_t N, int reinit, int count_update) {
+    if (c->halt) return;
     __shared__ uint32_t s_ntiles;
     if (threadIdx.x == 0) {
         uint32_t n = (uint32_t)c->n;
@@ -223,7 +237,7 @@ __global__ void __launch_bounds__(kThreads) k_ref_output(uint32_t* coord, uint32
                                                         const int8_t* rd, const uint8_t* tag,
                                                         const uint32_t* active, RefDims d,
                                                         RefCtl* ctl, int quirk) {
-    if (ctl->path != 0u) return;
+    if (ctl->halt || ctl->path != 0u) return;
     const uint64_t n = ctl->n;
     const uint64_t A = ctl->A;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
@@ -245,7 +259,7 @@ __global__ void __launch_bounds__(kThreads) k_ref_output(uint32_t* coord, uint32
 // MemSetSparseKernel<unsigned char> (MemSetFloat.cu:227-290) on the tag volume.
 __global__ void __launch_bounds__(kThreads) k_ref_clear_tag(uint8_t* tag, const uint32_t* active,
                                                            RefDims d, RefCtl* ctl) {
-    if (ctl->path != 0u) return;
+    if (ctl->halt || ctl->path != 0u) return;
     const uint64_t n = ctl->n;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x) {
@@ -259,7 +273,7 @@ __global__ void __launch_bounds__(kThreads) k_ref_clear_tag(uint8_t* tag, const 
 __global__ void __launch_bounds__(kThreads) k_ref_filter0(const uint32_t* coord,
                                                          const uint32_t* valid, uint8_t* tag,
                                                          RefDims d, RefCtl* ctl) {
-    if (ctl->path != 0u) return;
+    if (ctl->halt || ctl->path != 0u) return;
     const uint64_t n = ctl->n;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x)
@@ -274,7 +288,7 @@ __global__ void __launch_bounds__(kThreads) k_ref_filter0(const uint32_t* coord,
 __global__ void __launch_bounds__(kThreads) k_ref_filter(const uint32_t* coord, uint32_t* valid,
                                                         uint8_t* tag, RefDims d, RefCtl* ctl,
                                                         int e) {
-    if (ctl->path != 0u) return;
+    if (ctl->halt || ctl->path != 0u) return;
     const uint64_t n = ctl->n;
     const uint64_t base = (uint64_t)ctl->A * e;
     const uint8_t mark = (uint8_t)(e + 1);
@@ -295,7 +309,7 @@ __global__ void __launch_bounds__(kThreads) k_ref_filter(const uint32_t* coord, 
 // written in tiled order so that the stores coalesce.
 __global__ void __launch_bounds__(kThreads) k_ref_coord_init(uint32_t* coord, RefDims d,
                                                             const RefCtl* ctl, int force) {
-    if (!force && ctl->do_coord == 0u) return;
+    if (ctl->halt || (!force && ctl->do_coord == 0u)) return;
     const uint64_t N = (uint64_t)d.x * d.y * d.z;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < N;
          i += (uint64_t)gridDim.x * blockDim.x)
@@ -307,7 +321,7 @@ __global__ void __launch_bounds__(kThreads) k_ref_scatter(uint32_t* valid, const
                                                          const uint8_t* tag,
                                                          const uint32_t* active, RefDims d,
                                                          RefCtl* ctl, int quirk) {
-    if (ctl->path != 1u) return;
+    if (ctl->halt || ctl->path != 1u) return;
     const uint64_t n = ctl->n;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x) {
@@ -403,6 +417,7 @@ __global__ void __launch_bounds__(kThreads) k_ref_compact(const uint32_t* __rest
                                                          uint64_t* status) {
     constexpr int kItems = kTile / kThreads;  // 16, contiguous per thread
     __shared__ uint32_t s_tile;
+    if (ctl->halt) return;
     const uint32_t m = ctl->m, ntiles = ctl->ntiles, clear = ctl->clear;
     for (;;) {
         if (threadIdx.x == 0) s_tile = atomicAdd(&ctl->tile_counter, 1u);
@@ -439,6 +454,38 @@ __global__ void __launch_bounds__(kThreads) k_ref_compact(const uint32_t* __rest
             if (flags & (1u << q)) dst[o++] = src[base + q];
         if (tile == ntiles - 1 && threadIdx.x == 0) ctl->n = prefix + total;
     }
+}
+
+// The stopping rule of a run to convergence, evaluated on the device after
+// every iteration (the host then reads the count back once per chunk of
+// launched iterations instead of once per iteration): unless halted, count
+// the iteration; with the rule on, stop when n <= abs_thr, else count the
+// streak of iterations with n < rel * n0 and stop when it reaches patience.
+__global__ void k_ref_rule(RefCtl* c) {
+    if (c->halt) return;
+    c->done += 1ull;
+    if (!c->conv) return;
+    const unsigned long long n = c->n;
+    if (n <= c->abs_thr) {
+        c->halt = 1u;
+        return;
+    }
+    c->streak = ((double)n < c->rel * (double)c->n0) ? c->streak + 1 : 0;
+    if (c->streak >= c->patience) c->halt = 1u;
+}
+
+// The rule's state at the start of a step: n0 is the count the step starts
+// from.
+__global__ void k_ref_rule_start(RefCtl* c, int32_t conv, double rel, unsigned long long abs_thr,
+                                 int32_t patience) {
+    c->halt = 0u;
+    c->done = 0ull;
+    c->streak = 0;
+    c->conv = conv;
+    c->rel = rel;
+    c->abs_thr = abs_thr;
+    c->patience = patience;
+    c->n0 = c->n;
 }
 
 // Sum and sum of squares of the source where the export volume is <= 0
@@ -671,6 +718,8 @@ class RefEngine : public EngineBase {
         }
         k_ref_compact<<<B, kThreads, 0, stream>>>(coord_, valid_, active_, ctl_, status_);
         ++launches;
+        k_ref_rule<<<1, 1, 0, stream>>>(ctl_);
+        ++launches;
     }
 
     // A graph of one normal iteration for each buffer parity.
@@ -719,7 +768,11 @@ class RefEngine : public EngineBase {
         return (float)device_n() <= params.convergence_threshold && iterations_ > 500;
     }
 
-    // RequestUpdateSegmentation (Segmenter.cpp:759-1051).
+    // RequestUpdateSegmentation (Segmenter.cpp:759-1051).  With a stopping
+    // rule the rule runs on the device after every iteration (k_ref_rule)
+    // and the host reads its state back once per kRuleChunk launched
+    // iterations; iterations launched after it stopped do nothing, and the
+    // buffer swaps the host made for them are undone by parity.
     int step(int k, const lss_conv* conv) override {
         require_loaded();
         if (params_changed()) iterations_ = 0;
@@ -729,9 +782,11 @@ class RefEngine : public EngineBase {
         LSS_CUDA(cudaEventCreate(&e0));
         LSS_CUDA(cudaEventCreate(&e1));
         LSS_CUDA(cudaEventRecord(e0, stream));
-        int done = 0;
-        uint64_t n0 = conv ? device_n() : 0;
-        int streak = 0;
+        k_ref_rule_start<<<1, 1, 0, stream>>>(ctl_, conv ? 1 : 0, conv ? conv->rel_threshold : 0.0,
+                                              conv ? (unsigned long long)conv->abs_threshold : 0ull,
+                                              conv ? conv->patience : 0);
+        ++launches;
+        int launched = 0;
         for (int s = 0; s < k; ++s) {
             bool reinit = params_changed();
             if (reinit) {
@@ -739,24 +794,30 @@ class RefEngine : public EngineBase {
                 iterations_ = 0;
             }
             run_iteration(reinit);
-            ++iterations_;
-            ++done;
-            if (conv) {
-                uint64_t n = device_n();
-                if (n <= conv->abs_threshold) break;
-                if ((double)n < conv->rel_threshold * (double)n0) ++streak; else streak = 0;
-                if (streak >= conv->patience) break;
+            ++launched;
+            if (conv && launched % kRuleChunk == 0 && s + 1 < k) {
+                uint32_t halt = 0;
+                LSS_CUDA(cudaMemcpyAsync(&halt, &ctl_->halt, sizeof(halt), cudaMemcpyDeviceToHost, stream));
+                sync();
+                if (halt) break;
             }
         }
         LSS_CUDA(cudaEventRecord(e1, stream));
+        unsigned long long done = 0;
+        LSS_CUDA(cudaMemcpyAsync(&done, &ctl_->done, sizeof(done), cudaMemcpyDeviceToHost, stream));
+        LSS_CUDA(cudaMemsetAsync(&ctl_->halt, 0, sizeof(uint32_t), stream));  // rebuilds run again
         LSS_CUDA(cudaEventSynchronize(e1));
+        sync();
+        LSS_REQUIRE(done <= (unsigned long long)launched, LSS_ERR_STATE, "iteration count");
+        if (((unsigned long long)launched - done) & 1ull) swap();
+        iterations_ += (int)done;
         float ms = 0;
         cudaEventElapsedTime(&ms, e0, e1);
         last_ms_ = ms;
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         check_errors();
-        return done;
+        return (int)done;
     }
 
     uint64_t active_count() override { return loaded_ ? device_n() : 0; }

@@ -89,3 +89,74 @@ def test_ref_finished_rule_and_errors():
     assert s.request_update_segmentation(510) == 510
     assert s.is_segmentation_finished()
     assert s.request_update_segmentation(5) == 0  # finished: RequestUpdateSegmentation does nothing
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_ref_run_to_convergence_stops_where_the_rule_says(use_graph):
+    """The stopping rule of a run to convergence is evaluated on the device
+    after every iteration and read back once per chunk of launched
+    iterations; iterations launched after it stopped must change nothing.
+    The run stops at the iteration the rule, applied to the oracle's count
+    after every single iteration, names, with the oracle's state; a cap below
+    that runs exactly the cap."""
+    import aworkefficientgpualgorithmforlevelsetsegmentation_gb300 as lss
+    from aworkefficientgpualgorithmforlevelsetsegmentation_gb300 import phantoms as P
+
+    cfg = P.config2(0.25)
+    vol = np.clip(np.rint(cfg["image"] * 255.0), 0, 255).astype(np.uint8)
+    rel, patience = 1e-3, 5
+
+    def gpu():
+        s = lss.Segmenter(lss.MODE_REF, use_graph=use_graph)
+        s.load_volume(vol)
+        s.set_parameters(204, 26, 0.1, 0.25)
+        for (x, y, z, r) in cfg["spheres"]:
+            s.initialize_seed((x, y, z), r)
+        return s
+
+    c = O.RefOracle(vol, 0)
+    c.set_params(204, 26, 0.1, 0.25)
+    for (x, y, z, r) in cfg["spheres"]:
+        c.initialize_seed(x, y, z, r)
+    n0, streak, it = c.n, 0, 0
+    while it < 2000:
+        c.step(1)
+        it += 1
+        n = c.n
+        if n <= 0:
+            break
+        streak = streak + 1 if n < rel * n0 else 0
+        if streak >= patience:
+            break
+    assert 40 < it < 2000
+    s = gpu()
+    assert s.step_until_converged(rel, patience, 2000) == it
+    assert s.stats()["iterations"] == it
+    assert s.get_active_element_count() == c.n
+    assert np.array_equal(s.active(), c.active())
+    assert np.array_equal(s.read_phi(), c.read_phi())
+    assert np.array_equal(s.get_saveable_segmentation(), c.read_mask())
+    # A cap that falls inside a chunk of launched iterations.
+    cap = it - 3
+    s2 = gpu()
+    assert s2.step_until_converged(rel, patience, cap) == cap
+    c2 = O.RefOracle(vol, 0)
+    c2.set_params(204, 26, 0.1, 0.25)
+    for (x, y, z, r) in cfg["spheres"]:
+        c2.initialize_seed(x, y, z, r)
+    c2.step(cap)
+    assert np.array_equal(s2.active(), c2.active())
+    assert np.array_equal(s2.read_phi(), c2.read_phi())
+    # The engine keeps working after a run that stopped early (its rebuilds
+    # and further steps are not halted).
+    s.clear_current_segmentation()
+    for (x, y, z, r) in cfg["spheres"]:
+        s.initialize_seed((x, y, z), r)
+    s.request_update_segmentation(7)
+    c3 = O.RefOracle(vol, 0)
+    c3.set_params(204, 26, 0.1, 0.25)
+    for (x, y, z, r) in cfg["spheres"]:
+        c3.initialize_seed(x, y, z, r)
+    c3.step(7)
+    assert np.array_equal(s.active(), c3.active())
+    assert np.array_equal(s.read_phi(), c3.read_phi())
