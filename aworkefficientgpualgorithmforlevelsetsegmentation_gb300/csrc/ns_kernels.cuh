@@ -518,6 +518,62 @@ __device__ __forceinline__ void ns_fetch_mask(const NsArgs& a, NsSmem<S, NT>& sm
     }
 }
 
+// The xy-dilated plane of mask word c for the pair of xy offsets `pair`
+// ((ox + 1) + 3 (oy + 1)): its part that lands in that neighbour column.
+template <class S>
+__host__ __device__ __forceinline__ uint64_t xy_plane(uint64_t c, int pair, int nbh) {
+    const int ox = pair % 3 - 1, oy = pair / 3 - 1;
+    if (nbh == 26) return dil_y<S>(dil_x<S>(c, ox), oy);
+    if (ox == 0 && oy == 0) return dil_x<S>(c, 0) | dil_y<S>(c, 0);
+    if (ox == 0 || oy == 0) return ox ? dil_x<S>(c, ox) : dil_y<S>(c, oy);
+    return 0ull;
+}
+
+// Word w of the neighbour at (ox, oy, oz), with one z-plane per mask word,
+// from the 9 x WORDS xy-dilated planes xyp (xy_plane, WORDS per pair) and
+// the changed mask word W(q): an OR of up to three planes.  Equals
+// dilate_word.
+template <class S, class WF>
+__host__ __device__ __forceinline__ uint64_t plane_word(const unsigned long long* xyp, WF W, int ox, int oy, int oz,
+                                                        int w, int nbh) {
+    const unsigned long long* xy = xyp + ((oy + 1) * 3 + (ox + 1)) * S::WORDS;
+    const bool center = ox == 0 && oy == 0;
+    if (nbh == 26)
+        return oz == 0 ? (xy[w] | (w > 0 ? xy[w - 1] : 0ull) | (w < S::WORDS - 1 ? xy[w + 1] : 0ull))
+                       : (oz < 0 ? (w == S::WORDS - 1 ? xy[0] : 0ull) : (w == 0 ? xy[S::WORDS - 1] : 0ull));
+    if (oz == 0) return xy[w] | (center ? ((w > 0 ? W(w - 1) : 0ull) | (w < S::WORDS - 1 ? W(w + 1) : 0ull)) : 0ull);
+    return center ? (oz < 0 ? (w == S::WORDS - 1 ? W(0) : 0ull) : (w == 0 ? W(S::WORDS - 1) : 0ull)) : 0ull;
+}
+
+// The work items of a brick's neighbour words.  With one z-plane per mask
+// word a neighbour above or below the brick receives one word only (the
+// plane next to the brick), so the 9 neighbours of the brick's own layer
+// take WORDS items each and the 18 others one item each; otherwise item t is
+// word t % WORDS of neighbour t / WORDS.  Item t (< dilate_items<S>()) ->
+// neighbour slot (ox + 1) + 3 (oy + 1) + 9 (oz + 1) and word w; returns
+// whether it is the only word of its neighbour.
+template <class S>
+__host__ __device__ constexpr int dilate_layer_items() {
+    return S::XY == 64 ? 9 * S::WORDS : 27 * S::WORDS;
+}
+template <class S>
+__host__ __device__ constexpr int dilate_items() {
+    return S::XY == 64 ? dilate_layer_items<S>() + 18 : dilate_layer_items<S>();
+}
+template <class S>
+__host__ __device__ __forceinline__ bool dilate_item(int t, int& slot, int& w) {
+    constexpr int LAYER = dilate_layer_items<S>();
+    if (t < LAYER) {
+        slot = (S::XY == 64 ? 9 : 0) + t / S::WORDS;  // with planes: the layer oz = 0
+        w = t % S::WORDS;
+        return false;
+    }
+    const int q = t - LAYER;  // q < 9: the layer below, else above
+    slot = q < 9 ? q : q + 9;
+    w = q < 9 ? S::WORDS - 1 : 0;
+    return true;
+}
+
 // Phase 1 of a brick's dilation with one z-plane per mask word (XY == 64):
 // the 9 x WORDS xy-dilated planes of the changed mask cw (ballot words),
 // once each, into xy.  Threads t0, t0 + stride, ...
@@ -525,53 +581,30 @@ template <class S>
 __device__ __forceinline__ void dilate_planes(const NsVol& V, const uint32_t* cw, unsigned long long* xy,
                                               int t0, int stride) {
     for (int t = t0; t < 9 * S::WORDS; t += stride) {
-        const int pair = t / S::WORDS, w = t % S::WORDS;
-        const int ox = pair % 3 - 1, oy = pair / 3 - 1;
-        const uint64_t c = (uint64_t)cw[2 * w] | ((uint64_t)cw[2 * w + 1] << 32);
-        uint64_t v;
-        if (V.nbh == 26) v = dil_y<S>(dil_x<S>(c, ox), oy);
-        else if (ox == 0 && oy == 0) v = dil_x<S>(c, 0) | dil_y<S>(c, 0);
-        else if (ox == 0 || oy == 0) v = ox ? dil_x<S>(c, ox) : dil_y<S>(c, oy);
-        else v = 0ull;
-        xy[t] = v;
+        const int w = t % S::WORDS;
+        xy[t] = xy_plane<S>((uint64_t)cw[2 * w] | ((uint64_t)cw[2 * w + 1] << 32), t / S::WORDS, V.nbh);
     }
 }
 
 // Phase 2: each thread computes one word of one neighbour of brick b (origin
-// x0, y0, z0) and ORs it into the next masks (parity p ^ 1); one thread per
-// neighbour sets its membership bit in bits[sn] (reductions, no round trip).
-// With one z-plane per mask word each neighbour word is an OR of up to three
-// xy-dilated planes, and a neighbour above or below the brick receives one
-// word only (the plane next to the brick): the 9 neighbours of the brick's
-// own layer take WORDS threads each and the 18 others one thread each.
-// Otherwise thread t computes word t % WORDS of neighbour t / WORDS.
-// Threads t0, t0 + STRIDE, ...; STRIDE is a multiple of 32 and every lane of
-// a calling warp takes part (ballots).
+// x0, y0, z0; the items of dilate_item) and ORs it into the next masks
+// (parity p ^ 1); one thread per neighbour sets its membership bit in
+// bits[sn] (reductions, no round trip).  Threads t0, t0 + STRIDE, ...;
+// STRIDE is a multiple of 32 and every lane of a calling warp takes part
+// (ballots).
 template <class S, int STRIDE>
 __device__ __forceinline__ void dilate_scatter(const NsArgs& a, const NsVol& V, const uint32_t* cw,
                                                const unsigned long long* xyp, uint32_t b, int x0, int y0,
                                                int z0, uint32_t p, uint32_t sn, int t0) {
     static_assert(STRIDE % 32 == 0, "whole warps");
     auto W = [&](int q) -> uint64_t { return (uint64_t)cw[2 * q] | ((uint64_t)cw[2 * q + 1] << 32); };
-    constexpr bool kPlanes = S::XY == 64;  // one z-plane per mask word
-    constexpr int LAYER = kPlanes ? 9 * S::WORDS : 27 * S::WORDS;  // grouped items
-    constexpr int ITEMS = kPlanes ? LAYER + 18 : LAYER;
+    constexpr int ITEMS = dilate_items<S>();
     constexpr int ROUNDS = (ITEMS + STRIDE - 1) / STRIDE;
 #pragma unroll
     for (int r = 0; r < ROUNDS; ++r) {
         const int t = t0 + r * STRIDE;
-        // Item t: neighbour slot (ox, oy, oz) and word w; `single`: the only
-        // word of its neighbour.
-        const bool single = t >= LAYER;
         int slot, w;
-        if (!single) {
-            slot = (kPlanes ? 9 : 0) + t / S::WORDS;  // kPlanes: the layer oz = 0
-            w = t % S::WORDS;
-        } else {
-            const int q = t - LAYER;  // q < 9: the layer below, else above
-            slot = q < 9 ? q : q + 9;
-            w = q < 9 ? S::WORDS - 1 : 0;
-        }
+        const bool single = dilate_item<S>(t, slot, w);
         uint64_t x = 0ull;
         uint32_t nb = 0;
         if (t < ITEMS) {
@@ -581,23 +614,8 @@ __device__ __forceinline__ void dilate_scatter(const NsArgs& a, const NsVol& V, 
             // (bricks in the padding beyond the volume hold none).
             const int lx = V.nx - bx * S::X, ly = V.ny - by * S::Y, lz = V.nz - bz * S::Z;
             if (bx >= 0 && by >= 0 && bz >= 0 && lx > 0 && ly > 0 && lz > 0) {
-                if constexpr (kPlanes) {
-                    const unsigned long long* xy = xyp + ((oy + 1) * 3 + (ox + 1)) * S::WORDS;
-                    const bool center = ox == 0 && oy == 0;
-                    if (V.nbh == 26) {
-                        x = oz == 0 ? (xy[w] | (w > 0 ? xy[w - 1] : 0ull) | (w < S::WORDS - 1 ? xy[w + 1] : 0ull))
-                                    : (oz < 0 ? (w == S::WORDS - 1 ? xy[0] : 0ull)
-                                              : (w == 0 ? xy[S::WORDS - 1] : 0ull));
-                    } else if (oz == 0) {
-                        x = xy[w] | (center ? ((w > 0 ? W(w - 1) : 0ull) | (w < S::WORDS - 1 ? W(w + 1) : 0ull)) : 0ull);
-                    } else {
-                        x = center ? (oz < 0 ? (w == S::WORDS - 1 ? W(0) : 0ull)
-                                             : (w == 0 ? W(S::WORDS - 1) : 0ull))
-                                   : 0ull;
-                    }
-                } else {
-                    x = dilate_word<S>(cw, ox, oy, oz, w, V.nbh);
-                }
+                if constexpr (S::XY == 64) x = plane_word<S>(xyp, W, ox, oy, oz, w, V.nbh);
+                else x = dilate_word<S>(cw, ox, oy, oz, w, V.nbh);
                 if (lx < S::X || ly < S::Y || lz < S::Z)
                     x &= inside_mask<S>(w, min(lx, S::X), min(ly, S::Y), min(lz, S::Z));
                 nb = b + (int32_t)((oz * V.nby + oy) * V.nbx + ox);
@@ -605,7 +623,7 @@ __device__ __forceinline__ void dilate_scatter(const NsArgs& a, const NsVol& V, 
             }
         }
         // The WORDS threads of a grouped neighbour are adjacent lanes of one
-        // warp (LAYER is a multiple of WORDS).
+        // warp (the layer's item count is a multiple of WORDS).
         const uint32_t bal = __ballot_sync(0xffffffffu, x != 0ull);
         const int lane = t & 31, g0 = lane & ~(S::WORDS - 1);
         const uint32_t gmask = (S::WORDS >= 32 ? 0xffffffffu : ((1u << S::WORDS) - 1u)) << g0;

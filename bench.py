@@ -142,12 +142,12 @@ def sum_over_ranks(ws, value: float) -> float:
 # the key's first field (profiles/k_ns_persistent_config2_256.md gives the
 # capture); a build from other sources reports null rather than a stale
 # figure.
-DRAM_TRAFFIC = {("6b9bb85714f5", "config2_256", 8, 8, 8, 256): 15818240}
+DRAM_TRAFFIC = {("33ce358840f2", "config2_256", 8, 8, 8, 256): 15782912}
 KERNEL_SOURCES = ("ns_kernels.cuh", "ns_engine.cu", "tma.cuh", "common.cuh")
 # The same for one adjoint call on config 4 (its two kernels: the forward,
 # with the call's set-up and the loss as phases, and the reverse), from
 # the capture in profiles/k_adj_config4_192.md.
-ADJOINT_TRAFFIC = {("b64285c6dd33", "config4_192"): 93274368}
+ADJOINT_TRAFFIC = {("3154f73a7bde", "config4_192"): 93294592}
 ADJOINT_SOURCES = ("ns_adjoint.cu", "ns_kernels.cuh", "common.cuh")
 
 

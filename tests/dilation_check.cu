@@ -1,8 +1,9 @@
 // Host-side check of the bit-parallel brick dilation (dilate_slot,
 // dilate_word, inside_mask in csrc/ns_kernels.cuh) against a brute-force
 // dilation, for every brick shape, both neighbourhoods and every neighbour
-// slot; and the rank-selection helpers nth_set_bit and div_magic against
-// plain loops and division.  Built and run by tests/test_dilation_host.py
+// slot; of the kernels' work split of it (xy_plane, plane_word,
+// dilate_item); and the rank-selection helpers nth_set_bit and div_magic
+// against plain loops and division.  Built and run by tests/test_dilation_host.py
 // (no GPU needed).
 #include "ns_kernels.cuh"
 #include <cstdio>
@@ -49,6 +50,46 @@ template <class S> int check(std::mt19937_64& rng, int nbh) {
     }
     return bad;
 }
+// The per-brick work split of the kernels' dilation: xy_plane + plane_word
+// (one z-plane a mask word) equal dilate_word, and the items of dilate_item
+// cover each (neighbour, word) at most once and every word that can be
+// non-zero (the words they skip are zero for every mask).
+template <class S> int check_items(std::mt19937_64& rng, int nbh) {
+    int bad = 0;
+    int seen[27][S::WORDS] = {};
+    for (int t = 0; t < dilate_items<S>(); ++t) {
+        int slot = -1, w = -1;
+        const bool single = dilate_item<S>(t, slot, w);
+        if (slot < 0 || slot >= 27 || w < 0 || w >= S::WORDS) { ++bad; continue; }
+        ++seen[slot][w];
+        if (single != (t >= dilate_layer_items<S>())) ++bad;
+    }
+    for (int slot = 0; slot < 27; ++slot)
+        for (int w = 0; w < S::WORDS; ++w)
+            if (seen[slot][w] > 1) ++bad;
+    for (int trial = 0; trial < 2000; ++trial) {
+        uint64_t c[S::WORDS];
+        for (int w = 0; w < S::WORDS; ++w) {
+            c[w] = rng();
+            for (int q = 0; q < trial % 4; ++q) c[w] &= rng();
+        }
+        uint32_t c32[2 * S::WORDS];
+        for (int w = 0; w < S::WORDS; ++w) { c32[2 * w] = (uint32_t)c[w]; c32[2 * w + 1] = (uint32_t)(c[w] >> 32); }
+        unsigned long long xy[9 * S::WORDS];
+        for (int t = 0; t < 9 * S::WORDS; ++t) xy[t] = xy_plane<S>(c[t % S::WORDS], t / S::WORDS, nbh);
+        auto W = [&](int q) -> uint64_t { return c[q]; };
+        for (int slot = 0; slot < 27; ++slot) {
+            const int ox = slot % 3 - 1, oy = (slot / 3) % 3 - 1, oz = slot / 9 - 1;
+            for (int w = 0; w < S::WORDS; ++w) {
+                const uint64_t want = dilate_word<S>(c32, ox, oy, oz, w, nbh);
+                if (!seen[slot][w] && want) ++bad;
+                if constexpr (S::XY == 64)
+                    if (plane_word<S>(xy, W, ox, oy, oz, w, nbh) != want) ++bad;
+            }
+        }
+    }
+    return bad;
+}
 int check_select(std::mt19937_64& rng) {
     int bad = 0;
     for (int trial = 0; trial < 20000; ++trial) {
@@ -80,6 +121,10 @@ int main() {
     for (int nbh : {26, 6}) {
         int a = check<Brick<8, 8, 8>>(rng, nbh), b = check<Brick<8, 8, 4>>(rng, nbh), c = check<Brick<4, 4, 4>>(rng, nbh);
         printf("nbh %d: 888 %d, 884 %d, 444 %d\n", nbh, a, b, c);
+        bad += a + b + c;
+        a = check_items<Brick<8, 8, 8>>(rng, nbh), b = check_items<Brick<8, 8, 4>>(rng, nbh),
+        c = check_items<Brick<4, 4, 4>>(rng, nbh);
+        printf("items, nbh %d: 888 %d, 884 %d, 444 %d\n", nbh, a, b, c);
         bad += a + b + c;
     }
     printf(bad ? "FAIL\n" : "OK\n");
