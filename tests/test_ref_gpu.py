@@ -118,17 +118,24 @@ def test_ref_run_to_convergence_stops_where_the_rule_says(use_graph):
     c.set_params(204, 26, 0.1, 0.25)
     for (x, y, z, r) in cfg["spheres"]:
         c.initialize_seed(x, y, z, r)
-    n0, streak, it = c.n, 0, 0
-    while it < 2000:
+    n0, ns = c.n, []
+
+    def stop_at(rel_, patience_, abs_):
+        streak = 0
+        for i, n in enumerate(ns):
+            if n <= abs_:
+                return i + 1
+            streak = streak + 1 if n < rel_ * n0 else 0
+            if streak >= patience_:
+                return i + 1
+        return None
+
+    it = None
+    while it is None and len(ns) < 2000:
         c.step(1)
-        it += 1
-        n = c.n
-        if n <= 0:
-            break
-        streak = streak + 1 if n < rel * n0 else 0
-        if streak >= patience:
-            break
-    assert 40 < it < 2000
+        ns.append(c.n)
+        it = stop_at(rel, patience, 0)
+    assert it is not None and 40 < it < 2000
     s = gpu()
     assert s.step_until_converged(rel, patience, 2000) == it
     assert s.stats()["iterations"] == it
@@ -147,6 +154,11 @@ def test_ref_run_to_convergence_stops_where_the_rule_says(use_graph):
     c2.step(cap)
     assert np.array_equal(s2.active(), c2.active())
     assert np.array_equal(s2.read_phi(), c2.read_phi())
+    # The absolute threshold: the run stops at the first count at or below
+    # it (a count the run passes through about half way).
+    abs_thr = ns[it // 2]
+    s4 = gpu()
+    assert s4.step_until_converged(rel, patience, 2000, abs_threshold=abs_thr) == stop_at(rel, patience, abs_thr)
     # The engine keeps working after a run that stopped early (its rebuilds
     # and further steps are not halted).
     s.clear_current_segmentation()
