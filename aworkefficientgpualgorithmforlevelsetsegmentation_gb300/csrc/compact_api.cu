@@ -3,9 +3,10 @@
 // Cuda.cpp:699-758), which wraps CUDPP 1.1's cudppCompact.
 //
 // Stable: dst receives src[i] for every i < n with valid[i] != 0, in index
-// order.  Single pass with decoupled lookback over tiles of 4096 elements; the
-// count is written to device memory (the reference copies it to the host
-// after every 2^25-element chunk).
+// order.  Single pass with decoupled lookback over tiles of 4096 elements
+// (16-byte coalesced loads, a warp-parallel lookback); the count is written
+// to device memory (the reference copies it to the host after every
+// 2^25-element chunk).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -21,6 +22,8 @@ namespace lss {
 constexpr int kCompactThreads = 256;
 constexpr int kCompactItems = 16;
 constexpr int kCompactTile = kCompactThreads * kCompactItems;
+constexpr int kCompactWarps = kCompactThreads / 32;
+constexpr int kCompactSeg = kCompactTile / kCompactWarps;  // 512 elements a warp: 4 chunks of 128
 
 struct CompactScratch {
     uint64_t* status;        // one word per tile, zero before the pass
@@ -28,6 +31,69 @@ struct CompactScratch {
     uint32_t* err;
 };
 
+// Exclusive prefix of `tile` by decoupled lookback, one warp (all 32 lanes
+// call it): lane 0 publishes the tile's aggregate, then the warp reads the
+// status words of the 32 tiles before a window start at once; it adds the
+// values up to and including the nearest inclusive prefix, or moves the
+// window back by 32 when there is none.  A tile in the window that is not
+// published yet (before the nearest inclusive prefix) is read again, for
+// kWaitLimitNs at most (then the error bit is set and the sum so far
+// returned).  Lane 0 then publishes the tile's inclusive prefix.
+__device__ __forceinline__ uint64_t warp_tile_prefix(uint64_t* status, uint32_t tile, uint64_t aggregate,
+                                                     uint32_t* err) {
+    const int lane = threadIdx.x & 31;
+    if (tile == 0) {
+        if (lane == 0) st_release_u64(&status[0], kFlagP | (aggregate & kValMask));
+        return 0;
+    }
+    if (lane == 0) st_release_u64(&status[tile], kFlagA | (aggregate & kValMask));
+    uint64_t excl = 0;
+    int64_t j = (int64_t)tile - 1;  // the window is tiles j, j-1, ..., j-31 (lane order)
+    uint64_t t0 = 0;
+    for (;;) {
+        const int64_t idx = j - lane;
+        const uint64_t st = idx >= 0 ? ld_acquire_u64(&status[idx]) : kFlagP;  // before tile 0: prefix 0
+        const uint32_t flag = (uint32_t)(st >> 62);
+        const uint32_t pmask = __ballot_sync(0xffffffffu, flag == 2u);
+        const uint32_t zmask = __ballot_sync(0xffffffffu, flag == 0u);
+        const int first_p = pmask ? __ffs(pmask) - 1 : 32;
+        const uint32_t need = first_p == 32 ? 0xffffffffu : ((2u << first_p) - 1u);  // lanes 0..first_p
+        if (zmask & need) {
+            // Lane 0 keeps the time, so the whole warp gives up together.
+            int give_up = 0;
+            if (lane == 0) {
+                if (t0 == 0) t0 = globaltimer_ns();
+                else if (globaltimer_ns() - t0 > kWaitLimitNs) give_up = 1;
+            }
+            if (__shfl_sync(0xffffffffu, give_up, 0)) {
+                if (lane == 0) set_error(err, ERR_LOOKBACK_TIMEOUT);
+                break;
+            }
+            continue;
+        }
+        uint64_t v = ((need >> lane) & 1u) ? (st & kValMask) : 0ull;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        excl += v;
+        if (first_p < 32) break;
+        j -= 32;
+        t0 = 0;
+    }
+    if (lane == 0) st_release_u64(&status[tile], kFlagP | ((excl + aggregate) & kValMask));
+    return excl;
+}
+
+// Stable compaction, tiles of 4096 elements taken from a tile counter (so
+// every lookback waits on a resident block).  Warp w of a tile takes the 512
+// elements [512 w, 512 w + 512) as four chunks of 128, lane l the four
+// elements 4 l .. 4 l + 3 of each chunk, read as 16-byte loads (a warp's load
+// is 512 contiguous bytes; all eight loads of a thread are issued before any
+// is used).  Ranks: one warp inclusive scan of the four per-chunk counts
+// packed into the bytes of a word (a chunk holds at most 128), the warps'
+// totals by a block scan, the tile's prefix by warp 0's lookback.  A lane's
+// kept elements go to consecutive places, after those of the lanes before
+// it, so the stores of a chunk are contiguous too.  n need not be a multiple
+// of 4: the tail is read element by element.
 __global__ void __launch_bounds__(kCompactThreads) k_compact_u32(const uint32_t* __restrict__ src,
                                                                  const uint32_t* __restrict__ valid,
                                                                  uint32_t* __restrict__ dst,
@@ -35,24 +101,81 @@ __global__ void __launch_bounds__(kCompactThreads) k_compact_u32(const uint32_t*
                                                                  unsigned long long* count,
                                                                  CompactScratch sc) {
     __shared__ uint32_t s_tile;
+    __shared__ uint32_t s_warp[kCompactWarps];
+    __shared__ uint64_t s_prefix;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint64_t ntiles = (n + kCompactTile - 1) / kCompactTile;
+    const bool vec = ((uintptr_t)src % 16 == 0) && ((uintptr_t)valid % 16 == 0);
     for (;;) {
         if (threadIdx.x == 0) s_tile = atomicAdd(sc.tile_counter, 1u);
         __syncthreads();
         const uint32_t tile = s_tile;
-        __syncthreads();
         if (tile >= ntiles) break;
-        const uint64_t base = (uint64_t)tile * kCompactTile + (uint64_t)threadIdx.x * kCompactItems;
-        uint32_t flags = 0;
-        for (int q = 0; q < kCompactItems; ++q)
-            if (base + q < n && valid[base + q] != 0u) flags |= 1u << q;
-        uint32_t total;
-        const uint32_t off = block_exclusive_sum(__popc(flags), &total);
-        const uint64_t prefix = tile_exclusive_prefix(sc.status, tile, total, sc.err);
-        uint64_t o = prefix + off;
-        for (int q = 0; q < kCompactItems; ++q)
-            if (flags & (1u << q)) dst[o++] = src[base + q];
-        if (tile == ntiles - 1 && threadIdx.x == 0) *count = prefix + total;
+        const uint64_t seg = (uint64_t)tile * kCompactTile + (uint64_t)warp * kCompactSeg;
+        uint4 fv[4], sv[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint64_t i = seg + (uint64_t)q * 128 + (uint64_t)lane * 4;
+            if (vec && i + 4 <= n) {
+                fv[q] = *reinterpret_cast<const uint4*>(valid + i);
+                sv[q] = *reinterpret_cast<const uint4*>(src + i);
+            } else {
+                fv[q] = make_uint4(i < n ? valid[i] : 0u, i + 1 < n ? valid[i + 1] : 0u,
+                                   i + 2 < n ? valid[i + 2] : 0u, i + 3 < n ? valid[i + 3] : 0u);
+                sv[q] = make_uint4(i < n ? src[i] : 0u, i + 1 < n ? src[i + 1] : 0u, i + 2 < n ? src[i + 2] : 0u,
+                                   i + 3 < n ? src[i + 3] : 0u);
+            }
+        }
+        // Flags (bit e of nibble q) and the packed per-chunk counts.
+        uint32_t flags = 0, packed = 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint32_t f = (fv[q].x != 0u ? 1u : 0u) | (fv[q].y != 0u ? 2u : 0u) | (fv[q].z != 0u ? 4u : 0u) |
+                               (fv[q].w != 0u ? 8u : 0u);
+            flags |= f << (4 * q);
+            packed |= (uint32_t)__popc(f) << (8 * q);
+        }
+        uint32_t incl = packed;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const uint32_t totals = __shfl_sync(0xffffffffu, incl, 31);  // byte q: chunk q's count
+        const uint32_t excl_lane = incl - packed;
+        const uint32_t t0c = totals & 0xFFu, t1c = (totals >> 8) & 0xFFu, t2c = (totals >> 16) & 0xFFu;
+        const uint32_t wtotal = t0c + t1c + t2c + (totals >> 24);
+        if (lane == 0) s_warp[warp] = wtotal;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t w = lane < kCompactWarps ? s_warp[lane] : 0u;
+            uint32_t ws = w;
+#pragma unroll
+            for (int o = 1; o < kCompactWarps; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, ws, o);
+                if (lane >= o) ws += y;
+            }
+            const uint32_t ttotal = __shfl_sync(0xffffffffu, ws, kCompactWarps - 1);
+            if (lane < kCompactWarps) s_warp[lane] = ws - w;  // the warps' exclusive offsets
+            const uint64_t prefix = warp_tile_prefix(sc.status, tile, ttotal, sc.err);
+            if (lane == 0) {
+                s_prefix = prefix;
+                if (tile == ntiles - 1) *count = prefix + ttotal;
+            }
+        }
+        __syncthreads();
+        const uint64_t wbase = s_prefix + s_warp[warp];
+        const uint32_t cbase[4] = {0u, t0c, t0c + t1c, t0c + t1c + t2c};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            uint64_t o = wbase + cbase[q] + ((excl_lane >> (8 * q)) & 0xFFu);
+            const uint32_t f = (flags >> (4 * q)) & 0xFu;
+            if (f & 1u) dst[o++] = sv[q].x;
+            if (f & 2u) dst[o++] = sv[q].y;
+            if (f & 4u) dst[o++] = sv[q].z;
+            if (f & 8u) dst[o++] = sv[q].w;
+        }
+        __syncthreads();  // s_tile, s_warp and s_prefix free for the next tile
     }
 }
 
@@ -63,7 +186,16 @@ cudaError_t launch_compact_u32(const uint32_t* src, const uint32_t* valid, uint3
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const uint64_t ntiles = (n + kCompactTile - 1) / kCompactTile;
-    const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(ntiles, (uint64_t)sms * 4));
+    // Every block resident at once (tiles are taken in order by running
+    // blocks in any case, so a lookback never waits on a block not started).
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_compact_u32, kCompactThreads, 0) != cudaSuccess) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    per_sm = std::max(per_sm, 1);
+    const unsigned grid =
+        (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(ntiles, (uint64_t)sms * (uint64_t)per_sm));
     k_compact_u32<<<grid, kCompactThreads, 0, st>>>(src, valid, dst, n, (unsigned long long*)count, sc);
     return cudaGetLastError();
 }

@@ -11,12 +11,15 @@ import aworkefficientgpualgorithmforlevelsetsegmentation_gb300 as lss
 pytestmark = pytest.mark.gpu
 
 
-def compact_gpu(src, valid):
+def compact_gpu(src, valid, offset=0):
+    """offset > 0 places src and valid that many elements into their
+    allocations (4-byte aligned, not 16-byte: the element-wise reads)."""
     import torch
     L = lss.load()
-    pad = max(1, src.size)  # non-null device buffers even for n = 0
-    s = torch.zeros(pad, dtype=torch.int32, device="cuda")
-    v = torch.zeros(pad, dtype=torch.int32, device="cuda")
+    pad = max(1, src.size) + offset  # non-null device buffers even for n = 0
+    s0 = torch.zeros(pad, dtype=torch.int32, device="cuda")
+    v0 = torch.zeros(pad, dtype=torch.int32, device="cuda")
+    s, v = s0[offset:], v0[offset:]
     s[: src.size] = torch.from_numpy(src.astype(np.uint32).view(np.int32)).cuda()
     v[: src.size] = torch.from_numpy(valid.astype(np.uint32).view(np.int32)).cuda()
     d = torch.full((max(1, src.size),), -1, dtype=torch.int32, device="cuda")
@@ -36,6 +39,17 @@ def test_compact_matches_numpy(n, p):
     src = rng.integers(0, 2**32 - 1, size=n, dtype=np.uint64).astype(np.uint32)
     valid = (rng.random(n) < p).astype(np.uint32) * rng.integers(1, 7, size=n).astype(np.uint32)
     out, cnt = compact_gpu(src, valid)
+    ref = src[valid != 0]
+    assert cnt == ref.size
+    assert np.array_equal(out, ref)
+
+
+@pytest.mark.parametrize("n,offset", [(100_003, 1), (4097, 3)])
+def test_compact_unaligned_buffers(n, offset):
+    rng = np.random.default_rng(n + offset)
+    src = rng.integers(0, 2**32 - 1, size=n, dtype=np.uint64).astype(np.uint32)
+    valid = (rng.random(n) < 0.4).astype(np.uint32)
+    out, cnt = compact_gpu(src, valid, offset)
     ref = src[valid != 0]
     assert cnt == ref.size
     assert np.array_equal(out, ref)
