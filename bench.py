@@ -377,6 +377,7 @@ def run_ours(args, ws, rank, local):
         extra["adjoint"] = measure_adjoint(local, args.scale, 10, 3)
         extra["stress"] = measure_stress(local, args.scale, 2, 1)
         extra["ref_mode"] = measure_ref_mode(local, args.scale, 5, 2)
+        extra["compaction"] = measure_compaction(local, 10, 3)
     if rank == 0:
         cpu = None
         if not args.no_cpu:
@@ -721,6 +722,59 @@ def run_adjoint(args, ws, rank, local):
                 "e2e": {k: r["e2e"][k] for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step")},
                 "gpu_launches": r["gpu_launches_per_call"] * args.steps, "clocks": clk.summary()}
         print(json.dumps(line), flush=True)
+
+
+def measure_compaction(local, steps, warmup, n=1 << 28, frac=0.5):
+    """The kernel-level compaction (lss_compact_u32, the reference's
+    CudppCompact; lss_compact_u32_noalloc beside it at its largest size) on
+    2^28 elements (1 GiB each of values, flags and output), half of them kept.
+    Timed with CUDA events on the call's stream around each call (the call
+    allocates and frees its scratch stream-ordered, clears it, compacts,
+    reads its error word back and synchronises).  Roofline: 8 B an element
+    (flag and value) + 4 B a kept one, against the measured HBM peak."""
+    import ctypes as C
+    import torch
+    import aworkefficientgpualgorithmforlevelsetsegmentation_gb300 as lss
+
+    L = lss.load()
+    dev = torch.device(f"cuda:{local}")
+    g = torch.Generator(device=dev)
+    g.manual_seed(5)
+    stream = torch.cuda.Stream(device=dev)
+    peak, peak_kind = measured_peak()
+
+    def timed(fn, m):
+        src = torch.arange(m, dtype=torch.int32, device=dev)
+        valid = (torch.rand(m, device=dev, generator=g) < frac).to(torch.int32)
+        dst = torch.empty(m, dtype=torch.int32, device=dev)
+        cnt = torch.zeros(1, dtype=torch.int64, device=dev)
+        args = (C.c_void_p(src.data_ptr()), C.c_void_p(valid.data_ptr()), C.c_void_p(dst.data_ptr()), m,
+                C.c_void_p(cnt.data_ptr()), C.c_void_p(stream.cuda_stream))
+        torch.cuda.synchronize()
+        for _ in range(warmup):
+            assert fn(*args) == 0
+        ts = []
+        for _ in range(steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            assert fn(*args) == 0
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        kept = int(cnt.item())
+        same = bool(torch.equal(dst[:kept], src[valid.bool()]))
+        ms = statistics.median(ts)
+        alg = 8 * m + 4 * kept
+        del src, valid, dst
+        torch.cuda.empty_cache()
+        return {"n": m, "kept": kept, "ms_per_call": ms, "algorithmic_bytes": alg,
+                "achieved_gbs": alg / (ms / 1e3) / 1e9, "peak": peak, "peak_kind": peak_kind,
+                "frac": alg / (ms / 1e3) / 1e9 / peak, "matches_torch": same}
+
+    return {"lss_compact_u32": timed(L.lss_compact_u32, n),
+            "lss_compact_u32_noalloc": timed(L.lss_compact_u32_noalloc, 1 << 26),
+            "valid_fraction": frac, "bytes_model": "8 B an element (flag, value) + 4 B a kept element"}
 
 
 def measure_ref_mode(local, scale, steps, warmup):
