@@ -34,58 +34,6 @@ struct CompactScratch {
     uint32_t* err;
 };
 
-// Exclusive prefix of `tile` by decoupled lookback, one warp (all 32 lanes
-// call it): lane 0 publishes the tile's aggregate, then the warp reads the
-// status words of the 32 tiles before a window start at once; it adds the
-// values up to and including the nearest inclusive prefix, or moves the
-// window back by 32 when there is none.  A tile in the window that is not
-// published yet (before the nearest inclusive prefix) is read again, for
-// kWaitLimitNs at most (then the error bit is set and the sum so far
-// returned).  Lane 0 then publishes the tile's inclusive prefix.
-__device__ __forceinline__ uint64_t warp_tile_prefix(uint64_t* status, uint32_t tile, uint64_t aggregate,
-                                                     uint32_t* err) {
-    const int lane = threadIdx.x & 31;
-    if (tile == 0) {
-        if (lane == 0) st_release_u64(&status[0], kFlagP | (aggregate & kValMask));
-        return 0;
-    }
-    if (lane == 0) st_release_u64(&status[tile], kFlagA | (aggregate & kValMask));
-    uint64_t excl = 0;
-    int64_t j = (int64_t)tile - 1;  // the window is tiles j, j-1, ..., j-31 (lane order)
-    uint64_t t0 = 0;
-    for (;;) {
-        const int64_t idx = j - lane;
-        const uint64_t st = idx >= 0 ? ld_acquire_u64(&status[idx]) : kFlagP;  // before tile 0: prefix 0
-        const uint32_t flag = (uint32_t)(st >> 62);
-        const uint32_t pmask = __ballot_sync(0xffffffffu, flag == 2u);
-        const uint32_t zmask = __ballot_sync(0xffffffffu, flag == 0u);
-        const int first_p = pmask ? __ffs(pmask) - 1 : 32;
-        const uint32_t need = first_p == 32 ? 0xffffffffu : ((2u << first_p) - 1u);  // lanes 0..first_p
-        if (zmask & need) {
-            // Lane 0 keeps the time, so the whole warp gives up together.
-            int give_up = 0;
-            if (lane == 0) {
-                if (t0 == 0) t0 = globaltimer_ns();
-                else if (globaltimer_ns() - t0 > kWaitLimitNs) give_up = 1;
-            }
-            if (__shfl_sync(0xffffffffu, give_up, 0)) {
-                if (lane == 0) set_error(err, ERR_LOOKBACK_TIMEOUT);
-                break;
-            }
-            continue;
-        }
-        uint64_t v = ((need >> lane) & 1u) ? (st & kValMask) : 0ull;
-#pragma unroll
-        for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        excl += v;
-        if (first_p < 32) break;
-        j -= 32;
-        t0 = 0;
-    }
-    if (lane == 0) st_release_u64(&status[tile], kFlagP | ((excl + aggregate) & kValMask));
-    return excl;
-}
-
 // Stable compaction, tiles of kCompactTile elements taken from a tile counter (so
 // every lookback waits on a resident block).  Warp w of a tile takes the 512
 // elements [512 w, 512 w + 512) as four chunks of 128, lane l the four
