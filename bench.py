@@ -142,12 +142,12 @@ def sum_over_ranks(ws, value: float) -> float:
 # the key's first field (profiles/k_ns_persistent_config2_256.md gives the
 # capture); a build from other sources reports null rather than a stale
 # figure.
-DRAM_TRAFFIC = {("33ce358840f2", "config2_256", 8, 8, 8, 256): 15782912}
+DRAM_TRAFFIC = {("f03f39b20e6e", "config2_256", 8, 8, 8, 256): 16179968}
 KERNEL_SOURCES = ("ns_kernels.cuh", "ns_engine.cu", "tma.cuh", "common.cuh")
 # The same for one adjoint call on config 4 (its two kernels: the forward,
 # with the call's set-up and the loss as phases, and the reverse), from
 # the capture in profiles/k_adj_config4_192.md.
-ADJOINT_TRAFFIC = {("3154f73a7bde", "config4_192"): 93294592}
+ADJOINT_TRAFFIC = {("4d7505f8cf68", "config4_192"): 93272576}
 ADJOINT_SOURCES = ("ns_adjoint.cu", "ns_kernels.cuh", "common.cuh")
 
 
