@@ -3,10 +3,12 @@
 // Cuda.cpp:699-758), which wraps CUDPP 1.1's cudppCompact.
 //
 // Stable: dst receives src[i] for every i < n with valid[i] != 0, in index
-// order.  Single pass with decoupled lookback over tiles of 16384 elements
-// (16-byte coalesced loads, a warp-parallel lookback); the count is written
-// to device memory (the reference copies it to the host after every
-// 2^25-element chunk).
+// order.  Three stream-ordered kernels over tiles of 4096 elements: the
+// count of each tile (the flags streamed once), an exclusive scan of the
+// tile counts (decoupled lookback over 8192 counts a block), and the scatter
+// (flags and values streamed, each tile's kept values stored from its
+// prefix).  The count is written to device memory (the reference copies it
+// to the host after every 2^25-element chunk).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -19,63 +21,127 @@
 
 namespace lss {
 
-constexpr int kCompactThreads = 1024;
+constexpr int kCompactThreads = 256;
 constexpr int kCompactItems = 16;
-constexpr int kCompactTile = kCompactThreads * kCompactItems;
+constexpr int kCompactTile = kCompactThreads * kCompactItems;  // 4096 elements
 constexpr int kCompactWarps = kCompactThreads / 32;
 constexpr int kCompactSeg = kCompactTile / kCompactWarps;  // 512 elements a warp: 4 chunks of 128
-// 16384-element tiles (1024 threads, one block an SM): at 2^28 elements
-// 1.09 ms a call against 1.20 with 8192 (512 threads) and 1.25 with 4096
-// (256 threads): fewer tiles in flight for each lookback to walk past.
+static_assert(kCompactSeg == 512, "a warp's segment is four 128-element chunks");
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;  // tile counts a scan block takes
 
 struct CompactScratch {
-    uint64_t* status;        // one word per tile, zero before the pass
-    uint32_t* tile_counter;  // zero before the pass
+    uint64_t* counts;        // one word per tile: its count, then its exclusive prefix
+    uint64_t* status;        // one word per scan block, zero before the call
+    uint32_t* tile_counter;  // zero before the call
     uint32_t* err;
 };
 
-// Stable compaction, tiles of kCompactTile elements taken from a tile counter (so
-// every lookback waits on a resident block).  Warp w of a tile takes the 512
-// elements [512 w, 512 w + 512) as four chunks of 128, lane l the four
-// elements 4 l .. 4 l + 3 of each chunk, read as 16-byte loads (a warp's load
-// is 512 contiguous bytes; all eight loads of a thread are issued before any
-// is used).  Ranks: one warp inclusive scan of the four per-chunk counts
-// packed into the bytes of a word (a chunk holds at most 128), the warps'
-// totals by a block scan, the tile's prefix by warp 0's lookback.  A lane's
-// kept elements go to consecutive places, after those of the lanes before
-// it, so the stores of a chunk are contiguous too.  n need not be a multiple
-// of 4: the tail is read element by element.
-__global__ void __launch_bounds__(kCompactThreads) k_compact_u32(const uint32_t* __restrict__ src,
-                                                                 const uint32_t* __restrict__ valid,
-                                                                 uint32_t* __restrict__ dst,
-                                                                 uint64_t n,
-                                                                 unsigned long long* count,
-                                                                 CompactScratch sc) {
-    __shared__ uint32_t s_tile;
-    __shared__ uint32_t s_warp[kCompactWarps];
-    __shared__ uint64_t s_prefix;
+// Four elements from i: one 16-byte load when the buffer is aligned and all
+// four are inside, else element by element (0 past n).
+template <bool STREAM>
+__device__ __forceinline__ uint4 load_quad(const uint32_t* __restrict__ p, uint64_t i, uint64_t n, bool vec) {
+    if (vec && i + 4 <= n) {
+        const uint4* q = reinterpret_cast<const uint4*>(p + i);
+        return STREAM ? __ldcs(q) : *q;
+    }
+    return make_uint4(i < n ? p[i] : 0u, i + 1 < n ? p[i + 1] : 0u, i + 2 < n ? p[i + 2] : 0u,
+                      i + 3 < n ? p[i + 3] : 0u);
+}
+
+// Pass 1: the number of nonzero flags of each tile.  Warp w of a tile reads
+// the elements [512 w, 512 w + 512) as four chunks of 128 (lane l the four
+// elements 4 l .. 4 l + 3 of each chunk, 16-byte loads, a warp's load 512
+// contiguous bytes).  Tiles i, i + G, ... for block i of G.
+__global__ void __launch_bounds__(kCompactThreads) k_compact_count(const uint32_t* __restrict__ valid,
+                                                                   uint64_t n, uint64_t* __restrict__ counts) {
+    __shared__ uint32_t s_warp[2][kCompactWarps];  // by tile parity: one barrier a tile
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint64_t ntiles = (n + kCompactTile - 1) / kCompactTile;
-    const bool vec = ((uintptr_t)src % 16 == 0) && ((uintptr_t)valid % 16 == 0);
+    const bool vec = (uintptr_t)valid % 16 == 0;
+    int buf = 0;
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, buf ^= 1) {
+        const uint64_t i0 = tile * kCompactTile + (uint64_t)warp * kCompactSeg + (uint64_t)lane * 4;
+        uint4 fv[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) fv[q] = load_quad<false>(valid, i0 + (uint64_t)q * 128, n, vec);
+        uint32_t c = 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            c += (uint32_t)(fv[q].x != 0u) + (uint32_t)(fv[q].y != 0u) + (uint32_t)(fv[q].z != 0u) +
+                 (uint32_t)(fv[q].w != 0u);
+        c = __reduce_add_sync(0xffffffffu, c);
+        if (lane == 0) s_warp[buf][warp] = c;
+        __syncthreads();
+        if (warp == 0) {
+            const uint32_t t = __reduce_add_sync(0xffffffffu, lane < kCompactWarps ? s_warp[buf][lane] : 0u);
+            if (lane == 0) counts[tile] = t;
+        }
+        // s_warp[buf] is written again two tiles on, after the next barrier.
+    }
+}
+
+// Pass 2: the tile counts replaced in place by their exclusive prefix sums.
+// Blocks take 8192 counts at a time from a counter (so a lookback only waits
+// on blocks already running); the block's offset comes from the decoupled
+// lookback over the status words.  The last block writes the total count.
+__global__ void __launch_bounds__(kScanThreads) k_compact_scan(uint64_t ntiles, unsigned long long* total,
+                                                               CompactScratch sc) {
+    __shared__ uint32_t s_tile;
+    const uint64_t nscan = (ntiles + kScanTile - 1) / kScanTile;
     for (;;) {
         if (threadIdx.x == 0) s_tile = atomicAdd(sc.tile_counter, 1u);
         __syncthreads();
-        const uint32_t tile = s_tile;
-        if (tile >= ntiles) break;
-        const uint64_t seg = (uint64_t)tile * kCompactTile + (uint64_t)warp * kCompactSeg;
+        const uint32_t t = s_tile;
+        if (t >= nscan) break;
+        const uint64_t i0 = (uint64_t)t * kScanTile + (uint64_t)threadIdx.x * kScanItems;
+        uint64_t v[kScanItems], sum = 0;
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) {
+            v[k] = i0 + k < ntiles ? sc.counts[i0 + k] : 0ull;
+            sum += v[k];
+        }
+        uint64_t agg = 0;
+        const uint64_t ex = block_exclusive_sum64<true>(sum, &agg);
+        const uint64_t prefix = tile_exclusive_prefix(sc.status, t, agg, sc.err);  // ends with a barrier
+        uint64_t run = prefix + ex;
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) {
+            if (i0 + k < ntiles) sc.counts[i0 + k] = run;
+            run += v[k];
+        }
+        if (t == nscan - 1 && threadIdx.x == 0) *total = prefix + agg;
+    }
+}
+
+// Pass 3: each tile's kept values, stored from the tile's prefix.  The
+// elements of a thread are those of pass 1; ranks inside the tile: one warp
+// inclusive scan of the four per-chunk counts packed into the bytes of a
+// word (a chunk holds at most 128), the warps' totals through shared memory.
+// A lane's kept values go to consecutive places after those of the lanes
+// before it, so a chunk's stores are contiguous too.  The highest tiles come
+// first: pass 1 read their flags last, so they may still be in L2; the
+// loads here stream (evict first), each element being read for the last
+// time.
+__global__ void __launch_bounds__(kCompactThreads) k_compact_scatter(const uint32_t* __restrict__ src,
+                                                                     const uint32_t* __restrict__ valid,
+                                                                     uint32_t* __restrict__ dst, uint64_t n,
+                                                                     const uint64_t* __restrict__ prefix) {
+    __shared__ uint32_t s_warp[2][kCompactWarps];  // by tile parity: one barrier a tile
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint64_t ntiles = (n + kCompactTile - 1) / kCompactTile;
+    const bool vec = ((uintptr_t)src % 16 == 0) && ((uintptr_t)valid % 16 == 0);
+    int buf = 0;
+    for (uint64_t r = blockIdx.x; r < ntiles; r += gridDim.x, buf ^= 1) {
+        const uint64_t tile = ntiles - 1 - r;
+        const uint64_t base = prefix[tile];
+        const uint64_t i0 = tile * kCompactTile + (uint64_t)warp * kCompactSeg + (uint64_t)lane * 4;
         uint4 fv[4], sv[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-            const uint64_t i = seg + (uint64_t)q * 128 + (uint64_t)lane * 4;
-            if (vec && i + 4 <= n) {
-                fv[q] = *reinterpret_cast<const uint4*>(valid + i);
-                sv[q] = *reinterpret_cast<const uint4*>(src + i);
-            } else {
-                fv[q] = make_uint4(i < n ? valid[i] : 0u, i + 1 < n ? valid[i + 1] : 0u,
-                                   i + 2 < n ? valid[i + 2] : 0u, i + 3 < n ? valid[i + 3] : 0u);
-                sv[q] = make_uint4(i < n ? src[i] : 0u, i + 1 < n ? src[i + 1] : 0u, i + 2 < n ? src[i + 2] : 0u,
-                                   i + 3 < n ? src[i + 3] : 0u);
-            }
+            fv[q] = load_quad<true>(valid, i0 + (uint64_t)q * 128, n, vec);
+            sv[q] = load_quad<true>(src, i0 + (uint64_t)q * 128, n, vec);
         }
         // Flags (bit e of nibble q) and the packed per-chunk counts.
         uint32_t flags = 0, packed = 0;
@@ -95,27 +161,11 @@ __global__ void __launch_bounds__(kCompactThreads) k_compact_u32(const uint32_t*
         const uint32_t totals = __shfl_sync(0xffffffffu, incl, 31);  // byte q: chunk q's count
         const uint32_t excl_lane = incl - packed;
         const uint32_t t0c = totals & 0xFFu, t1c = (totals >> 8) & 0xFFu, t2c = (totals >> 16) & 0xFFu;
-        const uint32_t wtotal = t0c + t1c + t2c + (totals >> 24);
-        if (lane == 0) s_warp[warp] = wtotal;
+        if (lane == 0) s_warp[buf][warp] = t0c + t1c + t2c + (totals >> 24);
         __syncthreads();
-        if (warp == 0) {
-            uint32_t w = lane < kCompactWarps ? s_warp[lane] : 0u;
-            uint32_t ws = w;
-#pragma unroll
-            for (int o = 1; o < kCompactWarps; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(0xffffffffu, ws, o);
-                if (lane >= o) ws += y;
-            }
-            const uint32_t ttotal = __shfl_sync(0xffffffffu, ws, kCompactWarps - 1);
-            if (lane < kCompactWarps) s_warp[lane] = ws - w;  // the warps' exclusive offsets
-            const uint64_t prefix = warp_tile_prefix(sc.status, tile, ttotal, sc.err);
-            if (lane == 0) {
-                s_prefix = prefix;
-                if (tile == ntiles - 1) *count = prefix + ttotal;
-            }
-        }
-        __syncthreads();
-        const uint64_t wbase = s_prefix + s_warp[warp];
+        // s_warp[buf] is written again two tiles on, after the next barrier.
+        const uint64_t wbase =
+            base + __reduce_add_sync(0xffffffffu, lane < warp ? s_warp[buf][lane] : 0u);
         const uint32_t cbase[4] = {0u, t0c, t0c + t1c, t0c + t1c + t2c};
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -126,32 +176,121 @@ __global__ void __launch_bounds__(kCompactThreads) k_compact_u32(const uint32_t*
             if (f & 4u) dst[o++] = sv[q].z;
             if (f & 8u) dst[o++] = sv[q].w;
         }
-        __syncthreads();  // s_tile, s_warp and s_prefix free for the next tile
     }
 }
 
-// Launches the compaction with caller-provided (already zeroed) scratch.
-cudaError_t launch_compact_u32(const uint32_t* src, const uint32_t* valid, uint32_t* dst, uint64_t n,
-                               uint64_t* count, CompactScratch sc, cudaStream_t st) {
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const uint64_t ntiles = (n + kCompactTile - 1) / kCompactTile;
-    // Every block resident at once (tiles are taken in order by running
-    // blocks in any case, so a lookback never waits on a block not started).
+static unsigned resident_grid(const void* fn, int threads, int sms, uint64_t units) {
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_compact_u32, kCompactThreads, 0) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0) != cudaSuccess) {
         cudaGetLastError();
         per_sm = 1;
     }
     per_sm = std::max(per_sm, 1);
-    const unsigned grid =
-        (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(ntiles, (uint64_t)sms * (uint64_t)per_sm));
-    k_compact_u32<<<grid, kCompactThreads, 0, st>>>(src, valid, dst, n, (unsigned long long*)count, sc);
+    return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(units, (uint64_t)sms * (uint64_t)per_sm));
+}
+
+uint64_t compact_tiles(uint64_t n) { return (n + kCompactTile - 1) / kCompactTile; }
+uint64_t compact_scan_blocks(uint64_t n) { return (compact_tiles(n) + kScanTile - 1) / kScanTile; }
+// Scratch of a call, in words: the tile counts, the scan's status words, then
+// one word for the scan's block counter and the error word.
+uint64_t compact_scratch_words(uint64_t n) { return compact_tiles(n) + compact_scan_blocks(n) + 1 + 1; }
+
+// Points sc into words [0, compact_scratch_words(n)) of base.  The words from
+// *clear_from on are the ones to zero before the call.
+CompactScratch compact_scratch(uint64_t* base, uint64_t n, uint64_t* clear_from) {
+    CompactScratch sc;
+    const uint64_t nt = compact_tiles(n), ns = compact_scan_blocks(n);
+    sc.counts = base;
+    sc.status = base + nt;
+    sc.tile_counter = (uint32_t*)(base + nt + ns + 1);
+    sc.err = sc.tile_counter + 1;
+    *clear_from = nt;
+    return sc;
+}
+
+// Resident blocks of each pass on a device (every block of a pass resident
+// at once), worked out once per device.
+struct CompactGrids {
+    unsigned count, scan, scatter;
+};
+static std::mutex g_grid_mu;
+static CompactGrids g_grids[64] = {};
+
+static CompactGrids compact_grids(int dev) {
+    std::lock_guard<std::mutex> g(g_grid_mu);
+    const bool cached = dev >= 0 && dev < 64 && g_grids[dev].count != 0;
+    if (cached) return g_grids[dev];
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    sms = std::max(sms, 1);
+    const uint64_t all = ~0ull;
+    CompactGrids r;
+    r.count = resident_grid((const void*)k_compact_count, kCompactThreads, sms, all);
+    r.scan = resident_grid((const void*)k_compact_scan, kScanThreads, sms, all);
+    r.scatter = resident_grid((const void*)k_compact_scatter, kCompactThreads, sms, all);
+    if (dev >= 0 && dev < 64) g_grids[dev] = r;
+    return r;
+}
+
+// Launches the three passes with caller-provided scratch (status words,
+// block counter and error word zeroed).
+cudaError_t launch_compact_u32(const uint32_t* src, const uint32_t* valid, uint32_t* dst, uint64_t n,
+                               uint64_t* count, CompactScratch sc, cudaStream_t st) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const CompactGrids cg = compact_grids(dev);
+    const uint64_t nt = compact_tiles(n);
+    const unsigned g1 = (unsigned)std::min<uint64_t>(cg.count, nt);
+    const unsigned g3 = (unsigned)std::min<uint64_t>(cg.scatter, nt);
+    // Scan blocks take their counts in order from a counter, so a lookback
+    // never waits on a block not started.
+    const unsigned g2 = (unsigned)std::min<uint64_t>(cg.scan, compact_scan_blocks(n));
+    k_compact_count<<<g1, kCompactThreads, 0, st>>>(valid, n, sc.counts);
+    k_compact_scan<<<g2, kScanThreads, 0, st>>>(nt, (unsigned long long*)count, sc);
+    k_compact_scatter<<<g3, kCompactThreads, 0, st>>>(src, valid, dst, n, sc.counts);
     return cudaGetLastError();
 }
 
-uint64_t compact_status_words(uint64_t n) { return (n + kCompactTile - 1) / kCompactTile + 1; }
+}  // namespace lss
+
+namespace lss {
+
+// The allocating entry point's memory pool, one per device: stream-ordered
+// like the default pool, but it keeps up to kPoolKeep bytes reserved when
+// streams synchronise (the default pool hands its memory back at every
+// synchronisation, and mapping it again cost about 0.17 ms a call).
+constexpr uint64_t kPoolKeep = 64ull << 20;
+static std::mutex g_pool_mu;
+static cudaMemPool_t g_pools[64] = {};
+
+static lss_status compact_pool(cudaMemPool_t* out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return LSS_ERR_NO_DEVICE;
+    }
+    std::lock_guard<std::mutex> g(g_pool_mu);
+    if (!g_pools[dev]) {
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool = nullptr;
+        if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
+            cudaGetLastError();
+            return LSS_ERR_CUDA;
+        }
+        uint64_t keep = kPoolKeep;
+        if (cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess) {
+            cudaGetLastError();
+            cudaMemPoolDestroy(pool);
+            return LSS_ERR_CUDA;
+        }
+        g_pools[dev] = pool;
+    }
+    *out = g_pools[dev];
+    return LSS_OK;
+}
 
 }  // namespace lss
 
@@ -163,20 +302,21 @@ extern "C" lss_status lss_compact_u32(const uint32_t* d_src, const uint32_t* d_v
     if (n == 0) {
         return cudaMemsetAsync(d_count, 0, sizeof(uint64_t), st) == cudaSuccess ? LSS_OK : LSS_ERR_CUDA;
     }
-    // Scratch: status words, tile counter and error word, stream-ordered.
-    const uint64_t words = lss::compact_status_words(n);
-    const size_t bytes = words * 8 + 16;
+    // Scratch: tile counts, status words, block counter and error word,
+    // stream-ordered from the library's pool.
+    cudaMemPool_t pool = nullptr;
+    const lss_status ps = lss::compact_pool(&pool);
+    if (ps != LSS_OK) return ps;
+    const uint64_t words = lss::compact_scratch_words(n);
     void* scratch = nullptr;
-    if (cudaMallocAsync(&scratch, bytes, st) != cudaSuccess) {
+    if (cudaMallocFromPoolAsync(&scratch, words * 8, pool, st) != cudaSuccess) {
         cudaGetLastError();
         return LSS_ERR_OUT_OF_MEMORY;
     }
-    lss::CompactScratch sc;
-    sc.status = (uint64_t*)scratch;
-    sc.tile_counter = (uint32_t*)((char*)scratch + words * 8);
-    sc.err = sc.tile_counter + 1;
+    uint64_t clear_from = 0;
+    const lss::CompactScratch sc = lss::compact_scratch((uint64_t*)scratch, n, &clear_from);
     lss_status s = LSS_OK;
-    if (cudaMemsetAsync(scratch, 0, bytes, st) != cudaSuccess ||
+    if (cudaMemsetAsync((uint64_t*)scratch + clear_from, 0, (words - clear_from) * 8, st) != cudaSuccess ||
         lss::launch_compact_u32(d_src, d_valid, d_dst, n, d_count, sc, st) != cudaSuccess)
         s = LSS_ERR_CUDA;
     uint32_t err = 0;
@@ -197,17 +337,18 @@ extern "C" lss_status lss_compact_u32(const uint32_t* d_src, const uint32_t* d_v
 // cudaMalloc of their own would bypass its pool or its accounting).  For
 // them lss_compact_u32_noalloc keeps its scratch in this file-scope device
 // array instead of asking the stream-ordered allocator.  Every GPU that loads
-// the library holds the array (a little over 32 KiB) until the process exits.
+// the library holds the array (a little over 128 KiB) until the process exits.
 // The call reads the error word back and synchronises its stream before it
 // returns.
 namespace lss {
 
 // Largest n the allocation-free call accepts.
 constexpr uint64_t kNoAllocMaxElements = 1ull << 26;
-constexpr uint64_t kNoAllocStatusWords = kNoAllocMaxElements / kCompactTile + 1;
+constexpr uint64_t kNoAllocWords = kNoAllocMaxElements / kCompactTile +
+                                   (kNoAllocMaxElements / kCompactTile + kScanTile - 1) / kScanTile + 2;
 
-// Status words, then the tile counter and the error word (one u64).
-static __device__ __align__(256) uint64_t g_noalloc_scratch[kNoAllocStatusWords + 1];
+// The scratch of compact_scratch_words(n) for every n up to the maximum.
+static __device__ __align__(256) uint64_t g_noalloc_scratch[kNoAllocWords];
 
 // Device address of the array, looked up once per device with that device
 // current (in host code the symbol is only a host-side stand-in).
@@ -246,15 +387,13 @@ extern "C" lss_status lss_compact_u32_noalloc(const uint32_t* d_src, const uint3
     uint64_t* base = nullptr;
     lss_status s = lss::noalloc_scratch(&base);
     if (s != LSS_OK) return s;
-    const uint64_t words = lss::compact_status_words(n);  // <= kNoAllocStatusWords
-    lss::CompactScratch sc;
-    sc.status = base;
-    sc.tile_counter = (uint32_t*)(base + lss::kNoAllocStatusWords);
-    sc.err = sc.tile_counter + 1;
-    // The array keeps the previous call's contents: clear the words this call
-    // reads before writing them, plus the tile counter and the error word.
-    if (cudaMemsetAsync(base, 0, words * 8, st) != cudaSuccess ||
-        cudaMemsetAsync(sc.tile_counter, 0, 8, st) != cudaSuccess ||
+    const uint64_t words = lss::compact_scratch_words(n);  // <= kNoAllocWords
+    uint64_t clear_from = 0;
+    const lss::CompactScratch sc = lss::compact_scratch(base, n, &clear_from);
+    // The array keeps the previous call's contents: clear the status words,
+    // the block counter and the error word (the tile counts are written
+    // before they are read).
+    if (cudaMemsetAsync(base + clear_from, 0, (words - clear_from) * 8, st) != cudaSuccess ||
         lss::launch_compact_u32(d_src, d_valid, d_dst, n, d_count, sc, st) != cudaSuccess) {
         cudaGetLastError();
         return LSS_ERR_CUDA;

@@ -20,7 +20,8 @@ The default line also carries the other workloads, each measured briefly:
 config1 (128^3, 300 iterations, GPU and CPU), batch (48 mixed-size volumes,
 batched vs sequential plain), adjoint (192^3, K = 64), stress (512x512x768
 and the 150 GB mixed batch) and ref_mode (the reference's algorithm at
-256^3); --workload X runs one of them alone with the full step count.
+256^3) and compaction (lss_compact_u32 on 2^28 elements); --workload X runs
+one of them alone with the full step count.
 --impl reference: the CPU restatement of the path (the FP64 oracle, all host
 threads) on the same workload: one whole seeding + run to convergence, timed
 as --steps consecutive segments (W warm-up segments first), in a process
@@ -729,8 +730,9 @@ def measure_compaction(local, steps, warmup, n=1 << 28, frac=0.5):
     CudppCompact; lss_compact_u32_noalloc beside it at its largest size) on
     2^28 elements (1 GiB each of values, flags and output), half of them kept.
     Timed with CUDA events on the call's stream around each call (the call
-    allocates and frees its scratch stream-ordered, clears it, compacts,
-    reads its error word back and synchronises).  Roofline: 8 B an element
+    takes its scratch from the library's stream-ordered pool, clears it, runs
+    the count, scan and scatter passes, reads its error word back and
+    synchronises).  Roofline: 8 B an element
     (flag and value) + 4 B a kept one, against the measured HBM peak."""
     import ctypes as C
     import torch
@@ -775,6 +777,22 @@ def measure_compaction(local, steps, warmup, n=1 << 28, frac=0.5):
     return {"lss_compact_u32": timed(L.lss_compact_u32, n),
             "lss_compact_u32_noalloc": timed(L.lss_compact_u32_noalloc, 1 << 26),
             "valid_fraction": frac, "bytes_model": "8 B an element (flag, value) + 4 B a kept element"}
+
+
+def run_compaction(args, ws, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    with ClockSampler(local) as clk:
+        r = measure_compaction(local, args.steps, args.warmup)
+    if rank == 0:
+        c = r["lss_compact_u32"]
+        line = {"metric": "compaction_algorithmic_bytes_per_s", "value": c["achieved_gbs"], "unit": "GB/s",
+                "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": c["ms_per_call"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+                "data": "synthetic", "config": {"workload": "compact_u32_2^28_half_kept",
+                                                "l2": "inputs larger than L2 (1 GiB each)"},
+                "compaction": r, "gpu_launches": 3 * 2 * args.steps, "clocks": clk.summary()}
+        print(json.dumps(line), flush=True)
 
 
 def measure_ref_mode(local, scale, steps, warmup):
@@ -927,7 +945,7 @@ def main():
     ap.add_argument("--no-extra", action="store_true",
                     help="plain workload only (no config1/batch/adjoint/stress/ref_mode keys)")
     ap.add_argument("--workload", default="plain",
-                    choices=["plain", "batch", "stress", "tour", "adjoint", "ref"])
+                    choices=["plain", "batch", "stress", "tour", "adjoint", "ref", "compaction"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     ws, rank, local = dist_env()
@@ -946,6 +964,8 @@ def main():
         run_adjoint(args, ws, rank, local)
     elif args.workload == "ref":
         run_ref_mode(args, ws, rank, local)
+    elif args.workload == "compaction":
+        run_compaction(args, ws, rank, local)
     else:
         run_ours(args, ws, rank, local)
     if ws > 1:

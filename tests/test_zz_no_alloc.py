@@ -46,6 +46,19 @@ def test_no_alloc_matches_allocating_entry_point_twice():
         assert np.array_equal(b, src[valid != 0]), call
 
 
+def test_no_alloc_at_its_maximum_size():
+    """The fixed array holds the scratch of the largest accepted n (its tile
+    counts fill the array; two scan blocks)."""
+    L = lss.load()
+    rng = np.random.default_rng(26)
+    src = rng.integers(0, 2**32 - 1, size=MAX_ELEMENTS, dtype=np.uint64).astype(np.uint32)
+    valid = (rng.random(MAX_ELEMENTS) < 0.5).astype(np.uint32)
+    b, nb = _run(L.lss_compact_u32_noalloc, src, valid)
+    ref = src[valid != 0]
+    assert nb == ref.size
+    assert np.array_equal(b, ref)
+
+
 def test_no_alloc_refuses_sizes_above_its_maximum():
     import torch
     L = lss.load()
