@@ -4,11 +4,12 @@
 //
 // Stable: dst receives src[i] for every i < n with valid[i] != 0, in index
 // order.  Three stream-ordered kernels over tiles of 4096 elements: the
-// count of each tile (the flags streamed once), an exclusive scan of the
-// tile counts (decoupled lookback over 8192 counts a block), and the scatter
-// (flags and values streamed, each tile's kept values stored from its
-// prefix).  The count is written to device memory (the reference copies it
-// to the host after every 2^25-element chunk).
+// count of each tile, which also packs the flags into one bit an element
+// (the flags are read once); an exclusive scan of the tile counts
+// (decoupled lookback over 8192 counts a block); and the scatter, which
+// reads the packed bits and only the values they keep, and stores the kept
+// values from each tile's prefix.  The count is written to device memory
+// (the reference copies it to the host after every 2^25-element chunk).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -33,6 +34,7 @@ constexpr int kScanTile = kScanThreads * kScanItems;  // tile counts a scan bloc
 
 struct CompactScratch {
     uint64_t* counts;        // one word per tile: its count, then its exclusive prefix
+    uint16_t* bits;          // 16 flag bits per thread and tile (bit 4 q + e: element e of chunk q)
     uint64_t* status;        // one word per scan block, zero before the call
     uint32_t* tile_counter;  // zero before the call
     uint32_t* err;
@@ -50,28 +52,40 @@ __device__ __forceinline__ uint4 load_quad(const uint32_t* __restrict__ p, uint6
                       i + 3 < n ? p[i + 3] : 0u);
 }
 
-// Pass 1: the number of nonzero flags of each tile.  Warp w of a tile reads
-// the elements [512 w, 512 w + 512) as four chunks of 128 (lane l the four
-// elements 4 l .. 4 l + 3 of each chunk, 16-byte loads, a warp's load 512
-// contiguous bytes).  Tiles i, i + G, ... for block i of G.
+// Pass 1: the number of nonzero flags of each tile, and the flags packed.
+// Warp w of a tile reads the elements [512 w, 512 w + 512) as four chunks of
+// 128 (lane l the four elements 4 l .. 4 l + 3 of each chunk, 16-byte loads,
+// a warp's load 512 contiguous bytes); the thread's 16 flags go to one
+// 16-bit word (the tile's 256 words contiguous).  The flags are streamed
+// (evict first): the packed words are what the scatter reads.  Tiles i,
+// i + G, ... for block i of G.
 __global__ void __launch_bounds__(kCompactThreads) k_compact_count(const uint32_t* __restrict__ valid,
-                                                                   uint64_t n, uint64_t* __restrict__ counts) {
+                                                                   uint64_t n, uint64_t* __restrict__ counts,
+                                                                   uint16_t* __restrict__ bits,
+                                                                   uint64_t* __restrict__ clear,
+                                                                   uint64_t nclear) {
     __shared__ uint32_t s_warp[2][kCompactWarps];  // by tile parity: one barrier a tile
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint64_t ntiles = (n + kCompactTile - 1) / kCompactTile;
+    // The scan's status words, block counter and error word, zeroed here:
+    // the scan is the next kernel on the stream.
+    if (blockIdx.x == 0)
+        for (uint64_t i = threadIdx.x; i < nclear; i += kCompactThreads) clear[i] = 0ull;
     const bool vec = (uintptr_t)valid % 16 == 0;
     int buf = 0;
     for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, buf ^= 1) {
         const uint64_t i0 = tile * kCompactTile + (uint64_t)warp * kCompactSeg + (uint64_t)lane * 4;
         uint4 fv[4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) fv[q] = load_quad<false>(valid, i0 + (uint64_t)q * 128, n, vec);
-        uint32_t c = 0;
+        for (int q = 0; q < 4; ++q) fv[q] = load_quad<true>(valid, i0 + (uint64_t)q * 128, n, vec);
+        uint32_t flags = 0;
 #pragma unroll
         for (int q = 0; q < 4; ++q)
-            c += (uint32_t)(fv[q].x != 0u) + (uint32_t)(fv[q].y != 0u) + (uint32_t)(fv[q].z != 0u) +
-                 (uint32_t)(fv[q].w != 0u);
-        c = __reduce_add_sync(0xffffffffu, c);
+            flags |= ((fv[q].x != 0u ? 1u : 0u) | (fv[q].y != 0u ? 2u : 0u) | (fv[q].z != 0u ? 4u : 0u) |
+                      (fv[q].w != 0u ? 8u : 0u))
+                     << (4 * q);
+        bits[tile * kCompactThreads + threadIdx.x] = (uint16_t)flags;
+        const uint32_t c = __reduce_add_sync(0xffffffffu, (uint32_t)__popc(flags));
         if (lane == 0) s_warp[buf][warp] = c;
         __syncthreads();
         if (warp == 0) {
@@ -116,40 +130,46 @@ __global__ void __launch_bounds__(kScanThreads) k_compact_scan(uint64_t ntiles, 
 }
 
 // Pass 3: each tile's kept values, stored from the tile's prefix.  The
-// elements of a thread are those of pass 1; ranks inside the tile: one warp
+// elements of a thread are those of pass 1, its flags the 16 bits pass 1
+// packed; a value is loaded only where one of its four flags is set (16-byte
+// loads, streamed: each is read once).  Ranks inside the tile: one warp
 // inclusive scan of the four per-chunk counts packed into the bytes of a
 // word (a chunk holds at most 128), the warps' totals through shared memory.
-// A lane's kept values go to consecutive places after those of the lanes
-// before it, so a chunk's stores are contiguous too.  The highest tiles come
-// first: pass 1 read their flags last, so they may still be in L2; the
-// loads here stream (evict first), each element being read for the last
-// time.
+// A warp's kept values are gathered in order in a shared-memory row and
+// stored from there, 32 consecutive words an instruction.  The next tile's flag
+// bits and prefix are loaded one tile ahead, so the value loads wait on
+// nothing.
 __global__ void __launch_bounds__(kCompactThreads) k_compact_scatter(const uint32_t* __restrict__ src,
-                                                                     const uint32_t* __restrict__ valid,
+                                                                     const uint16_t* __restrict__ bits,
                                                                      uint32_t* __restrict__ dst, uint64_t n,
                                                                      const uint64_t* __restrict__ prefix) {
     __shared__ uint32_t s_warp[2][kCompactWarps];  // by tile parity: one barrier a tile
+    __shared__ uint32_t s_out[kCompactWarps][kCompactSeg];  // a staging row per warp
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint64_t ntiles = (n + kCompactTile - 1) / kCompactTile;
-    const bool vec = ((uintptr_t)src % 16 == 0) && ((uintptr_t)valid % 16 == 0);
+    const bool vec = (uintptr_t)src % 16 == 0;
     int buf = 0;
-    for (uint64_t r = blockIdx.x; r < ntiles; r += gridDim.x, buf ^= 1) {
-        const uint64_t tile = ntiles - 1 - r;
-        const uint64_t base = prefix[tile];
-        const uint64_t i0 = tile * kCompactTile + (uint64_t)warp * kCompactSeg + (uint64_t)lane * 4;
-        uint4 fv[4], sv[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            fv[q] = load_quad<true>(valid, i0 + (uint64_t)q * 128, n, vec);
-            sv[q] = load_quad<true>(src, i0 + (uint64_t)q * 128, n, vec);
+    uint32_t flags_next = 0;
+    uint64_t base_next = 0;
+    if (blockIdx.x < ntiles) {
+        flags_next = bits[(uint64_t)blockIdx.x * kCompactThreads + threadIdx.x];
+        base_next = prefix[blockIdx.x];
+    }
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, buf ^= 1) {
+        const uint32_t flags = flags_next;
+        const uint64_t base = base_next;
+        const uint64_t tn = tile + gridDim.x;
+        if (tn < ntiles) {
+            flags_next = bits[tn * kCompactThreads + threadIdx.x];
+            base_next = prefix[tn];
         }
-        // Flags (bit e of nibble q) and the packed per-chunk counts.
-        uint32_t flags = 0, packed = 0;
+        const uint64_t i0 = tile * kCompactTile + (uint64_t)warp * kCompactSeg + (uint64_t)lane * 4;
+        uint4 sv[4];
+        uint32_t packed = 0;
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-            const uint32_t f = (fv[q].x != 0u ? 1u : 0u) | (fv[q].y != 0u ? 2u : 0u) | (fv[q].z != 0u ? 4u : 0u) |
-                               (fv[q].w != 0u ? 8u : 0u);
-            flags |= f << (4 * q);
+            const uint32_t f = (flags >> (4 * q)) & 0xFu;
+            sv[q] = f ? load_quad<true>(src, i0 + (uint64_t)q * 128, n, vec) : make_uint4(0u, 0u, 0u, 0u);
             packed |= (uint32_t)__popc(f) << (8 * q);
         }
         uint32_t incl = packed;
@@ -161,21 +181,27 @@ __global__ void __launch_bounds__(kCompactThreads) k_compact_scatter(const uint3
         const uint32_t totals = __shfl_sync(0xffffffffu, incl, 31);  // byte q: chunk q's count
         const uint32_t excl_lane = incl - packed;
         const uint32_t t0c = totals & 0xFFu, t1c = (totals >> 8) & 0xFFu, t2c = (totals >> 16) & 0xFFu;
-        if (lane == 0) s_warp[buf][warp] = t0c + t1c + t2c + (totals >> 24);
-        __syncthreads();
-        // s_warp[buf] is written again two tiles on, after the next barrier.
-        const uint64_t wbase =
-            base + __reduce_add_sync(0xffffffffu, lane < warp ? s_warp[buf][lane] : 0u);
+        const uint32_t wtotal = t0c + t1c + t2c + (totals >> 24);
+        // The warp's kept values in order in its staging row, then stored
+        // from there as whole 128-byte rows of dst.
+        uint32_t* row = s_out[warp];
         const uint32_t cbase[4] = {0u, t0c, t0c + t1c, t0c + t1c + t2c};
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-            uint64_t o = wbase + cbase[q] + ((excl_lane >> (8 * q)) & 0xFFu);
+            uint32_t o = cbase[q] + ((excl_lane >> (8 * q)) & 0xFFu);
             const uint32_t f = (flags >> (4 * q)) & 0xFu;
-            if (f & 1u) dst[o++] = sv[q].x;
-            if (f & 2u) dst[o++] = sv[q].y;
-            if (f & 4u) dst[o++] = sv[q].z;
-            if (f & 8u) dst[o++] = sv[q].w;
+            if (f & 1u) row[o++] = sv[q].x;
+            if (f & 2u) row[o++] = sv[q].y;
+            if (f & 4u) row[o++] = sv[q].z;
+            if (f & 8u) row[o++] = sv[q].w;
         }
+        if (lane == 0) s_warp[buf][warp] = wtotal;
+        __syncthreads();  // also orders the staging row's writes before its reads
+        // s_warp[buf] is written again two tiles on, after the next barrier.
+        const uint64_t wbase =
+            base + __reduce_add_sync(0xffffffffu, lane < warp ? s_warp[buf][lane] : 0u);
+        for (uint32_t i = (uint32_t)lane; i < wtotal; i += 32) __stcs(dst + wbase + i, row[i]);
+        __syncwarp();  // the row is rewritten by this warp for the next tile
     }
 }
 
@@ -191,9 +217,13 @@ static unsigned resident_grid(const void* fn, int threads, int sms, uint64_t uni
 
 uint64_t compact_tiles(uint64_t n) { return (n + kCompactTile - 1) / kCompactTile; }
 uint64_t compact_scan_blocks(uint64_t n) { return (compact_tiles(n) + kScanTile - 1) / kScanTile; }
-// Scratch of a call, in words: the tile counts, the scan's status words, then
-// one word for the scan's block counter and the error word.
-uint64_t compact_scratch_words(uint64_t n) { return compact_tiles(n) + compact_scan_blocks(n) + 1 + 1; }
+// Scratch of a call, in 8-byte words: the tile counts, the packed flags (512
+// bytes a tile), the scan's status words, then one word for the scan's block
+// counter and the error word.
+constexpr uint64_t kBitsWordsPerTile = kCompactThreads * sizeof(uint16_t) / 8;
+uint64_t compact_scratch_words(uint64_t n) {
+    return compact_tiles(n) * (1 + kBitsWordsPerTile) + compact_scan_blocks(n) + 1 + 1;
+}
 
 // Points sc into words [0, compact_scratch_words(n)) of base.  The words from
 // *clear_from on are the ones to zero before the call.
@@ -201,10 +231,11 @@ CompactScratch compact_scratch(uint64_t* base, uint64_t n, uint64_t* clear_from)
     CompactScratch sc;
     const uint64_t nt = compact_tiles(n), ns = compact_scan_blocks(n);
     sc.counts = base;
-    sc.status = base + nt;
-    sc.tile_counter = (uint32_t*)(base + nt + ns + 1);
+    sc.bits = (uint16_t*)(base + nt);
+    sc.status = base + nt * (1 + kBitsWordsPerTile);
+    sc.tile_counter = (uint32_t*)(sc.status + ns + 1);
     sc.err = sc.tile_counter + 1;
-    *clear_from = nt;
+    *clear_from = nt * (1 + kBitsWordsPerTile);
     return sc;
 }
 
@@ -232,10 +263,13 @@ static CompactGrids compact_grids(int dev) {
     return r;
 }
 
-// Launches the three passes with caller-provided scratch (status words,
-// block counter and error word zeroed).
+// Launches the three passes on scratch of compact_scratch_words(n) words at
+// base (the count pass clears the words the scan needs zeroed).
 cudaError_t launch_compact_u32(const uint32_t* src, const uint32_t* valid, uint32_t* dst, uint64_t n,
-                               uint64_t* count, CompactScratch sc, cudaStream_t st) {
+                               uint64_t* count, uint64_t* base, cudaStream_t st) {
+    uint64_t clear_from = 0;
+    const CompactScratch sc = compact_scratch(base, n, &clear_from);
+    const uint64_t nclear = compact_scratch_words(n) - clear_from;
     int dev = 0;
     cudaGetDevice(&dev);
     const CompactGrids cg = compact_grids(dev);
@@ -245,9 +279,9 @@ cudaError_t launch_compact_u32(const uint32_t* src, const uint32_t* valid, uint3
     // Scan blocks take their counts in order from a counter, so a lookback
     // never waits on a block not started.
     const unsigned g2 = (unsigned)std::min<uint64_t>(cg.scan, compact_scan_blocks(n));
-    k_compact_count<<<g1, kCompactThreads, 0, st>>>(valid, n, sc.counts);
+    k_compact_count<<<g1, kCompactThreads, 0, st>>>(valid, n, sc.counts, sc.bits, base + clear_from, nclear);
     k_compact_scan<<<g2, kScanThreads, 0, st>>>(nt, (unsigned long long*)count, sc);
-    k_compact_scatter<<<g3, kCompactThreads, 0, st>>>(src, valid, dst, n, sc.counts);
+    k_compact_scatter<<<g3, kCompactThreads, 0, st>>>(src, sc.bits, dst, n, sc.counts);
     return cudaGetLastError();
 }
 
@@ -259,7 +293,7 @@ namespace lss {
 // like the default pool, but it keeps up to kPoolKeep bytes reserved when
 // streams synchronise (the default pool hands its memory back at every
 // synchronisation, and mapping it again cost about 0.17 ms a call).
-constexpr uint64_t kPoolKeep = 64ull << 20;
+constexpr uint64_t kPoolKeep = 128ull << 20;
 static std::mutex g_pool_mu;
 static cudaMemPool_t g_pools[64] = {};
 
@@ -302,8 +336,8 @@ extern "C" lss_status lss_compact_u32(const uint32_t* d_src, const uint32_t* d_v
     if (n == 0) {
         return cudaMemsetAsync(d_count, 0, sizeof(uint64_t), st) == cudaSuccess ? LSS_OK : LSS_ERR_CUDA;
     }
-    // Scratch: tile counts, status words, block counter and error word,
-    // stream-ordered from the library's pool.
+    // Scratch: tile counts, packed flags, status words, block counter and
+    // error word, stream-ordered from the library's pool.
     cudaMemPool_t pool = nullptr;
     const lss_status ps = lss::compact_pool(&pool);
     if (ps != LSS_OK) return ps;
@@ -316,8 +350,7 @@ extern "C" lss_status lss_compact_u32(const uint32_t* d_src, const uint32_t* d_v
     uint64_t clear_from = 0;
     const lss::CompactScratch sc = lss::compact_scratch((uint64_t*)scratch, n, &clear_from);
     lss_status s = LSS_OK;
-    if (cudaMemsetAsync((uint64_t*)scratch + clear_from, 0, (words - clear_from) * 8, st) != cudaSuccess ||
-        lss::launch_compact_u32(d_src, d_valid, d_dst, n, d_count, sc, st) != cudaSuccess)
+    if (lss::launch_compact_u32(d_src, d_valid, d_dst, n, d_count, (uint64_t*)scratch, st) != cudaSuccess)
         s = LSS_ERR_CUDA;
     uint32_t err = 0;
     if (s == LSS_OK && cudaMemcpyAsync(&err, sc.err, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess)
@@ -337,14 +370,14 @@ extern "C" lss_status lss_compact_u32(const uint32_t* d_src, const uint32_t* d_v
 // cudaMalloc of their own would bypass its pool or its accounting).  For
 // them lss_compact_u32_noalloc keeps its scratch in this file-scope device
 // array instead of asking the stream-ordered allocator.  Every GPU that loads
-// the library holds the array (a little over 128 KiB) until the process exits.
+// the library holds the array (a little over 8 MiB) until the process exits.
 // The call reads the error word back and synchronises its stream before it
 // returns.
 namespace lss {
 
 // Largest n the allocation-free call accepts.
 constexpr uint64_t kNoAllocMaxElements = 1ull << 26;
-constexpr uint64_t kNoAllocWords = kNoAllocMaxElements / kCompactTile +
+constexpr uint64_t kNoAllocWords = kNoAllocMaxElements / kCompactTile * (1 + kBitsWordsPerTile) +
                                    (kNoAllocMaxElements / kCompactTile + kScanTile - 1) / kScanTile + 2;
 
 // The scratch of compact_scratch_words(n) for every n up to the maximum.
@@ -387,14 +420,13 @@ extern "C" lss_status lss_compact_u32_noalloc(const uint32_t* d_src, const uint3
     uint64_t* base = nullptr;
     lss_status s = lss::noalloc_scratch(&base);
     if (s != LSS_OK) return s;
-    const uint64_t words = lss::compact_scratch_words(n);  // <= kNoAllocWords
+    // compact_scratch_words(n) <= kNoAllocWords.  The array keeps the
+    // previous call's contents: the count pass clears the words the scan
+    // reads before writing (the tile counts and packed flags are written
+    // before they are read).
     uint64_t clear_from = 0;
     const lss::CompactScratch sc = lss::compact_scratch(base, n, &clear_from);
-    // The array keeps the previous call's contents: clear the status words,
-    // the block counter and the error word (the tile counts are written
-    // before they are read).
-    if (cudaMemsetAsync(base + clear_from, 0, (words - clear_from) * 8, st) != cudaSuccess ||
-        lss::launch_compact_u32(d_src, d_valid, d_dst, n, d_count, sc, st) != cudaSuccess) {
+    if (lss::launch_compact_u32(d_src, d_valid, d_dst, n, d_count, base, st) != cudaSuccess) {
         cudaGetLastError();
         return LSS_ERR_CUDA;
     }

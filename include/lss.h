@@ -319,10 +319,10 @@ lss_status lss_adjoint_run(lss_engine* e, int32_t K, int32_t checkpoint_every,
 /* ≈ CudppCompact (code/gpuseg/code/src/cuda/Cuda.cpp:699-758) over CUDPP's
  * cudppCompact: stable compaction of d_src[i] for every i < n with
  * d_valid[i] != 0 into d_dst (device pointers, caller-owned).  The count is
- * written to *d_count in device memory.  Its scratch (one word per 4096
- * elements) comes from a stream-ordered memory pool of the library's own,
- * which keeps up to 64 MiB reserved between calls, and goes back to it before
- * the call ends; the call synchronises `stream` (a cudaStream_t, NULL = the
+ * written to *d_count in device memory.  Its scratch (n/8 bytes of packed
+ * flags and a word per 4096 elements) comes from a stream-ordered memory pool
+ * of the library's own, which keeps up to 128 MiB reserved between calls, and
+ * goes back to it before the call ends; the call synchronises `stream` (a cudaStream_t, NULL = the
  * legacy default stream) before returning. */
 lss_status lss_compact_u32(const uint32_t* d_src, const uint32_t* d_valid, uint32_t* d_dst,
                            uint64_t n, uint64_t* d_count, void* stream);
@@ -337,7 +337,7 @@ lss_status lss_compact_u32(const uint32_t* d_src, const uint32_t* d_valid, uint3
  * counterpart in the reference
  * (which allocates through CUDPP's plan).  Same arguments and result as
  * lss_compact_u32; allocates nothing: its scratch is a fixed device array of
- * the library (about 128 KiB, held by every GPU that loads the library until
+ * the library (about 8 MiB, held by every GPU that loads the library until
  * the process exits).  n above LSS_COMPACT_NOALLOC_MAX_ELEMENTS returns
  * LSS_ERR_CAPACITY without touching the buffers.  The first call on a device
  * looks the array up on that device (with that device current); make that
