@@ -205,14 +205,14 @@ __global__ void __launch_bounds__(kCompactThreads) k_compact_scatter(const uint3
     }
 }
 
-static unsigned resident_grid(const void* fn, int threads, int sms, uint64_t units) {
+// Blocks of fn that fit on the device at once.
+static unsigned resident_grid(const void* fn, int threads, int sms) {
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0) != cudaSuccess) {
         cudaGetLastError();
         per_sm = 1;
     }
-    per_sm = std::max(per_sm, 1);
-    return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(units, (uint64_t)sms * (uint64_t)per_sm));
+    return (unsigned)(std::max(per_sm, 1) * sms);
 }
 
 uint64_t compact_tiles(uint64_t n) { return (n + kCompactTile - 1) / kCompactTile; }
@@ -254,11 +254,10 @@ static CompactGrids compact_grids(int dev) {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     sms = std::max(sms, 1);
-    const uint64_t all = ~0ull;
     CompactGrids r;
-    r.count = resident_grid((const void*)k_compact_count, kCompactThreads, sms, all);
-    r.scan = resident_grid((const void*)k_compact_scan, kScanThreads, sms, all);
-    r.scatter = resident_grid((const void*)k_compact_scatter, kCompactThreads, sms, all);
+    r.count = resident_grid((const void*)k_compact_count, kCompactThreads, sms);
+    r.scan = resident_grid((const void*)k_compact_scan, kScanThreads, sms);
+    r.scatter = resident_grid((const void*)k_compact_scatter, kCompactThreads, sms);
     if (dev >= 0 && dev < 64) g_grids[dev] = r;
     return r;
 }
@@ -284,10 +283,6 @@ cudaError_t launch_compact_u32(const uint32_t* src, const uint32_t* valid, uint3
     k_compact_scatter<<<g3, kCompactThreads, 0, st>>>(src, sc.bits, dst, n, sc.counts);
     return cudaGetLastError();
 }
-
-}  // namespace lss
-
-namespace lss {
 
 // The allocating entry point's memory pool, one per device: stream-ordered
 // like the default pool, but it keeps up to kPoolKeep bytes reserved when
