@@ -53,9 +53,18 @@ def test_defaults_and_errors_without_device():
         has_gpu = torch.cuda.is_available()
     except Exception:
         has_gpu = False
+    # Kernel-level compaction: argument and size checks come before any
+    # device call (the pointers below are never dereferenced).
+    p = C.c_void_p(256)
+    assert L.lss_compact_u32(None, p, p, 5, p, None) == 1           # LSS_ERR_INVALID_ARGUMENT
+    assert L.lss_compact_u32(p, p, p, 1 << 40, p, None) == 9        # LSS_ERR_CAPACITY
+    assert L.lss_compact_u32_noalloc(p, p, None, 5, p, None) == 1
+    assert L.lss_compact_u32_noalloc(p, p, p, (1 << 26) + 1, p, None) == 9
     if not has_gpu:
         h = C.c_void_p()
         assert L.lss_create(C.byref(h), None) == 7  # LSS_ERR_NO_DEVICE
+        assert L.lss_compact_u32(p, p, p, 5, p, None) == 7
+        assert L.lss_compact_u32_noalloc(p, p, p, 5, p, None) == 7
 
 
 def test_phantoms_are_deterministic():
