@@ -34,8 +34,9 @@ def compact_gpu(src, valid, offset=0):
 
 @pytest.mark.parametrize("n,p", [(0, 0.5), (1, 1.0), (4095, 0.3), (4096, 0.5), (4097, 0.01),
                                  (100_003, 0.5), (3_000_000, 0.02), (1 << 22, 1.0),
+                                 # nothing kept; exactly one full scan block of tile counts;
                                  # more tile counts than one scan block takes (8192 x 4096)
-                                 (40_000_003, 0.3)])
+                                 (5_000_001, 0.0), (1 << 25, 0.5), (40_000_003, 0.3)])
 def test_compact_matches_numpy(n, p):
     rng = np.random.default_rng(n)
     src = rng.integers(0, 2**32 - 1, size=n, dtype=np.uint64).astype(np.uint32)
